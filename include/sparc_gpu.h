@@ -1,0 +1,213 @@
+/*
+ * sparc_gpu.h -- C ABI of the GB300 (sm_103a) SPARC time-stepping library.
+ *
+ * The reference (jishnub/sparc) has no plugin or FFI layer: its hot path is the
+ * `call step()` seam inside the Fortran TIMESTEPPING loop (driver.f90:424),
+ * operating on module globals (initialize.f90:24-153), and the outside world
+ * reaches it only through `mpiexec -np 1 ./sparc <src> <ls>` plus files
+ * (full.py:49,67; linesearch.py:47-52; data_forward.py:49-52).  Each entry
+ * point below names the reference routine (file:line) whose job it takes over.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (SPARC_OK = 0, negative on error)
+ *     and never exits or traps.  sparc_gpu_errstr() describes a status and
+ *     sparc_gpu_last_error() the last failure of a context in words.
+ *   - Host arrays are FP64 and caller-owned; the library copies in and out and
+ *     keeps no host pointer beyond a call.  Device memory belongs to the
+ *     context.
+ *   - 3-D fields are laid out as the reference's Fortran arrays a(nx,ny,nz):
+ *     x fastest, then y, then z  (C order [nz][ny][nx]).
+ *   - One context per host thread; calls on one context must be serialised by
+ *     the caller.  Contexts are independent (one CUDA stream each).
+ */
+#ifndef SPARC_GPU_H
+#define SPARC_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPARC_GPU_ABI_VERSION 1
+
+/* status codes */
+#define SPARC_OK 0
+#define SPARC_EINVAL (-1)     /* bad parameter or argument */
+#define SPARC_ENOMEM (-2)     /* device or host allocation failed */
+#define SPARC_ECUDA (-3)      /* a CUDA call failed */
+#define SPARC_ETIMEDOUT (-4)  /* a bounded device wait gave up */
+#define SPARC_ENAN (-5)       /* non-finite values detected in the state */
+#define SPARC_ESTATE (-6)     /* call out of order (e.g. no background yet) */
+#define SPARC_EIO (-7)        /* file read/write failed or corrupt */
+
+/* precision of the bulk field arithmetic */
+#define SPARC_FP64 0          /* plain: everything FP64 */
+#define SPARC_FP32 1          /* FP32 fields; FP64 set-up, profiles and kernel accumulation */
+
+/* source modes for sparc_gpu_set_source */
+#define SPARC_SRC_NONE 0
+#define SPARC_SRC_SERIES 1    /* forcing(t) = plane[0] * series[time]        (physics2d.f90:1066) */
+#define SPARC_SRC_LAGRANGE 2  /* forcing(t) = 7-point Lagrange interpolation of planes sampled
+                                 every cadforcing seconds (LAGRANGE_INTERP, physics.f90:678-737) */
+
+/* field indices of the displacement form (initialize.f90:515-527) */
+#define SPARC_XI_X 0
+#define SPARC_XI_Y 1
+#define SPARC_XI_Z 2
+#define SPARC_V_X 3
+#define SPARC_V_Y 4
+#define SPARC_V_Z 5
+
+/* Mirror of params.i (params.i:25-150) plus the Instruction-file flags
+ * (initialize.f90:1006-1051).  Lengths in cm, times in s, frequencies in Hz. */
+typedef struct sparc_params {
+    int nx, ny, nz;            /* params.i:25  (nx, ny powers of two; ny = 1 for option 17) */
+    int npmlbot, npmltop;      /* params.i:108 */
+    int option;                /* 4 = MP_QUIET_PML_3D_DISPL, 17 = MP_QUIET_PML_2D_DISPL (step.f90:74-110) */
+    int compute_forward;       /* Instruction 'spectral' */
+    int compute_adjoint;       /* Instruction 'adjoint' */
+    int damp_waves;            /* params.i:38 */
+    int src_k;                 /* 1-based source plane; 0 = e_rad (forward) / o_rad (adjoint) */
+    int precision;             /* SPARC_FP64 or SPARC_FP32 */
+    int nsrc;                  /* number of sources on the source axis (batch) */
+    double xlength, ylength, timestep;   /* params.i:26 */
+    double excitdep, obsheight;          /* params.i:150, :130 */
+    double cadforcing, outputcad;        /* params.i:47, :136 */
+    double nupeak, nuwidth;              /* params.i:64 */
+    double solartime;                    /* params.i:129 (hours) */
+} sparc_params;
+
+typedef struct sparc_ctx sparc_ctx;
+
+/* ---- life cycle ---------------------------------------------------------- */
+
+/* Replaces Initialize_all (initialize.f90:165-583): validates p, picks the
+ * device's current GPU, allocates all device state.  *out is NULL on error. */
+int sparc_gpu_create(const sparc_params* p, sparc_ctx** out);
+
+/* Releases device memory and the stream.  Accepts NULL. */
+void sparc_gpu_destroy(sparc_ctx* ctx);
+
+const char* sparc_gpu_errstr(int status);
+const char* sparc_gpu_last_error(const sparc_ctx* ctx);
+int sparc_gpu_abi_version(void);
+
+/* ---- set-up -------------------------------------------------------------- */
+
+/* Replaces solar_data (initialize.f90:728-774), the stretch set-up
+ * (initialize.f90:464-472), mp_Initialize_RHS / _2d (physics.f90:34-404,
+ * physics2d.f90:23-410), INIT_DAMPING (damping.f90:10-120) and
+ * INITIALIZE_STEP (step.f90:24-41).  Inputs are the six columns of the
+ * background file, one value per z-level, bottom first, in cgs units:
+ * z = r/R_sun, c, rho, p, g, Gamma_1.  All set-up arithmetic is FP64.
+ * Resets the state to zero and the time index to 0. */
+int sparc_gpu_set_background(sparc_ctx* ctx, const double* z, const double* c,
+                             const double* rho, const double* p0, const double* g,
+                             const double* gamma1);
+
+/* Source of source-axis slot src_idx.  planes: L horizontal planes (ny,nx),
+ * series: nseries values indexed by the time-step index (SPARC_SRC_SERIES).
+ * For SPARC_SRC_LAGRANGE the planes are vr(:,:,1..L) of LAGRANGE_INTERP
+ * sampled every cadforcing seconds and series is ignored.  Replaces the
+ * source set-up of DETERMINE_STATUS (driver.f90:591-695). */
+int sparc_gpu_set_source(sparc_ctx* ctx, int src_idx, int mode, const double* planes, int L,
+                         const double* series, int nseries);
+
+/* ---- time stepping --------------------------------------------------------- */
+
+/* nsteps iterations of the TIMESTEPPING body (driver.f90:412-424): forcing
+ * interpolation, STEP (step.f90:43-128: five LDDRK stages of the selected RHS,
+ * PML auxiliaries, FILTER_VARS_3D / _2D), then time = time + 1.  When surface
+ * recording is on, vz at o_rad is recorded whenever mod(time, steps) == 0
+ * (driver.f90:455-476). */
+int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
+
+int sparc_gpu_get_time(const sparc_ctx* ctx, int* time);
+int sparc_gpu_set_time(sparc_ctx* ctx, int time);
+
+/* ---- state in and out ------------------------------------------------------ */
+
+/* Field `field` (SPARC_XI_X..SPARC_V_Z) of slot src_idx into host (nz,ny,nx),
+ * or only plane k (1-based) into host (ny,nx) when k > 0.
+ * field 6..11 return the last RK-stage right-hand side scr(:,:,:,1..6), whose
+ * components 4..6 are the 'acc' fields of WRITE_OUT_PARTIAL_STATE
+ * (all_modules.f90:771-778). */
+int sparc_gpu_get_field(sparc_ctx* ctx, int src_idx, int field, int k, double* host);
+
+/* Whole state of one slot: a (6,nz,ny,nx) and the PML auxiliaries
+ * pmlvars (2,nzpml,ny,nx); pml may be NULL.  Replaces READ_IN_INITIAL_CONDITION /
+ * WRITE_OUT_FULL_STATE (all_modules.f90:533-694) in memory. */
+int sparc_gpu_set_state(sparc_ctx* ctx, int src_idx, const double* a, const double* pml);
+int sparc_gpu_get_state(sparc_ctx* ctx, int src_idx, double* a, double* pml);
+
+/* Surface seismogram recording (the vz_cc.bin stream, driver.f90:455-476):
+ * enable with room for max_records outputs per slot; fetch them as
+ * (nrec,ny,nx) FP64 records, the layout of write_binary_seq_2D
+ * (all_modules.f90:947-1006). */
+int sparc_gpu_record_surface(sparc_ctx* ctx, int enable, int max_records);
+int sparc_gpu_get_records(sparc_ctx* ctx, int src_idx, double* host, int* nrec);
+
+/* Checkpoint / restore of every slot (state, PML, time) to one file with a
+ * checksum; restore rejects a corrupt or mismatching file with SPARC_EIO. */
+int sparc_gpu_checkpoint(sparc_ctx* ctx, const char* path);
+int sparc_gpu_restore(sparc_ctx* ctx, const char* path);
+
+/* ---- sensitivity kernels (kernels.f90:197-311, 523-539) ------------------- */
+
+/* The forward-snapshot store: saves the spectral quantities that the kernel
+ * integral needs from the current state of forward context `fwd` into slot
+ * `snap` (0-based) of the store.  Allocates the store on first use for
+ * nsnap snapshots. */
+int sparc_gpu_snapshot(sparc_ctx* fwd, int snap, int nsnap);
+
+/* One accumulation of kernels.f90:276-311 for every slot: forward snapshot
+ * `snap` of `fwd` against the current state of adjoint context `adj`.
+ * Accumulators are FP64 and live in `adj`. */
+int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* adj);
+
+/* Resets the accumulators of `adj`. */
+int sparc_gpu_kernel_reset(sparc_ctx* adj);
+
+/* Final scaling (kernels.f90:523-539) into host arrays (nz,ny,nx): K_c, K_rho,
+ * hessian of slot src_idx (sum_slots != 0: summed over the source axis,
+ * the grad.py:158-165 sum). */
+int sparc_gpu_kernels(sparc_ctx* adj, int src_idx, int sum_slots, double* kc, double* krho,
+                      double* hessian);
+
+/* ---- primitives (the reference's derivative routines) ---------------------- */
+
+/* ddx / ddy (derivatives.f90:28-170) and ddz (derivatives.f90:10-24 with
+ * DBYD2 dbyd2.f90:8-237 + MTRIDAG mtridag.f90:94-111) of one host field
+ * (nz,ny,nx) using the context's grid; bc as in DBYD2 (0..3).  For bc 2 / 3
+ * dvar must carry the caller-set boundary plane (k = 1 / k = nz) on input. */
+int sparc_gpu_ddx(sparc_ctx* ctx, const double* var, double* dvar);
+int sparc_gpu_ddy(sparc_ctx* ctx, const double* var, double* dvar);
+int sparc_gpu_ddz(sparc_ctx* ctx, const double* var, double* dvar, int bc);
+
+/* damp_velocity (damping.f90:125-161) of one field: rhs -= damping(v). */
+int sparc_gpu_damp(sparc_ctx* ctx, const double* v, double* rhs);
+
+/* ---- measurement hooks ------------------------------------------------------ */
+
+/* The context's CUDA stream (a cudaStream_t), for event timing by the caller. */
+void* sparc_gpu_stream(sparc_ctx* ctx);
+
+/* Number of kernels this context has launched so far. */
+long long sparc_gpu_launch_count(const sparc_ctx* ctx);
+
+/* Device bytes held by the context. */
+long long sparc_gpu_device_bytes(const sparc_ctx* ctx);
+
+/* Set-up diagnostics: info[0..14] = e_rad, o_rad, delta_width, deltat,
+ * steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps,
+ * betas(1..5); ztab / ptab receive the FP64 z-profile and pencil tables
+ * (either may be NULL). */
+int sparc_gpu_info(sparc_ctx* ctx, double* info, double* ztab, double* ptab);
+
+/* Blocks until the context's stream is idle; SPARC_ENAN if check_finite and
+ * the state of any slot holds a non-finite value. */
+int sparc_gpu_sync(sparc_ctx* ctx, int check_finite);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPARC_GPU_H */

@@ -1,0 +1,1116 @@
+// C-ABI implementation of include/sparc_gpu.h: context life cycle, the FP64
+// host set-up that replaces the reference's initialisation routines, the
+// TIMESTEPPING loop body, state transfer, surface recording, sensitivity
+// kernels and checkpointing.  All device work runs on the context's stream.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "internal.cuh"
+#include "../../include/sparc_gpu.h"
+
+namespace {
+
+inline double R4(double x) { return (double)(float)x; }
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sparc_ctx {
+    sparc_params P;
+    int H, M, nz, S, nzpml;
+    long long fs, ps, NP, N;
+    int f32;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    long long launches = 0;
+    long long dev_bytes = 0;
+    std::vector<void*> allocs;
+
+    // host set-up (FP64)
+    bool have_bg = false;
+    double pi, rsun, normx, normy, dimc, dimrho, diml, deltat, stretchx, stretchy, delta_width;
+    double betas[5];
+    int e_rad, o_rad, steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps;
+    std::vector<double> zt_host;     // ZT_COUNT * nz
+    std::vector<double> pt_host;     // PT_COUNT * M
+    Compact<double> cc64;
+    int time = 0;
+
+    // device state (element type T; CT = T2)
+    void* a = nullptr; void* scr = nullptr; void* pml = nullptr; void* scrpml = nullptr;
+    void* ybuf = nullptr; void* pbuf = nullptr; void* rbuf = nullptr;
+    void* zt = nullptr; void* pt = nullptr;       // T tables
+    double* zt64 = nullptr; double* pt64 = nullptr;
+    double* tw_x = nullptr; double* tw_y = nullptr;
+    void* tmp = nullptr;          // FFT intermediate, nz*M complex T
+    void* phys = nullptr;         // one physical field, N reals T
+    double* phys64 = nullptr;     // N doubles
+    double2* spec64 = nullptr;    // nz*M complex double (primitives)
+    double2* spec64b = nullptr;
+    double2* tmp64 = nullptr;
+    int* d_flag = nullptr;
+
+    // sources
+    int src_mode = 0;
+    int src_L = 0;
+    void* planes = nullptr;       // [S][L][M] CT
+    double* series = nullptr;     // [S][nseries]
+    int nseries = 0;
+    std::vector<int> src_set;
+    int last_nw = 0; int last_widx[7]; double last_wts[7];
+
+    // surface records
+    int rec_on = 0, rec_max = 0, rec_n = 0;
+    void* rec = nullptr;          // [S][rec_max][M] CT
+
+    // kernels
+    void* store = nullptr; int store_n = 0;     // [nsnap][S][7][N] T
+    double* kacc = nullptr;                     // [S][3][N]
+    void* ktemp = nullptr;                      // [7][N] T
+};
+
+namespace {
+
+int fail(sparc_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail(c, SPARC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKL()                                                                      \
+    do {                                                                           \
+        cudaError_t e_ = cudaGetLastError();                                       \
+        if (e_ != cudaSuccess)                                                     \
+            return fail(c, SPARC_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int dalloc(sparc_ctx* c, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(c, SPARC_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    c->dev_bytes += (long long)bytes;
+    cudaMemsetAsync(*p, 0, bytes, c->stream);
+    return SPARC_OK;
+}
+
+size_t esz(const sparc_ctx* c) { return c->f32 ? sizeof(float) : sizeof(double); }
+size_t csz(const sparc_ctx* c) { return 2 * esz(c); }
+
+// ---------------------------------------------------------------------------
+// compact finite differences on the host (set-up only): DBYD2 / MTRIDAG
+// ---------------------------------------------------------------------------
+struct Tri {
+    std::vector<double> low, upp, betad, gam;
+};
+
+void compact_coeffs(int nz, Compact<double>& cc) {
+    double d2i = (double)(float)(nz - 1);                       // dbyd2.f90:49
+    cc.C1 = d2i * 7.0 / 9.0;                                    // dbyd2.f90:88
+    cc.C2 = d2i / 36.0;
+    cc.Cb[0] = -(double)(43.0f / 96.0f) * d2i;                  // dbyd2.f90:104-108 (REAL*4 ratios)
+    cc.Cb[1] = -(double)(5.0f / 6.0f) * d2i;
+    cc.Cb[2] = (double)(9.0f / 8.0f) * d2i;
+    cc.Cb[3] = (double)(1.0f / 6.0f) * d2i;
+    cc.Cb[4] = -(double)(1.0f / 96.0f) * d2i;
+    cc.Cf[0] = -(double)(10.0f / 3.0f) * d2i;                   // dbyd2.f90:122-125
+    cc.Cf[1] = -3.0 * d2i;
+    cc.Cf[2] = 6.0 * d2i;
+    cc.Cf[3] = (double)(1.0f / 3.0f) * d2i;
+    cc.alpha2 = 0.75;                                           // dbyd2.f90:157-162
+    cc.beta1 = 3.0;
+    cc.cnst = 1.0 / (0.75 - 3.0 * 0.125);
+}
+
+// matrix of DBYD2 for boundary code ibc (dbyd2.f90:152-196) and its Thomas
+// factorisation (mtridag.f90:95-99)
+Tri tri_for(int nz, int ibc) {
+    Tri t;
+    std::vector<double> uppr(nz + 1, 0.0), lowr(nz + 1, 0.0);
+    double alpha = (double)(1.0f / 3.0f);
+    for (int J = 3; J <= nz - 2; ++J) uppr[J] = alpha;
+    double alpha2 = 0.75, gamma2 = 0.125, alpha1 = 6.0, beta1 = 3.0;
+    double cnst = 1.0 / (alpha2 - beta1 * gamma2);
+    double up1 = (alpha1 * alpha2 - beta1) * cnst;
+    uppr[1] = (ibc % 2 == 0) ? 0.0 : up1;
+    uppr[2] = alpha2;
+    uppr[nz - 1] = gamma2;
+    for (int I = 1; I <= nz; ++I) lowr[I] = uppr[nz - I + 1];
+    lowr[nz] = (ibc != 1 && ibc != 2) ? 0.0 : up1;
+    t.low.assign(lowr.begin() + 1, lowr.end());
+    t.upp.assign(uppr.begin() + 1, uppr.end());
+    t.betad.assign(nz, 0.0);
+    t.gam.assign(nz, 0.0);
+    t.betad[0] = 1.0;
+    for (int J = 1; J < nz; ++J) {
+        t.gam[J] = t.upp[J - 1] / t.betad[J - 1];
+        t.betad[J] = 1.0 - t.low[J] * t.gam[J];
+    }
+    return t;
+}
+
+// ddz of one z-profile (dbyd2 + stretch), divisions as in mtridag.f90:100-107
+void host_dbyd2(const std::vector<double>& b, std::vector<double>& a, int ibc, const Compact<double>& cc,
+                const Tri& t) {
+    int n = (int)b.size();
+    std::vector<double> R(n, 0.0);
+    for (int j = 2; j <= n - 3; ++j) R[j] = cc.C1 * (b[j + 1] - b[j - 1]) + cc.C2 * (b[j + 2] - b[j - 2]);
+    R[1] = cc.Cb[0] * b[0] + cc.Cb[1] * b[1] + cc.Cb[2] * b[2] + cc.Cb[3] * b[3] + cc.Cb[4] * b[4];
+    R[n - 2] = -(cc.Cb[0] * b[n - 1] + cc.Cb[1] * b[n - 2] + cc.Cb[2] * b[n - 3] + cc.Cb[3] * b[n - 4] + cc.Cb[4] * b[n - 5]);
+    R[0] = (ibc == 1 || ibc == 3) ? cc.Cf[0] * b[0] + cc.Cf[1] * b[1] + cc.Cf[2] * b[2] + cc.Cf[3] * b[3] : 0.0;
+    R[n - 1] = (ibc == 1 || ibc == 2)
+                   ? -(cc.Cf[0] * b[n - 1] + cc.Cf[1] * b[n - 2] + cc.Cf[2] * b[n - 3] + cc.Cf[3] * b[n - 4])
+                   : 0.0;
+    if (ibc % 2 != 0) R[0] = (cc.alpha2 * R[0] - cc.beta1 * R[1]) * cc.cnst;
+    if (ibc == 1 || ibc == 2) R[n - 1] = (cc.alpha2 * R[n - 1] - cc.beta1 * R[n - 2]) * cc.cnst;
+    std::vector<double> ud(n);
+    ud[0] = R[0] / t.betad[0];
+    for (int J = 1; J < n; ++J) ud[J] = (R[J] - t.low[J] * ud[J - 1]) / t.betad[J];
+    for (int J = n - 2; J >= 0; --J) ud[J] = ud[J] - t.gam[J + 1] * ud[J + 1];
+    a = ud;
+}
+
+int upload(sparc_ctx* c, void* dst, const void* src, size_t bytes) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return SPARC_OK;
+}
+
+template <typename T> typename CplxOf<T>::type* CP(void* p) { return (typename CplxOf<T>::type*)p; }
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int sparc_gpu_abi_version(void) { return SPARC_GPU_ABI_VERSION; }
+
+const char* sparc_gpu_errstr(int s) {
+    switch (s) {
+        case SPARC_OK: return "ok";
+        case SPARC_EINVAL: return "invalid argument or parameter";
+        case SPARC_ENOMEM: return "out of memory";
+        case SPARC_ECUDA: return "CUDA error";
+        case SPARC_ETIMEDOUT: return "device wait timed out";
+        case SPARC_ENAN: return "non-finite value in the state";
+        case SPARC_ESTATE: return "call out of order";
+        case SPARC_EIO: return "file I/O error or corrupt checkpoint";
+        default: return "unknown status";
+    }
+}
+
+const char* sparc_gpu_last_error(const sparc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+static int validate(const sparc_params* p, std::string& why) {
+    auto pow2 = [](int n) { return n >= 4 && n <= 1024 && (n & (n - 1)) == 0; };
+    if (p->option != 4 && p->option != 17) { why = "option must be 4 or 17"; return 0; }
+    if (!pow2(p->nx)) { why = "nx must be a power of two in [4,1024]"; return 0; }
+    if (p->option == 17 && p->ny != 1) { why = "option 17 needs ny == 1"; return 0; }
+    if (p->option == 4 && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
+    if (p->nz < 16 || p->nz > 1024) { why = "nz must be in [16,1024]"; return 0; }
+    if (p->npmlbot < 2 || p->npmlbot > p->nz / 4 || p->npmltop < 0 || p->npmltop > p->nz / 4) {
+        why = "PML widths out of range"; return 0;
+    }
+    if (p->precision != SPARC_FP64 && p->precision != SPARC_FP32) { why = "bad precision"; return 0; }
+    if (p->nsrc < 1 || p->nsrc > 4096) { why = "nsrc out of range"; return 0; }
+    if (!(p->timestep > 0) || !(p->xlength > 0) || !(p->ylength > 0) || !(p->cadforcing > 0) || !(p->outputcad > 0)) {
+        why = "lengths and times must be positive"; return 0;
+    }
+    if (p->src_k < 0 || p->src_k > p->nz) { why = "src_k out of range"; return 0; }
+    return 1;
+}
+
+int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
+    if (!out) return SPARC_EINVAL;
+    *out = nullptr;
+    if (!p) return SPARC_EINVAL;
+    std::string why;
+    if (!validate(p, why)) return SPARC_EINVAL;
+    sparc_ctx* c = new sparc_ctx();
+    c->P = *p;
+    c->H = p->nx / 2 + 1;
+    c->M = p->ny * c->H;
+    c->nz = p->nz;
+    c->S = p->nsrc;
+    c->nzpml = p->npmlbot + p->npmltop;
+    c->fs = (long long)c->nz * c->M;
+    c->ps = (long long)std::max(c->nzpml, 1) * c->M;
+    c->NP = (long long)p->nx * p->ny;
+    c->N = c->NP * c->nz;
+    c->f32 = (p->precision == SPARC_FP32);
+    int rc = SPARC_OK;
+    auto bail = [&](int code) { sparc_gpu_destroy(c); return code; };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return SPARC_ECUDA;
+    }
+    size_t cs = csz(c), es = esz(c);
+    long long S = c->S;
+    if ((rc = dalloc(c, &c->a, (size_t)S * 6 * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->scr, (size_t)S * 6 * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->pml, (size_t)S * 2 * c->ps * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->scrpml, (size_t)S * 2 * c->ps * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->ybuf, (size_t)S * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->pbuf, (size_t)S * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->rbuf, (size_t)S * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->zt, (size_t)ZT_COUNT * c->nz * es))) return bail(rc);
+    if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
+    if (c->f32) {
+        if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
+        if ((rc = dalloc(c, (void**)&c->pt64, (size_t)PT_COUNT * c->M * 8))) return bail(rc);
+    } else {
+        c->zt64 = (double*)c->zt;
+        c->pt64 = (double*)c->pt;
+    }
+    if ((rc = dalloc(c, (void**)&c->tw_x, (size_t)p->nx * 8))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->tw_y, (size_t)std::max(p->ny, 2) * 8))) return bail(rc);
+    if ((rc = dalloc(c, &c->tmp, (size_t)c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->phys, (size_t)c->N * es))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->phys64, (size_t)c->N * 8))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->d_flag, 16))) return bail(rc);
+    // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
+    for (int dir = 0; dir < 2; ++dir) {
+        int n = dir == 0 ? p->nx : p->ny;
+        if (n < 2) continue;
+        std::vector<double> tw(n);
+        for (int q = 0; q < n / 2; ++q) {
+            double ang = 2.0 * M_PI * (double)q / (double)n;
+            tw[2 * q] = std::cos(ang);
+            tw[2 * q + 1] = std::sin(ang);
+        }
+        if ((rc = upload(c, dir == 0 ? c->tw_x : c->tw_y, tw.data(), n * 8))) return bail(rc);
+    }
+    c->src_set.assign(c->S, 0);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(SPARC_ECUDA);
+    *out = c;
+    return SPARC_OK;
+}
+
+void sparc_gpu_destroy(sparc_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    cudaGetLastError();
+    delete c;
+}
+
+void* sparc_gpu_stream(sparc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+long long sparc_gpu_launch_count(const sparc_ctx* c) { return c ? c->launches : 0; }
+long long sparc_gpu_device_bytes(const sparc_ctx* c) { return c ? c->dev_bytes : 0; }
+
+// ---------------------------------------------------------------------------
+// set-up: solar_data, stretch, mp_Initialize_RHS(_2d), INIT_DAMPING(_2D), INITIALIZE_STEP
+// ---------------------------------------------------------------------------
+int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin, const double* rhoin,
+                             const double* pin, const double* gin, const double* gamin) {
+    if (!c) return SPARC_EINVAL;
+    if (!zin || !cin || !rhoin || !pin || !gin || !gamin) return fail(c, SPARC_EINVAL, "null background array");
+    const sparc_params& P = c->P;
+    const int nz = c->nz, nx = P.nx, ny = P.ny;
+    const bool two_d = (P.option == 17);
+    for (int k = 0; k < nz; ++k) {
+        if (!std::isfinite(zin[k]) || !(cin[k] > 0) || !(rhoin[k] > 0) || !std::isfinite(pin[k]) || !std::isfinite(gin[k]))
+            return fail(c, SPARC_EINVAL, "background row " + std::to_string(k + 1) + " is not finite/positive");
+        if (k > 0 && !(zin[k] > zin[k - 1])) return fail(c, SPARC_EINVAL, "z must increase with row index");
+    }
+    c->pi = R4(3.14159265358979);            // initialize.f90:38 (REAL*4 literal)
+    c->rsun = R4(69598946770.0);
+    c->normx = 1.0 / (double)nx;
+    c->normy = 1.0 / (double)ny;
+    c->dimc = R4(1.0e6);                       // initialize.f90:751
+    c->dimrho = (double)1.0e-3f;               // initialize.f90:755
+    c->diml = c->rsun;
+    c->stretchx = c->rsun / R4(P.xlength);     // initialize.f90:223-224
+    c->stretchy = c->rsun / R4(P.ylength);
+    std::vector<double> z(zin, zin + nz), c2(nz), rho0(nz), p0(nz), g(nz), graw(nz);
+    for (int k = 0; k < nz; ++k) {             // initialize.f90:759-769
+        c2[k] = (cin[k] / c->dimc) * (cin[k] / c->dimc);
+        rho0[k] = rhoin[k] / c->dimrho;
+        p0[k] = pin[k] / (c->dimrho * (c->dimc * c->dimc));
+        g[k] = gin[k] * c->diml / (c->dimc * c->dimc);
+        graw[k] = g[k];
+    }
+    compact_coeffs(nz, c->cc64);
+    Tri tri[4] = {tri_for(nz, 0), tri_for(nz, 1), tri_for(nz, 2), tri_for(nz, 3)};
+    std::vector<double> unstretch, stretch(nz);
+    host_dbyd2(z, unstretch, 1, c->cc64, tri[1]);          // initialize.f90:464
+    for (int k = 0; k < nz; ++k) stretch[k] = 1.0 / unstretch[k];
+    c->deltat = P.timestep * c->dimc / c->diml;               // initialize.f90:472
+    // READ_PARAMETERS (initialize.f90:978-981), driver.f90:269-281
+    double ts = R4(P.timestep), cad = R4(P.cadforcing);
+    c->cadforcing_step = (int)std::floor(cad / ts);
+    c->maxtime = (int)std::floor((R4(P.solartime) * 3600.0 + 2.0 / R4(P.nupeak)) / ts) + 2;
+    c->maxtime = c->cadforcing_step * (c->maxtime / c->cadforcing_step);
+    c->forcing_length = c->maxtime / c->cadforcing_step + 1;
+    c->steps = (int)std::floor(R4(P.outputcad) / ts);
+    c->freq_filtering = (int)std::floor(60.0 / ts);
+    c->num_steps = (int)std::floor((double)c->maxtime * ts / cad) + 2;
+    c->num_steps = 2 * (c->num_steps / 2) + 2;
+    if (c->steps < 1 || c->freq_filtering < 1 || c->cadforcing_step < 1)
+        return fail(c, SPARC_EINVAL, "timestep too large for the output/forcing cadences");
+    // e_rad / o_rad (physics.f90:44-63; physics2d.f90:34-54)
+    {
+        double temp2 = 1.0 + R4(P.excitdep) / c->rsun, temp = 1.0;
+        for (int k = 0; k < nz; ++k)
+            if (std::fabs(z[k] - temp2) <= temp) { temp = std::fabs(z[k] - temp2); c->e_rad = k + 1; }
+        double temp_r = 1.0 + R4(P.obsheight) / c->rsun;
+        temp = 1.0;
+        for (int k = 0; k < nz; ++k)
+            if (std::fabs(z[k] - temp_r) <= temp) { temp = std::fabs(z[k] - temp_r); c->o_rad = k + 1; }
+        if (two_d) { c->e_rad = nz - 5; c->o_rad = nz - 1; }
+    }
+    int ksrc = P.src_k > 0 ? P.src_k : (P.compute_adjoint ? c->o_rad : c->e_rad);
+    if (ksrc < 2 || ksrc > nz - 1) return fail(c, SPARC_EINVAL, "source plane must lie strictly inside the box");
+    if (P.compute_adjoint) c->delta_width = 2.0 / (z[c->o_rad] - z[c->o_rad - 2]);
+    if (P.compute_forward) c->delta_width = 2.0 / (z[c->e_rad] - z[c->e_rad - 2]);
+    if (P.src_k > 0) c->delta_width = 2.0 / (z[ksrc] - z[ksrc - 2]);
+    // background gradients (physics.f90:204-208)
+    std::vector<double> rhoinv(nz), c2rho0(nz), gradrho0, gradp0;
+    for (int k = 0; k < nz; ++k) { rhoinv[k] = 1.0 / rho0[k]; c2rho0[k] = c2[k] * rho0[k]; }
+    host_dbyd2(rho0, gradrho0, 1, c->cc64, tri[1]);
+    host_dbyd2(p0, gradp0, 1, c->cc64, tri[1]);
+    for (int k = 0; k < nz; ++k) { gradrho0[k] *= stretch[k]; gradp0[k] *= stretch[k]; }
+    // PML profiles (physics.f90:255-303; physics2d.f90:293-342)
+    std::vector<double> az(nz), bz(nz);
+    {
+        int nb = P.npmlbot, nt = P.npmltop;
+        double fac_bot = two_d ? 3.0 * 3.0 : 2.0 * 3.0 * 3.0;
+        for (int k = 1; k <= nz; ++k) {
+            double alphaz = c->pi * R4(0.005) * c->diml / c->dimc, dampz = 0.0;
+            if (k < nb + 1) {
+                alphaz = c->pi * R4(0.005) * c->diml / c->dimc * (z[k - 1] - z[0]) / (z[nb - 1] - z[0]);
+                double tempin = std::sqrt(c2[0]);
+                double r = (z[nb - 1] - z[k - 1]) / (z[nb - 1] - z[0]);
+                dampz = fac_bot * tempin / (z[nb - 1] - z[0]) * (r * r);
+                double fdec = alphaz / (dampz + alphaz);
+                gradp0[k - 1] *= fdec;
+                gradrho0[k - 1] *= fdec;
+                g[k - 1] *= fdec;
+            }
+            if (k > nz - nt) {
+                alphaz = c->pi * R4(0.005) * c->diml / c->dimc * (z[nz - 1] - z[k - 1]) / (z[nz - 1] - z[nz - nt]);
+                double tempin = std::sqrt(c2[two_d ? nz - 6 : nz - 1]);
+                double r = (z[nz - nt] - z[k - 1]) / (z[nz - 1] - z[nz - nt]);
+                dampz = 3.0 * 3.0 * tempin / (z[nz - 1] - z[nz - nt]) * (r * r);
+                double fdec = alphaz / (dampz + alphaz);
+                gradp0[k - 1] *= fdec;
+                gradrho0[k - 1] *= fdec;
+                g[k - 1] *= fdec;
+            }
+            bz[k - 1] = -alphaz - dampz;
+            az[k - 1] = -dampz;
+        }
+    }
+    // LDDRK coefficients (step.f90:28-40), REAL*4 optimals
+    {
+        double opt3 = R4(0.1665579725791151184), opt4 = R4(0.03950410250586729987), opt5 = R4(0.007810706393337838236);
+        double b5 = 0.5, b4 = opt3 / b5, b3 = opt4 / (b5 * b4), b2 = opt5 / (b5 * b4 * b3);
+        c->betas[0] = 0.0;
+        c->betas[1] = b2 * c->deltat;
+        c->betas[2] = b3 * c->deltat;
+        c->betas[3] = b4 * c->deltat;
+        c->betas[4] = b5 * c->deltat;
+    }
+    // z table
+    c->zt_host.assign((size_t)ZT_COUNT * nz, 0.0);
+    auto ZR = [&](int row) { return &c->zt_host[(size_t)row * nz]; };
+    for (int k = 0; k < nz; ++k) {
+        ZR(ZT_STRETCH)[k] = stretch[k];
+        ZR(ZT_UNSTRETCH)[k] = unstretch[k];
+        ZR(ZT_C2RHO0)[k] = c2rho0[k];
+        ZR(ZT_GRADP0)[k] = gradp0[k];
+        ZR(ZT_RHO0)[k] = rho0[k];
+        ZR(ZT_GRADRHO0)[k] = gradrho0[k];
+        ZR(ZT_RHOINV)[k] = rhoinv[k];
+        ZR(ZT_G)[k] = g[k];
+        ZR(ZT_AZ)[k] = az[k];
+        ZR(ZT_BZ)[k] = bz[k];
+        ZR(ZT_C2)[k] = c2[k];
+        ZR(ZT_GRAW)[k] = graw[k];
+        for (int b = 0; b < 4; ++b) {
+            ZR(ZT_TH + 3 * b)[k] = tri[b].low[k];
+            ZR(ZT_TH + 3 * b + 1)[k] = 1.0 / tri[b].betad[k];
+            ZR(ZT_TH + 3 * b + 2)[k] = tri[b].gam[k];
+        }
+    }
+    // pencil table: derivative multipliers, damping rates, horizontal filter
+    c->pt_host.assign((size_t)PT_COUNT * c->M, 0.0);
+    {
+        const int H = c->H;
+        double constx = 2.0 * c->pi / R4(P.xlength) * c->rsun;    // damping.f90:21-22
+        double consty = 2.0 * c->pi / R4(P.ylength) * c->rsun;
+        double expo = (double)2.2f, six = (double)1.0e-6f;
+        for (int iky = 0; iky < ny; ++iky) {
+            int kys = (iky <= ny / 2) ? iky : iky - ny;             // signed y wavenumber
+            int kya = std::abs(kys);
+            for (int ikx = 0; ikx < H; ++ikx) {
+                size_t m = (size_t)iky * H + ikx;
+                // eyekx (initialize.f90:204-210) on the normalised spectrum; the
+                // c2r of the reference drops the Nyquist mode of the derivative
+                double kxm = (ikx == nx / 2) ? 0.0 : (double)ikx * c->normx * 2.0 * c->pi * (double)nx * c->stretchx;
+                double kym = 0.0;
+                if (ny > 1 && iky != ny / 2) kym = (double)kys * c->normy * 2.0 * c->pi * (double)ny * c->stretchy;
+                double jj = two_d ? 0.0 : (double)kya;
+                double ii = (double)ikx;
+                double kay = std::sqrt(constx * constx * (ii * ii) + consty * consty * (jj * jj));
+                double gam = c->diml / c->dimc * six * 150.0 * std::pow(kay / 902.0, expo);   // damping.f90:38
+                float fx = 1.0f / (1.0f + std::exp(((float)(ikx + 1) - (float)nx / 3.0f) * 1.0f));
+                double hf = (double)fx;
+                if (!two_d) {
+                    float fy = 1.0f / (1.0f + std::exp(((float)(kya + 1) - (float)ny / 3.0f) * 1.0f));
+                    hf = hf * (double)fy;
+                }
+                c->pt_host[PT_KX * (size_t)c->M + m] = kxm;
+                c->pt_host[PT_KY * (size_t)c->M + m] = kym;
+                c->pt_host[PT_DAMP * (size_t)c->M + m] = P.damp_waves && !two_d ? gam : 0.0;
+                c->pt_host[PT_HF * (size_t)c->M + m] = hf;
+            }
+        }
+    }
+    int rc;
+    if (c->f32) {
+        std::vector<float> zf(c->zt_host.begin(), c->zt_host.end()), pf(c->pt_host.begin(), c->pt_host.end());
+        if ((rc = upload(c, c->zt, zf.data(), zf.size() * 4))) return rc;
+        if ((rc = upload(c, c->pt, pf.data(), pf.size() * 4))) return rc;
+        if ((rc = upload(c, c->zt64, c->zt_host.data(), c->zt_host.size() * 8))) return rc;
+        if ((rc = upload(c, c->pt64, c->pt_host.data(), c->pt_host.size() * 8))) return rc;
+        CK(cudaStreamSynchronize(c->stream));
+    } else {
+        if ((rc = upload(c, c->zt, c->zt_host.data(), c->zt_host.size() * 8))) return rc;
+        if ((rc = upload(c, c->pt, c->pt_host.data(), c->pt_host.size() * 8))) return rc;
+    }
+    size_t cs = csz(c);
+    CK(cudaMemsetAsync(c->a, 0, (size_t)c->S * 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(c->scr, 0, (size_t)c->S * 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(c->pml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
+    CK(cudaMemsetAsync(c->scrpml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->time = 0;
+    c->rec_n = 0;
+    c->have_bg = true;
+    return SPARC_OK;
+}
+
+// diagnostic view of the set-up (tests): out[0..] = e_rad, o_rad, delta_width, deltat,
+// steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps, betas[5]
+int sparc_gpu_info(sparc_ctx* c, double* out, double* ztab, double* ptab) {
+    if (!c || !c->have_bg) return c ? fail(c, SPARC_ESTATE, "no background") : SPARC_EINVAL;
+    if (out) {
+        int n = 0;
+        out[n++] = c->e_rad; out[n++] = c->o_rad; out[n++] = c->delta_width; out[n++] = c->deltat;
+        out[n++] = c->steps; out[n++] = c->freq_filtering; out[n++] = c->maxtime; out[n++] = c->forcing_length;
+        out[n++] = c->cadforcing_step; out[n++] = c->num_steps;
+        for (int i = 0; i < 5; ++i) out[n++] = c->betas[i];
+    }
+    if (ztab) std::copy(c->zt_host.begin(), c->zt_host.end(), ztab);
+    if (ptab) std::copy(c->pt_host.begin(), c->pt_host.end(), ptab);
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// physical <-> spectral helpers
+// ---------------------------------------------------------------------------
+static int to_spec(sparc_ctx* c, const double* host_field, void* spec_dst, int nplanes) {
+    long long n = (long long)c->NP * nplanes;
+    CK(cudaMemcpyAsync(c->phys64, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
+    if (c->f32) {
+        launch_copy_convert<float>((float*)c->phys, c->phys64, n, c->stream);
+        fft_phys_to_spec<float>((const float*)c->phys, CP<float>(spec_dst), CP<float>(c->tmp), c->P.nx, c->P.ny, nplanes,
+                                c->tw_x, c->tw_y, c->stream);
+        c->launches += 3;
+    } else {
+        fft_phys_to_spec<double>(c->phys64, CP<double>(spec_dst), CP<double>(c->tmp), c->P.nx, c->P.ny, nplanes,
+                                 c->tw_x, c->tw_y, c->stream);
+        c->launches += 2;
+    }
+    CKL();
+    return SPARC_OK;
+}
+
+// spectral (device, T) -> physical FP64 on device (c->phys64)
+static int from_spec_dev(sparc_ctx* c, const void* spec_src, int nplanes) {
+    long long n = (long long)c->NP * nplanes;
+    if (c->f32) {
+        fft_spec_to_phys<float>(CP<float>((void*)spec_src), (float*)c->phys, CP<float>(c->tmp), c->P.nx, c->P.ny,
+                                nplanes, c->tw_x, c->tw_y, c->stream);
+        launch_copy_back<float>(c->phys64, (const float*)c->phys, n, c->stream);
+        c->launches += 3;
+    } else {
+        fft_spec_to_phys<double>(CP<double>((void*)spec_src), c->phys64, CP<double>(c->tmp), c->P.nx, c->P.ny, nplanes,
+                                 c->tw_x, c->tw_y, c->stream);
+        c->launches += 2;
+    }
+    CKL();
+    return SPARC_OK;
+}
+
+static int from_spec(sparc_ctx* c, const void* spec_src, double* host_field, int nplanes) {
+    int rc = from_spec_dev(c, spec_src, nplanes);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host_field, c->phys64, (size_t)c->NP * nplanes * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+static char* field_ptr(sparc_ctx* c, void* base, int src, int field, long long fstride_elems) {
+    return (char*)base + ((long long)src * 6 + field) * fstride_elems * csz(c);
+}
+
+int sparc_gpu_set_state(sparc_ctx* c, int src, const double* a, const double* pml) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (src < 0 || src >= c->S || !a) return fail(c, SPARC_EINVAL, "bad slot or null state");
+    for (int f = 0; f < 6; ++f) {
+        int rc = to_spec(c, a + (long long)f * c->N, field_ptr(c, c->a, src, f, c->fs), c->nz);
+        if (rc) return rc;
+    }
+    char* pbase = (char*)c->pml + (long long)src * 2 * c->ps * csz(c);
+    if (pml && c->nzpml > 0) {
+        for (int f = 0; f < 2; ++f) {
+            int rc = to_spec(c, pml + (long long)f * c->NP * c->nzpml, pbase + f * c->ps * csz(c), c->nzpml);
+            if (rc) return rc;
+        }
+    } else {
+        CK(cudaMemsetAsync(pbase, 0, 2 * c->ps * csz(c), c->stream));
+    }
+    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * csz(c), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+int sparc_gpu_get_state(sparc_ctx* c, int src, double* a, double* pml) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (src < 0 || src >= c->S || !a) return fail(c, SPARC_EINVAL, "bad slot or null buffer");
+    for (int f = 0; f < 6; ++f) {
+        int rc = from_spec(c, field_ptr(c, c->a, src, f, c->fs), a + (long long)f * c->N, c->nz);
+        if (rc) return rc;
+    }
+    if (pml && c->nzpml > 0) {
+        char* pbase = (char*)c->pml + (long long)src * 2 * c->ps * csz(c);
+        for (int f = 0; f < 2; ++f) {
+            int rc = from_spec(c, pbase + f * c->ps * csz(c), pml + (long long)f * c->NP * c->nzpml, c->nzpml);
+            if (rc) return rc;
+        }
+    }
+    return SPARC_OK;
+}
+
+int sparc_gpu_get_field(sparc_ctx* c, int src, int field, int k, double* host) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (src < 0 || src >= c->S || field < 0 || field > 11 || k < 0 || k > c->nz || !host)
+        return fail(c, SPARC_EINVAL, "bad slot, field, plane or buffer");
+    void* base = field < 6 ? c->a : c->scr;
+    char* fp = field_ptr(c, base, src, field % 6, c->fs);
+    if (k > 0) return from_spec(c, fp + (long long)(k - 1) * c->M * csz(c), host, 1);
+    return from_spec(c, fp, host, c->nz);
+}
+
+// ---------------------------------------------------------------------------
+// sources
+// ---------------------------------------------------------------------------
+int sparc_gpu_set_source(sparc_ctx* c, int src, int mode, const double* planes, int L, const double* series,
+                         int nseries) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad source slot");
+    if (mode == SPARC_SRC_NONE) {
+        c->src_set[src] = 0;
+        bool any = false;
+        for (int s : c->src_set) any = any || s;
+        if (!any) c->src_mode = 0;
+        return SPARC_OK;
+    }
+    if (mode != SPARC_SRC_SERIES && mode != SPARC_SRC_LAGRANGE) return fail(c, SPARC_EINVAL, "bad source mode");
+    if (!planes || L < 1) return fail(c, SPARC_EINVAL, "source needs at least one plane");
+    if (mode == SPARC_SRC_SERIES && (!series || nseries < 1)) return fail(c, SPARC_EINVAL, "series source needs a series");
+    if (mode == SPARC_SRC_SERIES) L = 1;
+    if (c->src_mode != 0 && c->src_mode != mode) return fail(c, SPARC_EINVAL, "all slots of a context share one source mode");
+    if (c->planes && L > c->src_L) return fail(c, SPARC_EINVAL, "plane count exceeds the first allocation");
+    size_t cs = csz(c);
+    int rc;
+    if (!c->planes) {
+        if ((rc = dalloc(c, &c->planes, (size_t)c->S * L * c->M * cs))) return rc;
+        c->src_L = L;
+    }
+    if (mode == SPARC_SRC_SERIES) {
+        if (!c->series) {
+            if ((rc = dalloc(c, (void**)&c->series, (size_t)c->S * nseries * 8))) return rc;
+            c->nseries = nseries;
+        }
+        if (nseries > c->nseries) return fail(c, SPARC_EINVAL, "series longer than the first allocation");
+        std::vector<double> ser(c->nseries, 0.0);
+        std::copy(series, series + nseries, ser.begin());
+        if ((rc = upload(c, c->series + (long long)src * c->nseries, ser.data(), c->nseries * 8))) return rc;
+    }
+    char* dst = (char*)c->planes + (long long)src * c->src_L * c->M * cs;
+    CK(cudaMemsetAsync(dst, 0, (size_t)c->src_L * c->M * cs, c->stream));
+    // planes are normalised spectra of the physical planes (ny,nx)
+    for (int l0 = 0; l0 < L; l0 += c->nz) {
+        int nl = std::min(c->nz, L - l0);
+        if ((rc = to_spec(c, planes + (long long)l0 * c->NP, dst + (long long)l0 * c->M * cs, nl))) return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->src_mode = mode;
+    c->src_set[src] = 1;
+    return SPARC_OK;
+}
+
+// LAGRANGE_INTERP weights (physics.f90:683-734) at the current time
+static void lagrange_weights(sparc_ctx* c, int& nw, int* widx, double* wts) {
+    double ts = R4(c->P.timestep), cad = R4(c->P.cadforcing);
+    double xt = (double)c->time * ts / cad;
+    int time1 = (int)std::floor(xt) + 1;
+    xt = c->time * ts;
+    double X[7];
+    for (int l = 0; l < 7; ++l) X[l] = (double)(time1 - 4 + l) * cad;
+    bool cond[7] = {X[0] >= 0, X[1] >= 0, X[2] >= 0, X[3] >= 0, true, time1 < c->num_steps, time1 < c->num_steps - 1};
+    nw = 0;
+    for (int l = 0; l < 7; ++l) {
+        if (!cond[l]) continue;
+        int idx = time1 - 4 + l;            // vr(:,:,time1-3+l), 0-based
+        if (idx < 0 || idx >= c->src_L) continue;
+        double den = 1.0, num = 1.0;
+        for (int r = 0; r < 7; ++r)
+            if (r != l) { den *= (X[l] - X[r]); num *= (xt - X[r]); }
+        widx[nw] = idx;
+        wts[nw] = num / den;
+        nw++;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// time stepping
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+template <typename T>
+static int do_steps(sparc_ctx* c, int nsteps) {
+    typedef typename CplxOf<T>::type CT;
+    const sparc_params& P = c->P;
+    StageArgs<T> A;
+    memset(&A, 0, sizeof(A));
+    A.a = CP<T>(c->a); A.scr = CP<T>(c->scr); A.pml = CP<T>(c->pml); A.scrpml = CP<T>(c->scrpml);
+    A.ybuf = CP<T>(c->ybuf); A.pbuf = CP<T>(c->pbuf); A.rbuf = CP<T>(c->rbuf);
+    A.zt = (const T*)c->zt; A.pt = (const T*)c->pt;
+    A.fs = c->fs; A.ps = c->ps; A.M = c->M; A.nz = c->nz;
+    A.npmlbot = P.npmlbot; A.npmltop = P.npmltop; A.option = P.option; A.damp = P.damp_waves && P.option == 4;
+    A.cc.C1 = (T)c->cc64.C1; A.cc.C2 = (T)c->cc64.C2;
+    for (int i = 0; i < 5; ++i) A.cc.Cb[i] = (T)c->cc64.Cb[i];
+    for (int i = 0; i < 4; ++i) A.cc.Cf[i] = (T)c->cc64.Cf[i];
+    A.cc.alpha2 = (T)c->cc64.alpha2; A.cc.beta1 = (T)c->cc64.beta1; A.cc.cnst = (T)c->cc64.cnst;
+    int ksrc = P.src_k > 0 ? P.src_k : (P.compute_adjoint ? c->o_rad : c->e_rad);
+    A.ksrc = ksrc - 1;
+    A.src_scale = (T)(c->delta_width / c->zt_host[ZT_RHO0 * c->nz + ksrc - 1]);
+    A.planes = CP<T>(c->planes); A.plane_ss = (long long)c->src_L * c->M; A.L = c->src_L;
+    A.mode = c->src_mode; A.series = c->series; A.nseries = c->nseries;
+    UpdateArgs<T> U;
+    U.a = A.a; U.scr = A.scr; U.pml = A.pml; U.scrpml = A.scrpml; U.pt = A.pt;
+    U.fs = c->fs; U.ps = c->ps; U.M = c->M; U.nz = c->nz; U.nzpml = c->nzpml; U.option = P.option;
+    U.dt = (T)c->deltat;
+    const bool two_d = P.option == 17;
+    for (int it = 0; it < nsteps; ++it) {
+        const int time = c->time;
+        // forcing of this step (driver.f90:419-422; physics2d.f90:1059)
+        A.time = time;
+        A.src_on = 0;
+        if (c->src_mode != 0) {
+            bool gate = !two_d || time <= c->forcing_length * c->cadforcing_step;
+            A.src_on = gate ? 1 : 0;
+            if (c->src_mode == SPARC_SRC_LAGRANGE) {
+                if (time <= c->forcing_length * c->cadforcing_step) {
+                    lagrange_weights(c, c->last_nw, c->last_widx, c->last_wts);
+                }   // else: forcing keeps its last value (driver.f90:421-422)
+                A.nw = c->last_nw;
+                for (int l = 0; l < A.nw; ++l) { A.widx[l] = c->last_widx[l]; A.wts[l] = (T)c->last_wts[l]; }
+            }
+        }
+        for (int rk = 0; rk < 5; ++rk) {
+            A.beta = (T)c->betas[rk];
+            A.has_scr = (rk > 0);
+            launch_stage<T>(A, c->S, c->stream);
+        }
+        U.hfilter = two_d ? ((time + 1) % c->freq_filtering == 0) : (time % c->freq_filtering == 0);
+        launch_update<T>(U, c->S, c->stream);
+        c->launches += 6;
+        CKL();
+        if (c->rec_on && time % c->steps == 0 && c->rec_n < c->rec_max) {
+            size_t cs = sizeof(CT);
+            CK(cudaMemcpy2DAsync((char*)c->rec + (size_t)c->rec_n * c->M * cs, (size_t)c->rec_max * c->M * cs,
+                                 (const char*)c->a + ((size_t)5 * c->fs + (size_t)(c->o_rad - 1) * c->M) * cs,
+                                 (size_t)6 * c->fs * cs, (size_t)c->M * cs, (size_t)c->S, cudaMemcpyDeviceToDevice,
+                                 c->stream));
+            c->rec_n++;
+        }
+        c->time++;
+    }
+    return SPARC_OK;
+}
+
+extern "C" {
+
+int sparc_gpu_step(sparc_ctx* c, int nsteps) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (nsteps < 0) return fail(c, SPARC_EINVAL, "nsteps < 0");
+    return c->f32 ? do_steps<float>(c, nsteps) : do_steps<double>(c, nsteps);
+}
+
+int sparc_gpu_get_time(const sparc_ctx* c, int* t) {
+    if (!c || !t) return SPARC_EINVAL;
+    *t = c->time;
+    return SPARC_OK;
+}
+int sparc_gpu_set_time(sparc_ctx* c, int t) {
+    if (!c || t < 0) return SPARC_EINVAL;
+    c->time = t;
+    return SPARC_OK;
+}
+
+int sparc_gpu_sync(sparc_ctx* c, int check_finite) {
+    if (!c) return SPARC_EINVAL;
+    CK(cudaStreamSynchronize(c->stream));
+    if (check_finite && c->have_bg) {
+        CK(cudaMemsetAsync(c->d_flag, 0, 4, c->stream));
+        long long n = (long long)c->S * 6 * c->fs * 2;
+        if (c->f32) launch_check_finite_f32((const float*)c->a, n, c->d_flag, c->stream);
+        else launch_check_finite_f64((const double*)c->a, n, c->d_flag, c->stream);
+        c->launches++;
+        int flag = 0;
+        CK(cudaMemcpyAsync(&flag, c->d_flag, 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (flag) return fail(c, SPARC_ENAN, "non-finite value in the state");
+    }
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// surface records
+// ---------------------------------------------------------------------------
+int sparc_gpu_record_surface(sparc_ctx* c, int enable, int max_records) {
+    if (!c) return SPARC_EINVAL;
+    if (!enable) { c->rec_on = 0; return SPARC_OK; }
+    if (max_records < 1) return fail(c, SPARC_EINVAL, "max_records < 1");
+    if (!c->rec || max_records > c->rec_max) {
+        if (c->rec) return fail(c, SPARC_EINVAL, "record buffer already allocated smaller");
+        int rc = dalloc(c, &c->rec, (size_t)c->S * max_records * c->M * csz(c));
+        if (rc) return rc;
+        c->rec_max = max_records;
+    }
+    c->rec_on = 1;
+    c->rec_n = 0;
+    return SPARC_OK;
+}
+
+int sparc_gpu_get_records(sparc_ctx* c, int src, double* host, int* nrec) {
+    if (!c || !nrec) return SPARC_EINVAL;
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
+    *nrec = c->rec_n;
+    if (!host || c->rec_n == 0) return SPARC_OK;
+    const char* base = (const char*)c->rec + (size_t)src * c->rec_max * c->M * csz(c);
+    for (int r0 = 0; r0 < c->rec_n; r0 += c->nz) {
+        int n = std::min(c->nz, c->rec_n - r0);
+        int rc = from_spec(c, base + (size_t)r0 * c->M * csz(c), host + (size_t)r0 * c->NP, n);
+        if (rc) return rc;
+    }
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// primitives (FP64, via the same transforms and tables)
+// ---------------------------------------------------------------------------
+static int ensure_spec64(sparc_ctx* c) {
+    if (c->spec64) return SPARC_OK;
+    int rc;
+    if ((rc = dalloc(c, (void**)&c->spec64, (size_t)c->fs * 16))) return rc;
+    if ((rc = dalloc(c, (void**)&c->spec64b, (size_t)c->fs * 16))) return rc;
+    if ((rc = dalloc(c, (void**)&c->tmp64, (size_t)c->fs * 16))) return rc;
+    return SPARC_OK;
+}
+
+static int prim_spectral(sparc_ctx* c, const double* var, double* dvar, int which, int subtract) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (!var || !dvar) return fail(c, SPARC_EINVAL, "null field");
+    if (which == 1 && c->P.ny == 1) return fail(c, SPARC_EINVAL, "ddy needs ny > 1");
+    int rc = ensure_spec64(c);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->phys64, var, c->N * 8, cudaMemcpyHostToDevice, c->stream));
+    fft_phys_to_spec<double>(c->phys64, c->spec64, c->tmp64, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
+    launch_spec_dxdy<double>(c->spec64b, c->spec64, c->pt64, which, c->M, c->nz, c->stream);
+    fft_spec_to_phys<double>(c->spec64b, c->phys64, c->tmp64, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
+    c->launches += 5;
+    CKL();
+    if (!subtract) {
+        CK(cudaMemcpyAsync(dvar, c->phys64, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } else {
+        std::vector<double> term(c->N);
+        CK(cudaMemcpyAsync(term.data(), c->phys64, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (long long q = 0; q < c->N; ++q) dvar[q] = dvar[q] - term[q];
+    }
+    return SPARC_OK;
+}
+
+int sparc_gpu_ddx(sparc_ctx* c, const double* var, double* dvar) { return prim_spectral(c, var, dvar, 0, 0); }
+int sparc_gpu_ddy(sparc_ctx* c, const double* var, double* dvar) { return prim_spectral(c, var, dvar, 1, 0); }
+int sparc_gpu_damp(sparc_ctx* c, const double* v, double* rhs) {
+    if (c && c->P.option != 4) return fail(c, SPARC_EINVAL, "damping is a 3-D operation");
+    return prim_spectral(c, v, rhs, 2, 1);
+}
+
+int sparc_gpu_ddz(sparc_ctx* c, const double* var, double* dvar, int bc) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (!var || !dvar || bc < 0 || bc > 3) return fail(c, SPARC_EINVAL, "bad field or bc (0..3)");
+    int rc = ensure_spec64(c);
+    if (rc) return rc;
+    double* din = (double*)c->spec64;     // reuse as two real fields
+    double* dout = c->phys64;
+    CK(cudaMemcpyAsync(din, var, c->N * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dout, dvar, c->N * 8, cudaMemcpyHostToDevice, c->stream));
+    launch_zderiv_real(c->zt64, c->cc64, din, dout, c->NP, c->nz, bc, c->stream);
+    c->launches++;
+    CKL();
+    CK(cudaMemcpyAsync(dvar, dout, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sensitivity kernels
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+template <typename T>
+static int derive_to_phys(sparc_ctx* c, int src, bool adjoint, T* out7) {
+    typedef typename CplxOf<T>::type CT;
+    const long long fs = c->fs, N = c->N;
+    CT* a = CP<T>(c->a) + (long long)src * 6 * fs;
+    CT* scr = CP<T>(c->scr) + (long long)src * 6 * fs;
+    CT* D = CP<T>(c->ybuf);
+    CT* D2 = CP<T>(c->pbuf);
+    CT* D3 = CP<T>(c->rbuf);
+    Compact<T> cc;
+    cc.C1 = (T)c->cc64.C1; cc.C2 = (T)c->cc64.C2;
+    for (int i = 0; i < 5; ++i) cc.Cb[i] = (T)c->cc64.Cb[i];
+    for (int i = 0; i < 4; ++i) cc.Cf[i] = (T)c->cc64.Cf[i];
+    cc.alpha2 = (T)c->cc64.alpha2; cc.beta1 = (T)c->cc64.beta1; cc.cnst = (T)c->cc64.cnst;
+    const T* zt = (const T*)c->zt;
+    const T* pt = (const T*)c->pt;
+    const int nx = c->P.nx, ny = c->P.ny, nz = c->nz, M = c->M;
+    const bool use_y = ny > 4;
+    auto tophys = [&](const CT* spec, T* dst) {
+        fft_spec_to_phys<T>(spec, dst, CP<T>(c->tmp), nx, ny, nz, c->tw_x, c->tw_y, c->stream);
+        c->launches += 2;
+    };
+    // divergence: ddxkern + ddykern + ddzkern(bc=1, filtered)  (COMPUTE_DIV kernels.f90:798-816)
+    const int fx = adjoint ? 3 : 0;
+    launch_zderiv<T>(zt, cc, a + (fx + 2) * fs, D, M, nz, 1, 1, nullptr, c->stream);
+    launch_spec_combine<T>(D, a + fx * fs, use_y ? a + (fx + 1) * fs : nullptr, pt, M, nz, c->stream);
+    c->launches += 2;
+    tophys(D, out7);
+    if (!adjoint) {
+        for (int q = 0; q < 3; ++q) tophys(scr + (3 + q) * fs, out7 + (1 + q) * N);   // f_acc
+        for (int q = 0; q < 3; ++q) tophys(a + q * fs, out7 + (4 + q) * N);           // f_xi
+    } else {
+        for (int q = 0; q < 3; ++q) tophys(a + (3 + q) * fs, out7 + (1 + q) * N);     // a_v
+        // grad(a_vz * grav) (kernels.f90:299-304)
+        launch_spec_scale_z<T>(D2, a + 5 * fs, zt, ZT_GRAW, M, nz, c->stream);
+        launch_spec_dxdy<T>(D3, D2, pt, 0, M, nz, c->stream);
+        c->launches += 2;
+        tophys(D3, out7 + 4 * N);
+        if (use_y) {
+            launch_spec_dxdy<T>(D3, D2, pt, 1, M, nz, c->stream);
+            c->launches++;
+            tophys(D3, out7 + 5 * N);
+        } else {
+            CK(cudaMemsetAsync(out7 + 5 * N, 0, N * sizeof(T), c->stream));
+        }
+        launch_zderiv<T>(zt, cc, D2, D3, M, nz, 1, 1, nullptr, c->stream);
+        c->launches++;
+        tophys(D3, out7 + 6 * N);
+    }
+    CKL();
+    return SPARC_OK;
+}
+
+extern "C" {
+
+int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (!c->store) {
+        if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
+        int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));
+        if (rc) return rc;
+        c->store_n = nsnap;
+    }
+    if (snap < 0 || snap >= c->store_n) return fail(c, SPARC_EINVAL, "snapshot index out of range");
+    for (int s = 0; s < c->S; ++s) {
+        char* dst = (char*)c->store + ((size_t)snap * c->S + s) * 7 * c->N * esz(c);
+        int rc = c->f32 ? derive_to_phys<float>(c, s, false, (float*)dst)
+                        : derive_to_phys<double>(c, s, false, (double*)dst);
+        if (rc) return rc;
+    }
+    return SPARC_OK;
+}
+
+int sparc_gpu_kernel_reset(sparc_ctx* c) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->kacc) {
+        int rc = dalloc(c, (void**)&c->kacc, (size_t)c->S * 3 * c->N * 8);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(c->kacc, 0, (size_t)c->S * 3 * c->N * 8, c->stream));
+    return SPARC_OK;
+}
+
+int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
+    if (!fwd || !c) return SPARC_EINVAL;
+    if (!c->have_bg || !fwd->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (!fwd->store || snap < 0 || snap >= fwd->store_n) return fail(c, SPARC_EINVAL, "no such forward snapshot");
+    if (fwd->S != c->S || fwd->N != c->N || fwd->f32 != c->f32) return fail(c, SPARC_EINVAL, "forward/adjoint contexts differ");
+    if (!c->kacc) { int rc = sparc_gpu_kernel_reset(c); if (rc) return rc; }
+    if (!c->ktemp) { int rc = dalloc(c, &c->ktemp, (size_t)7 * c->N * esz(c)); if (rc) return rc; }
+    // the forward store is written on the forward context's stream
+    CK(cudaStreamSynchronize(fwd->stream));
+    for (int s = 0; s < c->S; ++s) {
+        const char* f7 = (const char*)fwd->store + ((size_t)snap * c->S + s) * 7 * c->N * esz(c);
+        double* acc = c->kacc + (size_t)s * 3 * c->N;
+        int rc;
+        if (c->f32) {
+            rc = derive_to_phys<float>(c, s, true, (float*)c->ktemp);
+            if (rc) return rc;
+            launch_kernel_accum<float>(acc, (const float*)f7, (const float*)c->ktemp, c->zt64, c->NP, c->nz, c->P.ny > 4, c->stream);
+        } else {
+            rc = derive_to_phys<double>(c, s, true, (double*)c->ktemp);
+            if (rc) return rc;
+            launch_kernel_accum<double>(acc, (const double*)f7, (const double*)c->ktemp, c->zt64, c->NP, c->nz, c->P.ny > 4, c->stream);
+        }
+        c->launches++;
+        CKL();
+    }
+    return SPARC_OK;
+}
+
+int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* krho, double* hess) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->kacc) return fail(c, SPARC_ESTATE, "no kernel accumulation yet");
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
+    int stepskern = c->steps;                         // kernels.f90:190
+    double ts = R4(c->P.timestep);
+    double dimen = std::pow(c->diml * (double)1.0e-8f, -3.0);            // kernels.f90:523
+    if (c->P.ny <= 4) dimen = 1.0 / (c->diml * (double)1.0e-8f * R4(c->P.xlength) * (double)1.0e-8f);
+    double sc = stepskern * ts * dimen * 2.0, sr = stepskern * ts * dimen;
+    double* out = nullptr;
+    int rc = dalloc(c, (void**)&out, (size_t)3 * c->N * 8);
+    if (rc) return rc;
+    const double* acc = c->kacc + (sum_slots ? 0 : (size_t)src * 3 * c->N);
+    launch_kernel_finish(out, acc, c->zt64, c->NP, c->nz, sc, sr, sum_slots ? c->S : 1, 3 * c->N, c->stream);
+    c->launches++;
+    CKL();
+    if (kc) CK(cudaMemcpyAsync(kc, out, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (krho) CK(cudaMemcpyAsync(krho, out + c->N, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (hess) CK(cudaMemcpyAsync(hess, out + 2 * c->N, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // release the staging buffer
+    cudaFree(out);
+    c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)out), c->allocs.end());
+    c->dev_bytes -= (long long)3 * c->N * 8;
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// checkpoint / restore: raw spectral state of every slot + time, FNV-1a checksum
+// ---------------------------------------------------------------------------
+static uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h) {
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ULL; }
+    return h;
+}
+
+struct CkHeader {
+    char magic[8];
+    int32_t abi, nx, ny, nz, npmlbot, npmltop, option, precision, nsrc, time;
+    uint64_t payload_bytes, checksum;
+};
+
+int sparc_gpu_checkpoint(sparc_ctx* c, const char* path) {
+    if (!c || !path) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    std::vector<unsigned char> buf(na + np);
+    CK(cudaMemcpyAsync(buf.data(), c->a, na, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(buf.data() + na, c->pml, np, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CkHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, "SPARCGPU", 8);
+    h.abi = SPARC_GPU_ABI_VERSION; h.nx = c->P.nx; h.ny = c->P.ny; h.nz = c->nz;
+    h.npmlbot = c->P.npmlbot; h.npmltop = c->P.npmltop; h.option = c->P.option; h.precision = c->P.precision;
+    h.nsrc = c->S; h.time = c->time;
+    h.payload_bytes = buf.size();
+    h.checksum = fnv1a(buf.data(), buf.size(), 1469598103934665603ULL);
+    std::string tmp = std::string(path) + ".tmp";
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return fail(c, SPARC_EIO, std::string("cannot open ") + tmp);
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1 && fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp.c_str(), path) != 0) return fail(c, SPARC_EIO, "checkpoint write failed");
+    return SPARC_OK;
+}
+
+int sparc_gpu_restore(sparc_ctx* c, const char* path) {
+    if (!c || !path) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(c, SPARC_EIO, std::string("cannot open ") + path);
+    CkHeader h;
+    if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, "SPARCGPU", 8) != 0) {
+        fclose(f);
+        return fail(c, SPARC_EIO, "not a checkpoint file");
+    }
+    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    if (h.abi != SPARC_GPU_ABI_VERSION || h.nx != c->P.nx || h.ny != c->P.ny || h.nz != c->nz ||
+        h.npmlbot != c->P.npmlbot || h.npmltop != c->P.npmltop || h.option != c->P.option ||
+        h.precision != c->P.precision || h.nsrc != c->S || h.payload_bytes != na + np || h.time < 0) {
+        fclose(f);
+        return fail(c, SPARC_EIO, "checkpoint does not match this context");
+    }
+    std::vector<unsigned char> buf(na + np);
+    size_t got = fread(buf.data(), 1, buf.size(), f);
+    fclose(f);
+    if (got != buf.size()) return fail(c, SPARC_EIO, "checkpoint truncated");
+    if (fnv1a(buf.data(), buf.size(), 1469598103934665603ULL) != h.checksum)
+        return fail(c, SPARC_EIO, "checkpoint checksum mismatch");
+    CK(cudaMemcpyAsync(c->a, buf.data(), na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->pml, buf.data() + na, np, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->scr, 0, na, c->stream));
+    CK(cudaMemsetAsync(c->scrpml, 0, np, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->time = h.time;
+    return SPARC_OK;
+}
+
+}  // extern "C"

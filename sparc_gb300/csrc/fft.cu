@@ -1,0 +1,347 @@
+// Horizontal transforms between physical planes a(nx,ny) and the normalised
+// r2c half-spectrum state, written as shared-memory Stockham radix-2 FFTs
+// (the FFTW plans of initialize.f90:323-337 and damping.f90:46-58 are the
+// reference's counterpart; cuFFT is not used).
+//
+//   phys -> spec : rows_r2c   (two real rows packed as one complex FFT along x,
+//                              split by Hermitian symmetry, scaled 1/(nx*ny))
+//                  cols_fft   (complex FFT along y on tiles of kx columns)
+//   spec -> phys : cols_fft (inverse), rows_c2r (two rows per complex inverse
+//                  FFT; DC/Nyquist imaginary parts dropped as FFTW c2r does)
+//
+// Also: point-wise spectral multipliers and the sensitivity-kernel
+// accumulation of kernels.f90:273-311 on physical fields.
+#include "internal.cuh"
+
+// Stockham radix-2 over `count` sequences of length n stored back to back in
+// src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
+// cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
+template <typename T, typename CT>
+__device__ CT* smem_fft(CT* src, CT* dst, int n, int count, T sign, const double* __restrict__ tw) {
+    const int half = n >> 1;
+    const int total = half * count;
+    for (int Ns = 1; Ns < n; Ns <<= 1) {
+        const int stride = n / (2 * Ns);
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int seq = t / half, j = t - seq * half;
+            CT* s = src + seq * n;
+            CT* d = dst + seq * n;
+            const int k = j & (Ns - 1);
+            CT v0 = s[j], v1 = s[j + half];
+            const int q = k * stride;
+            const T c = (T)__ldg(&tw[2 * q]);
+            const T sn = sign * (T)__ldg(&tw[2 * q + 1]);
+            CT w;
+            w.x = v1.x * c - v1.y * sn;
+            w.y = v1.x * sn + v1.y * c;
+            const int idx = ((j - k) << 1) + k;
+            d[idx] = v0 + w;
+            d[idx + Ns] = v0 - w;
+        }
+        __syncthreads();
+        CT* tmp = src; src = dst; dst = tmp;
+    }
+    return src;
+}
+
+// phys (nrows rows of nx reals) -> out (nrows rows of H = nx/2+1 complex), scaled by `scale`
+template <typename T>
+__global__ void rows_r2c_kernel(const T* __restrict__ phys, typename CplxOf<T>::type* __restrict__ out,
+                                int nx, long long nrows, T scale, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* b0 = (CT*)smraw;
+    CT* b1 = b0 + nx;
+    const long long r0 = 2LL * blockIdx.x, r1 = r0 + 1;
+    const bool has1 = r1 < nrows;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        CT v;
+        v.x = phys[r0 * nx + i];
+        v.y = has1 ? phys[r1 * nx + i] : (T)0;
+        b0[i] = v;
+    }
+    __syncthreads();
+    CT* Z = smem_fft<T, CT>(b0, b1, nx, 1, (T)-1, tw);
+    const int H = nx / 2 + 1;
+    const T hs = (T)0.5 * scale;
+    for (int k = threadIdx.x; k < H; k += blockDim.x) {
+        CT zk = Z[k], zn = Z[(nx - k) & (nx - 1)];
+        CT x1, x2;
+        x1.x = (zk.x + zn.x) * hs;
+        x1.y = (zk.y - zn.y) * hs;
+        x2.x = (zk.y + zn.y) * hs;
+        x2.y = -(zk.x - zn.x) * hs;
+        out[r0 * H + k] = x1;
+        if (has1) out[r1 * H + k] = x2;
+    }
+}
+
+// in (nrows rows of H complex) -> phys (nrows rows of nx reals), inverse, unscaled
+template <typename T>
+__global__ void rows_c2r_kernel(const typename CplxOf<T>::type* __restrict__ in, T* __restrict__ phys,
+                                int nx, long long nrows, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* b0 = (CT*)smraw;
+    CT* b1 = b0 + nx;
+    const long long r0 = 2LL * blockIdx.x, r1 = r0 + 1;
+    const bool has1 = r1 < nrows;
+    const int H = nx / 2 + 1, half = nx / 2;
+    for (int k = threadIdx.x; k <= half; k += blockDim.x) {
+        CT x1 = in[r0 * H + k];
+        CT x2 = has1 ? in[r1 * H + k] : czero<CT>();
+        if (k == 0 || k == half) {
+            CT z; z.x = x1.x; z.y = x2.x;
+            b0[k] = z;
+        } else {
+            CT z;
+            z.x = x1.x - x2.y; z.y = x1.y + x2.x;
+            b0[k] = z;
+            z.x = x1.x + x2.y; z.y = -x1.y + x2.x;
+            b0[nx - k] = z;
+        }
+    }
+    __syncthreads();
+    CT* Z = smem_fft<T, CT>(b0, b1, nx, 1, (T)1, tw);
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        CT z = Z[i];
+        phys[r0 * nx + i] = z.x;
+        if (has1) phys[r1 * nx + i] = z.y;
+    }
+}
+
+// complex FFT along y on tiles of W kx-columns: data [plane][y][kx], H columns
+template <typename T>
+__global__ void cols_fft_kernel(const typename CplxOf<T>::type* __restrict__ in,
+                                typename CplxOf<T>::type* __restrict__ out, int ny, int H, int W, T sign,
+                                const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* b0 = (CT*)smraw;
+    CT* b1 = b0 + (long long)W * ny;
+    const int ntile = (H + W - 1) / W;
+    const long long plane = blockIdx.x / ntile;
+    const int kx0 = (blockIdx.x % ntile) * W;
+    const int w = min(W, H - kx0);
+    const long long base = plane * (long long)ny * H;
+    for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
+        int y = t / W, c = t - y * W;
+        b0[c * ny + y] = (c < w) ? in[base + (long long)y * H + kx0 + c] : czero<CT>();
+    }
+    __syncthreads();
+    CT* Z = smem_fft<T, CT>(b0, b1, ny, W, sign, tw);
+    for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
+        int y = t / W, c = t - y * W;
+        if (c < w) out[base + (long long)y * H + kx0 + c] = Z[c * ny + y];
+    }
+}
+
+static int col_tile(int ny) { return ny >= 1024 ? 4 : (ny >= 512 ? 8 : 16); }
+
+template <typename T>
+static void set_smem(const void* fn, size_t bytes) {
+    static size_t done = 0;
+    (void)done;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T>
+void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s) {
+    typedef typename CplxOf<T>::type CT;
+    const int H = nx / 2 + 1;
+    const long long nrows = (long long)ny * nplanes;
+    size_t sm = 2 * (size_t)nx * sizeof(CT);
+    int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
+    set_smem<T>((const void*)rows_r2c_kernel<T>, sm);
+    CT* dst = (ny == 1) ? spec : tmp;
+    rows_r2c_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(phys, dst, nx, nrows,
+                                                                     (T)(1.0 / ((double)nx * ny)), tw_x);
+    if (ny > 1) {
+        int W = col_tile(ny);
+        size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
+        set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
+        int ntile = (H + W - 1) / W;
+        cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(tmp, spec, ny, H, W, (T)-1, tw_y);
+    }
+}
+
+template <typename T>
+void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s) {
+    typedef typename CplxOf<T>::type CT;
+    const int H = nx / 2 + 1;
+    const long long nrows = (long long)ny * nplanes;
+    const CT* src = spec;
+    if (ny > 1) {
+        int W = col_tile(ny);
+        size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
+        set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
+        int ntile = (H + W - 1) / W;
+        cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, ny, H, W, (T)1, tw_y);
+        src = tmp;
+    }
+    size_t sm = 2 * (size_t)nx * sizeof(CT);
+    int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
+    set_smem<T>((const void*)rows_c2r_kernel<T>, sm);
+    rows_c2r_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(src, phys, nx, nrows, tw_x);
+}
+
+// out = out + i kx fx + i ky fy   (fy may be null)
+template <typename T>
+__global__ void spec_combine_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
+                                    const typename CplxOf<T>::type* fy, const T* __restrict__ pt, int M,
+                                    long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int m = (int)(t % M);
+    typename CplxOf<T>::type d = imul(pt[PT_KX * (long long)M + m], fx[t]);
+    if (fy) d = d + imul(pt[PT_KY * (long long)M + m], fy[t]);
+    out[t] = d + out[t];
+}
+
+// out(z) = in(z) * zt[row][z]
+template <typename T>
+__global__ void spec_scale_z_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
+                                    const T* __restrict__ zt, int row, int M, int nz) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)M * nz) return;
+    int z = (int)(t / M);
+    out[t] = in[t] * zt[row * nz + z];
+}
+
+// which: 0 -> i kx * in, 1 -> i ky * in, 2 -> damping rate * in
+template <typename T>
+__global__ void spec_dxdy_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
+                                 const T* __restrict__ pt, int which, int M, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int m = (int)(t % M);
+    if (which == 0) out[t] = imul(pt[PT_KX * (long long)M + m], in[t]);
+    else if (which == 1) out[t] = imul(pt[PT_KY * (long long)M + m], in[t]);
+    else out[t] = pt[PT_DAMP * (long long)M + m] * in[t];
+}
+
+// Sensitivity-kernel accumulation, kernels.f90:276-311.  fwd planes:
+// 0 div(f_xi), 1-3 f_acc (x,y,z), 4-6 f_xi (x,y,z); adj planes: 0 div(a_v),
+// 1-3 a_v, 4-6 grad(g a_vz).  acc: 0 kernelc2, 1 kernelrho, 2 hessian (FP64).
+template <typename T>
+__global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restrict__ fwd, const T* __restrict__ adj,
+                                    const double* __restrict__ zt64, long long NP, int nz, int use_y) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long N = NP * nz;
+    if (t >= N) return;
+    const int z = (int)(t / NP);
+    const double c2 = zt64[ZT_C2 * nz + z], g = zt64[ZT_GRAW * nz + z];
+    const double f1 = fwd[t], fax = fwd[N + t], fay = use_y ? (double)fwd[2 * N + t] : 0.0, faz = fwd[3 * N + t];
+    const double fxx = fwd[4 * N + t], fxy = use_y ? (double)fwd[5 * N + t] : 0.0, fxz = fwd[6 * N + t];
+    const double a1 = adj[t], avx = adj[N + t], avy = use_y ? (double)adj[2 * N + t] : 0.0, avz = adj[3 * N + t];
+    const double d31 = adj[4 * N + t], d32 = use_y ? (double)adj[5 * N + t] : 0.0, d33 = adj[6 * N + t];
+    acc[2 * N + t] = acc[2 * N + t] + faz * faz + fax * fax + fay * fay;
+    const double t1 = f1 * a1;
+    acc[t] = acc[t] + t1;
+    double kr = acc[N + t] + t1 * c2 + faz * avz + fax * avx + fay * avy;
+    kr = kr - g * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
+    acc[N + t] = kr;
+}
+
+// Final scaling kernels.f90:523-539, optionally summed over nsum slots
+__global__ void kernel_finish_kernel(double* __restrict__ out, const double* __restrict__ acc,
+                                     const double* __restrict__ zt64, long long NP, int nz, double scale_c,
+                                     double scale_r, int nsum, long long acc_ss) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long N = NP * nz;
+    if (t >= N) return;
+    const int z = (int)(t / NP);
+    const double r0 = zt64[ZT_RHO0 * nz + z], c2 = zt64[ZT_C2 * nz + z];
+    double kc = 0, kr = 0, h = 0;
+    for (int s = 0; s < nsum; ++s) {
+        const double* A = acc + s * acc_ss;
+        kc += -A[t] * r0 * c2 * scale_c;
+        kr += -r0 * A[N + t] * scale_r;
+        h += A[2 * N + t];
+    }
+    out[t] = kc;
+    out[N + t] = kr;
+    out[2 * N + t] = h;
+}
+
+template <typename T>
+__global__ void copy_convert_kernel(T* dst, const double* src, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (T)src[t];
+}
+template <typename T>
+__global__ void copy_back_kernel(double* dst, const T* src, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (double)src[t];
+}
+
+template <typename T>
+__global__ void finite_kernel(const T* p, long long n, int* flag) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; t < n; t += stride)
+        if (!isfinite(p[t])) { *flag = 1; return; }
+}
+
+static unsigned nblk(long long n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+template <typename T>
+void launch_spec_combine(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
+                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, cudaStream_t s) {
+    long long n = (long long)M * nz;
+    spec_combine_kernel<T><<<nblk(n), 256, 0, s>>>(out, fx, fy, pt, M, n);
+}
+template <typename T>
+void launch_spec_scale_z(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in, const T* zt, int row,
+                         int M, int nz, cudaStream_t s) {
+    spec_scale_z_kernel<T><<<nblk((long long)M * nz), 256, 0, s>>>(out, in, zt, row, M, nz);
+}
+template <typename T>
+void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in, const T* pt, int which,
+                      int M, int nz, cudaStream_t s) {
+    long long n = (long long)M * nz;
+    spec_dxdy_kernel<T><<<nblk(n), 256, 0, s>>>(out, in, pt, which, M, n);
+}
+template <typename T>
+void launch_kernel_accum(double* acc, const T* fwd, const T* adj, const double* zt64, long long NP, int nz, int use_y,
+                         cudaStream_t s) {
+    kernel_accum_kernel<T><<<nblk(NP * nz), 256, 0, s>>>(acc, fwd, adj, zt64, NP, nz, use_y);
+}
+void launch_kernel_finish(double* out, const double* acc, const double* zt64, long long NP, int nz, double scale_c,
+                          double scale_r, int nsum, long long acc_ss, cudaStream_t s) {
+    kernel_finish_kernel<<<nblk(NP * nz), 256, 0, s>>>(out, acc, zt64, NP, nz, scale_c, scale_r, nsum, acc_ss);
+}
+template <typename T> void launch_copy_convert(T* dst, const double* src, long long n, cudaStream_t s) {
+    copy_convert_kernel<T><<<nblk(n), 256, 0, s>>>(dst, src, n);
+}
+template <typename T> void launch_copy_back(double* dst, const T* src, long long n, cudaStream_t s) {
+    copy_back_kernel<T><<<nblk(n), 256, 0, s>>>(dst, src, n);
+}
+int launch_check_finite_f64(const double* p, long long n, int* flag, cudaStream_t s) {
+    finite_kernel<double><<<1024, 256, 0, s>>>(p, n, flag);
+    return 0;
+}
+int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t s) {
+    finite_kernel<float><<<1024, 256, 0, s>>>(p, n, flag);
+    return 0;
+}
+
+#define INST(T)                                                                                                   \
+    template void fft_phys_to_spec<T>(const T*, CplxOf<T>::type*, CplxOf<T>::type*, int, int, int, const double*, \
+                                      const double*, cudaStream_t);                                               \
+    template void fft_spec_to_phys<T>(const CplxOf<T>::type*, T*, CplxOf<T>::type*, int, int, int, const double*, \
+                                      const double*, cudaStream_t);                                               \
+    template void launch_spec_combine<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const CplxOf<T>::type*,       \
+                                         const T*, int, int, cudaStream_t);                                       \
+    template void launch_spec_scale_z<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int,      \
+                                         cudaStream_t);                                                           \
+    template void launch_spec_dxdy<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int,         \
+                                      cudaStream_t);                                                              \
+    template void launch_kernel_accum<T>(double*, const T*, const T*, const double*, long long, int, int,         \
+                                         cudaStream_t);                                                           \
+    template void launch_copy_convert<T>(T*, const double*, long long, cudaStream_t);                             \
+    template void launch_copy_back<T>(double*, const T*, long long, cudaStream_t);
+INST(double)
+INST(float)

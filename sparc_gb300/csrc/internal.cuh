@@ -1,0 +1,204 @@
+// Internal declarations shared by the CUDA translation units of libsparc_gpu.
+//
+// State representation.  For a background that depends on z only (the
+// quiet-Sun cases of the reference), every operator of the time step --
+// spectral x/y derivatives (derivatives.f90:28-170), the compact z derivative
+// (dbyd2.f90), the PML (displacement.f90:495-560), spectral damping
+// (damping.f90:125-161), the z and horizontal filters (physics.f90:741-833)
+// and the point-wise equations -- acts independently on each horizontal
+// Fourier mode (kx, ky).  The library therefore keeps the state as the 2-D
+// r2c half-spectrum of every z-plane (normalised by 1/(nx*ny)) and advances
+// each (kx, ky) z-pencil on its own.  Physical fields are produced only for
+// outputs, by the shared-memory FFT kernels of fft.cu.
+//
+// Layout in HBM (T = double or float, CT = T2 complex):
+//   spectral field:  [src][field][z][m],  m = ky*H + kx, H = nx/2+1, M = ny*H
+//   physical field:  [z][y][x] (Fortran a(nx,ny,nz))
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+template <typename T> struct CplxOf;
+template <> struct CplxOf<double> { typedef double2 type; };
+template <> struct CplxOf<float> { typedef float2 type; };
+
+__host__ __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 operator-(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 operator-(double2 a) { return make_double2(-a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 operator*(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__host__ __device__ __forceinline__ double2 operator*(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 operator-(float2 a) { return make_float2(-a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 operator*(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+__host__ __device__ __forceinline__ float2 operator*(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+template <typename CT> __host__ __device__ __forceinline__ CT czero();
+template <> __host__ __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <> __host__ __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
+template <typename V> __host__ __device__ __forceinline__ V vzero() { return V(0); }
+template <> __host__ __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
+template <> __host__ __device__ __forceinline__ float2 vzero<float2>() { return make_float2(0.f, 0.f); }
+
+// i*k*z for real k
+template <typename T, typename CT>
+__device__ __forceinline__ CT imul(T k, CT z) { CT r; r.x = -k * z.y; r.y = k * z.x; return r; }
+// complex * complex
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// ---- z-profile table (T, nz entries per row) -------------------------------
+enum ZTab {
+    ZT_STRETCH = 0, ZT_UNSTRETCH, ZT_C2RHO0, ZT_GRADP0, ZT_RHO0, ZT_GRADRHO0, ZT_RHOINV, ZT_G,
+    ZT_AZ, ZT_BZ, ZT_C2, ZT_GRAW,
+    ZT_TH = 12,          // per bc b in 0..3: ZT_TH + 3*b + {0: lowr, 1: 1/betad, 2: gam}
+    ZT_COUNT = ZT_TH + 12
+};
+// ---- pencil table (T, M entries per row) ------------------------------------
+enum PTab { PT_KX = 0, PT_KY, PT_DAMP, PT_HF, PT_COUNT };
+
+// Compact-FD right-hand-side coefficients (dbyd2.f90:88-196), FP64 set-up
+template <typename T> struct Compact {
+    T C1, C2;          // interior (dbyd2.f90:88-89)
+    T Cb[5];           // fourth-order near-boundary rows (dbyd2.f90:104-118)
+    T Cf[4];           // fifth-order boundary rows (dbyd2.f90:122-146)
+    T alpha2, beta1, cnst;   // boundary preconditioning (dbyd2.f90:157-173)
+};
+
+// Forward elimination of the compact-FD system for one pencil.
+// ld(j) returns b(j) (0-based); bot/top are caller-set boundary values used
+// for bc 2 (row 1) / bc 3 (row nz); y receives the eliminated values
+// UD(J) = (R(J) - A(J) UD(J-1)) / BETAD(J)  (mtridag.f90:100-104).
+template <typename V, typename T, typename Load>
+__device__ __forceinline__ void compact_forward(int nz, int bc, Load ld, V bot, V top,
+                                                const T* __restrict__ low, const T* __restrict__ ibd,
+                                                const Compact<T>& c, V* y, long long ys) {
+    V b0 = ld(0), b1 = ld(1), b2 = ld(2), b3 = ld(3), b4 = ld(4);
+    V R1 = c.Cb[0] * b0 + c.Cb[1] * b1 + c.Cb[2] * b2 + c.Cb[3] * b3 + c.Cb[4] * b4;
+    V R0;
+    if (bc == 0) R0 = vzero<V>();
+    else if (bc == 2) R0 = bot;
+    else {
+        R0 = c.Cf[0] * b0 + c.Cf[1] * b1 + c.Cf[2] * b2 + c.Cf[3] * b3;
+        R0 = (c.alpha2 * R0 - c.beta1 * R1) * c.cnst;
+    }
+    V ud = R0 * __ldg(&ibd[0]);
+    y[0] = ud;
+    ud = (R1 - __ldg(&low[1]) * ud) * __ldg(&ibd[1]);
+    y[ys] = ud;
+    V w0 = b0, w1 = b1, w2 = b2, w3 = b3, w4 = b4;
+    for (int j = 2; j <= nz - 3; ++j) {
+        V R = c.C1 * (w3 - w1) + c.C2 * (w4 - w0);
+        ud = (R - __ldg(&low[j]) * ud) * __ldg(&ibd[j]);
+        y[(long long)j * ys] = ud;
+        if (j + 3 <= nz - 1) { w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = ld(j + 3); }
+    }
+    V Rn2 = -(c.Cb[0] * w4 + c.Cb[1] * w3 + c.Cb[2] * w2 + c.Cb[3] * w1 + c.Cb[4] * w0);
+    V Rn1;
+    if (bc == 0) Rn1 = vzero<V>();
+    else if (bc == 3) Rn1 = top;
+    else {
+        Rn1 = -(c.Cf[0] * w4 + c.Cf[1] * w3 + c.Cf[2] * w2 + c.Cf[3] * w1);
+        Rn1 = (c.alpha2 * Rn1 - c.beta1 * Rn2) * c.cnst;
+    }
+    ud = (Rn2 - __ldg(&low[nz - 2]) * ud) * __ldg(&ibd[nz - 2]);
+    y[(long long)(nz - 2) * ys] = ud;
+    ud = (Rn1 - __ldg(&low[nz - 1]) * ud) * __ldg(&ibd[nz - 1]);
+    y[(long long)(nz - 1) * ys] = ud;
+}
+
+// z filter of FILTER_VARS_3D (physics.f90:758-786) / FILTER_VAR_Z
+// (kernels.f90:845-881) / FILTER_VARS_2D (physics2d.f90:531-561) applied to a
+// stream of values val(j); emit(j, filtered) is called for every j.
+// mode 0: rows 2..nz-1 written (3-D);  mode 1: rows 6..nz-1 written (2-D, kst=6)
+template <typename V, typename T, typename Load, typename Emit>
+__device__ __forceinline__ void zfilter_stream(int nz, int mode, Load val, Emit emit) {
+    const T h1 = (T)(0.5 * 0.41015625), h2 = (T)(0.5 * -0.234375), h3 = (T)(0.5 * 0.087890625);
+    const T h4 = (T)(0.5 * -0.01953125), h5 = (T)(0.5 * 0.001953125), c0 = (T)0.75390625, hf = (T)0.5;
+    // window w[q] = val(j - 5 + q)
+    V w0 = vzero<V>(), w1 = vzero<V>(), w2 = vzero<V>(), w3 = vzero<V>(), w4 = vzero<V>();
+    V w5 = val(0), w6 = val(1), w7 = val(2), w8 = val(3), w9 = val(4), w10 = val(5);
+    for (int j = 0; j < nz; ++j) {
+        V out;
+        bool near_bot = (j >= 1 && j <= 4), near_top = (j >= nz - 5 && j <= nz - 2);
+        if (j == 0 || j == nz - 1) out = w5;
+        else if (near_top) out = hf * (w6 + w4);
+        else if (near_bot) out = (mode == 0) ? hf * (w6 + w4) : w5;
+        else
+            out = c0 * w5 + h1 * (w4 + w6) + h2 * (w3 + w7) + h3 * (w2 + w8) + h4 * (w1 + w9) + h5 * (w0 + w10);
+        emit(j, out);
+        w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6; w6 = w7; w7 = w8; w8 = w9; w9 = w10;
+        if (j + 6 < nz) w10 = val(j + 6);
+    }
+}
+
+// ---- argument blocks ----------------------------------------------------------
+template <typename T> struct StageArgs {
+    typedef typename CplxOf<T>::type CT;
+    CT* a; CT* scr; CT* pml; CT* scrpml; CT* ybuf; CT* pbuf; CT* rbuf;
+    const T* zt; const T* pt;
+    long long fs;       // spectral field stride nz*M
+    long long ps;       // pml field stride nzpml*M
+    int M, nz, npmlbot, npmltop, option, damp;
+    int has_scr;
+    T beta;
+    Compact<T> cc;
+    // source injection at plane ksrc (0-based)
+    int src_on, ksrc;
+    T src_scale;                // delta_width / rho0(ksrc)
+    const CT* planes; long long plane_ss; int L;
+    int mode;                   // 1 series, 2 Lagrange
+    int nw; int widx[7]; T wts[7];
+    const double* series; int nseries; int time;
+};
+
+template <typename T> struct UpdateArgs {
+    typedef typename CplxOf<T>::type CT;
+    CT* a; CT* scr; CT* pml; CT* scrpml;
+    const T* pt;
+    long long fs, ps;
+    int M, nz, nzpml, option;
+    T dt;
+    int hfilter;        // apply horizontal spectral filter this step
+};
+
+// launchers (modal.cu)
+template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s);
+template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s);
+template <typename T>
+void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,
+                   typename CplxOf<T>::type* out, long long n1, int nz, int bc, int filter,
+                   const typename CplxOf<T>::type* top_plane, cudaStream_t s);
+void launch_zderiv_real(const double* zt, const Compact<double>& cc, const double* in, double* out,
+                        long long n1, int nz, int bc, cudaStream_t s);
+
+// transforms (fft.cu)
+template <typename T>
+void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);
+template <typename T>
+void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);
+
+// kernel (sensitivity) helpers (fft.cu)
+template <typename T>
+void launch_spec_combine(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
+                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, cudaStream_t s);
+template <typename T>
+void launch_spec_scale_z(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
+                         const T* zt, int row, int M, int nz, cudaStream_t s);
+template <typename T>
+void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
+                      const T* pt, int which, int M, int nz, cudaStream_t s);
+template <typename T>
+void launch_kernel_accum(double* acc /* 3*N */, const T* fwd /* 7*N */, const T* adj /* 7*N */,
+                         const double* zt64, long long NP, int nz, int use_y, cudaStream_t s);
+template <typename T>
+void launch_copy_convert(T* dst, const double* src, long long n, cudaStream_t s);
+template <typename T>
+void launch_copy_back(double* dst, const T* src, long long n, cudaStream_t s);
+void launch_spec_mult(double2* spec, const double* mult, long long M, int nplanes, cudaStream_t s);
+int launch_check_finite_f64(const double* p, long long n, int* flag, cudaStream_t s);
+int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t s);
+void launch_kernel_finish(double* out, const double* acc, const double* zt64, long long NP, int nz,
+                          double scale_c, double scale_r, int nsum, long long acc_ss, cudaStream_t s);

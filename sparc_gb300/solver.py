@@ -1,0 +1,212 @@
+"""Host-side mirror of the reference's time-stepping interface.
+
+``Solver`` owns one library context (one or many sources on the source axis)
+and exposes the operations the reference performs inside its executable:
+Initialize_all + solar_data + mp_Initialize_RHS + Initialize_step
+(constructor), DETERMINE_STATUS source set-up (``set_source_*``), the
+TIMESTEPPING loop body (``step``), the vz_cc.bin stream (``record_surface`` /
+``records``), WRITE_OUT_PARTIAL_STATE fields (``field``), checkpoints, and the
+sensitivity-kernel accumulation of kernels.f90.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+from .params import SparcParams
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Solver:
+    """One GPU solve (or a batch of ``p.nsrc`` solves sharing one background)."""
+
+    XI_X, XI_Y, XI_Z, V_X, V_Y, V_Z = range(6)
+
+    def __init__(self, p: SparcParams, table: np.ndarray):
+        p.validate()
+        self.p = p
+        self.L = native.load()
+        self._cp = native.c_params(p)
+        h = ctypes.c_void_p()
+        rc = self.L.sparc_gpu_create(ctypes.byref(self._cp), ctypes.byref(h))
+        if rc != 0:
+            raise native.SparcError(rc, self.L.sparc_gpu_errstr(rc).decode())
+        self.h = h
+        self.shape = (p.nz, p.ny, p.nx)
+        self.set_background(table)
+
+    # ---- plumbing ----
+    def _ck(self, rc: int):
+        if rc != 0:
+            msg = self.L.sparc_gpu_last_error(self.h).decode() if self.h else ""
+            raise native.SparcError(rc, f"{self.L.sparc_gpu_errstr(rc).decode()}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sparc_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- set-up ----
+    def set_background(self, table: np.ndarray):
+        t = _f64(table)
+        if t.shape != (self.p.nz, 6):
+            raise ValueError(f"background table must be ({self.p.nz}, 6)")
+        cols = [_f64(t[:, i]) for i in range(6)]
+        self._ck(self.L.sparc_gpu_set_background(self.h, *[_dp(c) for c in cols]))
+
+    def info(self) -> dict:
+        out = np.zeros(16)
+        self._ck(self.L.sparc_gpu_info(self.h, _dp(out), None, None))
+        keys = ["e_rad", "o_rad", "delta_width", "deltat", "steps", "freq_filtering", "maxtime",
+                "forcing_length", "cadforcing_step", "num_steps", "beta1", "beta2", "beta3", "beta4", "beta5"]
+        d = dict(zip(keys, out[:15].tolist()))
+        for k in ("e_rad", "o_rad", "steps", "freq_filtering", "maxtime", "forcing_length",
+                  "cadforcing_step", "num_steps"):
+            d[k] = int(d[k])
+        return d
+
+    def tables(self):
+        zt = np.zeros(24 * self.p.nz)
+        m = self.p.ny * (self.p.nx // 2 + 1)
+        pt = np.zeros(4 * m)
+        self._ck(self.L.sparc_gpu_info(self.h, None, _dp(zt), _dp(pt)))
+        return zt.reshape(24, self.p.nz), pt.reshape(4, m)
+
+    def set_source_series(self, plane: np.ndarray, series: np.ndarray, slot: int = 0):
+        """forcing(x, y, t_n) = plane(x, y) * series[n], injected at the source plane."""
+        pl = _f64(plane).reshape(1, self.p.ny, self.p.nx)
+        se = _f64(series)
+        self._ck(self.L.sparc_gpu_set_source(self.h, slot, native.SRC_SERIES, _dp(pl), 1, _dp(se), len(se)))
+
+    def set_source_lagrange(self, planes: np.ndarray, slot: int = 0):
+        """vr(:,:,1..L) sampled every cadforcing seconds (LAGRANGE_INTERP)."""
+        pl = _f64(planes).reshape(-1, self.p.ny, self.p.nx)
+        self._ck(self.L.sparc_gpu_set_source(self.h, slot, native.SRC_LAGRANGE, _dp(pl), pl.shape[0], None, 0))
+
+    def clear_source(self, slot: int = 0):
+        self._ck(self.L.sparc_gpu_set_source(self.h, slot, native.SRC_NONE, None, 0, None, 0))
+
+    # ---- stepping ----
+    def step(self, n: int = 1):
+        self._ck(self.L.sparc_gpu_step(self.h, int(n)))
+
+    @property
+    def time(self) -> int:
+        t = ctypes.c_int()
+        self._ck(self.L.sparc_gpu_get_time(self.h, ctypes.byref(t)))
+        return t.value
+
+    @time.setter
+    def time(self, t: int):
+        self._ck(self.L.sparc_gpu_set_time(self.h, int(t)))
+
+    def sync(self, check_finite: bool = False):
+        self._ck(self.L.sparc_gpu_sync(self.h, int(check_finite)))
+
+    @property
+    def stream_ptr(self) -> int:
+        return self.L.sparc_gpu_stream(self.h) or 0
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.sparc_gpu_launch_count(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.sparc_gpu_device_bytes(self.h))
+
+    # ---- state ----
+    def field(self, f: int, slot: int = 0, k: int = 0) -> np.ndarray:
+        shape = (self.p.ny, self.p.nx) if k > 0 else self.shape
+        out = np.zeros(shape)
+        self._ck(self.L.sparc_gpu_get_field(self.h, slot, f, k, _dp(out)))
+        return out
+
+    def state(self, slot: int = 0):
+        a = np.zeros((6,) + self.shape)
+        pml = np.zeros((2, self.p.nzpml, self.p.ny, self.p.nx))
+        self._ck(self.L.sparc_gpu_get_state(self.h, slot, _dp(a), _dp(pml)))
+        return a, pml
+
+    def set_state(self, a: np.ndarray, pml: np.ndarray | None = None, slot: int = 0):
+        a = _f64(a)
+        if a.shape != (6,) + self.shape:
+            raise ValueError("state must be (6, nz, ny, nx)")
+        pp = None
+        if pml is not None:
+            pml = _f64(pml)
+            pp = _dp(pml)
+        self._ck(self.L.sparc_gpu_set_state(self.h, slot, _dp(a), pp))
+
+    def record_surface(self, max_records: int, enable: bool = True):
+        self._ck(self.L.sparc_gpu_record_surface(self.h, int(enable), int(max_records)))
+
+    def records(self, slot: int = 0) -> np.ndarray:
+        n = ctypes.c_int()
+        self._ck(self.L.sparc_gpu_get_records(self.h, slot, None, ctypes.byref(n)))
+        out = np.zeros((n.value, self.p.ny, self.p.nx))
+        if n.value:
+            self._ck(self.L.sparc_gpu_get_records(self.h, slot, _dp(out), ctypes.byref(n)))
+        return out
+
+    def checkpoint(self, path: str):
+        self._ck(self.L.sparc_gpu_checkpoint(self.h, path.encode()))
+
+    def restore(self, path: str):
+        self._ck(self.L.sparc_gpu_restore(self.h, path.encode()))
+
+    # ---- primitives ----
+    def ddx(self, v):
+        v = _f64(v); d = np.zeros_like(v)
+        self._ck(self.L.sparc_gpu_ddx(self.h, _dp(v), _dp(d))); return d
+
+    def ddy(self, v):
+        v = _f64(v); d = np.zeros_like(v)
+        self._ck(self.L.sparc_gpu_ddy(self.h, _dp(v), _dp(d))); return d
+
+    def ddz(self, v, bc: int, d_init=None):
+        v = _f64(v)
+        d = np.zeros_like(v) if d_init is None else _f64(d_init).copy()
+        self._ck(self.L.sparc_gpu_ddz(self.h, _dp(v), _dp(d), int(bc))); return d
+
+    def damp(self, v, rhs):
+        v = _f64(v); r = _f64(rhs).copy()
+        self._ck(self.L.sparc_gpu_damp(self.h, _dp(v), _dp(r))); return r
+
+    # ---- sensitivity kernels ----
+    def snapshot(self, snap: int, nsnap: int):
+        self._ck(self.L.sparc_gpu_snapshot(self.h, int(snap), int(nsnap)))
+
+    def kernel_reset(self):
+        self._ck(self.L.sparc_gpu_kernel_reset(self.h))
+
+    def kernel_accumulate(self, fwd: "Solver", snap: int):
+        self._ck(self.L.sparc_gpu_kernel_accumulate(fwd.h, int(snap), self.h))
+
+    def kernels(self, slot: int = 0, sum_slots: bool = False):
+        kc = np.zeros(self.shape); kr = np.zeros(self.shape); hs = np.zeros(self.shape)
+        self._ck(self.L.sparc_gpu_kernels(self.h, slot, int(sum_slots), _dp(kc), _dp(kr), _dp(hs)))
+        return kc, kr, hs
