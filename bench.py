@@ -1,0 +1,417 @@
+"""Benchmark: grid-point-steps/s of the SPARC time step at 256x256x300.
+
+Workload (synthetic inputs, seeded): quiet-Sun polytrope box 256x256x300,
+200 Mm periodic, PML 10 top + 10 bottom, dt = 2 s.  One bench *step* = one
+time step of the forward solve AND one time step of the adjoint solve for
+every source on the source axis, with the sensitivity-kernel snapshot /
+accumulation (FP64 accumulators) at the 30 s output cadence, as in a
+forward x adjoint kernel run.  Point-steps per bench step = 2 * nsrc * N.
+
+  value       batched FP32 fields (FP64 set-up and kernel accumulation),
+              nsrc sources in one launch per kernel, inputs resident in HBM
+  fp64_plain  the plain single-source FP64 solve, same workload
+  e2e         batched FP32 through the public API with host buffers: source
+              upload (H2D), the steps, seismogram + summed-kernel read-back (D2H)
+  roofline    the dominant kernel (RK stage kernel, FP32 batched) against the
+              measured HBM copy bandwidth
+  cpu_baseline  the FP64 CPU oracle (a restatement of the reference) on a
+              bounded sample (rank 0, N = 1)
+
+--impl reference times the CPU oracle on the same configuration with all host
+threads (the reference itself is Fortran/MPI/FFTW and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpoint-steps/s at 256^2x300, batched FP32 vs plain FP64; p50/p99 solve latency"
+UNIT = "Mpoint-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nsrc", type=int, default=32)
+    ap.add_argument("--nplanes", type=int, default=64, help="adjoint source samples per source")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true", help="128x128x150 smoke-size workload")
+    return ap.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, x: float) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(small: bool):
+    from sparc_gb300.background import polytrope_table
+    from sparc_gb300.params import config_quiet_128, config_quiet_256
+    p = config_quiet_128() if small else config_quiet_256()
+    return p, polytrope_table(p.nz)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_pair(p, tab, nplanes, seed=0):
+    """Forward and adjoint solvers with seeded sources on every slot."""
+    from sparc_gb300 import sources
+    from sparc_gb300.solver import Solver
+    pf = p
+    pa = p.replace(compute_forward=False, compute_adjoint=True)
+    fwd, adj = Solver(pf, tab), Solver(pa, tab)
+    rng = np.random.default_rng(seed)
+    series = sources.ricker_series(p, 20000)
+    pix = sources.receiver_pixels(p)
+    for s in range(p.nsrc):
+        x0, y0 = rng.uniform(-60, 60, size=2)
+        fwd.set_source_series(sources.gaussian_plane(p, 1.0, x0, y0), series, slot=s)
+        res = rng.standard_normal((len(pix), nplanes)) * 1e-6
+        adj.set_source_lagrange(sources.adjoint_planes(p, res, pix), slot=s)
+    return fwd, adj
+
+
+def step_pair(fwd, adj, cad, nsnap_ring=2):
+    """One bench step: forward + adjoint step, kernel snapshot/accumulate at the cadence."""
+    t = fwd.time
+    fwd.step(1)
+    adj.step(1)
+    if t % cad == 0:
+        slot = (t // cad) % nsnap_ring
+        fwd.snapshot(slot, nsnap_ring)
+        adj.kernel_accumulate(fwd, slot)
+
+
+def timed_region(fwd, adj, steps, cad):
+    """Device time of `steps` bench steps across both contexts' streams."""
+    import torch
+    sf = torch.cuda.ExternalStream(fwd.stream_ptr)
+    sa = torch.cuda.ExternalStream(adj.stream_ptr)
+    torch.cuda.synchronize()
+    fwd.sync(); adj.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ea = torch.cuda.Event()
+    e0.record(sf)
+    sa.wait_event(e0)
+    per = []
+    l0 = fwd.launches + adj.launches
+    for _ in range(steps):
+        step_pair(fwd, adj, cad)
+    ea.record(sa)
+    sf.wait_event(ea)
+    e1.record(sf)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    launches = fwd.launches + adj.launches - l0
+    return e0.elapsed_time(e1), launches
+
+
+def stage_kernel_time(solver, reps=3):
+    """Average duration of the RK-stage kernel (stages 2..5) with CUDA events
+    on the launching stream."""
+    import torch
+    s = torch.cuda.ExternalStream(solver.stream_ptr)
+    solver.sync()
+    ts = []
+    for _ in range(reps):
+        for rk in (2, 3, 4, 5):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            solver.stage(rk)
+            e1.record(s)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+    return float(np.mean(ts)), ts
+
+
+def cpu_baseline(p, tab, steps=1):
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.Oracle(p.replace(precision="f64", nsrc=1), tab)
+    from sparc_gb300 import sources
+    o.set_source(1, sources.gaussian_plane(p)[None].copy(), sources.ricker_series(p, 100))
+    o.step(1)                       # warm-up (first-touch of the arrays)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": p.points * steps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} forward time step(s) of {p.nx}x{p.ny}x{p.nz} FP64 on the CPU oracle "
+                      f"(one source), {dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    p, tab = workload(args.small)
+    from oracle import oracle
+    from sparc_gb300 import sources
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    K = max(1, min(args.steps, 3))
+    W = max(0, min(args.warmup, 1))
+    pp = p.replace(precision="f64", nsrc=1)
+    o = oracle.Oracle(pp, tab)
+    o.set_source(1, sources.gaussian_plane(p)[None].copy(), sources.ricker_series(p, 100))
+    o.step(W)
+    t0 = time.perf_counter()
+    o.step(K)
+    dt = time.perf_counter() - t0
+    v = p.points * K / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1 if ws <= 1 else ws,
+        "steps": K, "warmup": W, "ms_per_step": dt * 1e3 / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"quiet-Sun {p.nx}x{p.ny}x{p.nz} forward time step, single source, FP64",
+                   "grid": [p.nx, p.ny, p.nz]},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{K} forward steps of {p.nx}x{p.ny}x{p.nz} after {W} warm-up; the "
+                                   "reference Fortran/MPI/FFTW cannot be built here, so the CPU oracle "
+                                   "(its line-for-line FP64 restatement) stands in"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    ws, rank, local = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    from sparc_gb300 import build as b
+    b.build()
+    from sparc_gb300 import bytes_model
+    p0, tab = workload(args.small)
+    K, W = max(1, args.steps), max(3, args.warmup)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    N = p0.points
+    out = {}
+
+    # ---- plain FP64, one source ----
+    if not args.skip_fp64:
+        p64 = p0.replace(precision="f64", nsrc=1)
+        fwd, adj = make_pair(p64, tab, args.nplanes, seed=rank)
+        cad = fwd.info()["steps"]
+        for _ in range(W):
+            step_pair(fwd, adj, cad)
+        barrier(ws)
+        ms, _ = timed_region(fwd, adj, K, cad)
+        ms = allmax(ws, ms)
+        out["fp64_plain"] = {"value": 2 * N * K * ws / (ms * 1e-3) / 1e6, "unit": UNIT,
+                             "ms_per_step": ms / K, "nsrc": 1, "dtype": "f64"}
+        fwd.close(); adj.close()
+        del fwd, adj
+
+    # ---- batched FP32 ----
+    S = args.nsrc
+    p32 = p0.replace(precision="f32", nsrc=S)
+    fwd, adj = make_pair(p32, tab, args.nplanes, seed=1000 + rank)
+    cad = fwd.info()["steps"]
+    for _ in range(W):
+        step_pair(fwd, adj, cad)
+    barrier(ws)
+    with ClockSampler(local) as clk:
+        ms, launches = timed_region(fwd, adj, K, cad)
+        # dominant kernel (RK stage, FP32 batched) timed on its own stream
+        st_ms, _ = stage_kernel_time(fwd)
+    ms = allmax(ws, ms)
+    value = 2 * N * S * K * ws / (ms * 1e-3) / 1e6
+    alg = bytes_model.stage_alg_bytes(p32, 2)
+    achieved = alg / (st_ms * 1e-3) / 1e9
+    clocks = clk.summary()
+    # per-step latency distribution of the batched solve
+    import torch
+    lat = []
+    for _ in range(min(K, 10)):
+        t0 = time.perf_counter()
+        step_pair(fwd, adj, cad)
+        fwd.sync(); adj.sync()
+        lat.append((time.perf_counter() - t0) * 1e3)
+    fwd.close(); adj.close()
+    del fwd, adj
+
+    # ---- e2e through the public API with host buffers (pinned) ----
+    e2e = None
+    if True:
+        from sparc_gb300 import sources
+        from sparc_gb300.solver import Solver
+        pa = p32.replace(compute_forward=False, compute_adjoint=True)
+        rng = np.random.default_rng(7)
+        pix = sources.receiver_pixels(p32)
+        series = sources.ricker_series(p32, 20000)
+
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+        plane_h = [pinned((p32.ny, p32.nx)) for _ in range(S)]
+        adj_h = [pinned((args.nplanes, p32.ny, p32.nx)) for _ in range(S)]
+        for s in range(S):
+            x0, y0 = rng.uniform(-60, 60, size=2)
+            plane_h[s][...] = sources.gaussian_plane(p32, 1.0, x0, y0)
+            adj_h[s][...] = sources.adjoint_planes(p32, rng.standard_normal((len(pix), args.nplanes)) * 1e-6, pix)
+        fwd, adj = Solver(p32, tab), Solver(pa, tab)
+        nrec = K // cad + 2
+        rec_h = pinned((nrec, p32.ny, p32.nx))
+        k_h = [pinned((p32.nz, p32.ny, p32.nx)) for _ in range(3)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(S):
+            fwd.set_source_series(plane_h[s], series, slot=s)
+            adj.set_source_lagrange(adj_h[s], slot=s)
+        fwd.record_surface(nrec)
+        for _ in range(K):
+            step_pair(fwd, adj, cad)
+        d2h = 0
+        for s in range(S):
+            r = fwd.records(slot=s)
+            rec_h[: r.shape[0]] = r
+            d2h += r.nbytes
+        kc, kr, hs = adj.kernels(sum_slots=True)
+        k_h[0][...] = kc; k_h[1][...] = kr; k_h[2][...] = hs
+        d2h += 3 * kc.nbytes
+        dt = time.perf_counter() - t0
+        h2d = S * (plane_h[0].nbytes + series.nbytes + adj_h[0].nbytes)
+        e2e = {"value": 2 * N * S * K * ws / dt / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d // K), "d2h_bytes_per_step": int(d2h // K),
+               "wall_s": dt}
+        fwd.close(); adj.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 set-up and kernel accumulation)", "data": "synthetic",
+        "config": {"workload": f"quiet-Sun {p0.nx}x{p0.ny}x{p0.nz} forward+adjoint time step with "
+                               f"sensitivity-kernel accumulation every {cad} steps, {S} sources batched",
+                   "grid": [p0.nx, p0.ny, p0.nz], "nsrc": S, "point_steps_per_step": 2 * N * S,
+                   "l2": "inputs larger than L2 (state of each context > 30 GB)",
+                   "adjoint_source_samples": args.nplanes},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "kernel": "stage_kernel<float>", "avg_launch_ms": st_ms,
+                     "alg_bytes_per_launch": alg, "impl_bytes_per_launch": bytes_model.stage_impl_bytes(p32, 2),
+                     "peak_source": f"{peak_src} hbm_gbs"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "what": "one batched forward+adjoint step, host-synchronised"},
+        "e2e": e2e,
+    }
+    if "fp64_plain" in out:
+        line["fp64_plain"] = out["fp64_plain"]
+        line["ratio_fp32_batched_over_fp64_plain"] = value / out["fp64_plain"]["value"]
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(p0, tab)
+        except Exception as e:  # the oracle is only the reported baseline
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                    "sample": f"failed: {e}"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

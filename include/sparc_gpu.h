@@ -121,6 +121,11 @@ int sparc_gpu_set_source(sparc_ctx* ctx, int src_idx, int mode, const double* pl
  * (driver.f90:455-476). */
 int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
 
+/* One RK stage rk = 1..5 of the current step (one pass of the do step_rk
+ * loop body, step.f90:49-112) without the update, the filters or a time
+ * advance: a fine-grained seam for timing the stage kernel on its own. */
+int sparc_gpu_stage(sparc_ctx* ctx, int rk);
+
 int sparc_gpu_get_time(const sparc_ctx* ctx, int* time);
 int sparc_gpu_set_time(sparc_ctx* ctx, int time);
 

@@ -1,0 +1,74 @@
+"""HBM byte model of the time step (used by bench.py for the roofline line).
+
+Units: one *field access* = one read or write of a whole spectral field of
+one source: M * nz complex values, M = ny * (nx/2 + 1), i.e. (nx/2+1)/nx of
+the bytes of the physical field (4.03 B per grid point in FP32, 8.06 B in
+FP64 at nx = 256).
+
+Algorithmic (compulsory) accesses of the spectral-column schedule:
+  RK stage 1 (temp = a):            read a (6 fields)           + write scr (6) = 12
+  RK stages 2-5 (temp = a+beta scr): read a (6) + read scr (6)  + write scr (6) = 18
+  update + filters:                  read a (6) + read scr (6)  + write a (6)   = 18
+  per step: 12 + 4*18 + 18 = 102 accesses.
+PML auxiliaries add 2 fields on nzpml planes per pass (counted exactly below).
+
+Implemented accesses of the current stage kernel (four z sweeps with the
+tridiagonal intermediates y, p', rho' round-tripping through global memory):
+  stage 2-5: S1 2r+1w, S2 11r+6w, S3 1r+1w, S4 4r+2w = 28;  stage 1: 21.
+The difference (10 accesses per stage) is the traffic that an on-chip schedule
+removes.
+"""
+from __future__ import annotations
+
+STAGE1_ALG = 12
+STAGE_ALG = 18
+UPDATE_ALG = 18
+STAGE1_IMPL = 21
+STAGE_IMPL = 28
+UPDATE_IMPL = 18
+
+
+def complex_bytes(precision: str) -> int:
+    return 16 if precision == "f64" else 8
+
+
+def field_bytes(p, nsrc: int | None = None) -> int:
+    """Bytes of one spectral field for all sources of a context."""
+    s = p.nsrc if nsrc is None else nsrc
+    return (p.nx // 2 + 1) * p.ny * p.nz * complex_bytes(p.precision) * s
+
+
+def pml_field_bytes(p, nsrc: int | None = None) -> int:
+    s = p.nsrc if nsrc is None else nsrc
+    return (p.nx // 2 + 1) * p.ny * p.nzpml * complex_bytes(p.precision) * s
+
+
+def stage_alg_bytes(p, rk: int) -> int:
+    """Algorithmic bytes of one launch of RK stage rk (1..5) for all sources."""
+    f = field_bytes(p)
+    pf = pml_field_bytes(p)
+    if rk == 1:
+        return STAGE1_ALG * f + (2 + 2) * pf        # read psi, write scrpml
+    return STAGE_ALG * f + (4 + 2) * pf             # read psi + scrpml, write scrpml
+
+
+def stage_impl_bytes(p, rk: int) -> int:
+    f = field_bytes(p)
+    pf = pml_field_bytes(p)
+    return (STAGE1_IMPL if rk == 1 else STAGE_IMPL) * f + (4 if rk == 1 else 6) * pf
+
+
+def update_alg_bytes(p) -> int:
+    return UPDATE_ALG * field_bytes(p) + 6 * pml_field_bytes(p)
+
+
+def step_alg_bytes(p) -> int:
+    return sum(stage_alg_bytes(p, rk) for rk in range(1, 6)) + update_alg_bytes(p)
+
+
+def step_impl_bytes(p) -> int:
+    return sum(stage_impl_bytes(p, rk) for rk in range(1, 6)) + update_alg_bytes(p)
+
+
+def alg_bytes_per_point_step(p) -> float:
+    return step_alg_bytes(p) / (p.points * p.nsrc)

@@ -705,10 +705,8 @@ static void lagrange_weights(sparc_ctx* c, int& nw, int* widx, double* wts) {
 }  // extern "C"
 
 template <typename T>
-static int do_steps(sparc_ctx* c, int nsteps) {
-    typedef typename CplxOf<T>::type CT;
+static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     const sparc_params& P = c->P;
-    StageArgs<T> A;
     memset(&A, 0, sizeof(A));
     A.a = CP<T>(c->a); A.scr = CP<T>(c->scr); A.pml = CP<T>(c->pml); A.scrpml = CP<T>(c->scrpml);
     A.ybuf = CP<T>(c->ybuf); A.pbuf = CP<T>(c->pbuf); A.rbuf = CP<T>(c->rbuf);
@@ -724,27 +722,41 @@ static int do_steps(sparc_ctx* c, int nsteps) {
     A.src_scale = (T)(c->delta_width / c->zt_host[ZT_RHO0 * c->nz + ksrc - 1]);
     A.planes = CP<T>(c->planes); A.plane_ss = (long long)c->src_L * c->M; A.L = c->src_L;
     A.mode = c->src_mode; A.series = c->series; A.nseries = c->nseries;
-    UpdateArgs<T> U;
     U.a = A.a; U.scr = A.scr; U.pml = A.pml; U.scrpml = A.scrpml; U.pt = A.pt;
     U.fs = c->fs; U.ps = c->ps; U.M = c->M; U.nz = c->nz; U.nzpml = c->nzpml; U.option = P.option;
     U.dt = (T)c->deltat;
-    const bool two_d = P.option == 17;
+}
+
+// forcing of the step at c->time (driver.f90:419-422; physics2d.f90:1059)
+template <typename T>
+static void set_forcing(sparc_ctx* c, StageArgs<T>& A) {
+    const bool two_d = c->P.option == 17;
+    const int time = c->time;
+    A.time = time;
+    A.src_on = 0;
+    if (c->src_mode != 0) {
+        bool gate = !two_d || time <= c->forcing_length * c->cadforcing_step;
+        A.src_on = gate ? 1 : 0;
+        if (c->src_mode == SPARC_SRC_LAGRANGE) {
+            if (time <= c->forcing_length * c->cadforcing_step) {
+                lagrange_weights(c, c->last_nw, c->last_widx, c->last_wts);
+            }   // else: forcing keeps its last value (driver.f90:421-422)
+            A.nw = c->last_nw;
+            for (int l = 0; l < A.nw; ++l) { A.widx[l] = c->last_widx[l]; A.wts[l] = (T)c->last_wts[l]; }
+        }
+    }
+}
+
+template <typename T>
+static int do_steps(sparc_ctx* c, int nsteps) {
+    typedef typename CplxOf<T>::type CT;
+    StageArgs<T> A;
+    UpdateArgs<T> U;
+    make_args<T>(c, A, U);
+    const bool two_d = c->P.option == 17;
     for (int it = 0; it < nsteps; ++it) {
         const int time = c->time;
-        // forcing of this step (driver.f90:419-422; physics2d.f90:1059)
-        A.time = time;
-        A.src_on = 0;
-        if (c->src_mode != 0) {
-            bool gate = !two_d || time <= c->forcing_length * c->cadforcing_step;
-            A.src_on = gate ? 1 : 0;
-            if (c->src_mode == SPARC_SRC_LAGRANGE) {
-                if (time <= c->forcing_length * c->cadforcing_step) {
-                    lagrange_weights(c, c->last_nw, c->last_widx, c->last_wts);
-                }   // else: forcing keeps its last value (driver.f90:421-422)
-                A.nw = c->last_nw;
-                for (int l = 0; l < A.nw; ++l) { A.widx[l] = c->last_widx[l]; A.wts[l] = (T)c->last_wts[l]; }
-            }
-        }
+        set_forcing<T>(c, A);
         for (int rk = 0; rk < 5; ++rk) {
             A.beta = (T)c->betas[rk];
             A.has_scr = (rk > 0);
@@ -774,6 +786,31 @@ int sparc_gpu_step(sparc_ctx* c, int nsteps) {
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     if (nsteps < 0) return fail(c, SPARC_EINVAL, "nsteps < 0");
     return c->f32 ? do_steps<float>(c, nsteps) : do_steps<double>(c, nsteps);
+}
+
+}  // extern "C"
+
+template <typename T>
+static int stage_only(sparc_ctx* c, int rk) {
+    StageArgs<T> A;
+    UpdateArgs<T> U;
+    make_args<T>(c, A, U);
+    set_forcing<T>(c, A);
+    A.beta = (T)c->betas[rk - 1];
+    A.has_scr = (rk > 1);
+    launch_stage<T>(A, c->S, c->stream);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+extern "C" {
+
+int sparc_gpu_stage(sparc_ctx* c, int rk) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (rk < 1 || rk > 5) return fail(c, SPARC_EINVAL, "rk must be 1..5");
+    return c->f32 ? stage_only<float>(c, rk) : stage_only<double>(c, rk);
 }
 
 int sparc_gpu_get_time(const sparc_ctx* c, int* t) {

@@ -30,7 +30,7 @@ SRC_NONE, SRC_SERIES, SRC_LAGRANGE = 0, 1, 2
 EXPORTS = [
     "sparc_gpu_create", "sparc_gpu_destroy", "sparc_gpu_errstr", "sparc_gpu_last_error",
     "sparc_gpu_abi_version", "sparc_gpu_set_background", "sparc_gpu_set_source",
-    "sparc_gpu_step", "sparc_gpu_get_time", "sparc_gpu_set_time", "sparc_gpu_get_field",
+    "sparc_gpu_step", "sparc_gpu_stage", "sparc_gpu_get_time", "sparc_gpu_set_time", "sparc_gpu_get_field",
     "sparc_gpu_set_state", "sparc_gpu_get_state", "sparc_gpu_record_surface",
     "sparc_gpu_get_records", "sparc_gpu_checkpoint", "sparc_gpu_restore",
     "sparc_gpu_snapshot", "sparc_gpu_kernel_accumulate", "sparc_gpu_kernel_reset",
@@ -85,6 +85,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_set_background": ([P, D, D, D, D, D, D], I),
         "sparc_gpu_set_source": ([P, I, I, D, I, D, I], I),
         "sparc_gpu_step": ([P, I], I),
+        "sparc_gpu_stage": ([P, I], I),
         "sparc_gpu_get_time": ([P, ctypes.POINTER(I)], I),
         "sparc_gpu_set_time": ([P, I], I),
         "sparc_gpu_get_field": ([P, I, I, I, D], I),

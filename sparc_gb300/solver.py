@@ -113,6 +113,10 @@ class Solver:
     def step(self, n: int = 1):
         self._ck(self.L.sparc_gpu_step(self.h, int(n)))
 
+    def stage(self, rk: int):
+        """Launch only RK stage rk (1..5) of the current step (timing hook)."""
+        self._ck(self.L.sparc_gpu_stage(self.h, int(rk)))
+
     @property
     def time(self) -> int:
         t = ctypes.c_int()
