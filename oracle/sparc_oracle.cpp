@@ -194,11 +194,11 @@ extern "C" int oracle_dbyd2(double* A, const double* B, long N1, int N2, int ibc
     double C1 = d2i * 7.0 / 9.0;                     // dbyd2.f90:88-89
     double C2 = d2i / 36.0;
     std::vector<double> uppr(N2 + 1, 0.0), lowr(N2 + 1, 0.0), diag(N2 + 1, 1.0);  // 1-based
-    if (ibc < 5) {
 #pragma omp parallel for schedule(static)
-        for (int I = 3; I <= N2 - 2; ++I)            // dbyd2.f90:94-99
-            for (long J = 0; J < N1; ++J)
-                Av(J, I - 1) = C1 * (Bv(J, I) - Bv(J, I - 2)) + C2 * (Bv(J, I + 1) - Bv(J, I - 3));
+    for (int I = 3; I <= N2 - 2; ++I)                // dbyd2.f90:94-99 (every ibc)
+        for (long J = 0; J < N1; ++J)
+            Av(J, I - 1) = C1 * (Bv(J, I) - Bv(J, I - 2)) + C2 * (Bv(J, I + 1) - Bv(J, I - 3));
+    if (ibc < 5) {
         // fourth-order near-boundary rows (dbyd2.f90:104-118); REAL*4 ratios
         C1 = -(double)(43.0f / 96.0f) * d2i;
         C2 = -(double)(5.0f / 6.0f) * d2i;

@@ -137,7 +137,7 @@ class SparcParams:
                 k, v = (s.strip() for s in part.split("=", 1))
                 k = k.lower()
                 if k in cls._KEYS:
-                    vals[k] = _eval_fortran_number(v)
+                    vals[k] = _eval_fortran_number(v, vals)
         for m in re.finditer(r"logical[^:\n]*::\s*(\w+)\s*=\s*\.(\w+)\.", body, re.I):
             vals["_" + m.group(1).lower()] = m.group(2).lower() == "true"
         kw = {k: cls._KEYS[k](v) for k, v in vals.items() if not k.startswith("_")}
@@ -162,13 +162,19 @@ class SparcParams:
         return p
 
 
-def _eval_fortran_number(s: str) -> float:
-    s = s.strip().lower().replace("d", "e")
-    s = s.replace("**", "^")
-    m = re.fullmatch(r"([-+\d.e]+)\s*\*\s*10\s*\^\s*\(?\s*([-+]?\d+)\s*\)?", s)
-    if m:
-        return float(m.group(1)) * 10.0 ** int(m.group(2))
-    return float(s)
+def _eval_fortran_number(s: str, known: dict | None = None) -> float:
+    """Evaluate a params.i constant expression: numbers (d/e exponents),
+    + - * / ** and parentheses, and names defined earlier in the file."""
+    expr = s.strip().lower()
+    expr = re.sub(r"(?<=[0-9.])d(?=[-+]?[0-9])", "e", expr)
+    if not re.fullmatch(r"[0-9a-z_.+\-*/() ]+", expr):
+        raise ValueError(f"unsupported params.i expression: {s!r}")
+    names = {k: v for k, v in (known or {}).items() if not k.startswith("_")}
+    bare = re.sub(r"(\d+\.?\d*|\.\d+)(e[-+]?\d+)?", " ", expr)
+    for tok in re.findall(r"[a-z_][a-z_0-9]*", bare):
+        if tok not in names:
+            raise ValueError(f"unknown name {tok!r} in {s!r}")
+    return float(eval(expr, {"__builtins__": {}}, names))
 
 
 # ---- the workload configurations of the benchmark suite (synthetic inputs) ----

@@ -1,0 +1,92 @@
+"""Generates tests/golden/oracle_golden.npz: outputs of the CPU oracle on small
+seeded cases (compact derivative for every boundary code, spectral
+derivatives, damping, three 3-D time steps with a forward source, thirty-one
+2-D time steps, one kernel accumulation).  Regenerate with
+    python tests/golden/make_golden.py
+The GPU parity tests compare the CUDA path against these fixtures as well as
+against the live oracle."""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from cases import small_params, small_params_2d, table_for  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+
+def golden_params():
+    return small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4)
+
+
+def golden_params_2d():
+    return small_params_2d(nx=32, nz=32, npmlbot=4, npmltop=4)
+
+
+def golden_inputs(p, seed):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
+    if p.ny == 1:
+        a[1] = 0.0
+        a[4] = 0.0
+    pml = rng.standard_normal((2, p.nzpml, p.ny, p.nx)) * 1e-5
+    pml[1, 0] = 0.0
+    x = (np.arange(p.nx) / p.nx - 0.5) * p.xlength / 1e8
+    if p.ny == 1:
+        plane = np.exp(-x ** 2 / 2.0)[None, :]
+    else:
+        X, Y = np.meshgrid(x, x)
+        plane = np.exp(-(X ** 2 + Y ** 2) / 2.0)
+    series = O.forward_source(p, 200) * 1e3
+    return a, pml, plane, series
+
+
+def compute():
+    O.build()
+    out = {}
+    rng = np.random.default_rng(42)
+    b = rng.standard_normal((24, 5))
+    for bc in (0, 1, 2, 3):
+        init = np.zeros_like(b)
+        init[0 if bc == 2 else -1] = rng.standard_normal(5) if bc in (2, 3) else 0.0
+        out[f"dbyd2_bc{bc}"] = O.dbyd2(b, bc, init)
+    p = golden_params()
+    tab = table_for(p)
+    o = O.Oracle(p, tab)
+    v = np.random.default_rng(43).standard_normal((p.nz, p.ny, p.nx))
+    out["ddx"] = o.ddx(v)
+    out["ddy"] = o.ddy(v)
+    out["ddz_bc1"] = o.ddz(v, 1)
+    out["damp"] = o.damp(v, np.zeros_like(v))
+    a, pml, plane, series = golden_inputs(p, 44)
+    o.set_state(a, pml)
+    o.set_source(1, plane[None].copy(), series)
+    o.step(3)
+    st, scr, pm = o.state()
+    out["step3_a"] = st
+    out["step3_pml"] = pm
+    p2 = golden_params_2d()
+    o2 = O.Oracle(p2, table_for(p2))
+    a, pml, plane, series = golden_inputs(p2, 45)
+    o2.set_state(a, pml)
+    o2.set_source(1, plane[None].copy(), series)
+    o2.step(31)
+    out["step31_2d_a"] = o2.state()[0]
+    # one kernel accumulation on seeded fields
+    rng = np.random.default_rng(46)
+    fwd = rng.standard_normal((6, p.nz, p.ny, p.nx))
+    adj = rng.standard_normal((3, p.nz, p.ny, p.nx))
+    o.kernel_reset()
+    graw = tab[:, 4] * o.info()["rsun"] / 1e12
+    o.kernel_accumulate(fwd, adj, graw)
+    out["kernels"] = o.kernel_finish(15)
+    return out
+
+
+if __name__ == "__main__":
+    res = compute()
+    np.savez_compressed(os.path.join(HERE, "oracle_golden.npz"), **res)
+    print({k: v.shape for k, v in res.items()})

@@ -1,0 +1,216 @@
+"""Known-answer tests of the CPU oracle (no GPU).  They pin the restatement to
+facts that follow from the reference's own coefficients and literal kinds."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import rel_l2, small_params, small_params_2d, table_for
+
+from oracle import oracle as O
+
+F32 = np.float32
+
+
+@pytest.fixture(scope="module")
+def orc():
+    O.build()
+    p = small_params()
+    return O.Oracle(p, table_for(p))
+
+
+@pytest.mark.parametrize("bc", [0, 1])
+def test_dbyd2_matches_dense_numpy_twin(bc):
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal((40, 7))
+    assert rel_l2(O.dbyd2(b, bc), O.dbyd2_numpy(b, bc)) < 1e-13
+
+
+def test_dbyd2_linear_ramp_carries_real4_alpha():
+    # interior rows of a linear ramp: R = d2i*5/3 and the solution is
+    # R / (1 + 2*alpha) with alpha the REAL*4 value of 1/3 (dbyd2.f90:152)
+    n2 = 200
+    b = np.arange(n2, dtype=np.float64)[:, None] * np.ones((1, 3))
+    a = O.dbyd2(b, 1)
+    d2i = float(n2 - 1)
+    alpha = float(F32(1.0) / F32(3.0))
+    expect = d2i * (d2i * 7.0 / 9.0 * 2.0 + d2i / 36.0 * 4.0) / d2i / (1.0 + 2.0 * alpha)
+    mid = a[60:140, 0]
+    assert np.allclose(mid, expect, rtol=1e-14, atol=0)
+    assert abs(expect / d2i - 1.0) > 1e-8          # not exact: the REAL*4 alpha shows
+
+
+def test_dbyd2_sixth_order_interior():
+    errs = []
+    for n2 in (129, 257):
+        xi = np.linspace(0.0, 1.0, n2)
+        b = np.sin(16 * np.pi * xi)[:, None]
+        a = O.dbyd2(b, 1)[:, 0]
+        exact = 16 * np.pi * np.cos(16 * np.pi * xi)
+        sl = slice(n2 // 4, 3 * n2 // 4)
+        errs.append(np.abs(a[sl] - exact[sl]).max())
+    assert errs[1] < errs[0] / 30.0
+
+
+@pytest.mark.parametrize("n2,tol", [(64, 1e-13), (24, 1e-8)])
+def test_dbyd2_periodic_matches_dense(n2, tol):
+    # The cyclic branch of MTRIDAG (mtridag.f90:19-64) back-substitutes row
+    # n2-1 with betau only, dropping the fill-in alpha*betas(n2-2) of size
+    # ~0.382**(n2-3): exact to round-off for n2 = 64, ~1e-9 off for n2 = 24.
+    rng = np.random.default_rng(9)
+    b = rng.standard_normal((n2, 3))
+    a = O.dbyd2(b, 5)
+    d2i = float(n2)
+    c1, c2 = d2i * 7.0 / 9.0, d2i / 36.0
+    rhs = c1 * (np.roll(b, -1, 0) - np.roll(b, 1, 0)) + c2 * (np.roll(b, -2, 0) - np.roll(b, 2, 0))
+    al = float(F32(1.0) / F32(3.0))
+    M = np.eye(n2) + al * (np.roll(np.eye(n2), 1, 1) + np.roll(np.eye(n2), -1, 1))
+    err = rel_l2(a, np.linalg.solve(M, rhs))
+    assert err < tol
+    if n2 == 24:
+        assert err > 1e-13       # the fill-in omission is visible at this size
+
+
+def test_dbyd2_rejects_bad_bc():
+    with pytest.raises(ValueError):
+        O.dbyd2(np.zeros((10, 2)), 6)
+
+
+def test_lddrk_amplification_polynomial(orc):
+    # G(z) = 1 + z + 0.5 z^2 + o3 z^3 + o4 z^4 + o5 z^5 with the REAL*4 optimals (step.f90:28-40)
+    info = orc.info()
+    b = [info[f"beta{i}"] / info["deltat"] for i in range(1, 6)]
+    assert b[0] == 0.0
+    c2, c3 = b[4], b[4] * b[3]
+    c4, c5 = c3 * b[2], c3 * b[2] * b[1]
+    assert c2 == 0.5
+    assert c3 == pytest.approx(float(F32(0.1665579725791151184)), rel=1e-15)
+    assert c4 == pytest.approx(float(F32(0.03950410250586729987)), rel=1e-15)
+    assert c5 == pytest.approx(float(F32(0.007810706393337838236)), rel=1e-15)
+
+
+def test_z_filter_coefficients_preserve_dc_and_kill_nyquist():
+    co = [0.75390625, 0.41015625, -0.234375, 0.087890625, -0.01953125, 0.001953125]
+    assert co[0] + sum(co[1:]) == 1.0
+    assert co[0] + sum(c * (-1) ** i for i, c in enumerate(co[1:], 1)) == 0.0
+
+
+def test_spectral_ddx_is_exact_and_drops_nyquist(orc):
+    p = orc.p
+    info = orc.info()
+    x = np.arange(p.nx) / p.nx
+    k = 3
+    v = np.broadcast_to(np.sin(2 * np.pi * k * x), (p.nz, p.ny, p.nx)).copy()
+    d = orc.ddx(v)
+    # eyekx uses the REAL*4 pi (initialize.f90:205)
+    expect = k * 2 * info["pi"] * np.cos(2 * np.pi * k * x) * info["stretchx"]
+    assert np.abs(d - expect).max() < 1e-11 * np.abs(expect).max()
+    nyq = np.broadcast_to(np.cos(np.pi * np.arange(p.nx)), (p.nz, p.ny, p.nx)).copy()
+    assert np.abs(orc.ddx(nyq)).max() < 1e-12
+
+
+def test_ddx_matches_numpy_fft_twin(orc):
+    rng = np.random.default_rng(2)
+    v = rng.standard_normal((orc.p.nz, orc.p.ny, orc.p.nx))
+    info = orc.info()
+    assert rel_l2(orc.ddx(v), O.fft_ddx_numpy(v, info["stretchx"], info["pi"])) < 1e-13
+    vt = np.ascontiguousarray(np.swapaxes(v, 1, 2))
+    dy = np.swapaxes(O.fft_ddx_numpy(vt, info["stretchy"], info["pi"]), 1, 2)
+    assert rel_l2(orc.ddy(v), dy) < 1e-13
+
+
+def test_damping_rates_formula(orc):
+    p = orc.p
+    info = orc.info()
+    pi, rsun = info["pi"], info["rsun"]
+    constx = 2.0 * pi / float(F32(p.xlength)) * rsun
+    h = p.nx // 2 + 1
+    i = np.arange(h)
+    j = np.arange(p.ny)
+    jj = np.where(j <= p.ny // 2, j, p.ny - j)
+    kay = np.sqrt(constx ** 2 * i[None, :] ** 2 + constx ** 2 * jj[:, None] ** 2)
+    rate = rsun / info["dimc"] * float(F32(1e-6)) * 150.0 * (kay / 902.0) ** float(F32(2.2)) / p.nx / p.ny
+    assert rel_l2(orc.damping_rates(), rate) < 1e-13
+
+
+def test_damping_is_a_real_symmetric_multiplier(orc):
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal((orc.p.nz, orc.p.ny, orc.p.nx))
+    r = orc.damp(v, np.zeros_like(v))
+    # linear, and the DC mode is untouched (rate 0 at k = 0)
+    assert rel_l2(orc.damp(2 * v, np.zeros_like(v)), 2 * r) < 1e-14
+    assert abs(r.mean()) < 1e-13 * np.abs(r).max()
+
+
+def test_forward_source_restatements_agree():
+    from sparc_gb300.sources import gabor_series
+    p = small_params()
+    a = O.forward_source(p, 3000)
+    b = gabor_series(p, 3000)
+    assert np.allclose(a, b, rtol=1e-14, atol=1e-14 * np.abs(a).max())
+    assert np.abs(a).max() > 0
+
+
+def test_setup_derived_quantities(orc):
+    p = orc.p
+    info = orc.info()
+    assert int(info["steps"]) == p.steps == 15
+    assert int(info["freq_filtering"]) == p.freq_filtering == 30
+    assert int(info["maxtime"]) == p.maxtime
+    assert int(info["forcing_length"]) == p.forcing_length
+    assert int(info["num_steps"]) == p.num_steps
+    tab = table_for(p)
+    z = tab[:, 0]
+    assert abs(z[int(info["e_rad"]) - 1] - (1 + p.excitdep / 69598945280.0)) <= np.diff(z).max()
+    assert info["rsun"] == float(F32(69598946770.0))
+    assert info["pi"] == float(F32(3.14159265358979))
+
+
+def test_pml_profiles(orc):
+    pr = orc.profiles()
+    nb, nt, nz = orc.p.npmlbot, orc.p.npmltop, orc.p.nz
+    # az = -dampz vanishes outside the PML; g and the gradients are scaled by
+    # functiondecay = alpha/(dampz+alpha), which is 0 at k = 1 (physics.f90:265-289)
+    assert np.all(pr["az"][nb:nz - nt] == 0.0)
+    assert np.all(pr["az"][:nb - 1] < 0)
+    assert pr["g"][0] == 0.0 and pr["gradp0_z"][0] == 0.0
+    assert pr["g"][nz - 1] == 0.0
+
+
+def test_oracle_step_is_linear():
+    p = small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4)
+    tab = table_for(p)
+    rng = np.random.default_rng(0)
+    a1 = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
+    a2 = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
+    out = []
+    for a in (a1, a2, a1 + a2):
+        o = O.Oracle(p, tab)
+        o.set_state(a)
+        o.step(3)
+        out.append(o.state()[0])
+    assert rel_l2(out[2], out[0] + out[1]) < 1e-12
+
+
+def test_oracle_2d_runs_and_conserves_zero_y_fields():
+    p = small_params_2d(nx=32, nz=32, npmlbot=4, npmltop=4)
+    o = O.Oracle(p, table_for(p))
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((6, p.nz, 1, p.nx)) * 1e-3
+    a[1] = 0; a[4] = 0
+    o.set_state(a)
+    o.step(31)
+    s = o.state()[0]
+    assert np.all(np.isfinite(s))
+    assert np.abs(s[1]).max() == 0 and np.abs(s[4]).max() == 0
+
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "oracle_golden.npz")
+
+
+def test_oracle_reproduces_golden_fixtures():
+    from golden.make_golden import compute
+    g = np.load(GOLDEN)
+    now = compute()
+    for k in g.files:
+        assert rel_l2(now[k], g[k]) < 1e-12, k
