@@ -212,6 +212,36 @@ int sparc_gpu_info(sparc_ctx* ctx, double* info, double* ztab, double* ptab);
  * the state of any slot holds a non-finite value. */
 int sparc_gpu_sync(sparc_ctx* ctx, int check_finite);
 
+/* ---- no-allocation entry point ---------------------------------------------- */
+
+/* Spectral -> physical transform of nplanes horizontal planes that allocates
+ * nothing.  This entry point has no counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc while they run: an
+ * application whose pool already owns the rest of HBM (any further
+ * cudaMalloc fails), or an output thread that must not make cudaMalloc /
+ * cudaFree synchronise the device under solves running on other streams.
+ * The caller passes its own device buffers:
+ *   spec  nplanes x ny x (nx/2+1) complex values of the context's precision
+ *         (double2 for SPARC_FP64, float2 for SPARC_FP32), the normalised
+ *         r2c half-spectrum in which the library keeps its state
+ *         (= rfft2(plane) / (nx*ny));
+ *   phys  nplanes x ny x nx reals of the context's precision (output).
+ * The work is queued on `stream` (a cudaStream_t; NULL = the context's
+ * stream) and the call returns without waiting for it.
+ *
+ * Scratch: one fixed 32 MiB device array inside the library (held by every
+ * GPU that loads it until the process exits).  A call needing more than
+ * that -- nplanes * ny * (nx/2+1) complex values when ny > 1 -- is rejected
+ * with SPARC_EINVAL and a message giving the largest allowed nplanes; split
+ * such work over several calls.  The first call on a device looks up the
+ * array's device address with that device current, so make the first call
+ * on each device before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (different streams or threads) race and
+ * must be serialised by the caller. */
+int sparc_gpu_spec_to_phys_noalloc(sparc_ctx* ctx, const void* spec, void* phys, int nplanes,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

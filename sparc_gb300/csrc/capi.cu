@@ -197,6 +197,18 @@ template <typename T> typename CplxOf<T>::type* CP(void* p) { return (typename C
 
 }  // namespace
 
+void sparc_internal_xform_info(const sparc_ctx* c, SparcXformInfo* out) {
+    out->nx = c->P.nx;
+    out->ny = c->P.ny;
+    out->M = c->M;
+    out->f32 = c->f32;
+    out->tw_x = c->tw_x;
+    out->tw_y = c->tw_y;
+    out->stream = c->stream;
+}
+void sparc_internal_set_error(sparc_ctx* c, const std::string& msg) { c->err = msg; }
+void sparc_internal_count_launches(sparc_ctx* c, int n) { c->launches += n; }
+
 // ===========================================================================
 extern "C" {
 

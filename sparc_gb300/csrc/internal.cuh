@@ -17,6 +17,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
 
 template <typename T> struct CplxOf;
 template <> struct CplxOf<double> { typedef double2 type; };
@@ -171,6 +172,19 @@ void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::
                    const typename CplxOf<T>::type* top_plane, cudaStream_t s);
 void launch_zderiv_real(const double* zt, const Compact<double>& cc, const double* in, double* out,
                         long long n1, int nz, int bc, cudaStream_t s);
+
+// geometry of a context for the no-allocation transform (noalloc.cu)
+#define SPARC_NOALLOC_SCRATCH_BYTES (32u << 20)
+struct sparc_ctx;
+struct SparcXformInfo {
+    int nx, ny, M, f32;
+    const double* tw_x;
+    const double* tw_y;
+    cudaStream_t stream;
+};
+__attribute__((visibility("hidden"))) void sparc_internal_xform_info(const sparc_ctx* c, SparcXformInfo* out);
+__attribute__((visibility("hidden"))) void sparc_internal_set_error(sparc_ctx* c, const std::string& msg);
+__attribute__((visibility("hidden"))) void sparc_internal_count_launches(sparc_ctx* c, int n);
 
 // transforms (fft.cu)
 template <typename T>
