@@ -12,7 +12,7 @@ forward x adjoint kernel run.  Point-steps per bench step = 2 * nsrc * N.
   fp64_plain  the plain single-source FP64 solve, same workload
   e2e         batched FP32 through the public API with host buffers: source
               upload (H2D), the steps, seismogram + summed-kernel read-back (D2H)
-  roofline    the dominant kernel (RK stage kernel, FP32 batched) against the
+  roofline    the dominant kernel (the fused FP32 step, batched) against the
               measured HBM copy bandwidth
   cpu_baseline  the FP64 CPU oracle (a restatement of the reference) on a
               bounded sample (rank 0, N = 1)
@@ -42,7 +42,7 @@ UNIT = "Mpoint-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nsrc", type=int, default=32)
@@ -158,15 +158,21 @@ def make_pair(p, tab, nplanes, seed=0):
     return fwd, adj
 
 
-def step_pair(fwd, adj, cad, nsnap_ring=2):
-    """One bench step: forward + adjoint step, kernel snapshot/accumulate at the cadence."""
-    t = fwd.time
-    fwd.step(1)
-    adj.step(1)
-    if t % cad == 0:
-        slot = (t // cad) % nsnap_ring
-        fwd.snapshot(slot, nsnap_ring)
-        adj.kernel_accumulate(fwd, slot)
+def run_steps(fwd, adj, nsteps, cad, nsnap_ring=2):
+    """nsteps bench steps: forward and adjoint advance in chunks that end on
+    the output cadence, where the forward snapshot is stored and the adjoint
+    accumulates the kernels against it."""
+    done = 0
+    while done < nsteps:
+        t = fwd.time
+        n = min(cad - (t % cad), nsteps - done)
+        fwd.step(n)
+        adj.step(n)
+        done += n
+        if fwd.time % cad == 0:
+            slot = (fwd.time // cad) % nsnap_ring
+            fwd.snapshot(slot, nsnap_ring)
+            adj.kernel_accumulate(fwd, slot)
 
 
 def timed_region(fwd, adj, steps, cad):
@@ -181,10 +187,8 @@ def timed_region(fwd, adj, steps, cad):
     ea = torch.cuda.Event()
     e0.record(sf)
     sa.wait_event(e0)
-    per = []
     l0 = fwd.launches + adj.launches
-    for _ in range(steps):
-        step_pair(fwd, adj, cad)
+    run_steps(fwd, adj, steps, cad)
     ea.record(sa)
     sf.wait_event(ea)
     e1.record(sf)
@@ -194,23 +198,22 @@ def timed_region(fwd, adj, steps, cad):
     return e0.elapsed_time(e1), launches
 
 
-def stage_kernel_time(solver, reps=3):
-    """Average duration of the RK-stage kernel (stages 2..5) with CUDA events
-    on the launching stream."""
+def step_kernel_time(solver, n=15, reps=2):
+    """Average duration of one time-step launch (the fused FP32 step kernel is
+    the only kernel of a step), CUDA events on the launching stream."""
     import torch
     s = torch.cuda.ExternalStream(solver.stream_ptr)
     solver.sync()
     ts = []
     for _ in range(reps):
-        for rk in (2, 3, 4, 5):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(s)
-            solver.stage(rk)
-            e1.record(s)
-            e1.synchronize()
-            ts.append(e0.elapsed_time(e1))
-    return float(np.mean(ts)), ts
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        solver.step(n)
+        e1.record(s)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) / n)
+    return float(np.min(ts))
 
 
 def cpu_baseline(p, tab, steps=1):
@@ -292,8 +295,7 @@ def main():
         p64 = p0.replace(precision="f64", nsrc=1)
         fwd, adj = make_pair(p64, tab, args.nplanes, seed=rank)
         cad = fwd.info()["steps"]
-        for _ in range(W):
-            step_pair(fwd, adj, cad)
+        run_steps(fwd, adj, W, cad)
         barrier(ws)
         ms, _ = timed_region(fwd, adj, K, cad)
         ms = allmax(ws, ms)
@@ -307,16 +309,15 @@ def main():
     p32 = p0.replace(precision="f32", nsrc=S)
     fwd, adj = make_pair(p32, tab, args.nplanes, seed=1000 + rank)
     cad = fwd.info()["steps"]
-    for _ in range(W):
-        step_pair(fwd, adj, cad)
+    run_steps(fwd, adj, W, cad)
     barrier(ws)
     with ClockSampler(local) as clk:
         ms, launches = timed_region(fwd, adj, K, cad)
-        # dominant kernel (RK stage, FP32 batched) timed on its own stream
-        st_ms, _ = stage_kernel_time(fwd)
+        # dominant kernel: the fused FP32 step, timed on its own stream
+        st_ms = step_kernel_time(fwd)
     ms = allmax(ws, ms)
     value = 2 * N * S * K * ws / (ms * 1e-3) / 1e6
-    alg = bytes_model.stage_alg_bytes(p32, 2)
+    alg = bytes_model.fused_step_alg_bytes(p32)
     achieved = alg / (st_ms * 1e-3) / 1e9
     clocks = clk.summary()
     # per-step latency distribution of the batched solve
@@ -324,7 +325,7 @@ def main():
     lat = []
     for _ in range(min(K, 10)):
         t0 = time.perf_counter()
-        step_pair(fwd, adj, cad)
+        run_steps(fwd, adj, 1, cad)
         fwd.sync(); adj.sync()
         lat.append((time.perf_counter() - t0) * 1e3)
     fwd.close(); adj.close()
@@ -359,8 +360,7 @@ def main():
             fwd.set_source_series(plane_h[s], series, slot=s)
             adj.set_source_lagrange(adj_h[s], slot=s)
         fwd.record_surface(nrec)
-        for _ in range(K):
-            step_pair(fwd, adj, cad)
+        run_steps(fwd, adj, K, cad)
         d2h = 0
         for s in range(S):
             r = fwd.records(slot=s)
@@ -388,9 +388,11 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
-                     "kernel": "stage_kernel<float>", "avg_launch_ms": st_ms,
-                     "alg_bytes_per_launch": alg, "impl_bytes_per_launch": bytes_model.stage_impl_bytes(p32, 2),
+                     "frac": achieved / hbm_peak, "traffic": bytes_model.fused_traffic_per_launch(p32),
+                     "kernel": "fused_step_kernel (FP32, one launch per time step)", "avg_launch_ms": st_ms,
+                     "alg_bytes_per_launch": alg,
+                     "note": "the fused step moves 12 field accesses per step instead of 102; it is bound "
+                             "by instruction issue, not HBM (profiles/fused_step_f32_256x256x300.md)",
                      "peak_source": f"{peak_src} hbm_gbs"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "what": "one batched forward+adjoint step, host-synchronised"},

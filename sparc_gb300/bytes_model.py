@@ -17,6 +17,13 @@ tridiagonal intermediates y, p', rho' round-tripping through global memory):
   stage 2-5: S1 2r+1w, S2 11r+6w, S3 1r+1w, S4 4r+2w = 28;  stage 1: 21.
 The difference (10 accesses per stage) is the traffic that an on-chip schedule
 removes.
+
+The fused FP32 step (fused.cu) keeps a pencil's state on chip for the whole
+step: per step it reads a (6 fields) and writes a (6 fields), plus the PML
+planes (2 fields on nzpml planes, read + write) and one source plane per
+source; the stage right-hand side scr (6 fields) is written only on steps whose
+outputs need it.  Its algorithmic and implemented counts coincide: 12 field
+accesses per step, against 102 for the per-stage schedule.
 """
 from __future__ import annotations
 
@@ -72,3 +79,25 @@ def step_impl_bytes(p) -> int:
 
 def alg_bytes_per_point_step(p) -> float:
     return step_alg_bytes(p) / (p.points * p.nsrc)
+
+
+FUSED_STEP = 12
+
+
+def fused_step_alg_bytes(p, write_scr: bool = False) -> int:
+    """Bytes of one fused-step launch (all sources)."""
+    f = field_bytes(p)
+    pf = pml_field_bytes(p)
+    plane = (p.nx // 2 + 1) * p.ny * complex_bytes(p.precision) * p.nsrc
+    return (FUSED_STEP + (6 if write_scr else 0)) * f + 4 * pf + plane
+
+
+#: DRAM traffic (read + write) of one fused-step launch per source, measured
+#: with ncu at 256x256x300 FP32 (profiles/fused_step_f32_256x256x300.md);
+#: traffic grows in proportion to the number of sources.
+MEASURED_FUSED_TRAFFIC_PER_SOURCE = {}
+
+
+def fused_traffic_per_launch(p):
+    v = MEASURED_FUSED_TRAFFIC_PER_SOURCE.get((p.nx, p.ny, p.nz, p.precision))
+    return None if v is None else v * p.nsrc

@@ -48,6 +48,8 @@ struct sparc_ctx {
     void* a = nullptr; void* scr = nullptr; void* pml = nullptr; void* scrpml = nullptr;
     void* ybuf = nullptr; void* pbuf = nullptr; void* rbuf = nullptr;
     void* zt = nullptr; void* pt = nullptr;       // T tables
+    float* scan = nullptr;                        // fused FP32 step: scan tables [4 bc][5][nz]
+    int use_fused = 0;
     double* zt64 = nullptr; double* pt64 = nullptr;
     double* tw_x = nullptr; double* tw_y = nullptr;
     void* tmp = nullptr;          // FFT intermediate, nz*M complex T
@@ -286,6 +288,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->zt, (size_t)ZT_COUNT * c->nz * es))) return bail(rc);
     if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
     if (c->f32) {
+        c->use_fused = fused_supported(c->nz) && getenv("SPARC_FP32_PER_STAGE") == nullptr;
+        if ((rc = dalloc(c, (void**)&c->scan, (size_t)4 * 5 * c->nz * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->pt64, (size_t)PT_COUNT * c->M * 8))) return bail(rc);
     } else {
@@ -500,6 +504,28 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     }
     int rc;
     if (c->f32) {
+        // scan tables of the fused FP32 step: the LU elimination multipliers
+        // and their chunk products (chunks of FUSED_CH levels)
+        std::vector<float> sc((size_t)4 * 5 * nz, 0.f);
+        for (int b = 0; b < 4; ++b) {
+            std::vector<double> ibd(nz), mm(nz), gg(nz), HH(nz), GG(nz);
+            for (int j = 0; j < nz; ++j) {
+                ibd[j] = 1.0 / tri[b].betad[j];
+                mm[j] = (j == 0) ? 0.0 : -tri[b].low[j] / tri[b].betad[j];
+                gg[j] = (j == nz - 1) ? 0.0 : -tri[b].gam[j + 1];
+            }
+            for (int j0 = 0; j0 < nz; j0 += FUSED_CH) {
+                int j1 = std::min(nz, j0 + FUSED_CH);
+                double pr = 1.0;
+                for (int j = j0; j < j1; ++j) { pr *= mm[j]; HH[j] = pr; }
+                pr = 1.0;
+                for (int j = j1 - 1; j >= j0; --j) { pr *= gg[j]; GG[j] = pr; }
+            }
+            const std::vector<double>* rows[5] = {&ibd, &mm, &HH, &gg, &GG};
+            for (int r = 0; r < 5; ++r)
+                for (int j = 0; j < nz; ++j) sc[((size_t)b * 5 + r) * nz + j] = (float)(*rows[r])[j];
+        }
+        if ((rc = upload(c, c->scan, sc.data(), sc.size() * 4))) return rc;
         std::vector<float> zf(c->zt_host.begin(), c->zt_host.end()), pf(c->pt_host.begin(), c->pt_host.end());
         if ((rc = upload(c, c->zt, zf.data(), zf.size() * 4))) return rc;
         if ((rc = upload(c, c->pt, pf.data(), pf.size() * 4))) return rc;
@@ -766,9 +792,37 @@ static int do_steps(sparc_ctx* c, int nsteps) {
     UpdateArgs<T> U;
     make_args<T>(c, A, U);
     const bool two_d = c->P.option == 17;
+    FusedArgs Fz;
+    const bool fused = c->use_fused && sizeof(T) == 4;
+    if (fused) {
+        memset(&Fz, 0, sizeof(Fz));
+        Fz.a = (float2*)c->a; Fz.scr = (float2*)c->scr; Fz.pml = (float2*)c->pml;
+        Fz.zt = (const float*)c->zt; Fz.pt = (const float*)c->pt; Fz.scan = c->scan;
+        Fz.fs = c->fs; Fz.ps = c->ps; Fz.M = c->M; Fz.nz = c->nz; Fz.nzpml = c->nzpml;
+        Fz.npmlbot = c->P.npmlbot; Fz.npmltop = c->P.npmltop; Fz.option = c->P.option;
+        Fz.damp = A.damp; Fz.W = (c->nz + 32 * FUSED_CH - 1) / (32 * FUSED_CH);
+        for (int i = 0; i < 5; ++i) Fz.betas[i] = (float)c->betas[i];
+        Fz.dt = (float)c->deltat;
+        Fz.cc.C1 = (float)c->cc64.C1; Fz.cc.C2 = (float)c->cc64.C2;
+        for (int i = 0; i < 5; ++i) Fz.cc.Cb[i] = (float)c->cc64.Cb[i];
+        for (int i = 0; i < 4; ++i) Fz.cc.Cf[i] = (float)c->cc64.Cf[i];
+        Fz.cc.alpha2 = (float)c->cc64.alpha2; Fz.cc.beta1 = (float)c->cc64.beta1; Fz.cc.cnst = (float)c->cc64.cnst;
+        Fz.ksrc = A.ksrc; Fz.src_scale = (float)A.src_scale;
+        Fz.planes = (const float2*)c->planes; Fz.plane_ss = A.plane_ss;
+        Fz.mode = A.mode; Fz.series = A.series; Fz.nseries = A.nseries;
+    }
     for (int it = 0; it < nsteps; ++it) {
         const int time = c->time;
         set_forcing<T>(c, A);
+        if (fused) {
+            Fz.time = time; Fz.src_on = A.src_on; Fz.nw = A.nw;
+            for (int l = 0; l < 7; ++l) { Fz.widx[l] = A.widx[l]; Fz.wts[l] = (float)A.wts[l]; }
+            Fz.hfilter = two_d ? ((time + 1) % c->freq_filtering == 0) : (time % c->freq_filtering == 0);
+            Fz.write_scr = (it == nsteps - 1) ? 1 : 0;
+            launch_fused(Fz, c->S, c->stream);
+            c->launches += 1;
+            CKL();
+        } else {
         for (int rk = 0; rk < 5; ++rk) {
             A.beta = (T)c->betas[rk];
             A.has_scr = (rk > 0);
@@ -778,6 +832,7 @@ static int do_steps(sparc_ctx* c, int nsteps) {
         launch_update<T>(U, c->S, c->stream);
         c->launches += 6;
         CKL();
+        }
         if (c->rec_on && time % c->steps == 0 && c->rec_n < c->rec_max) {
             size_t cs = sizeof(CT);
             CK(cudaMemcpy2DAsync((char*)c->rec + (size_t)c->rec_n * c->M * cs, (size_t)c->rec_max * c->M * cs,

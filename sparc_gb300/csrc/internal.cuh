@@ -163,6 +163,27 @@ template <typename T> struct UpdateArgs {
     int hfilter;        // apply horizontal spectral filter this step
 };
 
+// fused FP32 step (fused.cu)
+struct FusedArgs {
+    float2* a; float2* scr; float2* pml;
+    const float* zt; const float* pt; const float* scan;
+    long long fs, ps;
+    int M, nz, nzpml, npmlbot, npmltop, option, damp, W;
+    float betas[5];
+    float dt;
+    Compact<float> cc;
+    int hfilter, write_scr;
+    int src_on, ksrc;
+    float src_scale;
+    const float2* planes; long long plane_ss;
+    int mode, nw; int widx[7]; float wts[7];
+    const double* series; int nseries; int time;
+};
+constexpr int FUSED_CH = 5;
+size_t fused_smem_bytes(int nz, int nzpml, int W);
+int fused_supported(int nz);
+void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s);
+
 // launchers (modal.cu)
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s);
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s);

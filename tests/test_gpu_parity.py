@@ -289,3 +289,48 @@ def test_gpu_matches_committed_golden_fixtures(gpu_lib):
     st2, _ = s2.state()
     for f in (0, 2, 3, 5):
         assert rel_l2(st2[f], g["step31_2d_a"][f]) < TOL64, f
+
+
+@pytest.mark.parametrize("two_d", [False, True])
+def test_fused_fp32_step_matches_fp64(gpu_lib, oracle_mod, two_d):
+    """The fused FP32 step (state on chip, scan-based tridiagonal solves)
+    against the FP64 path: FP32 round-off only."""
+    from sparc_gb300.solver import Solver
+    p64 = small_params_2d() if two_d else small_params()
+    p32 = p64.replace(precision="f32")
+    tab = table_for(p64)
+    a0, pml0 = random_state(p64)
+    pml0[1, 0] = 0.0
+    plane = gaussian_plane(p64)
+    series = oracle_mod.forward_source(p64, 200) * 1e3
+    out = []
+    for p in (p64, p32):
+        g = Solver(p, tab)
+        g.set_state(a0, pml0)
+        g.set_source_series(plane, series)
+        g.step(37)                     # crosses the horizontal-filter steps
+        a, pml = g.state()
+        out.append((a, pml, np.stack([g.field(f) for f in range(6, 12)])))
+    (a64, pml64, s64), (a32, pml32, s32) = out
+    fields = (0, 2, 3, 5) if two_d else range(6)
+    for f in fields:
+        assert rel_l2(a32[f], a64[f]) < 2e-5, (f, rel_l2(a32[f], a64[f]))
+        assert rel_l2(s32[f], s64[f]) < 2e-4, (f, rel_l2(s32[f], s64[f]))
+    assert rel_l2(pml32, pml64) < 2e-5
+
+
+def test_fused_fp32_lagrange_source_matches_fp64(gpu_lib):
+    from sparc_gb300.solver import Solver
+    p64 = small_params(compute_forward=False, compute_adjoint=True)
+    tab = table_for(p64)
+    planes = np.random.default_rng(3).standard_normal((12, p64.ny, p64.nx)) * 1e-4
+    res = []
+    for p in (p64, p64.replace(precision="f32", nsrc=2)):
+        g = Solver(p, tab)
+        for s in range(p.nsrc):
+            g.set_source_lagrange(planes * (s + 1), slot=s)
+        g.step(40)
+        res.append([g.state(slot=s)[0] for s in range(p.nsrc)])
+    for f in range(6):
+        assert rel_l2(res[1][0][f], res[0][0][f]) < 2e-5, f
+        assert rel_l2(res[1][1][f], 2 * res[0][0][f]) < 2e-5, f
