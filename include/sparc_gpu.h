@@ -156,6 +156,14 @@ int sparc_gpu_get_records(sparc_ctx* ctx, int src_idx, double* host, int* nrec);
 int sparc_gpu_checkpoint(sparc_ctx* ctx, const char* path);
 int sparc_gpu_restore(sparc_ctx* ctx, const char* path);
 
+/* Device-resident copies of the whole state (a, PML auxiliaries, time index)
+ * of every slot, in `capacity` slots allocated by the first save; used to
+ * recompute forward segments in reverse order for the kernel integral,
+ * whose forward and adjoint snapshots pair in reversed time
+ * (kernels.f90:203,241).  Loading clears scr. */
+int sparc_gpu_save_device(sparc_ctx* ctx, int idx, int capacity);
+int sparc_gpu_load_device(sparc_ctx* ctx, int idx);
+
 /* ---- sensitivity kernels (kernels.f90:197-311, 523-539) ------------------- */
 
 /* The forward-snapshot store: saves the spectral quantities that the kernel
@@ -166,7 +174,9 @@ int sparc_gpu_snapshot(sparc_ctx* fwd, int snap, int nsnap);
 
 /* One accumulation of kernels.f90:276-311 for every slot: forward snapshot
  * `snap` of `fwd` against the current state of adjoint context `adj`.
- * Accumulators are FP64 and live in `adj`. */
+ * Accumulators are FP64 and live in `adj`.  The two contexts' streams are
+ * ordered by events: the accumulation waits for the snapshot, and later work
+ * on `fwd` waits for the accumulation (so the store slot may be reused). */
 int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* adj);
 
 /* Resets the accumulators of `adj`. */

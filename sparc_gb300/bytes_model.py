@@ -95,7 +95,7 @@ def fused_step_alg_bytes(p, write_scr: bool = False) -> int:
 #: DRAM traffic (read + write) of one fused-step launch per source, measured
 #: with ncu at 256x256x300 FP32 (profiles/fused_step_f32_256x256x300.md);
 #: traffic grows in proportion to the number of sources.
-MEASURED_FUSED_TRAFFIC_PER_SOURCE = {}
+MEASURED_FUSED_TRAFFIC_PER_SOURCE = {(256, 256, 300, "f32"): 921.7e6}
 
 
 def fused_traffic_per_launch(p):

@@ -29,6 +29,7 @@ struct sparc_ctx {
     long long fs, ps, NP, N;
     int f32;
     cudaStream_t stream = nullptr;
+    cudaEvent_t ev_done = nullptr;     // last cross-context hand-off on this stream
     std::string err;
     long long launches = 0;
     long long dev_bytes = 0;
@@ -73,6 +74,9 @@ struct sparc_ctx {
     int rec_on = 0, rec_max = 0, rec_n = 0;
     void* rec = nullptr;          // [S][rec_max][M] CT
 
+    // device-resident checkpoints (a + PML + time of every slot)
+    void* dck = nullptr; int dck_n = 0;
+    std::vector<int> dck_time;
     // kernels
     void* store = nullptr; int store_n = 0;     // [nsnap][S][7][N] T
     double* kacc = nullptr;                     // [S][3][N]
@@ -271,8 +275,10 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     c->f32 = (p->precision == SPARC_FP32);
     int rc = SPARC_OK;
     auto bail = [&](int code) { sparc_gpu_destroy(c); return code; };
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
+        if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return SPARC_ECUDA;
     }
@@ -324,6 +330,7 @@ void sparc_gpu_destroy(sparc_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : c->allocs) cudaFree(p);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -1098,8 +1105,10 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
     if (fwd->S != c->S || fwd->N != c->N || fwd->f32 != c->f32) return fail(c, SPARC_EINVAL, "forward/adjoint contexts differ");
     if (!c->kacc) { int rc = sparc_gpu_kernel_reset(c); if (rc) return rc; }
     if (!c->ktemp) { int rc = dalloc(c, &c->ktemp, (size_t)7 * c->N * esz(c)); if (rc) return rc; }
-    // the forward store is written on the forward context's stream
-    CK(cudaStreamSynchronize(fwd->stream));
+    // the forward snapshot is written on the forward context's stream: the
+    // adjoint stream waits for it (no host synchronisation)
+    CK(cudaEventRecord(fwd->ev_done, fwd->stream));
+    CK(cudaStreamWaitEvent(c->stream, fwd->ev_done, 0));
     for (int s = 0; s < c->S; ++s) {
         const char* f7 = (const char*)fwd->store + ((size_t)snap * c->S + s) * 7 * c->N * esz(c);
         double* acc = c->kacc + (size_t)s * 3 * c->N;
@@ -1116,6 +1125,10 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
         c->launches++;
         CKL();
     }
+    // later forward work (new snapshots into the same store slots) waits for
+    // these reads of the store
+    CK(cudaEventRecord(c->ev_done, c->stream));
+    CK(cudaStreamWaitEvent(fwd->stream, c->ev_done, 0));
     return SPARC_OK;
 }
 
@@ -1143,6 +1156,42 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     cudaFree(out);
     c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)out), c->allocs.end());
     c->dev_bytes -= (long long)3 * c->N * 8;
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device-resident checkpoints (checkpointed recomputation of the forward run)
+// ---------------------------------------------------------------------------
+int sparc_gpu_save_device(sparc_ctx* c, int idx, int capacity) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    if (!c->dck) {
+        if (capacity < 1) return fail(c, SPARC_EINVAL, "capacity < 1");
+        int rc = dalloc(c, &c->dck, (size_t)capacity * (na + np));
+        if (rc) return rc;
+        c->dck_n = capacity;
+        c->dck_time.assign(capacity, -1);
+    }
+    if (idx < 0 || idx >= c->dck_n) return fail(c, SPARC_EINVAL, "device checkpoint index out of range");
+    char* dst = (char*)c->dck + (size_t)idx * (na + np);
+    CK(cudaMemcpyAsync(dst, c->a, na, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(dst + na, c->pml, np, cudaMemcpyDeviceToDevice, c->stream));
+    c->dck_time[idx] = c->time;
+    return SPARC_OK;
+}
+
+int sparc_gpu_load_device(sparc_ctx* c, int idx) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->dck || idx < 0 || idx >= c->dck_n || c->dck_time[idx] < 0)
+        return fail(c, SPARC_EINVAL, "no such device checkpoint");
+    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    const char* src = (const char*)c->dck + (size_t)idx * (na + np);
+    CK(cudaMemcpyAsync(c->a, src, na, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->pml, src + na, np, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemsetAsync(c->scr, 0, na, c->stream));
+    CK(cudaMemsetAsync(c->scrpml, 0, np, c->stream));
+    c->time = c->dck_time[idx];
     return SPARC_OK;
 }
 

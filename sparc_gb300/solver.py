@@ -182,6 +182,12 @@ class Solver:
     def restore(self, path: str):
         self._ck(self.L.sparc_gpu_restore(self.h, path.encode()))
 
+    def save_device(self, idx: int, capacity: int):
+        self._ck(self.L.sparc_gpu_save_device(self.h, int(idx), int(capacity)))
+
+    def load_device(self, idx: int):
+        self._ck(self.L.sparc_gpu_load_device(self.h, int(idx)))
+
     # ---- primitives ----
     def ddx(self, v):
         v = _f64(v); d = np.zeros_like(v)

@@ -99,3 +99,15 @@ def test_byte_model():
     assert bytes_model.stage_alg_bytes(p, 2) == 18 * f + 6 * bytes_model.pml_field_bytes(p)
     per_pt = bytes_model.alg_bytes_per_point_step(p)
     assert 405 < per_pt < 425
+
+
+def test_compute_tt_recovers_a_shift():
+    from sparc_gb300.pipeline import compute_tt
+    dt = 30.0
+    t = np.arange(256) * dt
+    w = lambda tt: np.cos(2 * np.pi * 3e-3 * (tt - 3000)) * np.exp(-((tt - 3000) / 600.0) ** 2)
+    u0 = w(t)
+    for shift in (0.0, 12.0, -47.0, 95.0):
+        tau = compute_tt(u0, w(t - shift), dt)
+        assert abs(tau - shift) < 2.0, (shift, tau)
+    assert abs(compute_tt(u0, u0, dt)) < 1e-6
