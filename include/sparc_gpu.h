@@ -145,14 +145,30 @@ int sparc_gpu_set_state(sparc_ctx* ctx, int src_idx, const double* a, const doub
 int sparc_gpu_get_state(sparc_ctx* ctx, int src_idx, double* a, double* pml);
 
 /* Surface seismogram recording (the vz_cc.bin stream, driver.f90:455-476):
- * enable with room for max_records outputs per slot; fetch them as
- * (nrec,ny,nx) FP64 records, the layout of write_binary_seq_2D
- * (all_modules.f90:947-1006). */
+ * enable with room for max_records outputs per slot; record r of a slot is vz
+ * at o_rad after the step at slot time r*steps.  Fetch them as (nrec,ny,nx)
+ * FP64 records, the layout of write_binary_seq_2D (all_modules.f90:947-1006);
+ * nrec counts the outputs the slot has reached so far. */
 int sparc_gpu_record_surface(sparc_ctx* ctx, int enable, int max_records);
 int sparc_gpu_get_records(sparc_ctx* ctx, int src_idx, double* host, int* nrec);
 
+/* ---- continuous batching ---------------------------------------------------- */
+
+/* Every slot runs its own clock, slot time = context time - (context time at
+ * its last reset).  The source series index, LAGRANGE_INTERP, the horizontal
+ * filter cadence and the output cadence follow the slot time, so a request
+ * admitted into a free slot of a running batch starts at time 0 while sharing
+ * the batch's launches.  slot_reset clears the slot's state, PML, scr and
+ * records and restarts its clock at 0; its source stays as set. */
+int sparc_gpu_slot_reset(sparc_ctx* ctx, int src_idx);
+int sparc_gpu_slot_time(const sparc_ctx* ctx, int src_idx, int* slot_time);
+
+/* Only slots 0..nactive-1 are stepped (default: all). */
+int sparc_gpu_set_active(sparc_ctx* ctx, int nactive);
+
 /* Checkpoint / restore of every slot (state, PML, time) to one file with a
- * checksum; restore rejects a corrupt or mismatching file with SPARC_EIO. */
+ * checksum; restore rejects a corrupt or mismatching file with SPARC_EIO.
+ * A restore restarts every slot clock at the restored time index. */
 int sparc_gpu_checkpoint(sparc_ctx* ctx, const char* path);
 int sparc_gpu_restore(sparc_ctx* ctx, const char* path);
 

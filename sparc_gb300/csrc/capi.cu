@@ -68,11 +68,14 @@ struct sparc_ctx {
     double* series = nullptr;     // [S][nseries]
     int nseries = 0;
     std::vector<int> src_set;
-    int last_nw = 0; int last_widx[7]; double last_wts[7];
 
     // surface records
-    int rec_on = 0, rec_max = 0, rec_n = 0;
-    void* rec = nullptr;          // [S][rec_max][M] CT
+    int rec_on = 0, rec_max = 0;
+    void* rec = nullptr;          // [S][rec_max][M] CT, record r = output at slot time r*steps
+    // per-slot clocks (continuous batching)
+    int* d_t0 = nullptr;          // [S] device copy
+    std::vector<int> t0;          // slot time = time - t0[slot]
+    int active_n = 0;             // slots 0..active_n-1 are stepped
 
     // device-resident checkpoints (a + PML + time of every slot)
     void* dck = nullptr; int dck_n = 0;
@@ -308,6 +311,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->phys, (size_t)c->N * es))) return bail(rc);
     if ((rc = dalloc(c, (void**)&c->phys64, (size_t)c->N * 8))) return bail(rc);
     if ((rc = dalloc(c, (void**)&c->d_flag, 16))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->d_t0, (size_t)c->S * sizeof(int)))) return bail(rc);
+    c->t0.assign(c->S, 0);
+    c->active_n = c->S;
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
@@ -550,7 +556,9 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     CK(cudaMemsetAsync(c->scrpml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->time = 0;
-    c->rec_n = 0;
+    c->t0.assign(c->S, 0);
+    CK(cudaMemsetAsync(c->d_t0, 0, (size_t)c->S * sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     c->have_bg = true;
     return SPARC_OK;
 }
@@ -721,29 +729,6 @@ int sparc_gpu_set_source(sparc_ctx* c, int src, int mode, const double* planes, 
     return SPARC_OK;
 }
 
-// LAGRANGE_INTERP weights (physics.f90:683-734) at the current time
-static void lagrange_weights(sparc_ctx* c, int& nw, int* widx, double* wts) {
-    double ts = R4(c->P.timestep), cad = R4(c->P.cadforcing);
-    double xt = (double)c->time * ts / cad;
-    int time1 = (int)std::floor(xt) + 1;
-    xt = c->time * ts;
-    double X[7];
-    for (int l = 0; l < 7; ++l) X[l] = (double)(time1 - 4 + l) * cad;
-    bool cond[7] = {X[0] >= 0, X[1] >= 0, X[2] >= 0, X[3] >= 0, true, time1 < c->num_steps, time1 < c->num_steps - 1};
-    nw = 0;
-    for (int l = 0; l < 7; ++l) {
-        if (!cond[l]) continue;
-        int idx = time1 - 4 + l;            // vr(:,:,time1-3+l), 0-based
-        if (idx < 0 || idx >= c->src_L) continue;
-        double den = 1.0, num = 1.0;
-        for (int r = 0; r < 7; ++r)
-            if (r != l) { den *= (X[l] - X[r]); num *= (xt - X[r]); }
-        widx[nw] = idx;
-        wts[nw] = num / den;
-        nw++;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // time stepping
 // ---------------------------------------------------------------------------
@@ -766,30 +751,25 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.ksrc = ksrc - 1;
     A.src_scale = (T)(c->delta_width / c->zt_host[ZT_RHO0 * c->nz + ksrc - 1]);
     A.planes = CP<T>(c->planes); A.plane_ss = (long long)c->src_L * c->M; A.L = c->src_L;
-    A.mode = c->src_mode; A.series = c->series; A.nseries = c->nseries;
+    A.src_mode = c->src_mode; A.series = c->series; A.nseries = c->nseries;
+    A.clk.t0 = c->d_t0;
+    A.clk.freq = c->freq_filtering;
+    A.clk.two_d = (P.option == 17);
+    A.clk.gate = c->forcing_length * c->cadforcing_step;
+    A.clk.num_steps = c->num_steps;
+    A.clk.ts = R4(P.timestep);
+    A.clk.cad = R4(P.cadforcing);
     U.a = A.a; U.scr = A.scr; U.pml = A.pml; U.scrpml = A.scrpml; U.pt = A.pt;
     U.fs = c->fs; U.ps = c->ps; U.M = c->M; U.nz = c->nz; U.nzpml = c->nzpml; U.option = P.option;
     U.dt = (T)c->deltat;
+    U.clk = A.clk;
 }
 
-// forcing of the step at c->time (driver.f90:419-422; physics2d.f90:1059)
+// forcing of the step at c->time: the kernels evaluate the source of every
+// slot on its own clock (series index / LAGRANGE_INTERP / 2-D gate)
 template <typename T>
 static void set_forcing(sparc_ctx* c, StageArgs<T>& A) {
-    const bool two_d = c->P.option == 17;
-    const int time = c->time;
-    A.time = time;
-    A.src_on = 0;
-    if (c->src_mode != 0) {
-        bool gate = !two_d || time <= c->forcing_length * c->cadforcing_step;
-        A.src_on = gate ? 1 : 0;
-        if (c->src_mode == SPARC_SRC_LAGRANGE) {
-            if (time <= c->forcing_length * c->cadforcing_step) {
-                lagrange_weights(c, c->last_nw, c->last_widx, c->last_wts);
-            }   // else: forcing keeps its last value (driver.f90:421-422)
-            A.nw = c->last_nw;
-            for (int l = 0; l < A.nw; ++l) { A.widx[l] = c->last_widx[l]; A.wts[l] = (T)c->last_wts[l]; }
-        }
-    }
+    A.clk.time = c->time;
 }
 
 template <typename T>
@@ -798,7 +778,6 @@ static int do_steps(sparc_ctx* c, int nsteps) {
     StageArgs<T> A;
     UpdateArgs<T> U;
     make_args<T>(c, A, U);
-    const bool two_d = c->P.option == 17;
     FusedArgs Fz;
     const bool fused = c->use_fused && sizeof(T) == 4;
     if (fused) {
@@ -815,38 +794,35 @@ static int do_steps(sparc_ctx* c, int nsteps) {
         for (int i = 0; i < 4; ++i) Fz.cc.Cf[i] = (float)c->cc64.Cf[i];
         Fz.cc.alpha2 = (float)c->cc64.alpha2; Fz.cc.beta1 = (float)c->cc64.beta1; Fz.cc.cnst = (float)c->cc64.cnst;
         Fz.ksrc = A.ksrc; Fz.src_scale = (float)A.src_scale;
-        Fz.planes = (const float2*)c->planes; Fz.plane_ss = A.plane_ss;
-        Fz.mode = A.mode; Fz.series = A.series; Fz.nseries = A.nseries;
+        Fz.planes = (const float2*)c->planes; Fz.plane_ss = A.plane_ss; Fz.L = A.L;
+        Fz.src_mode = A.src_mode; Fz.series = A.series; Fz.nseries = A.nseries;
+        Fz.clk = A.clk;
     }
     for (int it = 0; it < nsteps; ++it) {
         const int time = c->time;
         set_forcing<T>(c, A);
         if (fused) {
-            Fz.time = time; Fz.src_on = A.src_on; Fz.nw = A.nw;
-            for (int l = 0; l < 7; ++l) { Fz.widx[l] = A.widx[l]; Fz.wts[l] = (float)A.wts[l]; }
-            Fz.hfilter = two_d ? ((time + 1) % c->freq_filtering == 0) : (time % c->freq_filtering == 0);
+            Fz.clk.time = time;
             Fz.write_scr = (it == nsteps - 1) ? 1 : 0;
-            launch_fused(Fz, c->S, c->stream);
+            launch_fused(Fz, c->active_n, c->stream);
             c->launches += 1;
             CKL();
         } else {
         for (int rk = 0; rk < 5; ++rk) {
             A.beta = (T)c->betas[rk];
             A.has_scr = (rk > 0);
-            launch_stage<T>(A, c->S, c->stream);
+            launch_stage<T>(A, c->active_n, c->stream);
         }
-        U.hfilter = two_d ? ((time + 1) % c->freq_filtering == 0) : (time % c->freq_filtering == 0);
-        launch_update<T>(U, c->S, c->stream);
+        U.clk.time = time;
+        launch_update<T>(U, c->active_n, c->stream);
         c->launches += 6;
         CKL();
         }
-        if (c->rec_on && time % c->steps == 0 && c->rec_n < c->rec_max) {
-            size_t cs = sizeof(CT);
-            CK(cudaMemcpy2DAsync((char*)c->rec + (size_t)c->rec_n * c->M * cs, (size_t)c->rec_max * c->M * cs,
-                                 (const char*)c->a + ((size_t)5 * c->fs + (size_t)(c->o_rad - 1) * c->M) * cs,
-                                 (size_t)6 * c->fs * cs, (size_t)c->M * cs, (size_t)c->S, cudaMemcpyDeviceToDevice,
-                                 c->stream));
-            c->rec_n++;
+        if (c->rec_on) {
+            launch_record<T>(CP<T>(c->a), CP<T>(c->rec), c->d_t0, time, c->steps, c->rec_max, c->fs, c->M,
+                             c->o_rad - 1, c->active_n, c->stream);
+            c->launches++;
+            CKL();
         }
         c->time++;
     }
@@ -872,7 +848,7 @@ static int stage_only(sparc_ctx* c, int rk) {
     set_forcing<T>(c, A);
     A.beta = (T)c->betas[rk - 1];
     A.has_scr = (rk > 1);
-    launch_stage<T>(A, c->S, c->stream);
+    launch_stage<T>(A, c->active_n, c->stream);
     c->launches++;
     CKL();
     return SPARC_OK;
@@ -928,22 +904,62 @@ int sparc_gpu_record_surface(sparc_ctx* c, int enable, int max_records) {
         if (rc) return rc;
         c->rec_max = max_records;
     }
+    CK(cudaMemsetAsync(c->rec, 0, (size_t)c->S * c->rec_max * c->M * csz(c), c->stream));
     c->rec_on = 1;
-    c->rec_n = 0;
     return SPARC_OK;
+}
+
+// records written so far for a slot: outputs at slot times 0, steps, 2*steps, ... < slot time
+static int slot_nrec(const sparc_ctx* c, int src) {
+    const int lt = c->time - c->t0[src];
+    if (lt <= 0 || !c->rec) return 0;
+    return std::min(c->rec_max, (lt - 1) / c->steps + 1);
 }
 
 int sparc_gpu_get_records(sparc_ctx* c, int src, double* host, int* nrec) {
     if (!c || !nrec) return SPARC_EINVAL;
     if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
-    *nrec = c->rec_n;
-    if (!host || c->rec_n == 0) return SPARC_OK;
+    const int n_rec = slot_nrec(c, src);
+    *nrec = n_rec;
+    if (!host || n_rec == 0) return SPARC_OK;
     const char* base = (const char*)c->rec + (size_t)src * c->rec_max * c->M * csz(c);
-    for (int r0 = 0; r0 < c->rec_n; r0 += c->nz) {
-        int n = std::min(c->nz, c->rec_n - r0);
+    for (int r0 = 0; r0 < n_rec; r0 += c->nz) {
+        int n = std::min(c->nz, n_rec - r0);
         int rc = from_spec(c, base + (size_t)r0 * c->M * csz(c), host + (size_t)r0 * c->NP, n);
         if (rc) return rc;
     }
+    return SPARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// continuous batching: per-slot clocks and the active-slot bound
+// ---------------------------------------------------------------------------
+int sparc_gpu_slot_reset(sparc_ctx* c, int src) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
+    const size_t cs = csz(c);
+    CK(cudaMemsetAsync(field_ptr(c, c->a, src, 0, c->fs), 0, 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync((char*)c->pml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
+    CK(cudaMemsetAsync((char*)c->scrpml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
+    if (c->rec) CK(cudaMemsetAsync((char*)c->rec + (size_t)src * c->rec_max * c->M * cs, 0, (size_t)c->rec_max * c->M * cs, c->stream));
+    c->t0[src] = c->time;
+    CK(cudaMemcpyAsync(c->d_t0 + src, &c->t0[src], sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+int sparc_gpu_slot_time(const sparc_ctx* c, int src, int* local_time) {
+    if (!c || !local_time || src < 0 || src >= c->S) return SPARC_EINVAL;
+    *local_time = c->time - c->t0[src];
+    return SPARC_OK;
+}
+
+int sparc_gpu_set_active(sparc_ctx* c, int nactive) {
+    if (!c) return SPARC_EINVAL;
+    if (nactive < 1 || nactive > c->S) return fail(c, SPARC_EINVAL, "nactive out of range");
+    c->active_n = nactive;
     return SPARC_OK;
 }
 
@@ -1261,6 +1277,8 @@ int sparc_gpu_restore(sparc_ctx* c, const char* path) {
     CK(cudaMemcpyAsync(c->pml, buf.data() + na, np, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->scr, 0, na, c->stream));
     CK(cudaMemsetAsync(c->scrpml, 0, np, c->stream));
+    c->t0.assign(c->S, 0);
+    CK(cudaMemsetAsync(c->d_t0, 0, (size_t)c->S * sizeof(int), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->time = h.time;
     return SPARC_OK;

@@ -209,7 +209,9 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     float2* ptile = xch + P * nz;                        // [2][nzpml][P]
     Aff* wbuf = (Aff*)(ptile + 2 * A.nzpml * P + 2);     // [P][W]
     float* zs = (float*)(wbuf + P * A.W);                // [ZS_COUNT][nz] z tables
-    float2* spt = (float2*)(zs + ZS_COUNT * nz + 2);     // [2][nzpml][P] PML right-hand sides
+    double* lagw = (double*)(zs + ((ZS_COUNT * nz + 1) & ~1));   // [8] Lagrange weights of this slot
+    int* lagi = (int*)(lagw + 8);                                 // [8]: idx[7], count
+    float2* spt = (float2*)(lagi + 8);                    // [2][nzpml][P] PML right-hand sides
     float2* rl = spt + 2 * nzpml_ * P;                   // [P][nz] rho' line
     const int pi = threadIdx.x / TP;                     // pencil within the CTA
     const int t = threadIdx.x - pi * TP;                 // chunk index
@@ -222,7 +224,6 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     float2* xp = xch + pi * nz;
     Aff* wb = wbuf + pi * W;
     const float* zt = A.zt;
-    const float* scan = A.scan;
     float2* gA = A.a + (long long)s * 6 * fs;
     float2* gS = A.scr + (long long)s * 6 * fs;
     float2* gP = A.pml + (long long)s * 2 * A.ps;
@@ -249,6 +250,15 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     for (int r = threadIdx.x; r < 2 * nzpml; r += nthr) {
         const float2* src = gP + (long long)r * M + m0;
         for (int q = 0; q < P; ++q) ptile[r * P + q] = (m0 + q < M) ? src[q] : make_float2(0.f, 0.f);
+    }
+    const int tl = A.clk.time - A.clk.t0[s];            // this slot's clock
+    const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
+    if (threadIdx.x == 0 && src_on && A.src_mode == 2) {
+        int idx[7];
+        double w[7];
+        const int n = lagrange_dev(A.clk, tl, A.L, idx, w);
+        for (int l = 0; l < 7; ++l) { lagw[l] = l < n ? w[l] : 0.0; lagi[l] = l < n ? idx[l] : 0; }
+        lagi[7] = n;
     }
     {
         const bool o3 = (A.option == 4);
@@ -279,15 +289,16 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     const int nb = A.npmlbot, nt = A.npmltop;
     // forcing of this step for this mode
     float2 F = make_float2(0.f, 0.f);
-    if (A.src_on && mvalid) {
+    if (src_on && mvalid) {
         const float2* pl = A.planes + (long long)s * A.plane_ss + m;
-        if (A.mode == 1) {
-            float w = (A.time < A.nseries) ? (float)A.series[(long long)s * A.nseries + A.time] : 0.f;
+        if (A.src_mode == 1) {
+            float w = (tl < A.nseries) ? (float)A.series[(long long)s * A.nseries + tl] : 0.f;
             F = w * pl[0];
         } else {
+            const int nw = lagi[7];
             #pragma unroll
             for (int l = 0; l < 7; ++l)
-                if (l < A.nw) F = F + A.wts[l] * pl[(long long)A.widx[l] * M];
+                if (l < nw) F = F + (float)lagw[l] * pl[(long long)lagi[l] * M];
         }
     }
 
@@ -397,7 +408,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
                 const float2 rh = rl[pi * nz + j];
                 if (opt3d) { rv = -ri * d; rv = rv - (gz * ri) * rh; }
                 else rv = -ri * (d + gz * rh);
-                if (A.src_on && j == A.ksrc) rv = rv + A.src_scale * F;
+                if (src_on && j == A.ksrc) rv = rv + A.src_scale * F;
                 if (A.damp) rv = rv - gd * vz;
                 const bool zero_row = opt3d ? (j == 0 || j == nz - 1) : (j == 0);
                 if (zero_row) { rv = make_float2(0.f, 0.f); vz = make_float2(0.f, 0.f); }
@@ -434,7 +445,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     const float h4 = 0.5f * -0.01953125f, h5 = 0.5f * 0.001953125f, c0 = 0.75390625f;
     #pragma unroll
     for (int f = 0; f < 6; ++f) {
-        const bool hfil = A.hfilter && (opt3d ? (f < 5) : true);
+        const bool hfil = slot_hfilter(A.clk, tl) && (opt3d ? (f < 5) : true);
         float2 out[CH];
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
@@ -504,7 +515,8 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
 
 size_t fused_smem_bytes(int nz, int nzpml, int W) {
     return (size_t)(6 * nz * P + P * nz + 2 * nzpml * P + 2) * sizeof(float2) + (size_t)P * W * sizeof(Aff) +
-           (size_t)ZS_COUNT * nz * sizeof(float) + (size_t)(2 + 2 * nzpml * P + P * nz) * sizeof(float2) + 16;
+           (size_t)(ZS_COUNT * nz + 2) * sizeof(float) + 8 * sizeof(double) + 8 * sizeof(int) +
+           (size_t)(2 + 2 * nzpml * P + P * nz) * sizeof(float2) + 16;
 }
 
 int fused_supported(int nz) { return nz <= 2 * 32 * CH; }

@@ -133,6 +133,58 @@ __device__ __forceinline__ void zfilter_stream(int nz, int mode, Load val, Emit 
     }
 }
 
+// ---- per-slot clocks (continuous batching) -------------------------------------
+// Every source slot runs its own time index tl = time - t0[slot]: the source
+// time series, LAGRANGE_INTERP, the horizontal-filter cadence and the output
+// cadence all follow tl, so a request admitted into a free slot of a running
+// batch starts at its own time 0 while sharing the batch's launches.
+struct SlotClock {
+    const int* t0;      // per-slot start (context time index at which the slot's clock read 0)
+    int time;           // context time index of the step being taken
+    int freq;           // freq_filtering (driver.f90:270)
+    int two_d;          // option 17 cadence/gating rules
+    int gate;           // forcing_length * cadforcing_step (driver.f90:421, physics2d.f90:1059)
+    int num_steps;      // num_steps of LAGRANGE_INTERP (driver.f90:280-281)
+    double ts, cad;     // timestep, cadforcing (REAL*4-rounded)
+};
+
+__device__ __forceinline__ bool slot_hfilter(const SlotClock& k, int tl) {
+    // FILTER_VARS_3D: mod(time, freq) = 0 (physics.f90:791); FILTER_VARS_2D: mod(time+1, freq) = 0 (physics2d.f90:566)
+    return tl >= 0 && (k.two_d ? ((tl + 1) % k.freq == 0) : (tl % k.freq == 0));
+}
+__device__ __forceinline__ bool slot_src_on(const SlotClock& k, int tl) {
+    return tl >= 0 && (!k.two_d || tl <= k.gate);
+}
+// LAGRANGE_INTERP (physics.f90:683-734) at local time tl: the weights of
+// vr(:,:,time1-3+l) (returned 0-based in idx), at most 7.  In 3-D the forcing
+// is not re-interpolated after the gate (driver.f90:421-422), i.e. it keeps the
+// value it had at the gate.
+__device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, int* idx, double* w) {
+    int t = tl;
+    if (!k.two_d && t > k.gate) t = k.gate;
+    double xt = (double)t * k.ts / k.cad;
+    const int time1 = (int)floor(xt) + 1;
+    xt = t * k.ts;
+    double X[7];
+    #pragma unroll
+    for (int l = 0; l < 7; ++l) X[l] = (double)(time1 - 4 + l) * k.cad;
+    int n = 0;
+    #pragma unroll
+    for (int l = 0; l < 7; ++l) {
+        bool cond = (l <= 3) ? (X[l] >= 0) : (l == 4 ? true : (l == 5 ? time1 < k.num_steps : time1 < k.num_steps - 1));
+        const int id = time1 - 4 + l;
+        if (!cond || id < 0 || id >= L) continue;
+        double den = 1.0, num = 1.0;
+        #pragma unroll
+        for (int r = 0; r < 7; ++r)
+            if (r != l) { den *= (X[l] - X[r]); num *= (xt - X[r]); }
+        idx[n] = id;
+        w[n] = num / den;
+        ++n;
+    }
+    return n;
+}
+
 // ---- argument blocks ----------------------------------------------------------
 template <typename T> struct StageArgs {
     typedef typename CplxOf<T>::type CT;
@@ -145,12 +197,11 @@ template <typename T> struct StageArgs {
     T beta;
     Compact<T> cc;
     // source injection at plane ksrc (0-based)
-    int src_on, ksrc;
+    int src_mode, ksrc;         // 0 none, 1 series, 2 Lagrange
     T src_scale;                // delta_width / rho0(ksrc)
     const CT* planes; long long plane_ss; int L;
-    int mode;                   // 1 series, 2 Lagrange
-    int nw; int widx[7]; T wts[7];
-    const double* series; int nseries; int time;
+    const double* series; int nseries;
+    SlotClock clk;
 };
 
 template <typename T> struct UpdateArgs {
@@ -160,7 +211,7 @@ template <typename T> struct UpdateArgs {
     long long fs, ps;
     int M, nz, nzpml, option;
     T dt;
-    int hfilter;        // apply horizontal spectral filter this step
+    SlotClock clk;      // the horizontal filter follows each slot's clock
 };
 
 // fused FP32 step (fused.cu)
@@ -172,12 +223,12 @@ struct FusedArgs {
     float betas[5];
     float dt;
     Compact<float> cc;
-    int hfilter, write_scr;
-    int src_on, ksrc;
+    int write_scr;
+    int src_mode, ksrc;
     float src_scale;
-    const float2* planes; long long plane_ss;
-    int mode, nw; int widx[7]; float wts[7];
-    const double* series; int nseries; int time;
+    const float2* planes; long long plane_ss; int L;
+    const double* series; int nseries;
+    SlotClock clk;
 };
 constexpr int FUSED_CH = 5;
 size_t fused_smem_bytes(int nz, int nzpml, int W);
@@ -187,6 +238,10 @@ void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s);
 // launchers (modal.cu)
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s);
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s);
+// surface record of vz at plane kplane for every slot whose clock is on the output cadence
+template <typename T>
+void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, int time, int steps,
+                   int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s);
 template <typename T>
 void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,
                    typename CplxOf<T>::type* out, long long n1, int nz, int bc, int filter,

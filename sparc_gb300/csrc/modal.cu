@@ -116,15 +116,22 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs<T> A) {
     // ---------------- S4: back substitution, RHS v_z, xi_z -------------------
     {
         const T* gam = zt + (ZT_TH + 3 * bcp + 2) * nz;
-        // forcing of this step for this mode
+        // forcing of this step for this mode, on this slot's clock
         CT F = czero<CT>();
-        if (A.src_on) {
+        const int tl = A.clk.time - A.clk.t0[s];
+        const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
+        if (src_on) {
             const CT* pl = A.planes + (long long)s * A.plane_ss + m;
-            if (A.mode == 1) {
-                T w = (A.time < A.nseries) ? (T)A.series[(long long)s * A.nseries + A.time] : (T)0;
+            if (A.src_mode == 1) {
+                T w = (tl < A.nseries) ? (T)A.series[(long long)s * A.nseries + tl] : (T)0;
                 F = w * pl[0];
             } else {
-                for (int l = 0; l < A.nw; ++l) F = F + A.wts[l] * pl[(long long)A.widx[l] * M];
+                int idx[7];
+                double w[7];
+                const int nw = lagrange_dev(A.clk, tl, A.L, idx, w);
+                #pragma unroll
+                for (int l = 0; l < 7; ++l)
+                    if (l < nw) F = F + (T)w[l] * pl[(long long)idx[l] * M];
             }
         }
         CT ud = y[(long long)(nz - 1) * M];
@@ -151,7 +158,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs<T> A) {
             } else {
                 rv = -ri * (dp + gz * r);
             }
-            if (A.src_on && j == A.ksrc) rv = rv + A.src_scale * F;
+            if (src_on && j == A.ksrc) rv = rv + A.src_scale * F;
             if (A.damp) rv = rv - gd * vz;
             bool zero_row = opt3d ? (j == 0 || j == nz - 1) : (j == 0);
             if (zero_row) { rv = czero<CT>(); vz = czero<CT>(); }
@@ -174,12 +181,13 @@ __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     const T dt = A.dt;
     const T hf = __ldg(&A.pt[PT_HF * M + m]);
     const bool opt3d = (A.option == 4);
+    const bool hstep = slot_hfilter(A.clk, A.clk.time - A.clk.t0[s]);
     for (int f = 0; f < 6; ++f) {
         CT* af = a + f * fs;
         const CT* sf = scr + f * fs;
         // FILTER_VARS_3D filters fields 1..5 horizontally (physics.f90:795,813);
         // FILTER_VARS_2D filters all six (physics2d.f90:569)
-        const bool hfil = A.hfilter && (opt3d ? (f < 5) : true);
+        const bool hfil = hstep && (opt3d ? (f < 5) : true);
         zfilter_stream<CT, T>(
             nz, opt3d ? 0 : 1,
             [&](int j) { long long o = (long long)j * M; return af[o] + dt * sf[o]; },
@@ -242,6 +250,33 @@ __global__ void __launch_bounds__(128) zderiv_real_kernel(const double* __restri
         o[(long long)j * n1] = ud * zt[ZT_STRETCH * nz + j];
     }
 }
+
+// vz of plane kplane into record tl/steps of each slot whose clock tl is on
+// the output cadence (driver.f90:455-476)
+template <typename T>
+__global__ void record_kernel(const typename CplxOf<T>::type* __restrict__ a, typename CplxOf<T>::type* __restrict__ rec,
+                              const int* __restrict__ t0, int time, int steps, int rec_max, long long fs, int M,
+                              int kplane) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (m >= M) return;
+    const int tl = time - t0[s];
+    if (tl < 0 || tl % steps != 0) return;
+    const int r = tl / steps;
+    if (r >= rec_max) return;
+    rec[((long long)s * rec_max + r) * M + m] = a[(long long)s * 6 * fs + 5 * fs + (long long)kplane * M + m];
+}
+
+template <typename T>
+void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, int time, int steps,
+                   int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s) {
+    dim3 grid((M + 255) / 256, nsrc);
+    record_kernel<T><<<grid, 256, 0, s>>>(a, rec, t0, time, steps, rec_max, fs, M, kplane);
+}
+template void launch_record<double>(const double2*, double2*, const int*, int, int, int, long long, int, int, int,
+                                    cudaStream_t);
+template void launch_record<float>(const float2*, float2*, const int*, int, int, int, long long, int, int, int,
+                                   cudaStream_t);
 
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s) {
     dim3 grid((A.M + 127) / 128, nsrc);

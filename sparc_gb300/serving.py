@@ -1,0 +1,239 @@
+"""Serving: continuous batching of solve requests on one GPU.
+
+A request is one forward solve, or a forward solve followed by its adjoint
+solve (adjoint source = the time-reversed surface residual at receivers on a
+ring around the source), on one of several grid sizes.  The engine keeps, per
+(grid size, role), pools of batched contexts -- fields resident in HBM, one
+CUDA stream each -- and runs an event loop:
+
+  * arrivals join a queue; a queued request is admitted into a free slot of a
+    pool of its grid size, or into a new pool if the HBM budget allows one
+    (admission by footprint); adjoint phases of finished forward runs are
+    admitted first;
+  * an admitted slot is reset and starts its own clock at 0 (per-slot clocks
+    of the library), so requests join a batch that is already running;
+  * every pool with work advances one output interval (steps of 30 s) per
+    round; pools run on their own streams, so their work overlaps;
+  * a slot whose clock reaches the request's length is finished: its
+    seismograms are read back and the slot is free for the next admission.
+
+Results do not depend on the mix: a slot's arithmetic is independent of the
+other slots of its batch and of other pools.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from . import sources
+from .background import polytrope_table
+from .params import SparcParams
+from .solver import Solver
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    grid: tuple            # (nx, ny, nz)
+    kind: str              # "fwd" or "fwd+adj"
+    nsteps: int            # time steps per phase (a multiple of the output cadence)
+    x0_mm: float
+    y0_mm: float
+    arrival: float         # seconds after the start of the stream
+    admitted: float = -1.0
+    finished: float = -1.0
+    records: np.ndarray | None = None        # forward surface vz records (nrec, ny, nx)
+    adj_records: np.ndarray | None = None    # adjoint surface vz records
+    phase: int = 0
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def grid_params(grid, precision: str, base: SparcParams | None = None) -> SparcParams:
+    nx, ny, nz = grid
+    b = base or SparcParams()
+    length = 200.0e8                          # 200 Mm periodic box for every grid size
+    return b.replace(nx=nx, ny=ny, nz=nz, xlength=length, ylength=length, npmlbot=10, npmltop=10,
+                     excitdep=-15000000.0, obsheight=20000000.0, precision=precision)
+
+
+class Pool:
+    """One batched context (one grid size, one role) with `slots` slots."""
+
+    def __init__(self, p: SparcParams, table, role: str, slots: int, max_records: int):
+        self.role = role
+        self.p = p.replace(nsrc=slots, compute_forward=(role == "fwd"), compute_adjoint=(role == "adj"))
+        self.solver = Solver(self.p, table)
+        self.solver.record_surface(max_records)
+        self.requests: list = [None] * slots
+        self.series = sources.ricker_series(self.p, 8 * max_records * self.p.steps)
+        self.max_records = max_records
+        self.bytes = self.solver.device_bytes
+
+    @property
+    def free(self) -> list:
+        return [i for i, r in enumerate(self.requests) if r is None]
+
+    @property
+    def busy(self) -> bool:
+        return any(r is not None for r in self.requests)
+
+    def admit(self, req: Request, planes=None):
+        slot = self.free[0]
+        s = self.solver
+        if self.role == "fwd":
+            s.set_source_series(sources.gaussian_plane(self.p, 1.0, req.x0_mm, req.y0_mm), self.series, slot=slot)
+        else:
+            # the source buffer is sized by its first use: pad to the maximum length
+            padded = np.zeros((self.max_records,) + planes.shape[1:])
+            padded[: min(len(planes), self.max_records)] = planes[: self.max_records]
+            s.set_source_lagrange(padded, slot=slot)
+        s.slot_reset(slot)
+        self.requests[slot] = req
+        s.set_active(max(i for i, r in enumerate(self.requests) if r is not None) + 1)
+        return slot
+
+    def advance(self, nsteps: int):
+        if self.busy:
+            self.solver.step(nsteps)
+
+    def collect(self) -> list:
+        done = []
+        for slot, req in enumerate(self.requests):
+            if req is not None and self.solver.slot_time(slot) >= req.nsteps:
+                done.append((req, self.solver.records(slot=slot)))
+                self.requests[slot] = None
+        if self.busy:
+            self.solver.set_active(max(i for i, r in enumerate(self.requests) if r is not None) + 1)
+        return done
+
+    def close(self):
+        self.solver.close()
+
+
+class Engine:
+    """Continuous-batching request loop on one GPU."""
+
+    def __init__(self, precision: str = "f32", hbm_budget: float = 200e9, slots: dict | None = None,
+                 max_steps: int = 7200, base: SparcParams | None = None):
+        self.precision = precision
+        self.budget = hbm_budget
+        self.slots = slots or {}
+        self.max_steps = max_steps
+        self.base = base
+        self.pools: list[Pool] = []
+        self.tables: dict = {}
+        self.cad = (base or SparcParams()).steps
+
+    def _table(self, nz):
+        if nz not in self.tables:
+            self.tables[nz] = polytrope_table(nz)
+        return self.tables[nz]
+
+    def _pool_for(self, grid, role) -> Pool | None:
+        for pl in self.pools:
+            if pl.role == role and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid) and pl.free:
+                return pl
+        # admission by footprint: a new pool only if it fits the HBM budget
+        p = grid_params(grid, self.precision, self.base)
+        slots = self.slots.get(tuple(grid), 4)
+        field = (p.nx // 2 + 1) * p.ny * p.nz * (8 if self.precision == "f32" else 16)
+        est = slots * field * (15 + (self.max_steps // self.cad + 1) / p.nz) + 64e6
+        used = sum(pl.bytes for pl in self.pools)
+        if used + est > self.budget:
+            return None
+        pl = Pool(p, self._table(p.nz), role, slots, self.max_steps // self.cad + 1)
+        self.pools.append(pl)
+        return pl
+
+    def _adjoint_planes(self, pl: Pool, req: Request):
+        pix = sources.receiver_pixels(pl.p, n=8, radius_mm=10.0, x0_mm=req.x0_mm, y0_mm=req.y0_mm)
+        res = np.stack([req.records[:, iy, ix] for (iy, ix) in pix])      # residual against zero data
+        return sources.adjoint_planes(pl.p, res, pix)
+
+    def run(self, requests: list[Request], time_scale: float = 1.0, max_wall: float = 3600.0) -> list[Request]:
+        pending = sorted(requests, key=lambda r: r.arrival)
+        queue: list[Request] = []
+        adj_queue: list[Request] = []
+        done: list[Request] = []
+        t_start = time.perf_counter()
+        while (pending or queue or adj_queue or any(pl.busy for pl in self.pools)):
+            now = (time.perf_counter() - t_start) / time_scale
+            if now > max_wall:
+                raise RuntimeError("serving stream exceeded its wall-clock limit")
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.pop(0))
+            # admission: adjoint phases first, then new requests (FIFO)
+            for q, role in ((adj_queue, "adj"), (queue, "fwd")):
+                keep = []
+                for req in q:
+                    pl = self._pool_for(req.grid, role)
+                    if pl is None:
+                        keep.append(req)
+                        continue
+                    if role == "fwd":
+                        req.admitted = now
+                        pl.admit(req)
+                    else:
+                        pl.admit(req, self._adjoint_planes(pl, req))
+                q[:] = keep
+            if not any(pl.busy for pl in self.pools):
+                if pending:
+                    time.sleep(max(0.0, min(0.01, (pending[0].arrival - now) * time_scale)))
+                continue
+            for pl in self.pools:            # every pool advances one output interval; streams overlap
+                pl.advance(self.cad)
+            for pl in self.pools:
+                for req, recs in pl.collect():
+                    t = (time.perf_counter() - t_start) / time_scale
+                    if pl.role == "fwd":
+                        req.records = recs
+                        if req.kind == "fwd+adj":
+                            req.phase = 1
+                            adj_queue.append(req)
+                            continue
+                    else:
+                        req.adj_records = recs
+                    req.finished = t
+                    done.append(req)
+        return done
+
+    def close(self):
+        for pl in self.pools:
+            pl.close()
+        self.pools = []
+
+
+def poisson_stream(n: int, rate: float = 4.0, seed: int = 0, mix=None, hours=(1.0, 4.0), dt: float = 2.0,
+                   cad: int = 15, compress: float = 1.0, p_adj: float = 0.5) -> list[Request]:
+    """Seeded request stream: Poisson arrivals, grid mix (60 % 128^2x150,
+    30 % 256^2x300, 10 % 512^2x300 by default), random source position,
+    forward-only or forward+adjoint, 1-4 h of solar time divided by
+    `compress` (time steps rounded up to the output cadence)."""
+    rng = np.random.default_rng(seed)
+    mix = mix or [((128, 128, 150), 0.6), ((256, 256, 300), 0.3), ((512, 512, 300), 0.1)]
+    grids = [g for g, _ in mix]
+    probs = np.array([w for _, w in mix], dtype=float)
+    probs /= probs.sum()
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        g = grids[rng.choice(len(grids), p=probs)]
+        hours_i = rng.uniform(*hours)
+        steps = int(np.ceil(hours_i * 3600.0 / dt / compress / cad)) * cad
+        half = 0.4 * 200.0
+        x0, y0 = rng.uniform(-half, half, size=2)
+        kind = "fwd+adj" if rng.random() < p_adj else "fwd"
+        out.append(Request(i, g, kind, steps, float(x0), float(y0), t))
+    return out
+
+
+def latency_stats(done: list[Request]) -> dict:
+    lat = np.array([r.latency for r in done])
+    return {"n": len(done), "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}

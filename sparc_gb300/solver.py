@@ -182,6 +182,18 @@ class Solver:
     def restore(self, path: str):
         self._ck(self.L.sparc_gpu_restore(self.h, path.encode()))
 
+    # ---- continuous batching ----
+    def slot_reset(self, slot: int):
+        self._ck(self.L.sparc_gpu_slot_reset(self.h, int(slot)))
+
+    def slot_time(self, slot: int) -> int:
+        t = ctypes.c_int()
+        self._ck(self.L.sparc_gpu_slot_time(self.h, int(slot), ctypes.byref(t)))
+        return t.value
+
+    def set_active(self, n: int):
+        self._ck(self.L.sparc_gpu_set_active(self.h, int(n)))
+
     def save_device(self, idx: int, capacity: int):
         self._ck(self.L.sparc_gpu_save_device(self.h, int(idx), int(capacity)))
 
