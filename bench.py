@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--small", action="store_true", help="128x128x150 smoke-size workload")
+    ap.add_argument("--serve-requests", type=int, default=32, help="requests of the serving stream (0: skip)")
+    ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
     return ap.parse_args()
 
 
@@ -216,6 +218,32 @@ def step_kernel_time(solver, n=15, reps=2):
     return float(np.min(ts))
 
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, seed: int = 0):
+    """Config-5 stream: Poisson arrivals (rate/s) of 1-4 h forward or
+    forward+adjoint requests on 128^2x150 / 256^2x300 / 512^2x300 (60/30/10 %),
+    request lengths divided by `compress`.  Latency = finish - arrival (wall)."""
+    from sparc_gb300.serving import Engine, latency_stats, poisson_stream
+    reqs = poisson_stream(n, rate=rate, seed=seed, compress=compress)
+    eng = Engine(precision=precision, hbm_budget=120e9,
+                 slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
+                 max_steps=max(r.nsteps for r in reqs))
+    t0 = time.perf_counter()
+    try:
+        done = eng.run(reqs, max_wall=240.0)
+    finally:
+        eng.close()
+    wall = time.perf_counter() - t0
+    pts = sum(r.grid[0] * r.grid[1] * r.grid[2] * r.nsteps * (2 if r.kind == "fwd+adj" else 1) for r in done)
+    st = latency_stats(done)
+    st.update({"precision": precision, "Mpoint_steps_per_s": pts / wall / 1e6, "wall_s": wall,
+               "compress": compress, "rate_per_s": rate})
+    return st
+
+
 def cpu_baseline(p, tab, steps=1):
     from oracle import oracle
     threads = os.cpu_count() or 1
@@ -291,6 +319,7 @@ def main():
     out = {}
 
     # ---- plain FP64, one source ----
+    log("plain FP64")
     if not args.skip_fp64:
         p64 = p0.replace(precision="f64", nsrc=1)
         fwd, adj = make_pair(p64, tab, args.nplanes, seed=rank)
@@ -305,6 +334,7 @@ def main():
         del fwd, adj
 
     # ---- batched FP32 ----
+    log("batched FP32")
     S = args.nsrc
     p32 = p0.replace(precision="f32", nsrc=S)
     fwd, adj = make_pair(p32, tab, args.nplanes, seed=1000 + rank)
@@ -332,6 +362,7 @@ def main():
     del fwd, adj
 
     # ---- e2e through the public API with host buffers (pinned) ----
+    log("e2e")
     e2e = None
     if True:
         from sparc_gb300 import sources
@@ -394,14 +425,26 @@ def main():
                      "note": "the fused step moves 12 field accesses per step instead of 102; it is bound "
                              "by instruction issue, not HBM (profiles/fused_step_f32_256x256x300.md)",
                      "peak_source": f"{peak_src} hbm_gbs"},
-        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                       "what": "one batched forward+adjoint step, host-synchronised"},
+        "step_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                            "what": "one batched forward+adjoint step, host-synchronised"},
         "e2e": e2e,
     }
+    if args.serve_requests > 0 and ws == 1:
+        line["serving"] = {}
+        for prec in ("f32", "f64"):
+            log(f"serving stream {prec}")
+            try:
+                line["serving"][prec] = serving_section(prec, args.serve_requests, args.serve_compress)
+            except Exception as e:   # reported, not fatal: the timed headline above is complete
+                line["serving"][prec] = {"error": str(e)}
+        line["serving"]["what"] = ("Poisson stream, 4 requests/s, 60/30/10 % of 128^2x150/256^2x300/512^2x300, "
+                                   "half forward+adjoint, 1-4 h of solar time compressed by serve-compress; "
+                                   "continuous batching with per-slot clocks")
     if "fp64_plain" in out:
         line["fp64_plain"] = out["fp64_plain"]
         line["ratio_fp32_batched_over_fp64_plain"] = value / out["fp64_plain"]["value"]
     if rank == 0 and ws == 1 and not args.skip_cpu:
+        log("cpu baseline")
         try:
             line["cpu_baseline"] = cpu_baseline(p0, tab)
         except Exception as e:  # the oracle is only the reported baseline

@@ -126,6 +126,7 @@ class Engine:
         self.max_steps = max_steps
         self.base = base
         self.pools: list[Pool] = []
+        self.max_pools_per_key = 2
         self.tables: dict = {}
         self.cad = (base or SparcParams()).steps
 
@@ -138,14 +139,23 @@ class Engine:
         for pl in self.pools:
             if pl.role == role and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid) and pl.free:
                 return pl
-        # admission by footprint: a new pool only if it fits the HBM budget
+        same = [pl for pl in self.pools if pl.role == role and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid)]
+        if len(same) >= self.max_pools_per_key:
+            return None
+        # admission by footprint: a new pool only if it fits the HBM budget,
+        # after releasing idle pools (least recently created first)
         p = grid_params(grid, self.precision, self.base)
         slots = self.slots.get(tuple(grid), 4)
         field = (p.nx // 2 + 1) * p.ny * p.nz * (8 if self.precision == "f32" else 16)
-        est = slots * field * (15 + (self.max_steps // self.cad + 1) / p.nz) + 64e6
-        used = sum(pl.bytes for pl in self.pools)
-        if used + est > self.budget:
-            return None
+        est = slots * field * (15 + (self.max_steps // self.cad + 1) / p.nz) + p.points * 12 + 64e6
+        if est > self.budget:
+            raise RuntimeError(f"a {grid} pool needs {est / 1e9:.1f} GB, above the HBM budget")
+        while sum(pl.bytes for pl in self.pools) + est > self.budget:
+            idle = [pl for pl in self.pools if not pl.busy]
+            if not idle:
+                return None
+            idle[0].close()
+            self.pools.remove(idle[0])
         pl = Pool(p, self._table(p.nz), role, slots, self.max_steps // self.cad + 1)
         self.pools.append(pl)
         return pl
@@ -155,7 +165,7 @@ class Engine:
         res = np.stack([req.records[:, iy, ix] for (iy, ix) in pix])      # residual against zero data
         return sources.adjoint_planes(pl.p, res, pix)
 
-    def run(self, requests: list[Request], time_scale: float = 1.0, max_wall: float = 3600.0) -> list[Request]:
+    def run(self, requests: list[Request], time_scale: float = 1.0, max_wall: float = 900.0) -> list[Request]:
         pending = sorted(requests, key=lambda r: r.arrival)
         queue: list[Request] = []
         adj_queue: list[Request] = []
@@ -163,7 +173,7 @@ class Engine:
         t_start = time.perf_counter()
         while (pending or queue or adj_queue or any(pl.busy for pl in self.pools)):
             now = (time.perf_counter() - t_start) / time_scale
-            if now > max_wall:
+            if (time.perf_counter() - t_start) > max_wall:
                 raise RuntimeError("serving stream exceeded its wall-clock limit")
             while pending and pending[0].arrival <= now:
                 queue.append(pending.pop(0))
@@ -184,6 +194,10 @@ class Engine:
             if not any(pl.busy for pl in self.pools):
                 if pending:
                     time.sleep(max(0.0, min(0.01, (pending[0].arrival - now) * time_scale)))
+                    continue
+                if queue or adj_queue:
+                    # nothing runs, nothing arrives, and the queue cannot be admitted
+                    raise RuntimeError("serving: queued requests cannot be admitted within the HBM budget")
                 continue
             for pl in self.pools:            # every pool advances one output interval; streams overlap
                 pl.advance(self.cad)
@@ -237,3 +251,33 @@ def latency_stats(done: list[Request]) -> dict:
     lat = np.array([r.latency for r in done])
     return {"n": len(done), "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}
+
+
+def main(argv=None):
+    """python -m sparc_gb300.serving --requests N --compress C --precision f32"""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--rate", type=float, default=4.0)
+    ap.add_argument("--compress", type=float, default=120.0)
+    ap.add_argument("--precision", default="f32")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--budget-gb", type=float, default=120.0)
+    a = ap.parse_args(argv)
+    reqs = poisson_stream(a.requests, rate=a.rate, seed=a.seed, compress=a.compress)
+    eng = Engine(precision=a.precision, hbm_budget=a.budget_gb * 1e9,
+                 slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
+                 max_steps=max(r.nsteps for r in reqs))
+    t0 = time.perf_counter()
+    done = eng.run(reqs)
+    wall = time.perf_counter() - t0
+    eng.close()
+    st = latency_stats(done)
+    pts = sum(r.grid[0] * r.grid[1] * r.grid[2] * r.nsteps * (2 if r.kind == "fwd+adj" else 1) for r in done)
+    st.update({"Mpoint_steps_per_s": pts / wall / 1e6, "wall_s": wall})
+    print(json.dumps(st))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,81 @@
+"""Host logic of the continuous-batching engine, with a fake pool (no GPU):
+admission by footprint, idle-pool eviction, no livelock, bounded pools."""
+import numpy as np
+import pytest
+
+from sparc_gb300 import serving
+
+
+class FakePool:
+    created = 0
+
+    def __init__(self, p, table, role, slots, max_records):
+        FakePool.created += 1
+        self.role = role
+        self.p = p.replace(nsrc=slots)
+        self.requests = [None] * slots
+        self.clock = [0] * slots
+        self.bytes = slots * (p.nx // 2 + 1) * p.ny * p.nz * 8 * 15
+        self.closed = False
+
+    free = serving.Pool.free
+    busy = serving.Pool.busy
+
+    def admit(self, req, planes=None):
+        slot = self.free[0]
+        self.requests[slot] = req
+        self.clock[slot] = 0
+        return slot
+
+    def advance(self, n):
+        for i, r in enumerate(self.requests):
+            if r is not None:
+                self.clock[i] += n
+
+    def collect(self):
+        out = []
+        for i, r in enumerate(self.requests):
+            if r is not None and self.clock[i] >= r.nsteps:
+                out.append((r, np.zeros((2, 1, 1))))
+                self.requests[i] = None
+        return out
+
+    def close(self):
+        self.closed = True
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    FakePool.created = 0
+    monkeypatch.setattr(serving, "Pool", FakePool)
+    monkeypatch.setattr(serving.Engine, "_adjoint_planes", lambda self, pl, req: None)
+    monkeypatch.setattr(serving, "polytrope_table", lambda nz: None)
+    return FakePool
+
+
+def test_idle_pools_are_evicted_when_the_budget_blocks(fake):
+    # a budget that holds one large pool or a few small ones, never both
+    grids = [(128, 128, 150), (256, 256, 300), (512, 512, 300)]
+    reqs = [serving.Request(i, grids[i % 3], ("fwd", "fwd+adj")[i % 2], 30 * (1 + i % 4), 0.0, 0.0, 0.01 * i)
+            for i in range(24)]
+    eng = serving.Engine("f32", hbm_budget=14e9,
+                         slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
+                         max_steps=max(r.nsteps for r in reqs))
+    done = eng.run(reqs, max_wall=30.0)
+    assert sorted(r.rid for r in done) == list(range(24))
+    assert all(r.finished >= r.arrival for r in done)
+    assert fake.created > len(eng.pools)                     # some pools were released on the way
+
+
+def test_pool_count_per_grid_is_bounded(fake):
+    reqs = [serving.Request(i, (128, 128, 150), "fwd", 30, 0.0, 0.0, 0.0) for i in range(40)]
+    eng = serving.Engine("f32", hbm_budget=1e12, slots={(128, 128, 150): 4}, max_steps=30)
+    done = eng.run(reqs, max_wall=30.0)
+    assert len(done) == 40 and len(eng.pools) <= eng.max_pools_per_key
+
+
+def test_a_pool_above_the_budget_is_an_error(fake):
+    reqs = [serving.Request(0, (512, 512, 300), "fwd", 30, 0.0, 0.0, 0.0)]
+    eng = serving.Engine("f64", hbm_budget=1e9, slots={(512, 512, 300): 2}, max_steps=30)
+    with pytest.raises(RuntimeError, match="above the HBM budget"):
+        eng.run(reqs, max_wall=30.0)
