@@ -81,6 +81,27 @@ def alg_bytes_per_point_step(p) -> float:
     return step_alg_bytes(p) / (p.points * p.nsrc)
 
 
+#: Compulsory field accesses per grid-point-step of the minimal per-stage
+#: schedule of the reference's physical-space formulation (displacement form,
+#: option 4, displacement.f90:482-658 within step.f90:43-128): per RK stage two
+#: horizontal passes (H1: read xi_x, xi_y from a and scr, write the horizontal
+#: divergence = 5; H2: read p', v_x, v_y from a and scr, write scr v_x, v_y,
+#: xi_x, xi_y = 9), the v_z damping pass (3) and two z-pencil passes (Z1: read
+#: xi_z from a and scr and the divergence, write p', rho' = 5; Z2: read p',
+#: rho', damped v_z and v_z from a and scr, write scr v_z, xi_z = 7), 29 per
+#: stage; the update with the z filter (read a and scr, write a: 18) and the
+#: horizontal filter every 30 steps (10 / 30).  5 * 29 + 18 + 1/3 = 163.33.
+#: This is the per-unit figure the roofline's `achieved` uses: the work of one
+#: grid-point-step is credited with the bytes that the minimal per-stage
+#: schedule must move for it, whatever the kernel itself moves.
+REFERENCE_SCHEDULE_ACCESSES = 5 * 29 + 18 + 10.0 / 30.0
+
+
+def reference_schedule_bytes_per_point_step(precision: str) -> float:
+    """653.3 B (FP32) / 1306.7 B (FP64) per grid-point-step."""
+    return REFERENCE_SCHEDULE_ACCESSES * (4 if precision == "f32" else 8)
+
+
 FUSED_STEP = 12
 
 

@@ -49,7 +49,7 @@ struct sparc_ctx {
     void* a = nullptr; void* scr = nullptr; void* pml = nullptr; void* scrpml = nullptr;
     void* ybuf = nullptr; void* pbuf = nullptr; void* rbuf = nullptr;
     void* zt = nullptr; void* pt = nullptr;       // T tables
-    float* scan = nullptr;                        // fused FP32 step: scan tables [4 bc][5][nz]
+    float* ftab = nullptr;                        // fused FP32 step: z table [FZ_COUNT][fused_nzp(nz)]
     int use_fused = 0;
     double* zt64 = nullptr; double* pt64 = nullptr;
     double* tw_x = nullptr; double* tw_y = nullptr;
@@ -298,7 +298,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
     if (c->f32) {
         c->use_fused = fused_supported(c->nz) && getenv("SPARC_FP32_PER_STAGE") == nullptr;
-        if ((rc = dalloc(c, (void**)&c->scan, (size_t)4 * 5 * c->nz * 4))) return bail(rc);
+        if (c->use_fused &&
+            (rc = dalloc(c, (void**)&c->ftab, (size_t)FZ_COUNT * fused_nzp(c->nz) * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->pt64, (size_t)PT_COUNT * c->M * 8))) return bail(rc);
     } else {
@@ -517,28 +518,52 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     }
     int rc;
     if (c->f32) {
-        // scan tables of the fused FP32 step: the LU elimination multipliers
-        // and their chunk products (chunks of FUSED_CH levels)
-        std::vector<float> sc((size_t)4 * 5 * nz, 0.f);
-        for (int b = 0; b < 4; ++b) {
-            std::vector<double> ibd(nz), mm(nz), gg(nz), HH(nz), GG(nz);
+        if (c->use_fused) {
+            // z table of the fused FP32 step, built in FP64 and rounded once:
+            // profile rows (with the buoyancy products g rho0/rho0 and
+            // g drho0/dz / rho0 folded), and the LU
+            // elimination multipliers of the xi_z and p' boundary codes with
+            // their chunk products (chunks of FUSED_CH levels; padding rows
+            // up to NZP carry zero multipliers)
+            const int NZP = fused_nzp(nz);
+            const bool d3 = (P.option == 4);
+            std::vector<float> ft((size_t)FZ_COUNT * NZP, 0.f);
+            auto put = [&](int row, int j, double v) { ft[(size_t)row * NZP + j] = (float)v; };
             for (int j = 0; j < nz; ++j) {
-                ibd[j] = 1.0 / tri[b].betad[j];
-                mm[j] = (j == 0) ? 0.0 : -tri[b].low[j] / tri[b].betad[j];
-                gg[j] = (j == nz - 1) ? 0.0 : -tri[b].gam[j + 1];
+                const double st = ZR(ZT_STRETCH)[j], ri = ZR(ZT_RHOINV)[j], g = ZR(ZT_G)[j];
+                put(FZ_ST, j, st);
+                put(FZ_C2R, j, ZR(ZT_C2RHO0)[j]);
+                put(FZ_GP, j, ZR(ZT_GRADP0)[j]);
+                put(FZ_RI, j, ri);
+                put(FZ_E1, j, g * ri * ZR(ZT_RHO0)[j]);
+                put(FZ_E2, j, g * ri * ZR(ZT_GRADRHO0)[j]);
+                put(FZ_RIST, j, ri * st);
+                put(FZ_AZ, j, ZR(ZT_AZ)[j]);
+                put(FZ_BZ, j, ZR(ZT_BZ)[j]);
             }
-            for (int j0 = 0; j0 < nz; j0 += FUSED_CH) {
-                int j1 = std::min(nz, j0 + FUSED_CH);
-                double pr = 1.0;
-                for (int j = j0; j < j1; ++j) { pr *= mm[j]; HH[j] = pr; }
-                pr = 1.0;
-                for (int j = j1 - 1; j >= j0; --j) { pr *= gg[j]; GG[j] = pr; }
+            const int bcs[2] = {d3 ? 1 : 3, d3 ? 0 : 2};
+            const int base[2] = {FZ_SX, FZ_SP};
+            for (int k = 0; k < 2; ++k) {
+                const int b = bcs[k];
+                std::vector<double> ibd(NZP, 0.0), mm(NZP, 0.0), gg(NZP, 0.0), HH(NZP, 0.0), GG(NZP, 0.0);
+                for (int j = 0; j < nz; ++j) {
+                    ibd[j] = 1.0 / tri[b].betad[j];
+                    mm[j] = (j == 0) ? 0.0 : -tri[b].low[j] / tri[b].betad[j];
+                    gg[j] = (j == nz - 1) ? 0.0 : -tri[b].gam[j + 1];
+                }
+                for (int j0 = 0; j0 < NZP; j0 += FUSED_CH) {
+                    const int j1 = j0 + FUSED_CH;
+                    double pr = 1.0;
+                    for (int j = j0; j < j1; ++j) { pr *= mm[j]; HH[j] = pr; }
+                    pr = 1.0;
+                    for (int j = j1 - 1; j >= j0; --j) { pr *= gg[j]; GG[j] = pr; }
+                }
+                const std::vector<double>* rows[5] = {&ibd, &mm, &HH, &gg, &GG};
+                for (int r = 0; r < 5; ++r)
+                    for (int j = 0; j < NZP; ++j) put(base[k] + r, j, (*rows[r])[j]);
             }
-            const std::vector<double>* rows[5] = {&ibd, &mm, &HH, &gg, &GG};
-            for (int r = 0; r < 5; ++r)
-                for (int j = 0; j < nz; ++j) sc[((size_t)b * 5 + r) * nz + j] = (float)(*rows[r])[j];
+            if ((rc = upload(c, c->ftab, ft.data(), ft.size() * 4))) return rc;
         }
-        if ((rc = upload(c, c->scan, sc.data(), sc.size() * 4))) return rc;
         std::vector<float> zf(c->zt_host.begin(), c->zt_host.end()), pf(c->pt_host.begin(), c->pt_host.end());
         if ((rc = upload(c, c->zt, zf.data(), zf.size() * 4))) return rc;
         if ((rc = upload(c, c->pt, pf.data(), pf.size() * 4))) return rc;
@@ -783,10 +808,11 @@ static int do_steps(sparc_ctx* c, int nsteps) {
     if (fused) {
         memset(&Fz, 0, sizeof(Fz));
         Fz.a = (float2*)c->a; Fz.scr = (float2*)c->scr; Fz.pml = (float2*)c->pml;
-        Fz.zt = (const float*)c->zt; Fz.pt = (const float*)c->pt; Fz.scan = c->scan;
+        Fz.ftab = c->ftab; Fz.pt = (const float*)c->pt;
+        Fz.unstr_top = (float)c->zt_host[(size_t)ZT_UNSTRETCH * c->nz + c->nz - 1];
         Fz.fs = c->fs; Fz.ps = c->ps; Fz.M = c->M; Fz.nz = c->nz; Fz.nzpml = c->nzpml;
         Fz.npmlbot = c->P.npmlbot; Fz.npmltop = c->P.npmltop; Fz.option = c->P.option;
-        Fz.damp = A.damp; Fz.W = (c->nz + 32 * FUSED_CH - 1) / (32 * FUSED_CH);
+        Fz.damp = A.damp; Fz.W = fused_w(c->nz);
         for (int i = 0; i < 5; ++i) Fz.betas[i] = (float)c->betas[i];
         Fz.dt = (float)c->deltat;
         Fz.cc.C1 = (float)c->cc64.C1; Fz.cc.C2 = (float)c->cc64.C2;

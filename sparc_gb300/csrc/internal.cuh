@@ -215,9 +215,15 @@ template <typename T> struct UpdateArgs {
 };
 
 // fused FP32 step (fused.cu)
+// z table of the fused FP32 step, [FZ_COUNT][NZP] (NZP = fused_nzp(nz), padded
+// rows zero): profile rows, then the five scan rows (1/betad, elimination
+// multiplier m, chunk products H of m, back-substitution multiplier g, chunk
+// products G of g) of the xi_z boundary code and of the p' boundary code
+enum { FZ_ST = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_RIST, FZ_AZ, FZ_BZ, FZ_SX = 9, FZ_SP = 14, FZ_COUNT = 19 };
 struct FusedArgs {
     float2* a; float2* scr; float2* pml;
-    const float* zt; const float* pt; const float* scan;
+    const float* ftab; const float* pt;
+    float unstr_top;
     long long fs, ps;
     int M, nz, nzpml, npmlbot, npmltop, option, damp, W;
     float betas[5];
@@ -233,6 +239,8 @@ struct FusedArgs {
 constexpr int FUSED_CH = 5;
 size_t fused_smem_bytes(int nz, int nzpml, int W);
 int fused_supported(int nz);
+int fused_w(int nz);
+int fused_nzp(int nz);
 void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s);
 
 // launchers (modal.cu)

@@ -86,6 +86,13 @@ def test_kernel_pipeline_fp32_against_fp64(gpu_lib):
     for q in ("kc", "krho", "hessian"):
         assert rel_l2(getattr(b, q), getattr(a, q)) < 1e-3, q
     dt = p64.timestep * p64.steps
-    shifts = [abs(compute_tt(a.seismograms[s, :, r], b.seismograms[s, :, r], dt))
-              for s in range(2) for r in range(len(pix))]
-    assert max(shifts) < 0.05
+    # travel times only where the wave has arrived: receivers whose FP64 rms is
+    # at least 1 % of the strongest receiver of that source (the others hold
+    # the precursor at 1e-4 of the peak, whose FP32 noise has no travel time)
+    shifts = []
+    for s in range(2):
+        rms = np.sqrt(np.mean(a.seismograms[s] ** 2, axis=0))
+        for r in range(len(pix)):
+            if rms[r] >= 1e-2 * rms.max():
+                shifts.append(abs(compute_tt(a.seismograms[s, :, r], b.seismograms[s, :, r], dt)))
+    assert len(shifts) >= 8 and max(shifts) < 0.05, shifts
