@@ -136,6 +136,150 @@ __global__ void cols_fft_kernel(const typename CplxOf<T>::type* __restrict__ in,
     }
 }
 
+// ---- two-pass transforms for n = R*R (R = 8, 16): n = R*n1 + n2,
+// k = k1 + R*k2.  Pass 1 (thread n2): R-point DFT over n1 of x[R n1 + n2],
+// times the twiddle W_n^(n2 k1); pass 2 (thread k1): R-point DFT over n2.
+// Each DFT runs in registers; one shared-memory exchange and one barrier per
+// CTA.  W_m^j = exp(sign 2 pi i j / m) comes from the FP64 table tw
+// (cos, sin of 2 pi q / n for q < n/2).
+
+template <typename T, typename CT>
+__device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, T sign) {
+    // W_n^q for 0 <= q < n
+    const int h = n >> 1;
+    const bool flip = q >= h;
+    const int r = flip ? q - h : q;
+    T c = (T)__ldg(&tw[2 * r]), sn = sign * (T)__ldg(&tw[2 * r + 1]);
+    if (flip) { c = -c; sn = -sn; }
+    CT w;
+    w.x = c;
+    w.y = sn;
+    return w;
+}
+
+// in-register DFT of length R (decimation in frequency): on return v[brev(k)]
+// holds X[k]; w[j] = W_R^j for j < R/2
+template <typename CT, int R>
+__device__ __forceinline__ void reg_dft(CT (&v)[R], const CT (&w)[R / 2]) {
+    #pragma unroll
+    for (int len = R; len >= 2; len >>= 1) {
+        const int half = len >> 1, step = R / len;
+        #pragma unroll
+        for (int b = 0; b < R; b += len) {
+            #pragma unroll
+            for (int k = 0; k < half; ++k) {
+                const CT a = v[b + k], c = v[b + k + half];
+                v[b + k] = a + c;
+                const CT d = a - c;
+                v[b + k + half] = (k == 0) ? d : cmul(d, w[k * step]);
+            }
+        }
+    }
+}
+
+template <int R>
+__host__ __device__ constexpr int brev(int k) {
+    int r = 0;
+    for (int b = 1, m = R >> 1; b < R; b <<= 1, m >>= 1)
+        if (k & b) r |= m;
+    return r;
+}
+
+// complex FFT along y (length ny = R*R) for NC = 256/R kx-columns per CTA;
+// data [plane][y][kx] with H columns per row
+template <typename T, int R>
+__global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<T>::type* __restrict__ in,
+                                                          typename CplxOf<T>::type* __restrict__ out, int H,
+                                                          T sign, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int n = R * R, NC = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* Z = (CT*)smraw;                                  // [k1][n2][c]
+    const int ntile = (H + NC - 1) / NC;
+    const long long plane = blockIdx.x / ntile;
+    const int kx0 = (blockIdx.x % ntile) * NC;
+    const int c = threadIdx.x % NC, r = threadIdx.x / NC;
+    const bool cv = kx0 + c < H;
+    const long long base = plane * (long long)n * H + kx0 + c;
+    CT w[R / 2];
+    #pragma unroll
+    for (int j = 0; j < R / 2; ++j) w[j] = tw_n<T, CT>(tw, j * R, n, sign);
+    // pass 1: thread n2 = r
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) v[n1] = cv ? in[base + (long long)(R * n1 + r) * H] : czero<CT>();
+    reg_dft<CT, R>(v, w);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = v[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, n, sign));
+        Z[(k1 * R + r) * NC + c] = y;
+    }
+    __syncthreads();
+    // pass 2: thread k1 = r
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) v[n2] = Z[(r * R + n2) * NC + c];
+    reg_dft<CT, R>(v, w);
+    if (cv) {
+        #pragma unroll
+        for (int k2 = 0; k2 < R; ++k2) out[base + (long long)(r + R * k2) * H] = v[brev<R>(k2)];
+    }
+}
+
+// inverse real transform along x (length nx = R*R), two rows per complex
+// FFT as rows_c2r_kernel, NP = 256/R row pairs per CTA
+template <typename T, int R>
+__global__ void __launch_bounds__(256) rows_c2r_sq_kernel(const typename CplxOf<T>::type* __restrict__ in,
+                                                          T* __restrict__ phys, long long nrows,
+                                                          const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int nx = R * R, H = nx / 2 + 1, half = nx / 2, NP = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* Z = (CT*)smraw;                                  // [pair][k1][R+1]
+    const int r = threadIdx.x % R, pp = threadIdx.x / R;
+    const long long r0 = 2LL * ((long long)blockIdx.x * NP + pp), r1 = r0 + 1;
+    const bool has0 = r0 < nrows, has1 = r1 < nrows;
+    CT w[R / 2];
+    #pragma unroll
+    for (int j = 0; j < R / 2; ++j) w[j] = tw_n<T, CT>(tw, j * R, nx, (T)1);
+    // pass 1: thread n2 = r gathers z[R n1 + n2] of the packed pair
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) {
+        const int idx = R * n1 + r;
+        const bool mirror = idx > half;
+        const int k = mirror ? nx - idx : idx;
+        const CT x1 = has0 ? in[r0 * H + k] : czero<CT>();
+        const CT x2 = has1 ? in[r1 * H + k] : czero<CT>();
+        CT z;
+        if (k == 0 || k == half) { z.x = x1.x; z.y = x2.x; }
+        else if (!mirror) { z.x = x1.x - x2.y; z.y = x1.y + x2.x; }
+        else { z.x = x1.x + x2.y; z.y = -x1.y + x2.x; }
+        v[n1] = z;
+    }
+    reg_dft<CT, R>(v, w);
+    CT* Zp = Z + pp * R * (R + 1);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = v[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, nx, (T)1));
+        Zp[k1 * (R + 1) + r] = y;
+    }
+    __syncthreads();
+    // pass 2: thread k1 = r
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) v[n2] = Zp[r * (R + 1) + n2];
+    reg_dft<CT, R>(v, w);
+    #pragma unroll
+    for (int k2 = 0; k2 < R; ++k2) {
+        const CT zz = v[brev<R>(k2)];
+        if (has0) phys[r0 * nx + r + R * k2] = zz.x;
+        if (has1) phys[r1 * nx + r + R * k2] = zz.y;
+    }
+}
+
+static int sq_radix(int n) { return n == 256 ? 16 : (n == 64 ? 8 : 0); }
+
 static int col_tile(int ny) { return ny >= 1024 ? 4 : (ny >= 512 ? 8 : 16); }
 
 template <typename T>
@@ -174,12 +318,40 @@ void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename Cp
     const long long nrows = (long long)ny * nplanes;
     const CT* src = spec;
     if (ny > 1) {
-        int W = col_tile(ny);
-        size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
-        set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
-        int ntile = (H + W - 1) / W;
-        cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, ny, H, W, (T)1, tw_y);
+        const int Ry = sq_radix(ny);
+        if (Ry == 16) {
+            const int ntile = (H + 15) / 16;
+            const size_t sm2 = (size_t)16 * 16 * 16 * sizeof(CT);
+            set_smem<T>((const void*)cols_fft_sq_kernel<T, 16>, sm2);
+            cols_fft_sq_kernel<T, 16><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y);
+        } else if (Ry == 8) {
+            const int ntile = (H + 31) / 32;
+            const size_t sm2 = (size_t)8 * 8 * 32 * sizeof(CT);
+            set_smem<T>((const void*)cols_fft_sq_kernel<T, 8>, sm2);
+            cols_fft_sq_kernel<T, 8><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y);
+        } else {
+            int W = col_tile(ny);
+            size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
+            set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
+            int ntile = (H + W - 1) / W;
+            cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, ny, H, W, (T)1, tw_y);
+        }
         src = tmp;
+    }
+    const int Rx = sq_radix(nx);
+    if (Rx == 16) {
+        const long long npairs = (nrows + 1) / 2;
+        const size_t sm = (size_t)16 * 16 * 17 * sizeof(CT);
+        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 16>, sm);
+        rows_c2r_sq_kernel<T, 16><<<(unsigned)((npairs + 15) / 16), 256, sm, s>>>(src, phys, nrows, tw_x);
+        return;
+    }
+    if (Rx == 8) {
+        const long long npairs = (nrows + 1) / 2;
+        const size_t sm = (size_t)32 * 8 * 9 * sizeof(CT);
+        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 8>, sm);
+        rows_c2r_sq_kernel<T, 8><<<(unsigned)((npairs + 31) / 32), 256, sm, s>>>(src, phys, nrows, tw_x);
+        return;
     }
     size_t sm = 2 * (size_t)nx * sizeof(CT);
     int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;

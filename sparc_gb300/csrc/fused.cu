@@ -31,6 +31,8 @@
 //     carry zero multipliers, so they never reach a real row.
 // HBM traffic per step: read a, write a (+ the PML planes and source planes),
 // and scr only on steps whose right-hand side is requested (outputs).
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace {
@@ -108,13 +110,15 @@ __device__ __forceinline__ Aff pencil_scan(Aff mine, int t, Aff* wb, int pi) {
 }
 
 // d/dz (without stretch) of the values of one exchange line (xp[j], j in
-// 0..NZP-1, ghosts at -2, -1, NZP, NZP+1) for the owned levels j0..j0+CH-1,
+// 0..NZP-1, ghosts at -2, -1, NZP, NZP+1; own[q] = xp[j0+q]) for the owned
+// levels j0..j0+CH-1,
 // boundary code BC (dbyd2.f90:94-173 for the right-hand side; top is the
 // caller-set value of bc 3).  tb: the five scan rows (ibd, m, H, g, G) of BC.
 template <int BC, int W>
-__device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const float* __restrict__ tb, int nz,
-                                       float2 top, int j0, bool lo, bool hi, int t, Aff* wbF, Aff* wbB, int pi,
-                                       const Compact<float> c, float2 (&out)[CH]) {
+__device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const float2 (&own)[CH],
+                                       const float* __restrict__ tb, int nz, float2 top, int j0, bool lo, bool hi,
+                                       int t, Aff* wbF, Aff* wbB, int pi, const Compact<float> c,
+                                       float2 (&out)[CH]) {
     constexpr int NZP = 160 * W;
     const float* ibd = tb;
     const float* mm = tb + NZP;
@@ -122,11 +126,17 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     const float* gg = tb + 3 * NZP;
     const float* GG = tb + 4 * NZP;
     float2 u[CH];
-    // interior right-hand side on every level (dbyd2.f90:88-92)
+    // interior right-hand side on every level (dbyd2.f90:88-92); the
+    // thread's own levels come from registers (own[q] == xp[j0+q]), the two
+    // levels on each side from the neighbours' entries of the line
     #pragma unroll
     for (int q = 0; q < CH; ++q) {
         const int j = j0 + q;
-        u[q] = c.C1 * (xp[j + 1] - xp[j - 1]) + c.C2 * (xp[j + 2] - xp[j - 2]);
+        const float2 bm2 = q >= 2 ? own[q - 2] : xp[j - 2];
+        const float2 bm1 = q >= 1 ? own[q - 1] : xp[j - 1];
+        const float2 bp1 = q + 1 < CH ? own[q + 1] : xp[j + 1];
+        const float2 bp2 = q + 2 < CH ? own[q + 2] : xp[j + 2];
+        u[q] = c.C1 * (bp1 - bm1) + c.C2 * (bp2 - bm2);
     }
     if (lo) {   // rows 0 and 1 (dbyd2.f90:104-173)
         const float2 b0 = xp[0], b1 = xp[1], b2 = xp[2], b3 = xp[3], b4 = xp[4];
@@ -231,7 +241,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     Aff* wbuf = (Aff*)(smraw + Ly.wbuf);                  // [4 scans][P][W]
     float* zs = (float*)(smraw + Ly.zs);                  // [FZ_COUNT][NZP]
     double* lagw = (double*)(smraw + Ly.lagw);            // [8] Lagrange weights of this slot
-    int* lagi = (int*)(smraw + Ly.lagi);                  // [8]: idx[7], count
+    int* lagi = (int*)(smraw + Ly.lagi);                  // [8]: sample index of each weight
     const int nthr = blockDim.x;
     const int pi = threadIdx.x / TP;                      // pencil within the CTA
     const int t = threadIdx.x - pi * TP;                  // chunk index
@@ -284,12 +294,13 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     }
     const int tl = A.clk.time - A.clk.t0[s];            // this slot's clock
     const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
-    if (threadIdx.x == 0 && src_on && A.src_mode == 2) {
-        int idx[7];
-        double w[7];
-        const int n = lagrange_dev(A.clk, tl, A.L, idx, w);
-        for (int l = 0; l < 7; ++l) { lagw[l] = l < n ? w[l] : 0.0; lagi[l] = l < n ? idx[l] : 0; }
-        lagi[7] = n;
+    if (threadIdx.x < 7 && src_on && A.src_mode == 2) {
+        // weight l on thread l (LAGRANGE_INTERP, physics.f90:683-734);
+        // samples that take no part get weight 0 and index 0
+        int id;
+        const double w = lagrange_weight(A.clk, tl, A.L, threadIdx.x, &id);
+        lagw[threadIdx.x] = w;
+        lagi[threadIdx.x] = id < 0 ? 0 : id;
     }
     for (int r = threadIdx.x; r < FZ_COUNT * NZP / 4; r += nthr)
         ((float4*)zs)[r] = __ldg((const float4*)A.ftab + r);
@@ -311,10 +322,9 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
             float w = (tl < A.nseries) ? (float)A.series[(long long)s * A.nseries + tl] : 0.f;
             F = w * pl[0];
         } else {
-            const int nw = lagi[7];
             #pragma unroll
             for (int l = 0; l < 7; ++l)
-                if (l < nw) F = F + (float)lagw[l] * pl[(long long)lagi[l] * M];
+                if (lagw[l] != 0.0) F = F + (float)lagw[l] * pl[(long long)lagi[l] * M];
         }
         F = A.src_scale * F;
     }
@@ -338,16 +348,17 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
     const float* ZBZ = zs + FZ_BZ * NZP;
     Aff* wb = wbuf + pi * W;                              // scan slot k at wb + k*P*W
 
-    for (int rk = 0; rk < 5; ++rk) {
-        // static parameter indices keep the argument block out of local memory
-        const float beta = rk == 0 ? A.betas[0] : rk == 1 ? A.betas[1] : rk == 2 ? A.betas[2]
-                         : rk == 3 ? A.betas[3] : A.betas[4];
-        const bool hs = rk > 0;
+    // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
+    // rather than a (stage 1), fixed at compile time
+    auto stage = [&](auto hs_c, const float beta) {
+        constexpr bool hs = decltype(hs_c)::value;
         // ---- temp xi_z into the first exchange line ----
+        float2 own[CH];
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             float2 v = TA(2, j0 + q);
             if (hs) v = v + beta * sc[2][q];
+            own[q] = v;
             xa[j0 + q] = v;
         }
         float2 top = make_float2(0.f, 0.f);
@@ -362,7 +373,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
         }
         pencil_sync(pi, TP);
         float2 d[CH];
-        zsolve<BCX, W>(xa, zs + FZ_SX * NZP, nz, top, j0, lo, hi, t, wb, wb + P * W, pi, A.cc, d);
+        zsolve<BCX, W>(xa, own, zs + FZ_SX * NZP, nz, top, j0, lo, hi, t, wb, wb + P * W, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) d[q] = d[q] * ZST[j0 + q];
         if (pml_t) {   // psi_vz (displacement.f90 PML rows)
@@ -394,6 +405,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
             const float2 p = -ZC2R[j] * div - ZGP[j] * xz;
             qt[q] = ZE1[j] * div + ZE2[j] * xz;            // -g rho'/rho0
             xb[j] = p;
+            own[q] = p;
             const float ri = ZRI[j];
             sc[3][q] = -ri * imul(kx, p) - gd * vx;
             sc[0][q] = vx;
@@ -411,7 +423,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
         }
         pencil_sync(pi, TP);
         // ---- dp'/dz, RHS v_z and xi_z ----
-        zsolve<BCP, W>(xb, zs + FZ_SP * NZP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, wb + 2 * P * W,
+        zsolve<BCP, W>(xb, own, zs + FZ_SP * NZP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, wb + 2 * P * W,
                        wb + 3 * P * W, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
@@ -445,6 +457,12 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
             for (int q = 0; q < CH; ++q)
                 if (j0 + q == nz - 1) sc[5][q] = sc[2][q] = make_float2(0.f, 0.f);
         }
+    };
+    stage(std::integral_constant<bool, false>(), 0.f);
+    for (int rk = 1; rk < 5; ++rk) {
+        // static parameter indices keep the argument block out of local memory
+        const float beta = rk == 1 ? A.betas[1] : rk == 2 ? A.betas[2] : rk == 3 ? A.betas[3] : A.betas[4];
+        stage(std::integral_constant<bool, true>(), beta);
     }
 
     // ---- update a += dt*scr, pml += dt*scrpml (step.f90:114-116) ----

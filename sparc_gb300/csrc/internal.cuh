@@ -159,27 +159,40 @@ __device__ __forceinline__ bool slot_src_on(const SlotClock& k, int tl) {
 // vr(:,:,time1-3+l) (returned 0-based in idx), at most 7.  In 3-D the forcing
 // is not re-interpolated after the gate (driver.f90:421-422), i.e. it keeps the
 // value it had at the gate.
-__device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, int* idx, double* w) {
+// One Lagrange weight l (0..6) of LAGRANGE_INTERP at local time tl: returns
+// the weight and sets *id to the 0-based sample index, or returns 0 with
+// *id = -1 when the sample l does not take part.
+__device__ __forceinline__ double lagrange_weight(const SlotClock& k, int tl, int L, int l, int* id) {
     int t = tl;
     if (!k.two_d && t > k.gate) t = k.gate;
     double xt = (double)t * k.ts / k.cad;
     const int time1 = (int)floor(xt) + 1;
     xt = t * k.ts;
-    double X[7];
+    const double Xl = (double)(time1 - 4 + l) * k.cad;
+    const bool cond = (l <= 3) ? (Xl >= 0) : (l == 4 ? true : (l == 5 ? time1 < k.num_steps : time1 < k.num_steps - 1));
+    const int i = time1 - 4 + l;
+    *id = -1;
+    if (!cond || i < 0 || i >= L) return 0.0;
+    double den = 1.0, num = 1.0;
     #pragma unroll
-    for (int l = 0; l < 7; ++l) X[l] = (double)(time1 - 4 + l) * k.cad;
+    for (int r = 0; r < 7; ++r) {
+        const double Xr = (double)(time1 - 4 + r) * k.cad;
+        if (r != l) { den *= (Xl - Xr); num *= (xt - Xr); }
+    }
+    *id = i;
+    return num / den;
+}
+
+// All weights, compacted: idx[0..n) and w[0..n).
+__device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, int* idx, double* w) {
     int n = 0;
     #pragma unroll
     for (int l = 0; l < 7; ++l) {
-        bool cond = (l <= 3) ? (X[l] >= 0) : (l == 4 ? true : (l == 5 ? time1 < k.num_steps : time1 < k.num_steps - 1));
-        const int id = time1 - 4 + l;
-        if (!cond || id < 0 || id >= L) continue;
-        double den = 1.0, num = 1.0;
-        #pragma unroll
-        for (int r = 0; r < 7; ++r)
-            if (r != l) { den *= (X[l] - X[r]); num *= (xt - X[r]); }
+        int id;
+        const double wl = lagrange_weight(k, tl, L, l, &id);
+        if (id < 0) continue;
         idx[n] = id;
-        w[n] = num / den;
+        w[n] = wl;
         ++n;
     }
     return n;
