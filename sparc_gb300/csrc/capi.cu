@@ -81,9 +81,10 @@ struct sparc_ctx {
     void* dck = nullptr; int dck_n = 0;
     std::vector<int> dck_time;
     // kernels
-    void* store = nullptr; int store_n = 0;     // [nsnap][S][7][N] T
+    void* store = nullptr; int store_n = 0;     // [nsnap][7][S][N] T (field-major within a snapshot)
     double* kacc = nullptr;                     // [S][3][N]
-    void* ktemp = nullptr;                      // [7][N] T
+    void* ktemp = nullptr;                      // [7][G][N] T, G = kernel_group(S)
+    void* gtmp = nullptr;                       // [G] spectral fields: transform scratch of a source group
 };
 
 namespace {
@@ -1010,7 +1011,7 @@ static int prim_spectral(sparc_ctx* c, const double* var, double* dvar, int whic
     if (rc) return rc;
     CK(cudaMemcpyAsync(c->phys64, var, c->N * 8, cudaMemcpyHostToDevice, c->stream));
     fft_phys_to_spec<double>(c->phys64, c->spec64, c->tmp64, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
-    launch_spec_dxdy<double>(c->spec64b, c->spec64, c->pt64, which, c->M, c->nz, c->stream);
+    launch_spec_dxdy<double>(c->spec64b, c->spec64, c->pt64, which, c->M, c->nz, 1, 0, 0, c->stream);
     fft_spec_to_phys<double>(c->spec64b, c->phys64, c->tmp64, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
     c->launches += 5;
     CKL();
@@ -1056,15 +1057,28 @@ int sparc_gpu_ddz(sparc_ctx* c, const double* var, double* dvar, int bc) {
 // ---------------------------------------------------------------------------
 }  // extern "C"
 
+// sources per batched snapshot / accumulation pass (bounds the scratch to
+// 7 physical + 1 spectral field per source of the group)
+static int kernel_group(int S) { return S < 8 ? S : 8; }
+
+// Physical fields of the kernel snapshot of sources s0..s0+G-1 into out
+// (field f of source s0+g at out + f*ofs + g*N).  Forward (kernels.f90:
+// 197-263): div(xi), f_acc = scr(v) (3), xi (3); adjoint: div(xi), v (3),
+// grad(g v_z) (3).  Every pass covers the whole group.
 template <typename T>
-static int derive_to_phys(sparc_ctx* c, int src, bool adjoint, T* out7) {
+static int derive_to_phys(sparc_ctx* c, int s0, int G, bool adjoint, T* out, long long ofs) {
     typedef typename CplxOf<T>::type CT;
     const long long fs = c->fs, N = c->N;
-    CT* a = CP<T>(c->a) + (long long)src * 6 * fs;
-    CT* scr = CP<T>(c->scr) + (long long)src * 6 * fs;
-    CT* D = CP<T>(c->ybuf);
+    CT* a = CP<T>(c->a) + (long long)s0 * 6 * fs;
+    CT* scr = CP<T>(c->scr) + (long long)s0 * 6 * fs;
+    CT* D = CP<T>(c->ybuf);      // [G][fs] each
     CT* D2 = CP<T>(c->pbuf);
     CT* D3 = CP<T>(c->rbuf);
+    if (!c->gtmp) {
+        int rc = dalloc(c, &c->gtmp, (size_t)kernel_group(c->S) * fs * 2 * esz(c));
+        if (rc) return rc;
+    }
+    CT* tmp = CP<T>(c->gtmp);
     Compact<T> cc;
     cc.C1 = (T)c->cc64.C1; cc.C2 = (T)c->cc64.C2;
     for (int i = 0; i < 5; ++i) cc.Cb[i] = (T)c->cc64.Cb[i];
@@ -1074,36 +1088,38 @@ static int derive_to_phys(sparc_ctx* c, int src, bool adjoint, T* out7) {
     const T* pt = (const T*)c->pt;
     const int nx = c->P.nx, ny = c->P.ny, nz = c->nz, M = c->M;
     const bool use_y = ny > 4;
-    auto tophys = [&](const CT* spec, T* dst) {
-        fft_spec_to_phys<T>(spec, dst, CP<T>(c->tmp), nx, ny, nz, c->tw_x, c->tw_y, c->stream);
+    // spectral fields of the group -> physical: src_ss = source stride of the input
+    auto tophys = [&](const CT* spec, long long src_ss, T* dst) {
+        fft_spec_to_phys_g<T>(spec, nz, src_ss, dst, tmp, nx, ny, G * nz, c->tw_x, c->tw_y, c->stream);
         c->launches += 2;
     };
     // divergence: ddxkern + ddykern + ddzkern(bc=1, filtered)  (COMPUTE_DIV kernels.f90:798-816)
     const int fx = adjoint ? 3 : 0;
-    launch_zderiv<T>(zt, cc, a + (fx + 2) * fs, D, M, nz, 1, 1, nullptr, c->stream);
-    launch_spec_combine<T>(D, a + fx * fs, use_y ? a + (fx + 1) * fs : nullptr, pt, M, nz, c->stream);
+    launch_zderiv<T>(zt, cc, a + (fx + 2) * fs, D, M, nz, 1, 1, nullptr, G, 6 * fs, fs, c->stream);
+    launch_spec_combine<T>(D, a + fx * fs, use_y ? a + (fx + 1) * fs : nullptr, pt, M, nz, G, fs, 6 * fs, c->stream);
     c->launches += 2;
-    tophys(D, out7);
+    tophys(D, fs, out);
     if (!adjoint) {
-        for (int q = 0; q < 3; ++q) tophys(scr + (3 + q) * fs, out7 + (1 + q) * N);   // f_acc
-        for (int q = 0; q < 3; ++q) tophys(a + q * fs, out7 + (4 + q) * N);           // f_xi
+        for (int q = 0; q < 3; ++q) tophys(scr + (3 + q) * fs, 6 * fs, out + (1 + q) * ofs);   // f_acc
+        for (int q = 0; q < 3; ++q) tophys(a + q * fs, 6 * fs, out + (4 + q) * ofs);           // f_xi
     } else {
-        for (int q = 0; q < 3; ++q) tophys(a + (3 + q) * fs, out7 + (1 + q) * N);     // a_v
+        for (int q = 0; q < 3; ++q) tophys(a + (3 + q) * fs, 6 * fs, out + (1 + q) * ofs);     // a_v
         // grad(a_vz * grav) (kernels.f90:299-304)
-        launch_spec_scale_z<T>(D2, a + 5 * fs, zt, ZT_GRAW, M, nz, c->stream);
-        launch_spec_dxdy<T>(D3, D2, pt, 0, M, nz, c->stream);
+        launch_spec_scale_z<T>(D2, a + 5 * fs, zt, ZT_GRAW, M, nz, G, fs, 6 * fs, c->stream);
+        launch_spec_dxdy<T>(D3, D2, pt, 0, M, nz, G, fs, fs, c->stream);
         c->launches += 2;
-        tophys(D3, out7 + 4 * N);
+        tophys(D3, fs, out + 4 * ofs);
         if (use_y) {
-            launch_spec_dxdy<T>(D3, D2, pt, 1, M, nz, c->stream);
+            launch_spec_dxdy<T>(D3, D2, pt, 1, M, nz, G, fs, fs, c->stream);
             c->launches++;
-            tophys(D3, out7 + 5 * N);
+            tophys(D3, fs, out + 5 * ofs);
         } else {
-            CK(cudaMemsetAsync(out7 + 5 * N, 0, N * sizeof(T), c->stream));
+            for (int g = 0; g < G; ++g)
+                CK(cudaMemsetAsync(out + 5 * ofs + (long long)g * N, 0, N * sizeof(T), c->stream));
         }
-        launch_zderiv<T>(zt, cc, D2, D3, M, nz, 1, 1, nullptr, c->stream);
+        launch_zderiv<T>(zt, cc, D2, D3, M, nz, 1, 1, nullptr, G, fs, fs, c->stream);
         c->launches++;
-        tophys(D3, out7 + 6 * N);
+        tophys(D3, fs, out + 6 * ofs);
     }
     CKL();
     return SPARC_OK;
@@ -1121,10 +1137,13 @@ int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
         c->store_n = nsnap;
     }
     if (snap < 0 || snap >= c->store_n) return fail(c, SPARC_EINVAL, "snapshot index out of range");
-    for (int s = 0; s < c->S; ++s) {
-        char* dst = (char*)c->store + ((size_t)snap * c->S + s) * 7 * c->N * esz(c);
-        int rc = c->f32 ? derive_to_phys<float>(c, s, false, (float*)dst)
-                        : derive_to_phys<double>(c, s, false, (double*)dst);
+    const int G = kernel_group(c->S);
+    const long long ofs = (long long)c->S * c->N;          // field stride of the store
+    for (int s0 = 0; s0 < c->S; s0 += G) {
+        const int g = std::min(G, c->S - s0);
+        char* dst = (char*)c->store + ((size_t)snap * 7 * c->S + s0) * c->N * esz(c);
+        int rc = c->f32 ? derive_to_phys<float>(c, s0, g, false, (float*)dst, ofs)
+                        : derive_to_phys<double>(c, s0, g, false, (double*)dst, ofs);
         if (rc) return rc;
     }
     return SPARC_OK;
@@ -1146,23 +1165,28 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
     if (!fwd->store || snap < 0 || snap >= fwd->store_n) return fail(c, SPARC_EINVAL, "no such forward snapshot");
     if (fwd->S != c->S || fwd->N != c->N || fwd->f32 != c->f32) return fail(c, SPARC_EINVAL, "forward/adjoint contexts differ");
     if (!c->kacc) { int rc = sparc_gpu_kernel_reset(c); if (rc) return rc; }
-    if (!c->ktemp) { int rc = dalloc(c, &c->ktemp, (size_t)7 * c->N * esz(c)); if (rc) return rc; }
+    const int G = kernel_group(c->S);
+    if (!c->ktemp) { int rc = dalloc(c, &c->ktemp, (size_t)7 * G * c->N * esz(c)); if (rc) return rc; }
     // the forward snapshot is written on the forward context's stream: the
     // adjoint stream waits for it (no host synchronisation)
     CK(cudaEventRecord(fwd->ev_done, fwd->stream));
     CK(cudaStreamWaitEvent(c->stream, fwd->ev_done, 0));
-    for (int s = 0; s < c->S; ++s) {
-        const char* f7 = (const char*)fwd->store + ((size_t)snap * c->S + s) * 7 * c->N * esz(c);
-        double* acc = c->kacc + (size_t)s * 3 * c->N;
+    const long long N = c->N, sfs = (long long)c->S * N;     // store field stride
+    for (int s0 = 0; s0 < c->S; s0 += G) {
+        const int g = std::min(G, c->S - s0);
+        const size_t f7 = ((size_t)snap * 7 * c->S + s0) * N;  // element offset of field 0, source s0
+        double* acc = c->kacc + (size_t)s0 * 3 * N;
         int rc;
         if (c->f32) {
-            rc = derive_to_phys<float>(c, s, true, (float*)c->ktemp);
+            rc = derive_to_phys<float>(c, s0, g, true, (float*)c->ktemp, (long long)g * N);
             if (rc) return rc;
-            launch_kernel_accum<float>(acc, (const float*)f7, (const float*)c->ktemp, c->zt64, c->NP, c->nz, c->P.ny > 4, c->stream);
+            launch_kernel_accum<float>(acc, (const float*)fwd->store + f7, sfs, (const float*)c->ktemp,
+                                       (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream);
         } else {
-            rc = derive_to_phys<double>(c, s, true, (double*)c->ktemp);
+            rc = derive_to_phys<double>(c, s0, g, true, (double*)c->ktemp, (long long)g * N);
             if (rc) return rc;
-            launch_kernel_accum<double>(acc, (const double*)f7, (const double*)c->ktemp, c->zt64, c->NP, c->nz, c->P.ny > 4, c->stream);
+            launch_kernel_accum<double>(acc, (const double*)fwd->store + f7, sfs, (const double*)c->ktemp,
+                                        (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream);
         }
         c->launches++;
         CKL();

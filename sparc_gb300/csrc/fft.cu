@@ -13,6 +13,13 @@
 // accumulation of kernels.f90:273-311 on physical fields.
 #include "internal.cuh"
 
+// offset of input plane p when planes come in groups of ppg, group g starting
+// at g * gstride (complex elements); pe = elements per plane
+__device__ __forceinline__ long long grp_off(long long p, int ppg, long long gstride, long long pe) {
+    const long long g = p / ppg;
+    return g * gstride + (p - g * ppg) * pe;
+}
+
 // Stockham radix-2 over `count` sequences of length n stored back to back in
 // src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
 // cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
@@ -79,7 +86,8 @@ __global__ void rows_r2c_kernel(const T* __restrict__ phys, typename CplxOf<T>::
 // in (nrows rows of H complex) -> phys (nrows rows of nx reals), inverse, unscaled
 template <typename T>
 __global__ void rows_c2r_kernel(const typename CplxOf<T>::type* __restrict__ in, T* __restrict__ phys,
-                                int nx, long long nrows, const double* __restrict__ tw) {
+                                int nx, long long nrows, const double* __restrict__ tw, int ny, int ppg,
+                                long long gstride) {
     typedef typename CplxOf<T>::type CT;
     extern __shared__ __align__(16) unsigned char smraw[];
     CT* b0 = (CT*)smraw;
@@ -87,9 +95,12 @@ __global__ void rows_c2r_kernel(const typename CplxOf<T>::type* __restrict__ in,
     const long long r0 = 2LL * blockIdx.x, r1 = r0 + 1;
     const bool has1 = r1 < nrows;
     const int H = nx / 2 + 1, half = nx / 2;
+    const long long pe = (long long)ny * H;
+    const long long o0 = grp_off(r0 / ny, ppg, gstride, pe) + (r0 % ny) * H;
+    const long long o1 = has1 ? grp_off(r1 / ny, ppg, gstride, pe) + (r1 % ny) * H : 0;
     for (int k = threadIdx.x; k <= half; k += blockDim.x) {
-        CT x1 = in[r0 * H + k];
-        CT x2 = has1 ? in[r1 * H + k] : czero<CT>();
+        CT x1 = in[o0 + k];
+        CT x2 = has1 ? in[o1 + k] : czero<CT>();
         if (k == 0 || k == half) {
             CT z; z.x = x1.x; z.y = x2.x;
             b0[k] = z;
@@ -114,7 +125,7 @@ __global__ void rows_c2r_kernel(const typename CplxOf<T>::type* __restrict__ in,
 template <typename T>
 __global__ void cols_fft_kernel(const typename CplxOf<T>::type* __restrict__ in,
                                 typename CplxOf<T>::type* __restrict__ out, int ny, int H, int W, T sign,
-                                const double* __restrict__ tw) {
+                                const double* __restrict__ tw, int ppg, long long gstride) {
     typedef typename CplxOf<T>::type CT;
     extern __shared__ __align__(16) unsigned char smraw[];
     CT* b0 = (CT*)smraw;
@@ -124,9 +135,10 @@ __global__ void cols_fft_kernel(const typename CplxOf<T>::type* __restrict__ in,
     const int kx0 = (blockIdx.x % ntile) * W;
     const int w = min(W, H - kx0);
     const long long base = plane * (long long)ny * H;
+    const long long ibase = grp_off(plane, ppg, gstride, (long long)ny * H);
     for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
         int y = t / W, c = t - y * W;
-        b0[c * ny + y] = (c < w) ? in[base + (long long)y * H + kx0 + c] : czero<CT>();
+        b0[c * ny + y] = (c < w) ? in[ibase + (long long)y * H + kx0 + c] : czero<CT>();
     }
     __syncthreads();
     CT* Z = smem_fft<T, CT>(b0, b1, ny, W, sign, tw);
@@ -190,7 +202,8 @@ __host__ __device__ constexpr int brev(int k) {
 template <typename T, int R>
 __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<T>::type* __restrict__ in,
                                                           typename CplxOf<T>::type* __restrict__ out, int H,
-                                                          T sign, const double* __restrict__ tw) {
+                                                          T sign, const double* __restrict__ tw, int ppg,
+                                                          long long gstride) {
     typedef typename CplxOf<T>::type CT;
     constexpr int n = R * R, NC = 256 / R;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -201,13 +214,14 @@ __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<
     const int c = threadIdx.x % NC, r = threadIdx.x / NC;
     const bool cv = kx0 + c < H;
     const long long base = plane * (long long)n * H + kx0 + c;
+    const long long ibase = grp_off(plane, ppg, gstride, (long long)n * H) + kx0 + c;
     CT w[R / 2];
     #pragma unroll
     for (int j = 0; j < R / 2; ++j) w[j] = tw_n<T, CT>(tw, j * R, n, sign);
     // pass 1: thread n2 = r
     CT v[R];
     #pragma unroll
-    for (int n1 = 0; n1 < R; ++n1) v[n1] = cv ? in[base + (long long)(R * n1 + r) * H] : czero<CT>();
+    for (int n1 = 0; n1 < R; ++n1) v[n1] = cv ? in[ibase + (long long)(R * n1 + r) * H] : czero<CT>();
     reg_dft<CT, R>(v, w);
     #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
@@ -231,7 +245,8 @@ __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<
 template <typename T, int R>
 __global__ void __launch_bounds__(256) rows_c2r_sq_kernel(const typename CplxOf<T>::type* __restrict__ in,
                                                           T* __restrict__ phys, long long nrows,
-                                                          const double* __restrict__ tw) {
+                                                          const double* __restrict__ tw, int ny, int ppg,
+                                                          long long gstride) {
     typedef typename CplxOf<T>::type CT;
     constexpr int nx = R * R, H = nx / 2 + 1, half = nx / 2, NP = 256 / R;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -239,6 +254,9 @@ __global__ void __launch_bounds__(256) rows_c2r_sq_kernel(const typename CplxOf<
     const int r = threadIdx.x % R, pp = threadIdx.x / R;
     const long long r0 = 2LL * ((long long)blockIdx.x * NP + pp), r1 = r0 + 1;
     const bool has0 = r0 < nrows, has1 = r1 < nrows;
+    const long long pe = (long long)ny * H;
+    const long long o0 = has0 ? grp_off(r0 / ny, ppg, gstride, pe) + (r0 % ny) * H : 0;
+    const long long o1 = has1 ? grp_off(r1 / ny, ppg, gstride, pe) + (r1 % ny) * H : 0;
     CT w[R / 2];
     #pragma unroll
     for (int j = 0; j < R / 2; ++j) w[j] = tw_n<T, CT>(tw, j * R, nx, (T)1);
@@ -249,8 +267,8 @@ __global__ void __launch_bounds__(256) rows_c2r_sq_kernel(const typename CplxOf<
         const int idx = R * n1 + r;
         const bool mirror = idx > half;
         const int k = mirror ? nx - idx : idx;
-        const CT x1 = has0 ? in[r0 * H + k] : czero<CT>();
-        const CT x2 = has1 ? in[r1 * H + k] : czero<CT>();
+        const CT x1 = has0 ? in[o0 + k] : czero<CT>();
+        const CT x2 = has1 ? in[o1 + k] : czero<CT>();
         CT z;
         if (k == 0 || k == half) { z.x = x1.x; z.y = x2.x; }
         else if (!mirror) { z.x = x1.x - x2.y; z.y = x1.y + x2.x; }
@@ -306,66 +324,81 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
         size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
         set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
         int ntile = (H + W - 1) / W;
-        cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(tmp, spec, ny, H, W, (T)-1, tw_y);
+        cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(tmp, spec, ny, H, W, (T)-1, tw_y,
+                                                                                   nplanes, 0LL);
     }
 }
 
 template <typename T>
-void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
-                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s) {
+void fft_spec_to_phys_g(const typename CplxOf<T>::type* spec, int ppg, long long gstride, T* phys,
+                        typename CplxOf<T>::type* tmp, int nx, int ny, int nplanes, const double* tw_x,
+                        const double* tw_y, cudaStream_t s) {
     typedef typename CplxOf<T>::type CT;
     const int H = nx / 2 + 1;
     const long long nrows = (long long)ny * nplanes;
     const CT* src = spec;
+    int rppg = ppg;
+    long long rgs = gstride;
     if (ny > 1) {
         const int Ry = sq_radix(ny);
+        const unsigned blocks16 = (unsigned)(((H + 15) / 16) * (long long)nplanes);
+        const unsigned blocks8 = (unsigned)(((H + 31) / 32) * (long long)nplanes);
         if (Ry == 16) {
-            const int ntile = (H + 15) / 16;
             const size_t sm2 = (size_t)16 * 16 * 16 * sizeof(CT);
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 16>, sm2);
-            cols_fft_sq_kernel<T, 16><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y);
+            cols_fft_sq_kernel<T, 16><<<blocks16, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride);
         } else if (Ry == 8) {
-            const int ntile = (H + 31) / 32;
             const size_t sm2 = (size_t)8 * 8 * 32 * sizeof(CT);
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 8>, sm2);
-            cols_fft_sq_kernel<T, 8><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y);
+            cols_fft_sq_kernel<T, 8><<<blocks8, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride);
         } else {
             int W = col_tile(ny);
             size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
             set_smem<T>((const void*)cols_fft_kernel<T>, sm2);
             int ntile = (H + W - 1) / W;
-            cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, ny, H, W, (T)1, tw_y);
+            cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(spec, tmp, ny, H, W, (T)1, tw_y,
+                                                                                       ppg, gstride);
         }
         src = tmp;
+        rppg = nplanes;      // tmp is contiguous
+        rgs = 0;
     }
     const int Rx = sq_radix(nx);
+    const long long npairs = (nrows + 1) / 2;
     if (Rx == 16) {
-        const long long npairs = (nrows + 1) / 2;
         const size_t sm = (size_t)16 * 16 * 17 * sizeof(CT);
         set_smem<T>((const void*)rows_c2r_sq_kernel<T, 16>, sm);
-        rows_c2r_sq_kernel<T, 16><<<(unsigned)((npairs + 15) / 16), 256, sm, s>>>(src, phys, nrows, tw_x);
+        rows_c2r_sq_kernel<T, 16><<<(unsigned)((npairs + 15) / 16), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
         return;
     }
     if (Rx == 8) {
-        const long long npairs = (nrows + 1) / 2;
         const size_t sm = (size_t)32 * 8 * 9 * sizeof(CT);
         set_smem<T>((const void*)rows_c2r_sq_kernel<T, 8>, sm);
-        rows_c2r_sq_kernel<T, 8><<<(unsigned)((npairs + 31) / 32), 256, sm, s>>>(src, phys, nrows, tw_x);
+        rows_c2r_sq_kernel<T, 8><<<(unsigned)((npairs + 31) / 32), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
         return;
     }
     size_t sm = 2 * (size_t)nx * sizeof(CT);
     int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
     set_smem<T>((const void*)rows_c2r_kernel<T>, sm);
-    rows_c2r_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(src, phys, nx, nrows, tw_x);
+    rows_c2r_kernel<T><<<(unsigned)npairs, thr, sm, s>>>(src, phys, nx, nrows, tw_x, ny, rppg, rgs);
+}
+
+template <typename T>
+void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s) {
+    fft_spec_to_phys_g<T>(spec, nplanes, 0LL, phys, tmp, nx, ny, nplanes, tw_x, tw_y, s);
 }
 
 // out = out + i kx fx + i ky fy   (fy may be null)
 template <typename T>
 __global__ void spec_combine_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
                                     const typename CplxOf<T>::type* fy, const T* __restrict__ pt, int M,
-                                    long long n) {
+                                    long long n, long long out_ss, long long in_ss) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
+    out += blockIdx.y * out_ss;
+    fx += blockIdx.y * in_ss;
+    if (fy) fy += blockIdx.y * in_ss;
     int m = (int)(t % M);
     typename CplxOf<T>::type d = imul(pt[PT_KX * (long long)M + m], fx[t]);
     if (fy) d = d + imul(pt[PT_KY * (long long)M + m], fy[t]);
@@ -375,9 +408,12 @@ __global__ void spec_combine_kernel(typename CplxOf<T>::type* out, const typenam
 // out(z) = in(z) * zt[row][z]
 template <typename T>
 __global__ void spec_scale_z_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
-                                    const T* __restrict__ zt, int row, int M, int nz) {
+                                    const T* __restrict__ zt, int row, int M, int nz, long long out_ss,
+                                    long long in_ss) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)M * nz) return;
+    out += blockIdx.y * out_ss;
+    in += blockIdx.y * in_ss;
     int z = (int)(t / M);
     out[t] = in[t] * zt[row * nz + z];
 }
@@ -385,36 +421,56 @@ __global__ void spec_scale_z_kernel(typename CplxOf<T>::type* out, const typenam
 // which: 0 -> i kx * in, 1 -> i ky * in, 2 -> damping rate * in
 template <typename T>
 __global__ void spec_dxdy_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
-                                 const T* __restrict__ pt, int which, int M, long long n) {
+                                 const T* __restrict__ pt, int which, int M, long long n, long long out_ss,
+                                 long long in_ss) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
+    out += blockIdx.y * out_ss;
+    in += blockIdx.y * in_ss;
     int m = (int)(t % M);
     if (which == 0) out[t] = imul(pt[PT_KX * (long long)M + m], in[t]);
     else if (which == 1) out[t] = imul(pt[PT_KY * (long long)M + m], in[t]);
     else out[t] = pt[PT_DAMP * (long long)M + m] * in[t];
 }
 
-// Sensitivity-kernel accumulation, kernels.f90:276-311.  fwd planes:
-// 0 div(f_xi), 1-3 f_acc (x,y,z), 4-6 f_xi (x,y,z); adj planes: 0 div(a_v),
-// 1-3 a_v, 4-6 grad(g a_vz).  acc: 0 kernelc2, 1 kernelrho, 2 hessian (FP64).
+// Sensitivity-kernel accumulation, kernels.f90:276-311, for nsrc sources at
+// once.  fwd planes (field stride fwd_fs, source stride N): 0 div(f_xi), 1-3
+// f_acc (x,y,z), 4-6 f_xi (x,y,z); adj planes (stride adj_fs): 0 div(a_v), 1-3
+// a_v, 4-6 grad(g a_vz).  acc [src][3][N]: kernelc2, kernelrho, hessian, FP64.
+// The time integral is FP64; the per-snapshot products are formed in T (the
+// fields' own precision).
 template <typename T>
-__global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restrict__ fwd, const T* __restrict__ adj,
-                                    const double* __restrict__ zt64, long long NP, int nz, int use_y) {
+__global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restrict__ fwd, long long fwd_fs,
+                                    const T* __restrict__ adj, long long adj_fs, const double* __restrict__ zt64,
+                                    long long NP, int nz, int use_y, int nsrc) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long N = NP * nz;
-    if (t >= N) return;
-    const int z = (int)(t / NP);
-    const double c2 = zt64[ZT_C2 * nz + z], g = zt64[ZT_GRAW * nz + z];
-    const double f1 = fwd[t], fax = fwd[N + t], fay = use_y ? (double)fwd[2 * N + t] : 0.0, faz = fwd[3 * N + t];
-    const double fxx = fwd[4 * N + t], fxy = use_y ? (double)fwd[5 * N + t] : 0.0, fxz = fwd[6 * N + t];
-    const double a1 = adj[t], avx = adj[N + t], avy = use_y ? (double)adj[2 * N + t] : 0.0, avz = adj[3 * N + t];
-    const double d31 = adj[4 * N + t], d32 = use_y ? (double)adj[5 * N + t] : 0.0, d33 = adj[6 * N + t];
-    acc[2 * N + t] = acc[2 * N + t] + faz * faz + fax * fax + fay * fay;
-    const double t1 = f1 * a1;
-    acc[t] = acc[t] + t1;
-    double kr = acc[N + t] + t1 * c2 + faz * avz + fax * avx + fay * avy;
-    kr = kr - g * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
-    acc[N + t] = kr;
+    if (t >= N * nsrc) return;
+    const long long g = t / N, i = t - g * N;
+    const int z = (int)(i / NP);
+    double* A = acc + g * 3 * N;
+    const T zero = (T)0;
+    const T f1 = fwd[t], fax = fwd[fwd_fs + t], fay = use_y ? fwd[2 * fwd_fs + t] : zero, faz = fwd[3 * fwd_fs + t];
+    const T fxx = fwd[4 * fwd_fs + t], fxy = use_y ? fwd[5 * fwd_fs + t] : zero, fxz = fwd[6 * fwd_fs + t];
+    const T a1 = adj[t], avx = adj[adj_fs + t], avy = use_y ? adj[2 * adj_fs + t] : zero, avz = adj[3 * adj_fs + t];
+    const T d31 = adj[4 * adj_fs + t], d32 = use_y ? adj[5 * adj_fs + t] : zero, d33 = adj[6 * adj_fs + t];
+    if constexpr (sizeof(T) == 8) {
+        const double c2 = zt64[ZT_C2 * nz + z], gr = zt64[ZT_GRAW * nz + z];
+        A[2 * N + i] = A[2 * N + i] + faz * faz + fax * fax + fay * fay;
+        const double t1 = f1 * a1;
+        A[i] = A[i] + t1;
+        double kr = A[N + i] + t1 * c2 + faz * avz + fax * avx + fay * avy;
+        kr = kr - gr * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
+        A[N + i] = kr;
+    } else {
+        const T c2 = (T)zt64[ZT_C2 * nz + z], gr = (T)zt64[ZT_GRAW * nz + z];
+        const T h = faz * faz + fax * fax + fay * fay;
+        const T t1 = f1 * a1;
+        const T kr = t1 * c2 + faz * avz + fax * avx + fay * avy - gr * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
+        A[2 * N + i] += (double)h;
+        A[i] += (double)t1;
+        A[N + i] += (double)kr;
+    }
 }
 
 // Final scaling kernels.f90:523-539, optionally summed over nsum slots
@@ -461,25 +517,27 @@ static unsigned nblk(long long n, int b = 256) { return (unsigned)((n + b - 1) /
 
 template <typename T>
 void launch_spec_combine(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
-                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, cudaStream_t s) {
+                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, int nsrc, long long out_ss,
+                         long long in_ss, cudaStream_t s) {
     long long n = (long long)M * nz;
-    spec_combine_kernel<T><<<nblk(n), 256, 0, s>>>(out, fx, fy, pt, M, n);
+    spec_combine_kernel<T><<<dim3(nblk(n), nsrc), 256, 0, s>>>(out, fx, fy, pt, M, n, out_ss, in_ss);
 }
 template <typename T>
 void launch_spec_scale_z(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in, const T* zt, int row,
-                         int M, int nz, cudaStream_t s) {
-    spec_scale_z_kernel<T><<<nblk((long long)M * nz), 256, 0, s>>>(out, in, zt, row, M, nz);
+                         int M, int nz, int nsrc, long long out_ss, long long in_ss, cudaStream_t s) {
+    spec_scale_z_kernel<T><<<dim3(nblk((long long)M * nz), nsrc), 256, 0, s>>>(out, in, zt, row, M, nz, out_ss, in_ss);
 }
 template <typename T>
 void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in, const T* pt, int which,
-                      int M, int nz, cudaStream_t s) {
+                      int M, int nz, int nsrc, long long out_ss, long long in_ss, cudaStream_t s) {
     long long n = (long long)M * nz;
-    spec_dxdy_kernel<T><<<nblk(n), 256, 0, s>>>(out, in, pt, which, M, n);
+    spec_dxdy_kernel<T><<<dim3(nblk(n), nsrc), 256, 0, s>>>(out, in, pt, which, M, n, out_ss, in_ss);
 }
 template <typename T>
-void launch_kernel_accum(double* acc, const T* fwd, const T* adj, const double* zt64, long long NP, int nz, int use_y,
-                         cudaStream_t s) {
-    kernel_accum_kernel<T><<<nblk(NP * nz), 256, 0, s>>>(acc, fwd, adj, zt64, NP, nz, use_y);
+void launch_kernel_accum(double* acc, const T* fwd, long long fwd_fs, const T* adj, long long adj_fs,
+                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s) {
+    kernel_accum_kernel<T><<<nblk(NP * nz * nsrc), 256, 0, s>>>(acc, fwd, fwd_fs, adj, adj_fs, zt64, NP, nz, use_y,
+                                                                nsrc);
 }
 void launch_kernel_finish(double* out, const double* acc, const double* zt64, long long NP, int nz, double scale_c,
                           double scale_r, int nsum, long long acc_ss, cudaStream_t s) {
@@ -505,14 +563,16 @@ int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t
                                       const double*, cudaStream_t);                                               \
     template void fft_spec_to_phys<T>(const CplxOf<T>::type*, T*, CplxOf<T>::type*, int, int, int, const double*, \
                                       const double*, cudaStream_t);                                               \
+    template void fft_spec_to_phys_g<T>(const CplxOf<T>::type*, int, long long, T*, CplxOf<T>::type*, int, int, \
+                                        int, const double*, const double*, cudaStream_t);                         \
     template void launch_spec_combine<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const CplxOf<T>::type*,       \
-                                         const T*, int, int, cudaStream_t);                                       \
-    template void launch_spec_scale_z<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int,      \
-                                         cudaStream_t);                                                           \
-    template void launch_spec_dxdy<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int,         \
-                                      cudaStream_t);                                                              \
-    template void launch_kernel_accum<T>(double*, const T*, const T*, const double*, long long, int, int,         \
-                                         cudaStream_t);                                                           \
+                                         const T*, int, int, int, long long, long long, cudaStream_t);            \
+    template void launch_spec_scale_z<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int, int, \
+                                         long long, long long, cudaStream_t);                                     \
+    template void launch_spec_dxdy<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int, int,    \
+                                      long long, long long, cudaStream_t);                                        \
+    template void launch_kernel_accum<T>(double*, const T*, long long, const T*, long long, const double*,       \
+                                         long long, int, int, int, cudaStream_t);                                 \
     template void launch_copy_convert<T>(T*, const double*, long long, cudaStream_t);                             \
     template void launch_copy_back<T>(double*, const T*, long long, cudaStream_t);
 INST(double)

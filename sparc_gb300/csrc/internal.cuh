@@ -266,7 +266,8 @@ void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* 
 template <typename T>
 void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,
                    typename CplxOf<T>::type* out, long long n1, int nz, int bc, int filter,
-                   const typename CplxOf<T>::type* top_plane, cudaStream_t s);
+                   const typename CplxOf<T>::type* top_plane, int nsrc, long long in_ss, long long out_ss,
+                   cudaStream_t s);
 void launch_zderiv_real(const double* zt, const Compact<double>& cc, const double* in, double* out,
                         long long n1, int nz, int bc, cudaStream_t s);
 
@@ -290,20 +291,32 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
 template <typename T>
 void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
                       int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);
+// the same with grouped input planes: plane p of the input starts at
+// spec + (p / ppg) * gstride + (p % ppg) * ny * (nx/2+1) (complex elements);
+// phys and tmp are contiguous
+template <typename T>
+void fft_spec_to_phys_g(const typename CplxOf<T>::type* spec, int ppg, long long gstride, T* phys,
+                        typename CplxOf<T>::type* tmp, int nx, int ny, int nplanes, const double* tw_x,
+                        const double* tw_y, cudaStream_t s);
 
 // kernel (sensitivity) helpers (fft.cu)
+// (nsrc sources on grid.y; out_ss / in_ss: per-source strides in elements)
 template <typename T>
 void launch_spec_combine(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* fx,
-                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, cudaStream_t s);
+                         const typename CplxOf<T>::type* fy, const T* pt, int M, int nz, int nsrc, long long out_ss,
+                         long long in_ss, cudaStream_t s);
 template <typename T>
 void launch_spec_scale_z(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
-                         const T* zt, int row, int M, int nz, cudaStream_t s);
+                         const T* zt, int row, int M, int nz, int nsrc, long long out_ss, long long in_ss,
+                         cudaStream_t s);
 template <typename T>
 void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
-                      const T* pt, int which, int M, int nz, cudaStream_t s);
+                      const T* pt, int which, int M, int nz, int nsrc, long long out_ss, long long in_ss,
+                      cudaStream_t s);
+// acc [nsrc][3][N]; fwd field f of source g at fwd + f*fwd_fs + g*N, adj likewise
 template <typename T>
-void launch_kernel_accum(double* acc /* 3*N */, const T* fwd /* 7*N */, const T* adj /* 7*N */,
-                         const double* zt64, long long NP, int nz, int use_y, cudaStream_t s);
+void launch_kernel_accum(double* acc, const T* fwd, long long fwd_fs, const T* adj, long long adj_fs,
+                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s);
 template <typename T>
 void launch_copy_convert(T* dst, const double* src, long long n, cudaStream_t s);
 template <typename T>

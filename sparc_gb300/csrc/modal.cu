@@ -210,12 +210,13 @@ __global__ void __launch_bounds__(128) zderiv_kernel(const T* __restrict__ zt, C
                                                      const typename CplxOf<T>::type* __restrict__ in,
                                                      typename CplxOf<T>::type* __restrict__ out,
                                                      long long n1, int nz, int bc, int filter,
-                                                     const typename CplxOf<T>::type* __restrict__ top_plane) {
+                                                     const typename CplxOf<T>::type* __restrict__ top_plane,
+                                                     long long in_ss, long long out_ss) {
     typedef typename CplxOf<T>::type CT;
     long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n1) return;
-    const CT* b = in + m;
-    CT* o = out + m;
+    const CT* b = in + blockIdx.y * in_ss + m;
+    CT* o = out + blockIdx.y * out_ss + m;
     CT top = top_plane ? top_plane[m] : czero<CT>();
     compact_forward<CT, T>(nz, bc, [&](int j) { return b[(long long)j * n1]; }, czero<CT>(), top,
                            zt + (ZT_TH + 3 * bc) * nz, zt + (ZT_TH + 3 * bc + 1) * nz, cc, o, n1);
@@ -289,8 +290,11 @@ template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaS
 template <typename T>
 void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,
                    typename CplxOf<T>::type* out, long long n1, int nz, int bc, int filter,
-                   const typename CplxOf<T>::type* top_plane, cudaStream_t s) {
-    zderiv_kernel<T><<<(unsigned)((n1 + 127) / 128), 128, 0, s>>>(zt, cc, in, out, n1, nz, bc, filter, top_plane);
+                   const typename CplxOf<T>::type* top_plane, int nsrc, long long in_ss, long long out_ss,
+                   cudaStream_t s) {
+    // top_plane (bc 3) is shared by the nsrc pencil sets
+    zderiv_kernel<T><<<dim3((unsigned)((n1 + 127) / 128), nsrc), 128, 0, s>>>(zt, cc, in, out, n1, nz, bc, filter,
+                                                                              top_plane, in_ss, out_ss);
 }
 void launch_zderiv_real(const double* zt, const Compact<double>& cc, const double* in, double* out,
                         long long n1, int nz, int bc, cudaStream_t s) {
@@ -302,6 +306,6 @@ template void launch_stage<float>(const StageArgs<float>&, int, cudaStream_t);
 template void launch_update<double>(const UpdateArgs<double>&, int, cudaStream_t);
 template void launch_update<float>(const UpdateArgs<float>&, int, cudaStream_t);
 template void launch_zderiv<double>(const double*, const Compact<double>&, const double2*, double2*, long long, int,
-                                    int, int, const double2*, cudaStream_t);
+                                    int, int, const double2*, int, long long, long long, cudaStream_t);
 template void launch_zderiv<float>(const float*, const Compact<float>&, const float2*, float2*, long long, int, int,
-                                   int, const float2*, cudaStream_t);
+                                   int, const float2*, int, long long, long long, cudaStream_t);
