@@ -82,6 +82,10 @@ struct sparc_ctx {
     std::vector<int> dck_time;
     // kernels
     void* store = nullptr; int store_n = 0;     // [nsnap][7][S][N] T (field-major within a snapshot)
+    // per store slot: recorded on the adjoint stream after its reads of the
+    // slot; a later snapshot into the slot waits for it
+    std::vector<cudaEvent_t> slot_ev;
+    std::vector<char> slot_pending;
     double* kacc = nullptr;                     // [S][3][N]
     void* ktemp = nullptr;                      // [7][G][N] T, G = kernel_group(S)
     void* gtmp = nullptr;                       // [G] spectral fields: transform scratch of a source group
@@ -339,6 +343,7 @@ void sparc_gpu_destroy(sparc_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev_done) cudaEventDestroy(c->ev_done);
+    for (cudaEvent_t e : c->slot_ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -1135,8 +1140,15 @@ int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
         int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));
         if (rc) return rc;
         c->store_n = nsnap;
+        c->slot_ev.assign(nsnap, nullptr);
+        c->slot_pending.assign(nsnap, 0);
+        for (int i = 0; i < nsnap; ++i) CK(cudaEventCreateWithFlags(&c->slot_ev[i], cudaEventDisableTiming));
     }
     if (snap < 0 || snap >= c->store_n) return fail(c, SPARC_EINVAL, "snapshot index out of range");
+    if (c->slot_pending[snap]) {           // an adjoint context still reads this slot
+        CK(cudaStreamWaitEvent(c->stream, c->slot_ev[snap], 0));
+        c->slot_pending[snap] = 0;
+    }
     const int G = kernel_group(c->S);
     const long long ofs = (long long)c->S * c->N;          // field stride of the store
     for (int s0 = 0; s0 < c->S; s0 += G) {
@@ -1191,10 +1203,10 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
         c->launches++;
         CKL();
     }
-    // later forward work (new snapshots into the same store slots) waits for
-    // these reads of the store
-    CK(cudaEventRecord(c->ev_done, c->stream));
-    CK(cudaStreamWaitEvent(fwd->stream, c->ev_done, 0));
+    // a later snapshot into this slot waits for these reads of it; the
+    // forward context's other work does not wait
+    CK(cudaEventRecord(fwd->slot_ev[snap], c->stream));
+    fwd->slot_pending[snap] = 1;
     return SPARC_OK;
 }
 
