@@ -1,0 +1,69 @@
+"""The reference's on-disk formats (vz_cc.bin, FITS BITPIX -64, kernel_info,
+timeline): layout checks and round trips, no GPU."""
+import numpy as np
+
+from sparc_gb300 import io
+from sparc_gb300.params import SparcParams
+
+
+def test_vz_cc_bin_is_fixed_records_x_fastest(tmp_path):
+    nx, ny = 6, 4
+    rec = np.arange(3 * ny * nx, dtype=np.float64).reshape(3, ny, nx)
+    path = str(tmp_path / "vz_cc.bin")
+    io.write_vz_cc_bin(path, rec)
+    raw = np.fromfile(path, dtype="=f8")
+    assert raw.size == 3 * nx * ny
+    # record k (1-based) at byte offset (k-1)*nx*ny*8, element (i, j) at j*nx + i
+    assert raw[1 * nx * ny + 2 * nx + 5] == rec[1, 2, 5]
+    # appending records as write_binary_seq_2D does, one per output
+    io.write_vz_cc_bin(path, rec[0] * -1.0, first_record=4)
+    back = io.read_vz_cc_bin(path, nx, ny)
+    assert back.shape == (4, ny, nx)
+    assert np.array_equal(back[:3], rec) and np.array_equal(back[3], -rec[0])
+
+
+def test_fits_header_and_data_layout(tmp_path):
+    a = np.random.default_rng(0).standard_normal((5, 3, 7))
+    path = str(tmp_path / "k.fits")
+    io.write_fits(path, a, {"TIME": 7200})
+    raw = open(path, "rb").read()
+    assert len(raw) % 2880 == 0
+    cards = [raw[i:i + 80].decode() for i in range(0, 2880, 80)]
+    assert cards[0].startswith("SIMPLE  =                    T")
+    assert cards[1].startswith("BITPIX  =                  -64")
+    assert cards[2].startswith("NAXIS   =                    3")
+    assert cards[3].startswith("NAXIS1  =                    7")     # nx first
+    assert cards[4].startswith("NAXIS2  =                    3")
+    assert cards[5].startswith("NAXIS3  =                    5")
+    assert any(c.startswith("TIME    =                 7200") for c in cards)
+    assert any(c.rstrip() == "END" for c in cards)
+    data = np.frombuffer(raw, dtype=">f8", count=a.size, offset=2880)
+    assert np.array_equal(data, a.ravel())                           # x fastest, big endian
+    back, hdr = io.read_fits(path, with_header=True)
+    assert np.array_equal(back, a) and hdr["TIME"] == 7200 and hdr["BITPIX"] == -64
+
+
+def test_fits_reads_float32_and_scaled(tmp_path):
+    a = np.arange(12, dtype=np.float32).reshape(3, 4)
+    hdr = b"".join([io._card("SIMPLE", True), io._card("BITPIX", -32), io._card("NAXIS", 2),
+                    io._card("NAXIS1", 4), io._card("NAXIS2", 3), io._card("BSCALE", 2.0),
+                    io._card("BZERO", 1.0), b"END".ljust(80)])
+    hdr += b" " * (-len(hdr) % 2880)
+    path = tmp_path / "f.fits"
+    path.write_bytes(hdr + a.astype(">f4").tobytes())
+    assert np.array_equal(io.read_fits(str(path)), a * 2.0 + 1.0)
+
+
+def test_forward_output_set(tmp_path):
+    p = SparcParams(nx=8, ny=4, nz=20, solartime=1.0)
+    rec = np.random.default_rng(1).standard_normal((5, 4, 8))
+    paths = io.write_forward_outputs(str(tmp_path), p, rec)
+    assert np.array_equal(io.read_vz_cc_bin(paths["vz_cc.bin"], 8, 4), rec)
+    assert np.array_equal(io.read_fits(paths["vz_cc.fits"]), rec)
+    tl = io.read_timeline(paths["timeline"])
+    assert tl.shape == (5, 2)
+    assert tl[0, 0] == 0 and tl[1, 0] == p.steps
+    assert tl[0, 1] == -3600.0 + p.timestep and tl[2, 1] == -3600.0 + (2 * p.steps + 1) * p.timestep
+    assert io.read_kernel_info(paths["kernel_info"]) == [0, p.maxtime]
+    k = io.write_kernels(str(tmp_path), "01", rec, 2 * rec, 3 * rec, time=p.maxtime)
+    assert np.array_equal(io.read_fits(k["kernel_rho"]), 2 * rec)
