@@ -121,6 +121,16 @@ int sparc_gpu_set_source(sparc_ctx* ctx, int src_idx, int mode, const double* pl
  * (driver.f90:455-476). */
 int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
 
+/* Pick the fastest of the launch variants that give identical results (the
+ * fused FP32 step's modes per CTA, 4 or 2; the per-stage kernels' threads per
+ * CTA, 128 or 64) by timing real steps: the call advances the solution by
+ * 4*steps ordinary time steps.  Steps are replayed from captured CUDA graphs
+ * (one per step count, captured on first use and after any change of launch
+ * arguments); SPARC_NO_GRAPHS in the environment at create time launches
+ * them directly.  choice / ms_per_step may be NULL.  No reference
+ * counterpart (tuning of this implementation). */
+int sparc_gpu_autotune(sparc_ctx* ctx, int steps, int* choice, float* ms_per_step);
+
 /* One RK stage rk = 1..5 of the current step (one pass of the do step_rk
  * loop body, step.f90:49-112) without the update, the filters or a time
  * advance: a fine-grained seam for timing the stage kernel on its own. */

@@ -51,6 +51,8 @@ struct sparc_ctx {
     void* zt = nullptr; void* pt = nullptr;       // T tables
     float* ftab = nullptr;                        // fused FP32 step: z table [FZ_COUNT][fused_nzp(nz)]
     int use_fused = 0;
+    int fused_pencils = 4;                        // modes per CTA of the fused step (autotuned)
+    int stage_block = 128;                        // threads per CTA of the per-stage kernels (autotuned)
     double* zt64 = nullptr; double* pt64 = nullptr;
     double* tw_x = nullptr; double* tw_y = nullptr;
     void* tmp = nullptr;          // FFT intermediate, nz*M complex T
@@ -74,6 +76,13 @@ struct sparc_ctx {
     void* rec = nullptr;          // [S][rec_max][M] CT, record r = output at slot time r*steps
     // per-slot clocks (continuous batching)
     int* d_t0 = nullptr;          // [S] device copy
+    int* d_time = nullptr;        // device copy of `time`, read by the step kernels
+    // captured step sequences, replayed as CUDA graphs: one per step count,
+    // valid while no kernel argument changed (epoch)
+    struct GraphEntry { int n; long long epoch; cudaGraphExec_t exec; long long nlaunch; };
+    std::vector<GraphEntry> graphs;
+    long long epoch = 0;
+    int use_graphs = 1;
     std::vector<int> t0;          // slot time = time - t0[slot]
     int active_n = 0;             // slots 0..active_n-1 are stepped
 
@@ -318,8 +327,12 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, (void**)&c->phys64, (size_t)c->N * 8))) return bail(rc);
     if ((rc = dalloc(c, (void**)&c->d_flag, 16))) return bail(rc);
     if ((rc = dalloc(c, (void**)&c->d_t0, (size_t)c->S * sizeof(int)))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->d_time, sizeof(int)))) return bail(rc);
+    launch_set_time(c->d_time, 0, c->stream);
     c->t0.assign(c->S, 0);
     c->active_n = c->S;
+    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr;
+    if (c->use_fused) fused_prepare(c->nz, c->nzpml);
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
@@ -344,6 +357,7 @@ void sparc_gpu_destroy(sparc_ctx* c) {
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev_done) cudaEventDestroy(c->ev_done);
     for (cudaEvent_t e : c->slot_ev) cudaEventDestroy(e);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -587,10 +601,12 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     CK(cudaMemsetAsync(c->scrpml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->time = 0;
+    launch_set_time(c->d_time, 0, c->stream);
     c->t0.assign(c->S, 0);
     CK(cudaMemsetAsync(c->d_t0, 0, (size_t)c->S * sizeof(int), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->have_bg = true;
+    c->epoch++;
     return SPARC_OK;
 }
 
@@ -736,11 +752,13 @@ int sparc_gpu_set_source(sparc_ctx* c, int src, int mode, const double* planes, 
     if (!c->planes) {
         if ((rc = dalloc(c, &c->planes, (size_t)c->S * L * c->M * cs))) return rc;
         c->src_L = L;
+        c->epoch++;
     }
     if (mode == SPARC_SRC_SERIES) {
         if (!c->series) {
             if ((rc = dalloc(c, (void**)&c->series, (size_t)c->S * nseries * 8))) return rc;
             c->nseries = nseries;
+            c->epoch++;
         }
         if (nseries > c->nseries) return fail(c, SPARC_EINVAL, "series longer than the first allocation");
         std::vector<double> ser(c->nseries, 0.0);
@@ -755,6 +773,7 @@ int sparc_gpu_set_source(sparc_ctx* c, int src, int mode, const double* planes, 
         if ((rc = to_spec(c, planes + (long long)l0 * c->NP, dst + (long long)l0 * c->M * cs, nl))) return rc;
     }
     CK(cudaStreamSynchronize(c->stream));
+    if (c->src_mode != mode) c->epoch++;      // the step kernels' arguments changed
     c->src_mode = mode;
     c->src_set[src] = 1;
     return SPARC_OK;
@@ -774,6 +793,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.zt = (const T*)c->zt; A.pt = (const T*)c->pt;
     A.fs = c->fs; A.ps = c->ps; A.M = c->M; A.nz = c->nz;
     A.npmlbot = P.npmlbot; A.npmltop = P.npmltop; A.option = P.option; A.damp = P.damp_waves && P.option == 4;
+    A.block = c->stage_block;
     A.cc.C1 = (T)c->cc64.C1; A.cc.C2 = (T)c->cc64.C2;
     for (int i = 0; i < 5; ++i) A.cc.Cb[i] = (T)c->cc64.Cb[i];
     for (int i = 0; i < 4; ++i) A.cc.Cf[i] = (T)c->cc64.Cf[i];
@@ -784,6 +804,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.planes = CP<T>(c->planes); A.plane_ss = (long long)c->src_L * c->M; A.L = c->src_L;
     A.src_mode = c->src_mode; A.series = c->series; A.nseries = c->nseries;
     A.clk.t0 = c->d_t0;
+    A.clk.time = c->d_time;
     A.clk.freq = c->freq_filtering;
     A.clk.two_d = (P.option == 17);
     A.clk.gate = c->forcing_length * c->cadforcing_step;
@@ -796,16 +817,13 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     U.clk = A.clk;
 }
 
-// forcing of the step at c->time: the kernels evaluate the source of every
-// slot on its own clock (series index / LAGRANGE_INTERP / 2-D gate)
+// Enqueue nsteps time steps on the context's stream: per step the fused FP32
+// kernel (or five stage launches and the update), the surface record, and
+// the advance of the device time.  The source of every slot is evaluated on
+// its own clock inside the kernels (series index / LAGRANGE_INTERP / 2-D
+// gate), from the device time, so the same sequence is valid at any time.
 template <typename T>
-static void set_forcing(sparc_ctx* c, StageArgs<T>& A) {
-    A.clk.time = c->time;
-}
-
-template <typename T>
-static int do_steps(sparc_ctx* c, int nsteps) {
-    typedef typename CplxOf<T>::type CT;
+static int enqueue_steps(sparc_ctx* c, int nsteps) {
     StageArgs<T> A;
     UpdateArgs<T> U;
     make_args<T>(c, A, U);
@@ -829,35 +847,87 @@ static int do_steps(sparc_ctx* c, int nsteps) {
         Fz.planes = (const float2*)c->planes; Fz.plane_ss = A.plane_ss; Fz.L = A.L;
         Fz.src_mode = A.src_mode; Fz.series = A.series; Fz.nseries = A.nseries;
         Fz.clk = A.clk;
+        Fz.pencils = c->fused_pencils;
     }
     for (int it = 0; it < nsteps; ++it) {
-        const int time = c->time;
-        set_forcing<T>(c, A);
         if (fused) {
-            Fz.clk.time = time;
             Fz.write_scr = (it == nsteps - 1) ? 1 : 0;
             launch_fused(Fz, c->active_n, c->stream);
             c->launches += 1;
             CKL();
         } else {
-        for (int rk = 0; rk < 5; ++rk) {
-            A.beta = (T)c->betas[rk];
-            A.has_scr = (rk > 0);
-            launch_stage<T>(A, c->active_n, c->stream);
-        }
-        U.clk.time = time;
-        launch_update<T>(U, c->active_n, c->stream);
-        c->launches += 6;
-        CKL();
+            for (int rk = 0; rk < 5; ++rk) {
+                A.beta = (T)c->betas[rk];
+                A.has_scr = (rk > 0);
+                launch_stage<T>(A, c->active_n, c->stream);
+            }
+            launch_update<T>(U, c->active_n, c->stream);
+            c->launches += 6;
+            CKL();
         }
         if (c->rec_on) {
-            launch_record<T>(CP<T>(c->a), CP<T>(c->rec), c->d_t0, time, c->steps, c->rec_max, c->fs, c->M,
+            launch_record<T>(CP<T>(c->a), CP<T>(c->rec), c->d_t0, c->d_time, c->steps, c->rec_max, c->fs, c->M,
                              c->o_rad - 1, c->active_n, c->stream);
             c->launches++;
             CKL();
         }
-        c->time++;
+        launch_tick(c->d_time, c->stream);
+        c->launches++;
+        CKL();
     }
+    return SPARC_OK;
+}
+
+// nsteps steps: replayed from a captured graph when the context allows it,
+// captured on first use of this step count (and again after any change of
+// kernel arguments); launched directly otherwise.
+template <typename T>
+static int do_steps(sparc_ctx* c, int nsteps) {
+    if (nsteps == 0) return SPARC_OK;
+    if (c->use_graphs) {
+        sparc_ctx::GraphEntry* ge = nullptr;
+        for (auto& g : c->graphs)
+            if (g.n == nsteps) { ge = &g; break; }
+        if (ge && ge->epoch != c->epoch) {
+            cudaGraphExecDestroy(ge->exec);
+            c->graphs.erase(c->graphs.begin() + (ge - c->graphs.data()));
+            ge = nullptr;
+        }
+        if (!ge) {
+            if (c->graphs.size() >= 8) {             // a few step counts per context
+                cudaGraphExecDestroy(c->graphs.front().exec);
+                c->graphs.erase(c->graphs.begin());
+            }
+            const long long l0 = c->launches;
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            bool ok = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            int rc = ok ? enqueue_steps<T>(c, nsteps) : SPARC_OK;
+            if (ok) ok = cudaStreamEndCapture(c->stream, &graph) == cudaSuccess && rc == SPARC_OK;
+            if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+            if (graph) cudaGraphDestroy(graph);
+            const long long nl = c->launches - l0;
+            c->launches = l0;
+            if (!ok) {
+                // no graphs for this context: launch directly from now on
+                cudaGetLastError();
+                if (exec) cudaGraphExecDestroy(exec);
+                c->use_graphs = 0;
+            } else {
+                c->graphs.push_back({nsteps, c->epoch, exec, nl});
+                ge = &c->graphs.back();
+            }
+        }
+        if (ge) {
+            CK(cudaGraphLaunch(ge->exec, c->stream));
+            c->launches += ge->nlaunch;
+            c->time += nsteps;
+            return SPARC_OK;
+        }
+    }
+    int rc = enqueue_steps<T>(c, nsteps);
+    if (rc) return rc;
+    c->time += nsteps;
     return SPARC_OK;
 }
 
@@ -870,6 +940,42 @@ int sparc_gpu_step(sparc_ctx* c, int nsteps) {
     return c->f32 ? do_steps<float>(c, nsteps) : do_steps<double>(c, nsteps);
 }
 
+int sparc_gpu_autotune(sparc_ctx* c, int steps, int* choice, float* ms_per_step) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (steps < 1) return fail(c, SPARC_EINVAL, "steps < 1");
+    const bool fused = c->use_fused && c->f32;
+    const int cand[2] = {fused ? 4 : 128, fused ? 2 : 64};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 0.f;
+    int pick = cand[0];
+    for (int v : cand) {
+        if (fused) c->fused_pencils = v; else c->stage_block = v;
+        c->epoch++;
+        int rc = c->f32 ? do_steps<float>(c, steps) : do_steps<double>(c, steps);   // capture and warm
+        if (!rc) {
+            CK(cudaEventRecord(e0, c->stream));
+            rc = c->f32 ? do_steps<float>(c, steps) : do_steps<double>(c, steps);
+            CK(cudaEventRecord(e1, c->stream));
+        }
+        if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= steps;
+        if (v == cand[0] || ms < best) { best = ms; pick = v; }
+    }
+    if (fused) c->fused_pencils = pick; else c->stage_block = pick;
+    c->epoch++;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (choice) *choice = pick;
+    if (ms_per_step) *ms_per_step = best;
+    return SPARC_OK;
+}
+
 }  // extern "C"
 
 template <typename T>
@@ -877,7 +983,6 @@ static int stage_only(sparc_ctx* c, int rk) {
     StageArgs<T> A;
     UpdateArgs<T> U;
     make_args<T>(c, A, U);
-    set_forcing<T>(c, A);
     A.beta = (T)c->betas[rk - 1];
     A.has_scr = (rk > 1);
     launch_stage<T>(A, c->active_n, c->stream);
@@ -903,6 +1008,8 @@ int sparc_gpu_get_time(const sparc_ctx* c, int* t) {
 int sparc_gpu_set_time(sparc_ctx* c, int t) {
     if (!c || t < 0) return SPARC_EINVAL;
     c->time = t;
+    launch_set_time(c->d_time, t, c->stream);
+    CKL();
     return SPARC_OK;
 }
 
@@ -928,6 +1035,7 @@ int sparc_gpu_sync(sparc_ctx* c, int check_finite) {
 // ---------------------------------------------------------------------------
 int sparc_gpu_record_surface(sparc_ctx* c, int enable, int max_records) {
     if (!c) return SPARC_EINVAL;
+    c->epoch++;
     if (!enable) { c->rec_on = 0; return SPARC_OK; }
     if (max_records < 1) return fail(c, SPARC_EINVAL, "max_records < 1");
     if (!c->rec || max_records > c->rec_max) {
@@ -991,6 +1099,7 @@ int sparc_gpu_slot_time(const sparc_ctx* c, int src, int* local_time) {
 int sparc_gpu_set_active(sparc_ctx* c, int nactive) {
     if (!c) return SPARC_EINVAL;
     if (nactive < 1 || nactive > c->S) return fail(c, SPARC_EINVAL, "nactive out of range");
+    if (c->active_n != nactive) c->epoch++;
     c->active_n = nactive;
     return SPARC_OK;
 }
@@ -1270,6 +1379,7 @@ int sparc_gpu_load_device(sparc_ctx* c, int idx) {
     CK(cudaMemsetAsync(c->scr, 0, na, c->stream));
     CK(cudaMemsetAsync(c->scrpml, 0, np, c->stream));
     c->time = c->dck_time[idx];
+    launch_set_time(c->d_time, c->time, c->stream);
     return SPARC_OK;
 }
 
@@ -1343,6 +1453,7 @@ int sparc_gpu_restore(sparc_ctx* c, const char* path) {
     CK(cudaMemsetAsync(c->d_t0, 0, (size_t)c->S * sizeof(int), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->time = h.time;
+    launch_set_time(c->d_time, c->time, c->stream);
     return SPARC_OK;
 }
 

@@ -38,7 +38,6 @@
 namespace {
 
 constexpr int CH = FUSED_CH;   // z-levels per thread
-constexpr int P = 4;           // modes per CTA
 constexpr int GZ = 5;          // ghost rows of the tile on each side (reach of the z filter)
 constexpr int GX = 2;          // ghost entries of an exchange line on each side (compact stencil)
 
@@ -204,7 +203,7 @@ __device__ __forceinline__ int pmlidx(int j, int nz, int nb, int nt) {
 struct FusedLayout {
     int tile, xa, xb, ptile, spt, wbuf, zs, lagw, lagi, total;
 };
-__host__ __device__ inline FusedLayout fused_layout(int W, int nzpml) {
+__host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
     const int NZP = 160 * W, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX;
     FusedLayout L;
     int o = 0;
@@ -225,14 +224,16 @@ __host__ __device__ inline FusedLayout fused_layout(int W, int nzpml) {
 
 }  // namespace
 
-template <bool D3, int W>
-__global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
+// P modes per CTA (2 or 4): every pencil's arithmetic is the same for either,
+// so the results are too; the launch bounds keep 128 registers per thread.
+template <bool D3, int W, int P>
+__global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
     constexpr int TP = 32 * W, NZP = TP * CH, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX;
     constexpr int BCX = D3 ? 1 : 3, BCP = D3 ? 0 : 2;
     const int nz = A.nz, M = A.M, nzpml = A.nzpml, nb = A.npmlbot, nt = A.npmltop;
     const long long fs = A.fs;
-    const FusedLayout Ly = fused_layout(W, nzpml);
+    const FusedLayout Ly = fused_layout(P, W, nzpml);
     float2* tile = (float2*)(smraw + Ly.tile);            // [6][P][LZ], level j at GZ + j
     float2* xab = (float2*)(smraw + Ly.xa);               // [P][LX], level j at GX + j
     float2* xbb = (float2*)(smraw + Ly.xb);
@@ -279,11 +280,13 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
         const float2* src = gA + f * fs + (long long)z * M + m0;
         float2* dst = tile + f * P * LZ + GZ + z;
         if (vec) {
-            float4 v0 = *(const float4*)src, v1 = *(const float4*)(src + 2);
-            dst[0] = make_float2(v0.x, v0.y);
-            dst[LZ] = make_float2(v0.z, v0.w);
-            dst[2 * LZ] = make_float2(v1.x, v1.y);
-            dst[3 * LZ] = make_float2(v1.z, v1.w);
+            // P complex values per row: P/2 float4, exactly the CTA's modes
+            #pragma unroll
+            for (int v = 0; v < P / 2; ++v) {
+                const float4 x = *(const float4*)(src + 2 * v);
+                dst[(2 * v) * LZ] = make_float2(x.x, x.y);
+                dst[(2 * v + 1) * LZ] = make_float2(x.z, x.w);
+            }
         } else {
             for (int q = 0; q < P; ++q) dst[q * LZ] = (m0 + q < M) ? src[q] : make_float2(0.f, 0.f);
         }
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
         const float2* src = gP + (long long)r * M + m0;
         for (int q = 0; q < P; ++q) ptile[r * P + q] = (m0 + q < M) ? src[q] : make_float2(0.f, 0.f);
     }
-    const int tl = A.clk.time - A.clk.t0[s];            // this slot's clock
+    const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
     const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
     if (threadIdx.x < 7 && src_on && A.src_mode == 2) {
         // weight l on thread l (LAGRANGE_INTERP, physics.f90:683-734);
@@ -534,9 +537,11 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
         float2* dst = gA + f * fs + (long long)z * M + m0;
         const float2* srcp = tile + f * P * LZ + GZ + z;
         if (vec) {
-            float2 w0 = srcp[0], w1 = srcp[LZ], w2 = srcp[2 * LZ], w3 = srcp[3 * LZ];
-            *(float4*)dst = make_float4(w0.x, w0.y, w1.x, w1.y);
-            *(float4*)(dst + 2) = make_float4(w2.x, w2.y, w3.x, w3.y);
+            #pragma unroll
+            for (int v = 0; v < P / 2; ++v) {
+                const float2 w0 = srcp[(2 * v) * LZ], w1 = srcp[(2 * v + 1) * LZ];
+                *(float4*)(dst + 2 * v) = make_float4(w0.x, w0.y, w1.x, w1.y);
+            }
         } else {
             for (int q = 0; q < P; ++q)
                 if (m0 + q < M) dst[q] = srcp[q * LZ];
@@ -560,9 +565,11 @@ __global__ void __launch_bounds__(256, 2) fused_step_kernel(const FusedArgs A) {
             float2* dst = gS + f * fs + (long long)z * M + m0;
             const float2* srcp = tile + f * P * LZ + GZ + z;
             if (vec) {
-                float2 w0 = srcp[0], w1 = srcp[LZ], w2 = srcp[2 * LZ], w3 = srcp[3 * LZ];
-                *(float4*)dst = make_float4(w0.x, w0.y, w1.x, w1.y);
-                *(float4*)(dst + 2) = make_float4(w2.x, w2.y, w3.x, w3.y);
+                #pragma unroll
+                for (int v = 0; v < P / 2; ++v) {
+                    const float2 w0 = srcp[(2 * v) * LZ], w1 = srcp[(2 * v + 1) * LZ];
+                    *(float4*)(dst + 2 * v) = make_float4(w0.x, w0.y, w1.x, w1.y);
+                }
             } else {
                 for (int q = 0; q < P; ++q)
                     if (m0 + q < M) dst[q] = srcp[q * LZ];
@@ -576,26 +583,50 @@ int fused_nzp(int nz) { return 32 * CH * fused_w(nz); }
 
 size_t fused_smem_bytes(int nz, int nzpml, int W) {
     (void)nz;
-    return (size_t)fused_layout(W, nzpml).total;
+    return (size_t)fused_layout(4, W, nzpml).total;
 }
 
 // nz >= 16 keeps the boundary rows of the two ends in different threads
 int fused_supported(int nz) { return nz >= 16 && nz <= 2 * 32 * CH; }
 
-template <bool D3, int W>
-static void launch_fused_t(const FusedArgs& A, int nsrc, cudaStream_t s) {
-    const size_t sm = fused_smem_bytes(A.nz, A.nzpml, W);
-    cudaFuncSetAttribute((const void*)fused_step_kernel<D3, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <bool D3, int W, int P>
+static void fused_attr(int nzpml) {
+    const size_t sm = (size_t)fused_layout(P, W, nzpml).total;
+    cudaFuncSetAttribute((const void*)fused_step_kernel<D3, W, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
+}
+
+// Dynamic shared-memory limits of every variant a context may launch, set
+// once at context creation (not while a launch sequence is being captured).
+void fused_prepare(int nz, int nzpml) {
+    const int W = fused_w(nz);
+    if (W == 1) {
+        fused_attr<true, 1, 2>(nzpml); fused_attr<true, 1, 4>(nzpml);
+        fused_attr<false, 1, 2>(nzpml); fused_attr<false, 1, 4>(nzpml);
+    } else {
+        fused_attr<true, 2, 2>(nzpml); fused_attr<true, 2, 4>(nzpml);
+        fused_attr<false, 2, 2>(nzpml); fused_attr<false, 2, 4>(nzpml);
+    }
+}
+
+template <bool D3, int W, int P>
+static void launch_fused_t(const FusedArgs& A, int nsrc, cudaStream_t s) {
+    const size_t sm = (size_t)fused_layout(P, W, A.nzpml).total;
     dim3 grid((A.M + P - 1) / P, nsrc);
-    fused_step_kernel<D3, W><<<grid, P * 32 * W, sm, s>>>(A);
+    fused_step_kernel<D3, W, P><<<grid, P * 32 * W, sm, s>>>(A);
+}
+
+template <bool D3, int W>
+static void launch_fused_p(const FusedArgs& A, int nsrc, cudaStream_t s) {
+    if (A.pencils == 2) launch_fused_t<D3, W, 2>(A, nsrc, s);
+    else launch_fused_t<D3, W, 4>(A, nsrc, s);
 }
 
 void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s) {
     const bool d3 = (A.option == 4);
     if (A.W == 1) {
-        if (d3) launch_fused_t<true, 1>(A, nsrc, s); else launch_fused_t<false, 1>(A, nsrc, s);
+        if (d3) launch_fused_p<true, 1>(A, nsrc, s); else launch_fused_p<false, 1>(A, nsrc, s);
     } else {
-        if (d3) launch_fused_t<true, 2>(A, nsrc, s); else launch_fused_t<false, 2>(A, nsrc, s);
+        if (d3) launch_fused_p<true, 2>(A, nsrc, s); else launch_fused_p<false, 2>(A, nsrc, s);
     }
 }

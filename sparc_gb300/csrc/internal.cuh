@@ -140,7 +140,7 @@ __device__ __forceinline__ void zfilter_stream(int nz, int mode, Load val, Emit 
 // batch starts at its own time 0 while sharing the batch's launches.
 struct SlotClock {
     const int* t0;      // per-slot start (context time index at which the slot's clock read 0)
-    int time;           // context time index of the step being taken
+    const int* time;    // device counter: context time index of the step being taken
     int freq;           // freq_filtering (driver.f90:270)
     int two_d;          // option 17 cadence/gating rules
     int gate;           // forcing_length * cadforcing_step (driver.f90:421, physics2d.f90:1059)
@@ -207,6 +207,7 @@ template <typename T> struct StageArgs {
     long long ps;       // pml field stride nzpml*M
     int M, nz, npmlbot, npmltop, option, damp;
     int has_scr;
+    int block;          // threads per CTA (64 or 128; same results, a tuning choice)
     T beta;
     Compact<T> cc;
     // source injection at plane ksrc (0-based)
@@ -248,8 +249,10 @@ struct FusedArgs {
     const float2* planes; long long plane_ss; int L;
     const double* series; int nseries;
     SlotClock clk;
+    int pencils;        // modes per CTA: 2 or 4 (same results; a tuning choice)
 };
 constexpr int FUSED_CH = 5;
+void fused_prepare(int nz, int nzpml);
 size_t fused_smem_bytes(int nz, int nzpml, int W);
 int fused_supported(int nz);
 int fused_w(int nz);
@@ -261,8 +264,11 @@ template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStr
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s);
 // surface record of vz at plane kplane for every slot whose clock is on the output cadence
 template <typename T>
-void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, int time, int steps,
-                   int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s);
+void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, const int* time,
+                   int steps, int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s);
+// the device time counter: set, and advance by one step
+void launch_set_time(int* time, int value, cudaStream_t s);
+void launch_tick(int* time, cudaStream_t s);
 template <typename T>
 void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,
                    typename CplxOf<T>::type* out, long long n1, int nz, int bc, int filter,

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs<T> A) {
         const T* gam = zt + (ZT_TH + 3 * bcp + 2) * nz;
         // forcing of this step for this mode, on this slot's clock
         CT F = czero<CT>();
-        const int tl = A.clk.time - A.clk.t0[s];
+        const int tl = *A.clk.time - A.clk.t0[s];
         const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
         if (src_on) {
             const CT* pl = A.planes + (long long)s * A.plane_ss + m;
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     const T dt = A.dt;
     const T hf = __ldg(&A.pt[PT_HF * M + m]);
     const bool opt3d = (A.option == 4);
-    const bool hstep = slot_hfilter(A.clk, A.clk.time - A.clk.t0[s]);
+    const bool hstep = slot_hfilter(A.clk, *A.clk.time - A.clk.t0[s]);
     for (int f = 0; f < 6; ++f) {
         CT* af = a + f * fs;
         const CT* sf = scr + f * fs;
@@ -256,12 +256,12 @@ __global__ void __launch_bounds__(128) zderiv_real_kernel(const double* __restri
 // the output cadence (driver.f90:455-476)
 template <typename T>
 __global__ void record_kernel(const typename CplxOf<T>::type* __restrict__ a, typename CplxOf<T>::type* __restrict__ rec,
-                              const int* __restrict__ t0, int time, int steps, int rec_max, long long fs, int M,
-                              int kplane) {
+                              const int* __restrict__ t0, const int* __restrict__ time, int steps, int rec_max,
+                              long long fs, int M, int kplane) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int s = blockIdx.y;
     if (m >= M) return;
-    const int tl = time - t0[s];
+    const int tl = *time - t0[s];
     if (tl < 0 || tl % steps != 0) return;
     const int r = tl / steps;
     if (r >= rec_max) return;
@@ -269,19 +269,28 @@ __global__ void record_kernel(const typename CplxOf<T>::type* __restrict__ a, ty
 }
 
 template <typename T>
-void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, int time, int steps,
-                   int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s) {
+void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, const int* time,
+                   int steps, int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s) {
     dim3 grid((M + 255) / 256, nsrc);
     record_kernel<T><<<grid, 256, 0, s>>>(a, rec, t0, time, steps, rec_max, fs, M, kplane);
 }
-template void launch_record<double>(const double2*, double2*, const int*, int, int, int, long long, int, int, int,
-                                    cudaStream_t);
-template void launch_record<float>(const float2*, float2*, const int*, int, int, int, long long, int, int, int,
+template void launch_record<double>(const double2*, double2*, const int*, const int*, int, int, long long, int, int,
+                                    int, cudaStream_t);
+template void launch_record<float>(const float2*, float2*, const int*, const int*, int, int, long long, int, int, int,
                                    cudaStream_t);
 
+// The context's time lives on the device so that a captured sequence of
+// steps replays at any time: the step kernels read it, and one thread
+// advances it after each step.
+__global__ void set_time_kernel(int* time, int value) { *time = value; }
+__global__ void tick_kernel(int* time) { *time = *time + 1; }
+void launch_set_time(int* time, int value, cudaStream_t s) { set_time_kernel<<<1, 1, 0, s>>>(time, value); }
+void launch_tick(int* time, cudaStream_t s) { tick_kernel<<<1, 1, 0, s>>>(time); }
+
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s) {
-    dim3 grid((A.M + 127) / 128, nsrc);
-    stage_kernel<T><<<grid, 128, 0, s>>>(A);
+    const int b = A.block == 64 ? 64 : 128;
+    dim3 grid((A.M + b - 1) / b, nsrc);
+    stage_kernel<T><<<grid, b, 0, s>>>(A);
 }
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s) {
     dim3 grid((A.M + 127) / 128, nsrc);

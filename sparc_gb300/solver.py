@@ -113,6 +113,15 @@ class Solver:
     def step(self, n: int = 1):
         self._ck(self.L.sparc_gpu_step(self.h, int(n)))
 
+    def autotune(self, steps: int = 1) -> dict:
+        """Time each launch variant that gives identical results over real
+        steps (4*steps of them) and keep the fastest; returns the choice."""
+        choice = ctypes.c_int(0)
+        ms = ctypes.c_float(0.0)
+        self._ck(self.L.sparc_gpu_autotune(self.h, int(steps), ctypes.byref(choice), ctypes.byref(ms)))
+        key = "modes_per_cta" if (self.p.precision == "f32" and self.p.nz <= 320) else "threads_per_cta"
+        return {key: choice.value, "ms_per_step": ms.value}
+
     def stage(self, rk: int):
         """Launch only RK stage rk (1..5) of the current step (timing hook)."""
         self._ck(self.L.sparc_gpu_stage(self.h, int(rk)))

@@ -1,0 +1,64 @@
+"""Captured step sequences (CUDA graphs, replayed at any time from the device
+clock) and the autotuner: both must leave results bit-for-bit unchanged."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import gaussian_plane, random_state, small_params, table_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(p, tab, graphs: bool):
+    from sparc_gb300.solver import Solver
+    if not graphs:
+        os.environ["SPARC_NO_GRAPHS"] = "1"
+    try:
+        return Solver(p, tab)
+    finally:
+        os.environ.pop("SPARC_NO_GRAPHS", None)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_graph_replay_equals_direct_launches(gpu_lib, prec):
+    from sparc_gb300 import sources
+    p = small_params(precision=prec, nsrc=2)
+    tab = table_for(p)
+    a0, pml0 = random_state(p)
+    plane = gaussian_plane(p)
+    series = sources.ricker_series(p, 400) * 1e3
+    out = []
+    for graphs in (True, False):
+        s = _solver(p, tab, graphs)
+        for slot in range(2):
+            s.set_state(a0 * (slot + 1), pml0, slot=slot)
+            s.set_source_series(plane, series, slot=slot)
+        s.record_surface(8)
+        for n in (7, 15, 15, 3, 15):          # replays of one graph at different times, and new counts
+            s.step(n)
+        s.slot_reset(1)                       # device-side clock change between replays
+        s.step(15)
+        out.append(([s.state(slot=k)[0] for k in range(2)], [s.records(slot=k) for k in range(2)], s.time))
+    (sa, ra, ta), (sb, rb, tb) = out
+    assert ta == tb == 70
+    for k in range(2):
+        assert np.array_equal(sa[k], sb[k]), k
+        assert np.array_equal(ra[k], rb[k]), k
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_autotune_keeps_results(gpu_lib, prec):
+    from sparc_gb300.solver import Solver
+    p = small_params(precision=prec)
+    tab = table_for(p)
+    a0, pml0 = random_state(p)
+    s1, s2 = Solver(p, tab), Solver(p, tab)
+    for s in (s1, s2):
+        s.set_state(a0, pml0)
+    pick = s1.autotune(2)                      # 8 ordinary steps
+    assert list(pick.values())[0] in (2, 4, 64, 128) and pick["ms_per_step"] > 0
+    s1.step(3)
+    s2.step(11)
+    assert s1.time == s2.time == 11
+    assert np.array_equal(s1.state()[0], s2.state()[0])
