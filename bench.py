@@ -244,6 +244,42 @@ def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, 
     return st
 
 
+def small_step_latency(n=60):
+    """Per-step device time of a 128x128x150 single-source FP32 forward solve
+    (the 1-h configuration's grid), steps replayed from captured graphs vs
+    launched one by one: where launch overhead is visible."""
+    import torch
+    from sparc_gb300 import sources
+    from sparc_gb300.background import polytrope_table
+    from sparc_gb300.params import config_quiet_128
+    from sparc_gb300.solver import Solver
+    p = config_quiet_128().replace(precision="f32", nsrc=1)
+    tab = polytrope_table(p.nz)
+    out = {}
+    for mode in ("graphs", "direct"):
+        if mode == "direct":
+            os.environ["SPARC_NO_GRAPHS"] = "1"
+        try:
+            s = Solver(p, tab)
+        finally:
+            os.environ.pop("SPARC_NO_GRAPHS", None)
+        s.set_source_series(sources.gaussian_plane(p), sources.ricker_series(p, 4000))
+        s.record_surface(n // p.steps + 2)
+        st = torch.cuda.ExternalStream(s.stream_ptr)
+        s.step(p.steps)
+        s.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(n // p.steps):
+            s.step(p.steps)
+        e1.record(st)
+        e1.synchronize()
+        out[mode + "_us_per_step"] = e0.elapsed_time(e1) * 1e3 / (n // p.steps * p.steps)
+        s.close()
+    out["grid"] = [p.nx, p.ny, p.nz]
+    return out
+
+
 def cpu_baseline(p, tab, steps=1):
     from oracle import oracle
     threads = os.cpu_count() or 1
@@ -342,6 +378,9 @@ def main():
     p32 = p0.replace(precision="f32", nsrc=S)
     fwd, adj = make_pair(p32, tab, args.nplanes, seed=1000 + rank)
     cad = fwd.info()["steps"]
+    # launch variants with identical results, picked by timing real steps
+    # (part of the warm-up: 4 steps per context)
+    tuning = {"forward": fwd.autotune(1), "adjoint": adj.autotune(1)}
     run_steps(fwd, adj, W, cad)
     barrier(ws)
     with ClockSampler(local) as clk:
@@ -442,6 +481,10 @@ def main():
                             "what": "one batched forward+adjoint step, host-synchronised"},
         "e2e": e2e,
     }
+    line["tuning"] = tuning
+    if ws == 1:
+        log("small-grid step latency")
+        line["small_grid_step"] = small_step_latency()
     if args.serve_requests > 0 and ws == 1:
         line["serving"] = {}
         for prec in ("f32", "f64"):

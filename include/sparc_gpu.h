@@ -241,7 +241,10 @@ long long sparc_gpu_device_bytes(const sparc_ctx* ctx);
 /* Set-up diagnostics: info[0..14] = e_rad, o_rad, delta_width, deltat,
  * steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps,
  * betas(1..5); ztab / ptab receive the FP64 z-profile and pencil tables
- * (either may be NULL). */
+ * (either may be NULL): ztab holds SPARC_ZTAB_ROWS rows of nz values, ptab
+ * SPARC_PTAB_ROWS rows of ny*(nx/2+1) values. */
+#define SPARC_ZTAB_ROWS 25
+#define SPARC_PTAB_ROWS 4
 int sparc_gpu_info(sparc_ctx* ctx, double* info, double* ztab, double* ptab);
 
 /* Blocks until the context's stream is idle; SPARC_ENAN if check_finite and

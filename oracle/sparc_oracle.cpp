@@ -393,7 +393,7 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     m.nx = P->nx; m.ny = P->ny; m.nz = P->nz;
     m.NP = (long)m.nx * m.ny; m.N = m.NP * m.nz;
     m.nzpml = P->npmlbot + P->npmltop;
-    m.dimfive = 6;                                   // displacement form (initialize.f90:310-312)
+    m.dimfive = P->option == 2 ? 5 : 6;              // velocity / displacement form (initialize.f90:310-312)
     m.pi = R4(3.14159265358979);                     // initialize.f90:38 (REAL*4 literal)
     m.rsun = R4(69598946770.0);
     m.normx = 1.0 / (double)m.nx; m.normy = 1.0 / (double)m.ny;
@@ -651,6 +651,71 @@ static void rhs_option4(Model& m) {
 }
 
 // ----------------------------------------------------------------------------
+// MP_QUIET_PML_3D (pml.f90:12-76), option 2: velocity form, fields rho, v_x,
+// v_y, v_z, p (initialize.f90:498-508); PML_BOUNDARY_ACCOUNTING_3D
+// (pml.f90:213-231) for psi_vz and psi_p
+// ----------------------------------------------------------------------------
+static void rhs_option2(Model& m) {
+    long N = m.N, NP = m.NP; int nz = m.nz;
+    double* rho = &m.temp_step[0];
+    double* v_x = &m.temp_step[N];
+    double* v_y = &m.temp_step[2 * N];
+    double* v_z = &m.temp_step[3 * N];
+    double* p = &m.temp_step[4 * N];
+    double* RHScont = &m.scr[0]; double* RHSv_x = &m.scr[N]; double* RHSv_y = &m.scr[2 * N];
+    double* RHSv_z = &m.scr[3 * N]; double* RHSp = &m.scr[4 * N];
+    double* dvxdx = m.dvxdx.data(); double* dvydy = m.dvydy.data(); double* dvzdz = m.gradvz.data();
+    double* gradp_x = &m.gradp[0]; double* gradp_y = &m.gradp[N]; double* gradp_z = &m.gradp[2 * N];
+    long PS = NP * m.nzpml;
+    double* psivz = &m.psipml[0]; double* psip = &m.psipml[PS];
+    double* RHSpsivz = &m.scrpml[0]; double* RHSpsip = &m.scrpml[PS];
+    int nb = m.P.npmlbot, nt = m.P.npmltop;
+
+    ddxyz(m, v_x, dvxdx, v_y, dvydy, v_z, dvzdz, 1);
+    ddxyz(m, p, gradp_x, p, gradp_y, p, gradp_z, 0);
+    int pmlindex = 0;
+    for (int k = 1; k <= nz; ++k) {
+        if (k <= nb || k >= nz - nt + 1) {
+            pmlindex++;
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1), ip = q + NP * (pmlindex - 1);
+                RHSpsip[ip] = m.az[id] * gradp_z[id] + m.bzpml[id] * psip[ip];
+                gradp_z[id] = gradp_z[id] + psip[ip];
+                RHSpsivz[ip] = m.az[id] * dvzdz[id] + m.bzpml[id] * psivz[ip];
+                dvzdz[id] = dvzdz[id] + psivz[ip];
+            }
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < N; ++q) {
+        m.div[q] = dvxdx[q] + dvydy[q] + dvzdz[q];
+        RHScont[q] = -m.gradrho0_z[q] * v_z[q] - m.rho0[q] * m.div[q];
+        RHSv_x[q] = -m.rhoinv[q] * gradp_x[q];
+        RHSv_y[q] = -m.rhoinv[q] * gradp_y[q];
+    }
+    int kc = m.P.src_k > 0 ? m.P.src_k : m.e_rad;
+    for (int k = 1; k <= nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * (k - 1);
+            RHSv_z[id] = -m.rhoinv[id] * (gradp_z[id] + rho[id] * m.g[k - 1]);
+            if (std::abs(k - kc) <= 4 && m.src_mode != 0)
+                RHSv_z[id] = RHSv_z[id] + m.forcing[q] * m.source_dep[k - 1];
+        }
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < N; ++q) RHSp[q] = -m.c2rho0[q] * m.div[q] - v_z[q] * m.gradp0_z[q];
+    for (int l = 0; l < 5; ++l)
+        for (long q = 0; q < NP; ++q) {
+            m.scr[l * N + q] = 0.0;
+            m.scr[l * N + q + NP * (nz - 1)] = 0.0;
+        }
+    if (m.P.damp_waves) {
+        damp_velocity(m, v_x, RHSv_x);
+        damp_velocity(m, v_y, RHSv_y);
+        damp_velocity(m, v_z, RHSv_z);
+    }
+}
+
+// ----------------------------------------------------------------------------
 // MP_QUIET_PML_2D_DISPL (physics2d.f90:948-1105), option 17 (ny = 1)
 // ----------------------------------------------------------------------------
 static void rhs_option17(Model& m) {
@@ -858,7 +923,8 @@ static void lagrange_interp(Model& m) {
     }
 }
 
-// STEP (step.f90:43-128) for displacement options 4 / 17 (USE_PML, no horizontal PML)
+// STEP (step.f90:43-128) for options 2, 4 and 17 (USE_PML, no horizontal PML);
+// in the velocity form the sixth field is unused and stays zero
 static void step(Model& m) {
     long N6 = m.N * 6, NPML = (long)m.NP * m.nzpml * 2;
     for (int rk = 1; rk <= 5; ++rk) {
@@ -872,13 +938,14 @@ static void step(Model& m) {
             for (long q = 0; q < NPML; ++q) m.psipml[q] = m.pmlvars[q] + b * m.scrpml[q];
         }
         if (m.P.option == 4) rhs_option4(m);
+        else if (m.P.option == 2) rhs_option2(m);
         else rhs_option17(m);
     }
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < N6; ++q) m.a[q] = m.a[q] + m.deltat * m.scr[q];
     for (long q = 0; q < NPML; ++q) m.pmlvars[q] = m.pmlvars[q] + m.deltat * m.scrpml[q];
-    if (m.P.option == 4) filter_vars_3d(m);
-    else filter_vars_2d(m);
+    if (m.P.option == 17) filter_vars_2d(m);
+    else filter_vars_3d(m);
 }
 
 // ----------------------------------------------------------------------------

@@ -255,10 +255,10 @@ const char* sparc_gpu_last_error(const sparc_ctx* c) { return c ? c->err.c_str()
 
 static int validate(const sparc_params* p, std::string& why) {
     auto pow2 = [](int n) { return n >= 4 && n <= 1024 && (n & (n - 1)) == 0; };
-    if (p->option != 4 && p->option != 17) { why = "option must be 4 or 17"; return 0; }
+    if (p->option != 2 && p->option != 4 && p->option != 17) { why = "option must be 2, 4 or 17"; return 0; }
     if (!pow2(p->nx)) { why = "nx must be a power of two in [4,1024]"; return 0; }
     if (p->option == 17 && p->ny != 1) { why = "option 17 needs ny == 1"; return 0; }
-    if (p->option == 4 && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
+    if (p->option != 17 && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
     if (p->nz < 16 || p->nz > 1024) { why = "nz must be in [16,1024]"; return 0; }
     if (p->npmlbot < 2 || p->npmlbot > p->nz / 4 || p->npmltop < 0 || p->npmltop > p->nz / 4) {
         why = "PML widths out of range"; return 0;
@@ -311,7 +311,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->zt, (size_t)ZT_COUNT * c->nz * es))) return bail(rc);
     if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
     if (c->f32) {
-        c->use_fused = fused_supported(c->nz) && getenv("SPARC_FP32_PER_STAGE") == nullptr;
+        // the fused step covers the displacement forms (options 4, 17)
+        c->use_fused = fused_supported(c->nz) && p->option != 2 && getenv("SPARC_FP32_PER_STAGE") == nullptr;
         if (c->use_fused &&
             (rc = dalloc(c, (void**)&c->ftab, (size_t)FZ_COUNT * fused_nzp(c->nz) * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
@@ -496,6 +497,10 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
         ZR(ZT_BZ)[k] = bz[k];
         ZR(ZT_C2)[k] = c2[k];
         ZR(ZT_GRAW)[k] = graw[k];
+        // source_dep(k) = exp(-10.0**(7.0)*4.0*(z(k)-z(e_rad))**2.0), the
+        // REAL*4 product of the literals times a REAL*8 square (physics.f90:109)
+        const double dzs = z[k] - z[c->e_rad - 1];
+        ZR(ZT_SRCDEP)[k] = std::exp(-R4(1.0e7 * 4.0) * (dzs * dzs));
         for (int b = 0; b < 4; ++b) {
             ZR(ZT_TH + 3 * b)[k] = tri[b].low[k];
             ZR(ZT_TH + 3 * b + 1)[k] = 1.0 / tri[b].betad[k];
@@ -612,6 +617,7 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
 
 // diagnostic view of the set-up (tests): out[0..] = e_rad, o_rad, delta_width, deltat,
 // steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps, betas[5]
+static_assert(ZT_COUNT == SPARC_ZTAB_ROWS && PT_COUNT == SPARC_PTAB_ROWS, "table rows of the header");
 int sparc_gpu_info(sparc_ctx* c, double* out, double* ztab, double* ptab) {
     if (!c || !c->have_bg) return c ? fail(c, SPARC_ESTATE, "no background") : SPARC_EINVAL;
     if (out) {
@@ -792,13 +798,14 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.ybuf = CP<T>(c->ybuf); A.pbuf = CP<T>(c->pbuf); A.rbuf = CP<T>(c->rbuf);
     A.zt = (const T*)c->zt; A.pt = (const T*)c->pt;
     A.fs = c->fs; A.ps = c->ps; A.M = c->M; A.nz = c->nz;
-    A.npmlbot = P.npmlbot; A.npmltop = P.npmltop; A.option = P.option; A.damp = P.damp_waves && P.option == 4;
+    A.npmlbot = P.npmlbot; A.npmltop = P.npmltop; A.option = P.option; A.damp = P.damp_waves && P.option != 17;
     A.block = c->stage_block;
     A.cc.C1 = (T)c->cc64.C1; A.cc.C2 = (T)c->cc64.C2;
     for (int i = 0; i < 5; ++i) A.cc.Cb[i] = (T)c->cc64.Cb[i];
     for (int i = 0; i < 4; ++i) A.cc.Cf[i] = (T)c->cc64.Cf[i];
     A.cc.alpha2 = (T)c->cc64.alpha2; A.cc.beta1 = (T)c->cc64.beta1; A.cc.cnst = (T)c->cc64.cnst;
-    int ksrc = P.src_k > 0 ? P.src_k : (P.compute_adjoint ? c->o_rad : c->e_rad);
+    // the velocity form centres its source on e_rad in either direction (pml.f90:49)
+    int ksrc = P.src_k > 0 ? P.src_k : (P.compute_adjoint && P.option != 2 ? c->o_rad : c->e_rad);
     A.ksrc = ksrc - 1;
     A.src_scale = (T)(c->delta_width / c->zt_host[ZT_RHO0 * c->nz + ksrc - 1]);
     A.planes = CP<T>(c->planes); A.plane_ss = (long long)c->src_L * c->M; A.L = c->src_L;
@@ -866,8 +873,9 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
             CKL();
         }
         if (c->rec_on) {
+            // v_z: field 6 of the displacement forms, field 4 of the velocity form
             launch_record<T>(CP<T>(c->a), CP<T>(c->rec), c->d_t0, c->d_time, c->steps, c->rec_max, c->fs, c->M,
-                             c->o_rad - 1, c->active_n, c->stream);
+                             c->o_rad - 1, c->P.option == 2 ? 3 : 5, c->active_n, c->stream);
             c->launches++;
             CKL();
         }
@@ -1144,7 +1152,7 @@ static int prim_spectral(sparc_ctx* c, const double* var, double* dvar, int whic
 int sparc_gpu_ddx(sparc_ctx* c, const double* var, double* dvar) { return prim_spectral(c, var, dvar, 0, 0); }
 int sparc_gpu_ddy(sparc_ctx* c, const double* var, double* dvar) { return prim_spectral(c, var, dvar, 1, 0); }
 int sparc_gpu_damp(sparc_ctx* c, const double* v, double* rhs) {
-    if (c && c->P.option != 4) return fail(c, SPARC_EINVAL, "damping is a 3-D operation");
+    if (c && c->P.option == 17) return fail(c, SPARC_EINVAL, "damping is a 3-D operation");
     return prim_spectral(c, v, rhs, 2, 1);
 }
 
@@ -1244,6 +1252,7 @@ extern "C" {
 int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (c->P.option == 2) return fail(c, SPARC_EINVAL, "sensitivity kernels need the displacement form");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
         int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));

@@ -53,7 +53,8 @@ enum ZTab {
     ZT_STRETCH = 0, ZT_UNSTRETCH, ZT_C2RHO0, ZT_GRADP0, ZT_RHO0, ZT_GRADRHO0, ZT_RHOINV, ZT_G,
     ZT_AZ, ZT_BZ, ZT_C2, ZT_GRAW,
     ZT_TH = 12,          // per bc b in 0..3: ZT_TH + 3*b + {0: lowr, 1: 1/betad, 2: gam}
-    ZT_COUNT = ZT_TH + 12
+    ZT_SRCDEP = ZT_TH + 12,   // source_dep (physics.f90:109), the velocity-form source profile
+    ZT_COUNT
 };
 // ---- pencil table (T, M entries per row) ------------------------------------
 enum PTab { PT_KX = 0, PT_KY, PT_DAMP, PT_HF, PT_COUNT };
@@ -262,10 +263,10 @@ void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s);
 // launchers (modal.cu)
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s);
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s);
-// surface record of vz at plane kplane for every slot whose clock is on the output cadence
+// surface record of field `field` (v_z) at plane kplane for every slot whose clock is on the output cadence
 template <typename T>
 void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, const int* time,
-                   int steps, int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s);
+                   int steps, int rec_max, long long fs, int M, int kplane, int field, int nsrc, cudaStream_t s);
 // the device time counter: set, and advance by one step
 void launch_set_time(int* time, int value, cudaStream_t s);
 void launch_tick(int* time, cudaStream_t s);

@@ -168,6 +168,130 @@ __global__ void __launch_bounds__(128) stage_kernel(const StageArgs<T> A) {
     }
 }
 
+// One RK stage of MP_QUIET_PML_3D (pml.f90:12-76), the velocity form with
+// fields rho, v_x, v_y, v_z, p (initialize.f90:498-508).  Its two z
+// derivatives are independent of each other:
+//   S1 (up)   compact RHS of d(v_z)/dz (bc 1), forward elimination -> y
+//   S2 (down) back substitution, stretch, PML psi_vz, div; the RHS of rho and
+//             p are staged in rb / pb, because rho and p are still read as
+//             stage arguments below
+//   S3 (up)   compact RHS of dp/dz (bc 0), forward elimination -> y
+//   S4 (down) back substitution, stretch, PML psi_p; RHS v_x, v_y, v_z (with
+//             rho g, and the source forcing*source_dep over |k - e_rad| <= 4),
+//             the staged RHS; rows 1 and nz zeroed; then the damping of v,
+//             which the reference applies after the zeroing (pml.f90:57-72)
+template <typename T>
+__global__ void __launch_bounds__(128) stage_velocity_kernel(const StageArgs<T> A) {
+    typedef typename CplxOf<T>::type CT;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= A.M) return;
+    const int s = blockIdx.y;
+    const int nz = A.nz;
+    const long long M = A.M, fs = A.fs;
+    CT* __restrict__ a = A.a + (long long)s * 6 * fs + m;
+    CT* __restrict__ scr = A.scr + (long long)s * 6 * fs + m;
+    CT* __restrict__ pml = A.pml + (long long)s * 2 * A.ps + m;
+    CT* __restrict__ spml = A.scrpml + (long long)s * 2 * A.ps + m;
+    CT* __restrict__ y = A.ybuf + (long long)s * fs + m;
+    CT* __restrict__ pb = A.pbuf + (long long)s * fs + m;
+    CT* __restrict__ rb = A.rbuf + (long long)s * fs + m;
+    const T* __restrict__ zt = A.zt;
+    const T kx = __ldg(&A.pt[PT_KX * M + m]);
+    const T ky = __ldg(&A.pt[PT_KY * M + m]);
+    const T gd = A.damp ? __ldg(&A.pt[PT_DAMP * M + m]) : (T)0;
+    const T beta = A.beta;
+    const bool hs = A.has_scr != 0;
+    const int nb = A.npmlbot, nt = A.npmltop;
+    auto temp = [&](int f, int j) -> CT {
+        long long o = f * fs + (long long)j * M;
+        CT v = a[o];
+        if (hs) v = v + beta * scr[o];
+        return v;
+    };
+    auto pmlidx = [&](int j) -> int { return j < nb ? j : (j >= nz - nt ? nb + (j - (nz - nt)) : -1); };
+
+    // S1: d(v_z)/dz, bc 1
+    compact_forward<CT, T>(nz, 1, [&](int j) { return temp(3, j); }, czero<CT>(), czero<CT>(),
+                           zt + (ZT_TH + 3) * nz, zt + (ZT_TH + 4) * nz, A.cc, y, M);
+    // S2: div, staged RHS of rho (RHScont) and p (RHSp)
+    {
+        const T* gam = zt + (ZT_TH + 5) * nz;
+        CT ud = y[(long long)(nz - 1) * M];
+        for (int j = nz - 1; j >= 0; --j) {
+            if (j < nz - 1) ud = y[(long long)j * M] - __ldg(&gam[j + 1]) * ud;
+            CT dz = ud * __ldg(&zt[ZT_STRETCH * nz + j]);
+            const int ip = pmlidx(j);
+            if (ip >= 0) {
+                long long o = (long long)ip * M;
+                CT psi = pml[o];
+                if (hs) psi = psi + beta * spml[o];
+                spml[o] = __ldg(&zt[ZT_AZ * nz + j]) * dz + __ldg(&zt[ZT_BZ * nz + j]) * psi;
+                dz = dz + psi;
+            }
+            const CT vz = temp(3, j);
+            const CT div = imul(kx, temp(1, j)) + imul(ky, temp(2, j)) + dz;
+            const long long o = (long long)j * M;
+            rb[o] = -__ldg(&zt[ZT_GRADRHO0 * nz + j]) * vz - __ldg(&zt[ZT_RHO0 * nz + j]) * div;
+            pb[o] = -__ldg(&zt[ZT_C2RHO0 * nz + j]) * div - vz * __ldg(&zt[ZT_GRADP0 * nz + j]);
+        }
+    }
+    // S3: dp/dz, bc 0
+    compact_forward<CT, T>(nz, 0, [&](int j) { return temp(4, j); }, czero<CT>(), czero<CT>(),
+                           zt + ZT_TH * nz, zt + (ZT_TH + 1) * nz, A.cc, y, M);
+    // S4
+    {
+        const T* gam = zt + (ZT_TH + 2) * nz;
+        CT F = czero<CT>();
+        const int tl = *A.clk.time - A.clk.t0[s];
+        const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
+        if (src_on) {
+            const CT* pl = A.planes + (long long)s * A.plane_ss + m;
+            if (A.src_mode == 1) {
+                T w = (tl < A.nseries) ? (T)A.series[(long long)s * A.nseries + tl] : (T)0;
+                F = w * pl[0];
+            } else {
+                int idx[7];
+                double w[7];
+                const int nw = lagrange_dev(A.clk, tl, A.L, idx, w);
+                #pragma unroll
+                for (int l = 0; l < 7; ++l)
+                    if (l < nw) F = F + (T)w[l] * pl[(long long)idx[l] * M];
+            }
+        }
+        CT ud = y[(long long)(nz - 1) * M];
+        for (int j = nz - 1; j >= 0; --j) {
+            if (j < nz - 1) ud = y[(long long)j * M] - __ldg(&gam[j + 1]) * ud;
+            CT dp = ud * __ldg(&zt[ZT_STRETCH * nz + j]);
+            const int ip = pmlidx(j);
+            if (ip >= 0) {
+                long long o = (long long)ip * M + A.ps;
+                CT psi = pml[o];
+                if (hs) psi = psi + beta * spml[o];
+                spml[o] = __ldg(&zt[ZT_AZ * nz + j]) * dp + __ldg(&zt[ZT_BZ * nz + j]) * psi;
+                dp = dp + psi;
+            }
+            const long long o = (long long)j * M;
+            const CT r = temp(0, j), vx = temp(1, j), vy = temp(2, j), vz = temp(3, j), p = temp(4, j);
+            const T ri = __ldg(&zt[ZT_RHOINV * nz + j]);
+            const T gz = __ldg(&zt[ZT_G * nz + j]);
+            CT rvx = -ri * imul(kx, p);
+            CT rvy = -ri * imul(ky, p);
+            CT rvz = -ri * (dp + gz * r);
+            if (src_on && abs(j - A.ksrc) <= 4) rvz = rvz + __ldg(&zt[ZT_SRCDEP * nz + j]) * F;
+            CT rc = rb[o], rp = pb[o];
+            if (j == 0 || j == nz - 1) {
+                rc = rp = rvx = rvy = rvz = czero<CT>();
+            }
+            if (A.damp) { rvx = rvx - gd * vx; rvy = rvy - gd * vy; rvz = rvz - gd * vz; }
+            scr[0 * fs + o] = rc;
+            scr[1 * fs + o] = rvx;
+            scr[2 * fs + o] = rvy;
+            scr[3 * fs + o] = rvz;
+            scr[4 * fs + o] = rp;
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     typedef typename CplxOf<T>::type CT;
@@ -180,7 +304,7 @@ __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     const CT* __restrict__ scr = A.scr + (long long)s * 6 * fs + m;
     const T dt = A.dt;
     const T hf = __ldg(&A.pt[PT_HF * M + m]);
-    const bool opt3d = (A.option == 4);
+    const bool opt3d = (A.option != 17);
     const bool hstep = slot_hfilter(A.clk, *A.clk.time - A.clk.t0[s]);
     for (int f = 0; f < 6; ++f) {
         CT* af = a + f * fs;
@@ -257,7 +381,7 @@ __global__ void __launch_bounds__(128) zderiv_real_kernel(const double* __restri
 template <typename T>
 __global__ void record_kernel(const typename CplxOf<T>::type* __restrict__ a, typename CplxOf<T>::type* __restrict__ rec,
                               const int* __restrict__ t0, const int* __restrict__ time, int steps, int rec_max,
-                              long long fs, int M, int kplane) {
+                              long long fs, int M, int kplane, int field) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int s = blockIdx.y;
     if (m >= M) return;
@@ -265,19 +389,19 @@ __global__ void record_kernel(const typename CplxOf<T>::type* __restrict__ a, ty
     if (tl < 0 || tl % steps != 0) return;
     const int r = tl / steps;
     if (r >= rec_max) return;
-    rec[((long long)s * rec_max + r) * M + m] = a[(long long)s * 6 * fs + 5 * fs + (long long)kplane * M + m];
+    rec[((long long)s * rec_max + r) * M + m] = a[(long long)s * 6 * fs + field * fs + (long long)kplane * M + m];
 }
 
 template <typename T>
 void launch_record(const typename CplxOf<T>::type* a, typename CplxOf<T>::type* rec, const int* t0, const int* time,
-                   int steps, int rec_max, long long fs, int M, int kplane, int nsrc, cudaStream_t s) {
+                   int steps, int rec_max, long long fs, int M, int kplane, int field, int nsrc, cudaStream_t s) {
     dim3 grid((M + 255) / 256, nsrc);
-    record_kernel<T><<<grid, 256, 0, s>>>(a, rec, t0, time, steps, rec_max, fs, M, kplane);
+    record_kernel<T><<<grid, 256, 0, s>>>(a, rec, t0, time, steps, rec_max, fs, M, kplane, field);
 }
 template void launch_record<double>(const double2*, double2*, const int*, const int*, int, int, long long, int, int,
-                                    int, cudaStream_t);
+                                    int, int, cudaStream_t);
 template void launch_record<float>(const float2*, float2*, const int*, const int*, int, int, long long, int, int, int,
-                                   cudaStream_t);
+                                   int, cudaStream_t);
 
 // The context's time lives on the device so that a captured sequence of
 // steps replays at any time: the step kernels read it, and one thread
@@ -290,7 +414,8 @@ void launch_tick(int* time, cudaStream_t s) { tick_kernel<<<1, 1, 0, s>>>(time);
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s) {
     const int b = A.block == 64 ? 64 : 128;
     dim3 grid((A.M + b - 1) / b, nsrc);
-    stage_kernel<T><<<grid, b, 0, s>>>(A);
+    if (A.option == 2) stage_velocity_kernel<T><<<grid, b, 0, s>>>(A);
+    else stage_kernel<T><<<grid, b, 0, s>>>(A);
 }
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s) {
     dim3 grid((A.M + 127) / 128, nsrc);

@@ -25,6 +25,7 @@ SPARC_EIO = -7
 SPARC_FP64 = 0
 SPARC_FP32 = 1
 SRC_NONE, SRC_SERIES, SRC_LAGRANGE = 0, 1, 2
+ZTAB_ROWS, PTAB_ROWS = 25, 4      # SPARC_ZTAB_ROWS / SPARC_PTAB_ROWS of the header
 
 #: every function the header declares (checked by the CPU test suite)
 EXPORTS = [

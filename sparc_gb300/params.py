@@ -19,9 +19,10 @@ import re
 import numpy as np
 
 #: option codes of step.f90:74-110 that this framework implements
+OPT_QUIET_PML_3D = 2           # pml.f90:12 (MP_QUIET_PML_3D), velocity form
 OPT_QUIET_PML_3D_DISPL = 4     # displacement.f90:482 (MP_QUIET_PML_3D_DISPL)
 OPT_QUIET_PML_2D_DISPL = 17    # physics2d.f90:948 (MP_QUIET_PML_2D_DISPL)
-SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL)
+SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL)
 
 
 def r4(x: float) -> float:
@@ -126,8 +127,10 @@ class SparcParams:
     @classmethod
     def from_params_i(cls, text: str, **overrides) -> "SparcParams":
         """Parse the ``parameter(name = value, ...)`` statements of a params.i
-        file.  Logical switches map as: USE_PML must be true, DISPL must be
-        true, MAGNETIC/FLOWS must be false (the supported options)."""
+        file.  Logical switches map as PARSE_OPTIONS (initialize.f90:778-824)
+        does for the supported options: USE_PML must be true, DISPL selects
+        option 4 (true) or the velocity form, option 2 (false), and
+        MAGNETIC/FLOWS must be false."""
         vals: dict = {}
         body = re.sub(r"!.*", "", text)
         for m in re.finditer(r"parameter\s*\((.*?)\)\s*$", body, re.I | re.M | re.S):
@@ -145,6 +148,8 @@ class SparcParams:
             raise ValueError("MAGNETIC/FLOWS backgrounds are not supported by this framework")
         if "_damp_waves" in vals:
             kw["damp_waves"] = vals["_damp_waves"]
+        if vals.get("_displ") is False:
+            kw["option"] = OPT_QUIET_PML_3D
         kw.update(overrides)
         p = cls(**kw)
         p.validate()
@@ -158,6 +163,8 @@ class SparcParams:
         two_d = len(lines) > 1 and lines[1].upper() == "2D"
         p = self.replace(compute_forward=(kind == "spectral"), compute_adjoint=(kind == "adjoint"))
         if two_d:
+            if self.option == OPT_QUIET_PML_3D:
+                raise ValueError("the 2-D velocity form (option 6) is not supported")
             p = p.replace(option=OPT_QUIET_PML_2D_DISPL, ny=1)
         return p
 

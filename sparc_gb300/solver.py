@@ -89,11 +89,11 @@ class Solver:
         return d
 
     def tables(self):
-        zt = np.zeros(24 * self.p.nz)
+        zt = np.zeros(native.ZTAB_ROWS * self.p.nz)
         m = self.p.ny * (self.p.nx // 2 + 1)
-        pt = np.zeros(4 * m)
+        pt = np.zeros(native.PTAB_ROWS * m)
         self._ck(self.L.sparc_gpu_info(self.h, None, _dp(zt), _dp(pt)))
-        return zt.reshape(24, self.p.nz), pt.reshape(4, m)
+        return zt.reshape(native.ZTAB_ROWS, self.p.nz), pt.reshape(native.PTAB_ROWS, m)
 
     def set_source_series(self, plane: np.ndarray, series: np.ndarray, slot: int = 0):
         """forcing(x, y, t_n) = plane(x, y) * series[n], injected at the source plane."""

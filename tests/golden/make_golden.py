@@ -1,7 +1,7 @@
 """Generates tests/golden/oracle_golden.npz: outputs of the CPU oracle on small
 seeded cases (compact derivative for every boundary code, spectral
 derivatives, damping, three 3-D time steps with a forward source, thirty-one
-2-D time steps, one kernel accumulation).  Regenerate with
+2-D time steps, thirty-one velocity-form steps, one kernel accumulation).  Regenerate with
     python tests/golden/make_golden.py
 The GPU parity tests compare the CUDA path against these fixtures as well as
 against the live oracle."""
@@ -26,12 +26,23 @@ def golden_params_2d():
     return small_params_2d(nx=32, nz=32, npmlbot=4, npmltop=4)
 
 
+def golden_params_vel():
+    """Velocity form (option 2): fields rho, v_x, v_y, v_z, p."""
+    return small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4, option=2)
+
+
 def golden_inputs(p, seed):
     rng = np.random.default_rng(seed)
     a = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
     if p.ny == 1:
         a[1] = 0.0
         a[4] = 0.0
+    if p.option == 2:
+        # five fields in the velocity form; a velocity perturbation at rest
+        # density and pressure (a random pressure would be scaled by 1/rho0)
+        a[0] = 0.0
+        a[4] = 0.0
+        a[5] = 0.0
     pml = rng.standard_normal((2, p.nzpml, p.ny, p.nx)) * 1e-5
     pml[1, 0] = 0.0
     x = (np.arange(p.nx) / p.nx - 0.5) * p.xlength / 1e8
@@ -75,6 +86,15 @@ def compute():
     o2.set_source(1, plane[None].copy(), series)
     o2.step(31)
     out["step31_2d_a"] = o2.state()[0]
+    pv = golden_params_vel()
+    ov = O.Oracle(pv, table_for(pv))
+    a, pml, plane, series = golden_inputs(pv, 47)
+    ov.set_state(a, pml)
+    ov.set_source(1, plane[None].copy(), series)
+    ov.step(31)
+    st, _, pm = ov.state()
+    out["step31_vel_a"] = st
+    out["step31_vel_pml"] = pm
     # one kernel accumulation on seeded fields
     rng = np.random.default_rng(46)
     fwd = rng.standard_normal((6, p.nz, p.ny, p.nx))

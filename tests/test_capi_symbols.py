@@ -53,3 +53,13 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(native, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         native.load(str(tmp_path / "nope.so"))
+
+
+def test_table_row_counts_match_header():
+    """The binding sizes the diagnostic tables from the header's row counts."""
+    import re
+    from sparc_gb300 import native
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "sparc_gpu.h")).read()
+    rows = dict(re.findall(r"#define (SPARC_[ZP]TAB_ROWS) (\d+)", hdr))
+    assert int(rows["SPARC_ZTAB_ROWS"]) == native.ZTAB_ROWS
+    assert int(rows["SPARC_PTAB_ROWS"]) == native.PTAB_ROWS

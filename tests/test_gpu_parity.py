@@ -293,6 +293,68 @@ def test_kernel_accumulation_source_groups(gpu_lib, prec):
             assert np.array_equal(many[s][q], alone[q]), (s, q)
 
 
+def _velocity_state(p, seed):
+    a, pml = random_state(p, seed=seed)
+    a[0] = 0.0          # rest density and pressure: the velocity form's natural seed
+    a[4] = 0.0
+    a[5] = 0.0
+    return a, pml
+
+
+@pytest.mark.parametrize("nsteps,mode", [(1, 1), (5, 1), (31, 1), (31, 2)])
+def test_velocity_form_matches_oracle(gpu_lib, oracle_mod, nsteps, mode):
+    """Option 2 (MP_QUIET_PML_3D, pml.f90:12-76): rho, v_x, v_y, v_z, p with the
+    9-plane source_dep forcing, the PML accounting and the damping."""
+    p = small_params(option=2)
+    g, o = make_pair(p, oracle_mod, gpu_lib)
+    a0, pml0 = _velocity_state(p, 21)
+    g.set_state(a0, pml0)
+    o.set_state(a0, pml0)
+    if mode == 1:
+        plane = gaussian_plane(p)
+        series = oracle_mod.forward_source(p, 200) * 1e3
+        g.set_source_series(plane, series)
+        o.set_source(1, plane[None].copy(), series)
+    else:
+        planes = np.random.default_rng(5).standard_normal((12, p.ny, p.nx)) * 1e-4
+        g.set_source_lagrange(planes)
+        o.set_source(2, planes, None)
+    g.step(nsteps)
+    o.step(nsteps)
+    ag, pg = g.state()
+    ao, _, po = o.state()
+    for f in range(5):
+        assert rel_l2(ag[f], ao[f]) < TOL64, (f, rel_l2(ag[f], ao[f]))
+    assert np.abs(ag[5]).max() == 0
+    assert rel_l2(pg, po) < TOL64
+
+
+def test_velocity_form_fp32_and_records(gpu_lib, oracle_mod):
+    """FP32 (per-stage kernels) against FP64, and the surface records of the
+    velocity form come from v_z (its fourth field)."""
+    from sparc_gb300.solver import Solver
+    p64 = small_params(option=2)
+    tab = table_for(p64)
+    a0, pml0 = _velocity_state(p64, 22)
+    plane = gaussian_plane(p64)
+    series = oracle_mod.forward_source(p64, 200) * 1e3
+    out = []
+    for p in (p64, p64.replace(precision="f32")):
+        g = Solver(p, tab)
+        g.set_state(a0, pml0)
+        g.set_source_series(plane, series)
+        g.record_surface(4)
+        g.step(31)
+        a, _ = g.state()
+        out.append((a, g.records(), g.info()["o_rad"]))
+    (a64, r64, orad), (a32, r32, _) = out
+    for f in range(5):
+        assert rel_l2(a32[f], a64[f]) < 2e-5, (f, rel_l2(a32[f], a64[f]))
+    assert r64.shape[0] >= 3
+    assert rel_l2(r64[2], a64[3, orad - 1]) < 1e-14      # record 2 = v_z after the step at time 30
+    assert rel_l2(r32[2], r64[2]) < 1e-4
+
+
 def test_gpu_matches_committed_golden_fixtures(gpu_lib):
     import os
     import sys
@@ -324,6 +386,18 @@ def test_gpu_matches_committed_golden_fixtures(gpu_lib):
     st2, _ = s2.state()
     for f in (0, 2, 3, 5):
         assert rel_l2(st2[f], g["step31_2d_a"][f]) < TOL64, f
+    from golden.make_golden import golden_params_vel
+    pv = golden_params_vel()
+    sv = Solver(pv, table_for(pv))
+    a, pml, plane, series = golden_inputs(pv, 47)
+    sv.set_state(a, pml)
+    sv.set_source_series(plane, series)
+    sv.step(31)
+    stv, pmv = sv.state()
+    for f in range(5):
+        assert rel_l2(stv[f], g["step31_vel_a"][f]) < TOL64, f
+    assert np.abs(stv[5]).max() == 0
+    assert rel_l2(pmv, g["step31_vel_pml"]) < TOL64
 
 
 @pytest.mark.parametrize("two_d,nz", [(False, 48), (True, 48), (False, 161), (False, 196), (True, 300)])
