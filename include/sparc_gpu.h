@@ -121,6 +121,19 @@ int sparc_gpu_set_source(sparc_ctx* ctx, int src_idx, int mode, const double* pl
  * (driver.f90:455-476). */
 int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
 
+/* Option 10 (MP_MHD_PML_3D_DISPL, displacement.f90:663-849): the 3-D cgs
+ * background that READ_IN_FIELD reads (all_modules.f90:486-513) -- density,
+ * sound speed, pressure and B_x, B_y, B_z, each nx*ny*nz values in the
+ * Fortran order a(nx,ny,nz) -- after sparc_gpu_set_background has set the
+ * quiet column (z grid, gravity, Gamma_1, and the column the source planes
+ * are searched on).  Replaces the magnetic parts of mp_Initialize_RHS
+ * (physics.f90:62-161, 204-208, 255-303, 356-363).  For option 10 the state
+ * is physical (get_field / get_state return it without transforms) and the
+ * PML arrays of set_state / get_state hold six auxiliaries (psi_vz, psi_p,
+ * psi_dzbx, psi_dzby, psi_induction_bx, psi_induction_by) of nzpml planes. */
+int sparc_gpu_set_mhd_background(sparc_ctx* ctx, const double* rho, const double* c, const double* p,
+                                 const double* bx, const double* by, const double* bz);
+
 /* Pick the fastest of the launch variants that give identical results (the
  * fused FP32 step's modes per CTA, 4 or 2; the per-stage kernels' threads per
  * CTA, 128 or 64) by timing real steps: the call advances the solution by

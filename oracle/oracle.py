@@ -79,6 +79,7 @@ def lib():
             "oracle_kernel_reset": [P], "oracle_kernel_accumulate": [P, D, D, D],
             "oracle_kernel_finish": [P, D, ctypes.c_int],
             "oracle_plane_r2c": [P, D, D],
+            "oracle_set_mhd": [P, D, D, D, D, D, D], "oracle_mhd_profiles": [P, D],
         }.items():
             f = getattr(L, name)
             f.argtypes = args
@@ -189,11 +190,30 @@ class Oracle:
             pml = np.ascontiguousarray(pml, dtype=np.float64)
         lib().oracle_set_state(self.h, _dp(a), _dp(pml) if pml is not None else None)
 
+    @property
+    def npv(self) -> int:
+        """PML auxiliary fields: 6 for the MHD displacement form (option 10), else 2."""
+        return 6 if self.p.option == 10 else 2
+
+    def set_mhd(self, rho, c, p, bx, by, bz):
+        """3-D cgs background of option 10 (as READ_IN_FIELD reads it), (nz, ny, nx)."""
+        arrs = [np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape) for v in (rho, c, p, bx, by, bz)]
+        if lib().oracle_set_mhd(self.h, *[_dp(v) for v in arrs]) != 0:
+            raise RuntimeError("oracle_set_mhd needs option 10")
+
+    def mhd_profiles(self) -> dict:
+        out = np.zeros((15,) + self.shape)
+        if lib().oracle_mhd_profiles(self.h, _dp(out)) != 0:
+            raise RuntimeError("no MHD background")
+        names = ["box", "boy", "boz", "curlbox", "curlboy", "curlboz", "gradrho0_x", "gradrho0_y",
+                 "gradp0_x", "gradp0_y", "gradrho0_z", "gradp0_z", "az", "bzpml", "spongexyz"]
+        return dict(zip(names, out))
+
     def state(self):
         p = self.p
         a = np.zeros((6,) + self.shape)
         scr = np.zeros((6,) + self.shape)
-        pml = np.zeros((2, max(p.npmlbot + p.npmltop, 1), p.ny, p.nx))
+        pml = np.zeros((self.npv, max(p.npmlbot + p.npmltop, 1), p.ny, p.nx))
         lib().oracle_get_state(self.h, _dp(a), _dp(pml), _dp(scr))
         return a, scr, pml
 

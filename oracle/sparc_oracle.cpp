@@ -270,7 +270,13 @@ struct Model {
     double pi, rsun, normx, normy, dimc, dimrho, diml, dimb, deltat;
     double stretchx, stretchy, delta_width;
     int e_rad, o_rad, steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps;
-    std::vector<double> x, y, z, stretch, unstretch, g, gam1, source_dep, cq, rhoq;
+    std::vector<double> x, y, z, stretch, unstretch, g, graw, gam1, source_dep, cq, rhoq;
+    int npv = 2;       // PML auxiliary fields: 2 (quiet), 6 (MHD displacement form)
+    // MHD background (option 10): B0, its curl as the reference forms it, the
+    // horizontal background gradients, the sponge, the per-pixel source planes
+    std::vector<double> box, boy, boz, curlbox, curlboy, curlboz, gradrho0_x, gradrho0_y, gradp0_x, gradp0_y;
+    std::vector<double> spongez, spongexyz, delta_width_2d;
+    std::vector<int> erad_2d, orad_2d;
     std::vector<cplx> eyekx, eyeky;
     std::vector<double> decay_coeff_x, decay_coeff_y;
     // 3-D background (quiet Sun still carries full arrays, as the reference does)
@@ -425,7 +431,7 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     m.diml = m.rsun;
     m.dimb = std::sqrt(4.0 * m.pi * m.dimc * m.dimc * m.dimrho);
     long N = m.N, NP = m.NP;
-    m.z.resize(nz); m.g.resize(nz); m.gam1.resize(nz); m.cq.resize(nz); m.rhoq.resize(nz);
+    m.z.resize(nz); m.g.resize(nz); m.graw.resize(nz); m.gam1.resize(nz); m.cq.resize(nz); m.rhoq.resize(nz);
     m.c2.assign(N, 0); m.rho0.assign(N, 0); m.p0.assign(N, 0); m.c_speed.assign(N, 0);
     for (int k = 0; k < nz; ++k) {
         const double* d = table + 6 * k;
@@ -439,6 +445,7 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
             m.rho0[q + NP * k] = r0; m.p0[q + NP * k] = pp;
         }
         m.g[k] = d[4] * m.diml / (m.dimc * m.dimc);
+        m.graw[k] = m.g[k];
         m.gam1[k] = d[5];
         m.cq[k] = d[1] / m.dimc;
         m.rhoq[k] = d[2] / m.dimrho;
@@ -558,7 +565,8 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     }
     // state
     m.a.assign(N * 6, 0); m.temp_step.assign(N * 6, 0); m.scr.assign(N * 6, 0);
-    long npml = (long)NP * std::max(m.nzpml, 1) * 2;
+    m.npv = P->option == 10 ? 6 : 2;
+    long npml = (long)NP * std::max(m.nzpml, 1) * m.npv;
     m.scrpml.assign(npml, 0); m.pmlvars.assign(npml, 0); m.psipml.assign(npml, 0);
     m.gradp.assign(N * 3, 0); m.dvxdx.assign(N, 0); m.dvydy.assign(N, 0); m.gradvz.assign(N, 0);
     m.div.assign(N, 0); m.scratch.assign(N * 2, 0);
@@ -713,6 +721,261 @@ static void rhs_option2(Model& m) {
         damp_velocity(m, v_y, RHSv_y);
         damp_velocity(m, v_z, RHSv_z);
     }
+}
+
+// ----------------------------------------------------------------------------
+// MHD background (option 10): the magnetic parts of mp_Initialize_RHS
+// (physics.f90:62-161, 204-208, 255-303, 356-363) in the reference's order,
+// applied after the quiet set-up.  Inputs are the 3-D cgs arrays that
+// READ_IN_FIELD reads (all_modules.f90:486-513), (nz, ny, nx) C order.
+// ----------------------------------------------------------------------------
+static void setup_mhd(Model& m, const double* rho, const double* cs, const double* pr,
+                      const double* bx, const double* by, const double* bz) {
+    long N = m.N, NP = m.NP; int nx = m.nx, ny = m.ny, nz = m.nz;
+    // erad_2d / orad_2d (physics.f90:62-87): the search runs before
+    // READ_IN_FIELD, on the density of solar_data (the quiet column); the
+    // loop bounds are clamped to the box
+    m.erad_2d.assign(NP, 0); m.orad_2d.assign(NP, 0); m.delta_width_2d.assign(NP, 0.0);
+    for (long q = 0; q < NP; ++q) {
+        double temp = 1.0;
+        for (int k = std::max(1, m.e_rad - 50); k <= std::min(nz, m.e_rad + 10); ++k)
+            if (std::fabs(m.rhoq[m.e_rad - 1] - m.rho0[q + NP * (k - 1)]) <= temp) {
+                temp = std::fabs(m.rhoq[m.e_rad - 1] - m.rho0[q + NP * (k - 1)]);
+                m.erad_2d[q] = k;
+            }
+        temp = 1.0;
+        for (int k = std::max(1, m.o_rad - 50); k <= std::min(nz, m.o_rad + 10); ++k)
+            if (std::fabs(m.rhoq[m.o_rad - 1] - m.rho0[q + NP * (k - 1)]) <= temp) {
+                temp = std::fabs(m.rhoq[m.o_rad - 1] - m.rho0[q + NP * (k - 1)]);
+                m.orad_2d[q] = k;
+            }
+        const int k2 = m.P.compute_adjoint ? m.orad_2d[q] : m.erad_2d[q];
+        m.delta_width_2d[q] = 2.0 / (m.z[k2] - m.z[k2 - 2]);
+    }
+    // spongez (physics.f90:104-108); PERIODIC: spongexyz(:,:,k) = spongez(k)
+    m.spongez.assign(nz, 0.0); m.spongexyz.assign(N, 0.0);
+    for (int k = 0; k < nz; ++k) {
+        m.spongez[k] = 200.0 / (1.0 + std::exp((R4(1.002) - m.z[k]) / R4(0.0001)))
+                     + 300.0 / (1.0 + std::exp((m.z[k] - (m.z[0] + R4(0.005))) / R4(0.0005)));
+        for (long q = 0; q < NP; ++q) m.spongexyz[q + NP * k] = m.spongez[k];
+    }
+    // READ_IN_FIELD
+    m.box.assign(N, 0); m.boy.assign(N, 0); m.boz.assign(N, 0);
+    for (long q = 0; q < N; ++q) {
+        m.rho0[q] = rho[q] / m.dimrho;
+        m.c_speed[q] = cs[q] / m.dimc;
+        m.p0[q] = pr[q] / (m.dimrho * std::pow(m.dimc, 2.0));
+        m.box[q] = bx[q] / m.dimb; m.boy[q] = by[q] / m.dimb; m.boz[q] = bz[q] / m.dimb;
+        m.c2[q] = std::pow(m.c_speed[q], 2.0);
+    }
+    // reduction of the field (physics.f90:116-129): the top taper is REAL*4
+    std::vector<double> red(N);
+    for (int k = 0; k < nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * k;
+            red[id] = (std::pow(m.boz[id], 2.0) + std::pow(m.box[id], 2.0) + std::pow(m.boy[id], 2.0))
+                    / (m.rho0[id] * std::pow(m.cq[k], 2.0));
+        }
+    for (long q = 0; q < N; ++q) red[q] = 8.0 / (8.0 + red[q]);
+    for (int k1 = nz - 10; k1 <= nz; ++k1) {
+        if (k1 < 1) continue;
+        const float t = (float)(k1 - nz) / 10.0f;
+        const double f = (double)std::pow(t, 4.0f);
+        for (long q = 0; q < NP; ++q) red[q + NP * (k1 - 1)] *= f;
+    }
+    for (long q = 0; q < N; ++q) {
+        const double s = std::pow(red[q], 0.5);
+        m.box[q] *= s; m.boy[q] *= s; m.boz[q] *= s;
+    }
+    // curl B0 as formed at physics.f90:131-159: the d/dz parts are discarded
+    m.curlbox.assign(N, 0); m.curlboy.assign(N, 0); m.curlboz.assign(N, 0);
+    ddx(m, m.boy.data(), m.curlboz.data());
+    ddy(m, m.box.data(), red.data());
+    for (long q = 0; q < N; ++q) m.curlboz[q] = m.curlboz[q] - red[q];
+    ddy(m, m.boz.data(), m.curlbox.data());
+    ddx(m, m.boz.data(), red.data());
+    for (long q = 0; q < N; ++q) m.curlboy[q] = 0.0 - red[q];
+    // physics.f90:204-208
+    for (long q = 0; q < N; ++q) { m.rhoinv[q] = 1.0 / m.rho0[q]; m.c2rho0[q] = m.c2[q] * m.rho0[q]; }
+    ddz(m, m.rho0.data(), m.gradrho0_z.data(), 1);
+    ddz(m, m.p0.data(), m.gradp0_z.data(), 1);
+    // PML profiles with the magnetic wave speed (physics.f90:255-303)
+    {
+        int nb = m.P.npmlbot, nt = m.P.npmltop;
+        std::vector<double> tempin(N);
+        for (long q = 0; q < N; ++q)
+            tempin[q] = std::pow(m.c2[q] + (std::pow(m.box[q], 2.0) + std::pow(m.boy[q], 2.0)
+                                            + std::pow(m.boz[q], 2.0)) / m.rho0[q], 0.5);
+        for (int k = 1; k <= nz; ++k) {
+            double alphaz = m.pi * R4(0.005) * m.diml / m.dimc;
+            if (k < nb + 1) alphaz = m.pi * R4(0.005) * m.diml / m.dimc * (m.z[k - 1] - m.z[0]) / (m.z[nb - 1] - m.z[0]);
+            if (k > nz - nt) alphaz = m.pi * R4(0.005) * m.diml / m.dimc * (m.z[nz - 1] - m.z[k - 1]) / (m.z[nz - 1] - m.z[nz - nt]);
+            double fdec00 = 1.0;
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1);
+                double dampz = 0.0, fdec = 1.0;
+                if (k < nb + 1) {
+                    double r = (m.z[nb - 1] - m.z[k - 1]) / (m.z[nb - 1] - m.z[0]);
+                    dampz = 2.0 * 3.0 * 3.0 * tempin[q] / (m.z[nb - 1] - m.z[0]) * (r * r);
+                    fdec = alphaz / (dampz + alphaz);
+                    m.gradp0_z[id] *= fdec; m.gradrho0_z[id] *= fdec;
+                }
+                if (k > nz - nt) {
+                    double r = (m.z[nz - nt] - m.z[k - 1]) / (m.z[nz - 1] - m.z[nz - nt]);
+                    dampz = 3.0 * 3.0 * tempin[q + NP * (long)(nz - 1)] / (m.z[nz - 1] - m.z[nz - nt]) * (r * r);
+                    fdec = alphaz / (dampz + alphaz);
+                    m.gradp0_z[id] *= fdec; m.gradrho0_z[id] *= fdec;
+                }
+                if (q == 0) fdec00 = fdec;
+                m.bzpml[id] = -alphaz - dampz;
+                m.az[id] = -dampz;
+            }
+            m.g[k - 1] = (k < nb + 1 || k > nz - nt) ? m.graw[k - 1] * fdec00 : m.graw[k - 1];
+        }
+    }
+    // horizontal background gradients (physics.f90:356-363)
+    m.gradrho0_x.assign(N, 0); m.gradrho0_y.assign(N, 0); m.gradp0_x.assign(N, 0); m.gradp0_y.assign(N, 0);
+    ddx(m, m.rho0.data(), m.gradrho0_x.data());
+    ddy(m, m.rho0.data(), m.gradrho0_y.data());
+    ddx(m, m.p0.data(), m.gradp0_x.data());
+    ddy(m, m.p0.data(), m.gradp0_y.data());
+    (void)nx; (void)ny;
+}
+
+static inline void cross3(double ax, double ay, double az, double bx, double by, double bz,
+                          double& cx, double& cy, double& cz) {
+    cx = ay * bz - az * by;
+    cy = az * bx - ax * bz;
+    cz = ax * by - ay * bx;
+}
+
+// ----------------------------------------------------------------------------
+// MP_MHD_PML_3D_DISPL (displacement.f90:663-849), option 10: the PML sits at
+// the bottom only (k <= npmlbot) with six auxiliaries: psi_vz, psi_p,
+// psi_dzbx, psi_dzby, psi_induction_bx, psi_induction_by (initialize.f90:
+// 487-490, 560-566); the top has the sponge over the last 36 planes
+// ----------------------------------------------------------------------------
+static void rhs_option10(Model& m) {
+    long N = m.N, NP = m.NP; int nz = m.nz;
+    double* xi_x = &m.temp_step[0]; double* xi_y = &m.temp_step[N]; double* xi_z = &m.temp_step[2 * N];
+    double* v_x = &m.temp_step[3 * N]; double* v_y = &m.temp_step[4 * N]; double* v_z = &m.temp_step[5 * N];
+    double* RHSxi_x = &m.scr[0]; double* RHSxi_y = &m.scr[N]; double* RHSxi_z = &m.scr[2 * N];
+    double* RHSv_x = &m.scr[3 * N]; double* RHSv_y = &m.scr[4 * N]; double* RHSv_z = &m.scr[5 * N];
+    long PS = NP * m.nzpml;
+    double* psivz = &m.psipml[0]; double* psip = &m.psipml[PS];
+    double* psidzbx = &m.psipml[2 * PS]; double* psidzby = &m.psipml[3 * PS];
+    double* psiibx = &m.psipml[4 * PS]; double* psiiby = &m.psipml[5 * PS];
+    double* RHSpsivz = &m.scrpml[0]; double* RHSpsip = &m.scrpml[PS];
+    double* RHSpsidzbx = &m.scrpml[2 * PS]; double* RHSpsidzby = &m.scrpml[3 * PS];
+    double* RHSpsiibx = &m.scrpml[4 * PS]; double* RHSpsiiby = &m.scrpml[5 * PS];
+    int nb = m.P.npmlbot;
+    std::vector<double> flux1(N), flux2(N), flux3(N), dxixdx(N), dxiydy(N), dxizdz(N), p(N), rho(N);
+    std::vector<double> gradp_x(N), gradp_y(N), gradp_z(N), bxv(N), byv(N), bzv(N), dzflux1(N), dzflux2(N);
+    std::vector<double> curlbx(N), curlby(N), curlbz(N), dzbx(N), dzby(N);
+    for (long q = 0; q < N; ++q) {
+        flux1[q] = -(xi_z[q] * m.boy[q] - xi_y[q] * m.boz[q]);
+        flux2[q] = -(xi_x[q] * m.boz[q] - xi_z[q] * m.box[q]);
+        flux3[q] = -(xi_y[q] * m.box[q] - xi_x[q] * m.boy[q]);
+    }
+    ddxyz(m, xi_x, dxixdx.data(), xi_y, dxiydy.data(), xi_z, dxizdz.data(), 1);
+    auto pml_bottom = [&](double* deriv, double* psi, double* rhs) {
+        for (int k = 1; k <= nb; ++k)
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1), ip = q + NP * (k - 1);
+                rhs[ip] = m.az[id] * deriv[id] + m.bzpml[id] * psi[ip];
+                deriv[id] = deriv[id] + psi[ip];
+            }
+    };
+    pml_bottom(dxizdz.data(), psivz, RHSpsivz);
+    for (long q = 0; q < N; ++q) {
+        const double div = dxixdx[q] + dxiydy[q] + dxizdz[q];
+        p[q] = -m.c2rho0[q] * div - xi_z[q] * m.gradp0_z[q] - xi_x[q] * m.gradp0_x[q] - xi_y[q] * m.gradp0_y[q];
+        rho[q] = -m.rho0[q] * div - xi_z[q] * m.gradrho0_z[q] - xi_x[q] * m.gradrho0_x[q] - xi_y[q] * m.gradrho0_y[q];
+    }
+    ddxyz(m, p.data(), gradp_x.data(), p.data(), gradp_y.data(), p.data(), gradp_z.data(), 0);
+    pml_bottom(gradp_z.data(), psip, RHSpsip);
+    // induction: b = curl(xi x B0) from the fluxes (displacement.f90:716-757)
+    ddx(m, flux3.data(), byv.data());
+    ddy(m, flux3.data(), bxv.data());
+    ddz(m, flux2.data(), dzflux2.data(), 1);
+    ddx(m, flux2.data(), bzv.data());
+    ddy(m, flux1.data(), flux3.data());
+    ddz(m, flux1.data(), dzflux1.data(), 1);
+    for (int k = 1; k <= nb; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * (k - 1), ip = id;
+            RHSpsiibx[ip] = m.az[id] * dzflux2[id] + m.bzpml[id] * psiibx[ip];
+            dzflux2[id] = dzflux2[id] + psiibx[ip];
+            RHSpsiiby[ip] = m.az[id] * dzflux1[id] + m.bzpml[id] * psiiby[ip];
+            dzflux1[id] = dzflux1[id] + psiiby[ip];
+        }
+    for (long q = 0; q < N; ++q) {
+        bxv[q] = bxv[q] - dzflux2[q];
+        byv[q] = -byv[q] + dzflux1[q];
+        bzv[q] = bzv[q] - flux3[q];
+    }
+    // curl b (displacement.f90:759-787)
+    ddx(m, byv.data(), curlbz.data());
+    ddy(m, bzv.data(), curlbx.data());
+    ddz(m, bxv.data(), dzbx.data(), 1);
+    ddx(m, bzv.data(), curlby.data());
+    ddy(m, bxv.data(), flux1.data());
+    ddz(m, byv.data(), dzby.data(), 1);
+    for (int k = 1; k <= nb; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * (k - 1), ip = id;
+            RHSpsidzbx[ip] = m.az[id] * dzbx[id] + m.bzpml[id] * psidzbx[ip];
+            dzbx[id] = dzbx[id] + psidzbx[ip];
+            RHSpsidzby[ip] = m.az[id] * dzby[id] + m.bzpml[id] * psidzby[ip];
+            dzby[id] = dzby[id] + psidzby[ip];
+        }
+    for (long q = 0; q < N; ++q) {
+        curlbx[q] = curlbx[q] - dzby[q];
+        curlby[q] = -curlby[q] + dzbx[q];
+        curlbz[q] = curlbz[q] - flux1[q];
+    }
+    for (long q = 0; q < N; ++q) {
+        double f1, f2, f3;
+        cross3(curlbx[q], curlby[q], curlbz[q], m.box[q], m.boy[q], m.boz[q], f1, f2, f3);
+        RHSv_x[q] = m.rhoinv[q] * (-gradp_x[q] + f1);
+        RHSv_y[q] = m.rhoinv[q] * (-gradp_y[q] + f2);
+        RHSv_z[q] = m.rhoinv[q] * (-gradp_z[q] + f3);
+        cross3(m.curlbox[q], m.curlboy[q], m.curlboz[q], bxv[q], byv[q], bzv[q], f1, f2, f3);
+        RHSv_x[q] = RHSv_x[q] + m.rhoinv[q] * f1;
+        RHSv_y[q] = RHSv_y[q] + m.rhoinv[q] * f2;
+        RHSv_z[q] = RHSv_z[q] + m.rhoinv[q] * f3;
+    }
+    for (int k = std::max(1, nz - 35); k <= nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * (k - 1);
+            RHSv_x[id] = RHSv_x[id] - m.spongexyz[id] * v_x[id];
+            RHSv_y[id] = RHSv_y[id] - m.spongexyz[id] * v_y[id];
+            RHSv_z[id] = RHSv_z[id] - m.spongexyz[id] * v_z[id];
+        }
+    for (int k = 0; k < nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * k;
+            RHSv_z[id] = RHSv_z[id] - m.rhoinv[id] * rho[id] * m.g[k];
+        }
+    for (long q = 0; q < N; ++q) { RHSxi_x[q] = v_x[q]; RHSxi_y[q] = v_y[q]; RHSxi_z[q] = v_z[q]; }
+    if (m.P.damp_waves) {
+        damp_velocity(m, v_x, RHSv_x);
+        damp_velocity(m, v_y, RHSv_y);
+        damp_velocity(m, v_z, RHSv_z);
+    }
+    // kernel-mode source on the per-pixel planes while time <= forcing_length*cadforcing_step
+    if (m.src_mode != 0 && m.time <= m.forcing_length * m.cadforcing_step) {
+        for (long q = 0; q < NP; ++q) {
+            const int k2 = m.P.src_k > 0 ? m.P.src_k : (m.P.compute_adjoint ? m.orad_2d[q] : m.erad_2d[q]);
+            long id = q + NP * (k2 - 1);
+            RHSv_z[id] = RHSv_z[id] + m.forcing[q] / m.rho0[id] * m.delta_width_2d[q];
+        }
+    }
+    for (int l = 0; l < 6; ++l)
+        for (long q = 0; q < NP; ++q) {
+            m.scr[l * N + q + NP * (nz - 1)] = 0.0;
+            m.scr[l * N + q] = 0.0;
+        }
 }
 
 // ----------------------------------------------------------------------------
@@ -926,7 +1189,7 @@ static void lagrange_interp(Model& m) {
 // STEP (step.f90:43-128) for options 2, 4 and 17 (USE_PML, no horizontal PML);
 // in the velocity form the sixth field is unused and stays zero
 static void step(Model& m) {
-    long N6 = m.N * 6, NPML = (long)m.NP * m.nzpml * 2;
+    long N6 = m.N * 6, NPML = (long)m.NP * m.nzpml * m.npv;
     for (int rk = 1; rk <= 5; ++rk) {
         if (rk == 1) {
             m.temp_step = m.a;
@@ -939,6 +1202,7 @@ static void step(Model& m) {
         }
         if (m.P.option == 4) rhs_option4(m);
         else if (m.P.option == 2) rhs_option2(m);
+        else if (m.P.option == 10) rhs_option10(m);
         else rhs_option17(m);
     }
 #pragma omp parallel for schedule(static)
@@ -1023,14 +1287,14 @@ int oracle_set_source(void* h, int mode, const double* planes, int L, const doub
 int oracle_set_state(void* h, const double* a, const double* pml) {
     Model& m = *(Model*)h;
     std::copy(a, a + m.N * 6, m.a.begin());
-    if (pml) std::copy(pml, pml + (long)m.NP * m.nzpml * 2, m.pmlvars.begin());
+    if (pml) std::copy(pml, pml + (long)m.NP * m.nzpml * m.npv, m.pmlvars.begin());
     return 0;
 }
 
 int oracle_get_state(void* h, double* a, double* pml, double* scr) {
     Model& m = *(Model*)h;
     if (a) std::copy(m.a.begin(), m.a.end(), a);
-    if (pml) std::copy(m.pmlvars.begin(), m.pmlvars.begin() + (long)m.NP * m.nzpml * 2, pml);
+    if (pml) std::copy(m.pmlvars.begin(), m.pmlvars.begin() + (long)m.NP * m.nzpml * m.npv, pml);
     if (scr) std::copy(m.scr.begin(), m.scr.end(), scr);
     return 0;
 }
@@ -1054,6 +1318,27 @@ int oracle_step(void* h, int nsteps) {
 }
 
 int oracle_set_time(void* h, int t) { ((Model*)h)->time = t; return 0; }
+
+// MHD background of option 10 (3-D cgs arrays, (nz, ny, nx) C order)
+int oracle_set_mhd(void* h, const double* rho, const double* c, const double* p, const double* bx,
+                   const double* by, const double* bz) {
+    Model& m = *(Model*)h;
+    if (m.P.option != 10) return -1;
+    setup_mhd(m, rho, c, p, bx, by, bz);
+    return 0;
+}
+
+// MHD diagnostics: out = [box, boy, boz, curlbox, curlboy, curlboz, gradrho0_x, gradrho0_y,
+// gradp0_x, gradp0_y, gradrho0_z, gradp0_z, az, bzpml, spongexyz] (15 * N)
+int oracle_mhd_profiles(void* h, double* out) {
+    Model& m = *(Model*)h;
+    if (m.box.empty()) return -1;
+    const std::vector<double>* v[15] = {&m.box, &m.boy, &m.boz, &m.curlbox, &m.curlboy, &m.curlboz,
+                                        &m.gradrho0_x, &m.gradrho0_y, &m.gradp0_x, &m.gradp0_y,
+                                        &m.gradrho0_z, &m.gradp0_z, &m.az, &m.bzpml, &m.spongexyz};
+    for (int i = 0; i < 15; ++i) std::copy(v[i]->begin(), v[i]->end(), out + (long)i * m.N);
+    return 0;
+}
 
 // Individual primitives, exposed for KATs and GPU parity tests.
 int oracle_ddx(void* h, const double* var, double* dvar) { ddx(*(Model*)h, var, dvar); return 0; }

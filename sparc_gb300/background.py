@@ -81,3 +81,51 @@ def write_polytrope(path: str, table: np.ndarray) -> None:
     with open(path, "w") as f:
         for row in table:
             f.write("%.6f %.6e %.6e %.6e %.6e %12.6f\n" % tuple(row))
+
+
+def flux_tube_background(p, table: np.ndarray, b_surf: float = 2000.0, r_surf_mm: float = 3.0,
+                         x0_mm: float = 0.0, y0_mm: float = 0.0, b_max_ratio: float = 4.0,
+                         p_floor: float = 0.2):
+    """Axisymmetric self-similar magnetic flux tube on the quiet column, as the
+    3-D cgs arrays the reference reads for a magnetic run (rho, c, p, B_x,
+    B_y, B_z; READ_IN_FIELD, all_modules.f90:486-513), each (nz, ny, nx).
+
+    Field from an azimuthal vector potential in FP64,
+        A_phi(r, z) = (Phi / 2 pi r) (1 - exp(-r^2 / R(z)^2)),  Phi = pi b_surf R0^2,
+    so B = curl(A_phi e_phi) is divergence-free with a Gaussian profile
+    B_z = B_axis(z) exp(-r^2/R^2), B_axis R^2 = b_surf R0^2 (flux
+    conservation, self-similar), B_r = r B_z R'(z) / R.  The axis strength
+    follows p_quiet(z)^(1/4) relative to z = 0 (a tube that narrows with
+    depth), bounded to [b_surf / b_max_ratio, b_surf * b_max_ratio].
+    Balance: horizontal pressure balance of a thin tube, p = p_quiet - B^2 / 8pi,
+    floored at p_floor * p_quiet (the evacuated core), and rho scaled with p
+    at the quiet temperature (c unchanged).  This is a synthetic test
+    background in approximate magnetohydrostatic balance, not the reference's
+    own tube model (whose generator needs modules absent from it).
+    """
+    nx, ny, nz = p.nx, p.ny, p.nz
+    z_cm = (table[:, 0] - 1.0) * RSUN_CM
+    c_q, rho_q, p_q = table[:, 1], table[:, 2], table[:, 3]
+    k0 = int(np.argmin(np.abs(z_cm)))
+    b_axis = b_surf * (p_q / p_q[k0]) ** 0.25
+    b_axis = np.clip(b_axis, b_surf / b_max_ratio, b_surf * b_max_ratio)
+    r0 = r_surf_mm * 1e8
+    R = r0 * np.sqrt(b_surf / b_axis)                       # flux conservation
+    dRdz = np.gradient(R, z_cm)
+    x = (np.arange(nx) / nx - 0.5) * p.xlength - x0_mm * 1e8
+    y = (np.arange(ny) / ny - 0.5) * p.ylength - y0_mm * 1e8
+    X, Y = np.meshgrid(x, y)                               # (ny, nx)
+    r2 = X ** 2 + Y ** 2
+    bz = np.empty((nz, ny, nx)); bx = np.empty_like(bz); by = np.empty_like(bz)
+    for k in range(nz):
+        g = np.exp(-r2 / R[k] ** 2)
+        bz[k] = b_axis[k] * g
+        br_over_r = b_axis[k] * g * dRdz[k] / R[k]            # B_r / r
+        bx[k] = br_over_r * X
+        by[k] = br_over_r * Y
+    b2 = bx ** 2 + by ** 2 + bz ** 2
+    pq = p_q[:, None, None]
+    pres = np.maximum(pq - b2 / (8.0 * np.pi), p_floor * pq)
+    rho = rho_q[:, None, None] * pres / pq
+    c = np.broadcast_to(c_q[:, None, None], (nz, ny, nx)).copy()
+    return rho, c, pres, bx, by, bz

@@ -9,134 +9,11 @@
 #include <string>
 #include <vector>
 #include <algorithm>
-#include "internal.cuh"
-#include "../../include/sparc_gpu.h"
+
+#include "ctx.cuh"
 
 namespace {
 
-inline double R4(double x) { return (double)(float)x; }
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-}  // namespace
-
-struct sparc_ctx {
-    sparc_params P;
-    int H, M, nz, S, nzpml;
-    long long fs, ps, NP, N;
-    int f32;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev_done = nullptr;     // last cross-context hand-off on this stream
-    std::string err;
-    long long launches = 0;
-    long long dev_bytes = 0;
-    std::vector<void*> allocs;
-
-    // host set-up (FP64)
-    bool have_bg = false;
-    double pi, rsun, normx, normy, dimc, dimrho, diml, deltat, stretchx, stretchy, delta_width;
-    double betas[5];
-    int e_rad, o_rad, steps, freq_filtering, maxtime, forcing_length, cadforcing_step, num_steps;
-    std::vector<double> zt_host;     // ZT_COUNT * nz
-    std::vector<double> pt_host;     // PT_COUNT * M
-    Compact<double> cc64;
-    int time = 0;
-
-    // device state (element type T; CT = T2)
-    void* a = nullptr; void* scr = nullptr; void* pml = nullptr; void* scrpml = nullptr;
-    void* ybuf = nullptr; void* pbuf = nullptr; void* rbuf = nullptr;
-    void* zt = nullptr; void* pt = nullptr;       // T tables
-    float* ftab = nullptr;                        // fused FP32 step: z table [FZ_COUNT][fused_nzp(nz)]
-    int use_fused = 0;
-    int fused_pencils = 4;                        // modes per CTA of the fused step (autotuned)
-    int stage_block = 128;                        // threads per CTA of the per-stage kernels (autotuned)
-    double* zt64 = nullptr; double* pt64 = nullptr;
-    double* tw_x = nullptr; double* tw_y = nullptr;
-    void* tmp = nullptr;          // FFT intermediate, nz*M complex T
-    void* phys = nullptr;         // one physical field, N reals T
-    double* phys64 = nullptr;     // N doubles
-    double2* spec64 = nullptr;    // nz*M complex double (primitives)
-    double2* spec64b = nullptr;
-    double2* tmp64 = nullptr;
-    int* d_flag = nullptr;
-
-    // sources
-    int src_mode = 0;
-    int src_L = 0;
-    void* planes = nullptr;       // [S][L][M] CT
-    double* series = nullptr;     // [S][nseries]
-    int nseries = 0;
-    std::vector<int> src_set;
-
-    // surface records
-    int rec_on = 0, rec_max = 0;
-    void* rec = nullptr;          // [S][rec_max][M] CT, record r = output at slot time r*steps
-    // per-slot clocks (continuous batching)
-    int* d_t0 = nullptr;          // [S] device copy
-    int* d_time = nullptr;        // device copy of `time`, read by the step kernels
-    // captured step sequences, replayed as CUDA graphs: one per step count,
-    // valid while no kernel argument changed (epoch)
-    struct GraphEntry { int n; long long epoch; cudaGraphExec_t exec; long long nlaunch; };
-    std::vector<GraphEntry> graphs;
-    long long epoch = 0;
-    int use_graphs = 1;
-    std::vector<int> t0;          // slot time = time - t0[slot]
-    int active_n = 0;             // slots 0..active_n-1 are stepped
-
-    // device-resident checkpoints (a + PML + time of every slot)
-    void* dck = nullptr; int dck_n = 0;
-    std::vector<int> dck_time;
-    // kernels
-    void* store = nullptr; int store_n = 0;     // [nsnap][7][S][N] T (field-major within a snapshot)
-    // per store slot: recorded on the adjoint stream after its reads of the
-    // slot; a later snapshot into the slot waits for it
-    std::vector<cudaEvent_t> slot_ev;
-    std::vector<char> slot_pending;
-    double* kacc = nullptr;                     // [S][3][N]
-    void* ktemp = nullptr;                      // [7][G][N] T, G = kernel_group(S)
-    void* gtmp = nullptr;                       // [G] spectral fields: transform scratch of a source group
-};
-
-namespace {
-
-int fail(sparc_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg;
-    return code;
-}
-
-#define CK(call)                                                                   \
-    do {                                                                           \
-        cudaError_t e_ = (call);                                                   \
-        if (e_ != cudaSuccess)                                                     \
-            return fail(c, SPARC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-#define CKL()                                                                      \
-    do {                                                                           \
-        cudaError_t e_ = cudaGetLastError();                                       \
-        if (e_ != cudaSuccess)                                                     \
-            return fail(c, SPARC_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
-    } while (0)
-
-int dalloc(sparc_ctx* c, void** p, size_t bytes) {
-    if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        cudaGetLastError();
-        return fail(c, SPARC_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
-    }
-    c->allocs.push_back(*p);
-    c->dev_bytes += (long long)bytes;
-    cudaMemsetAsync(*p, 0, bytes, c->stream);
-    return SPARC_OK;
-}
-
-size_t esz(const sparc_ctx* c) { return c->f32 ? sizeof(float) : sizeof(double); }
-size_t csz(const sparc_ctx* c) { return 2 * esz(c); }
 
 // ---------------------------------------------------------------------------
 // compact finite differences on the host (set-up only): DBYD2 / MTRIDAG
@@ -211,12 +88,7 @@ void host_dbyd2(const std::vector<double>& b, std::vector<double>& a, int ibc, c
     a = ud;
 }
 
-int upload(sparc_ctx* c, void* dst, const void* src, size_t bytes) {
-    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
-    return SPARC_OK;
-}
 
-template <typename T> typename CplxOf<T>::type* CP(void* p) { return (typename CplxOf<T>::type*)p; }
 
 }  // namespace
 
@@ -255,7 +127,10 @@ const char* sparc_gpu_last_error(const sparc_ctx* c) { return c ? c->err.c_str()
 
 static int validate(const sparc_params* p, std::string& why) {
     auto pow2 = [](int n) { return n >= 4 && n <= 1024 && (n & (n - 1)) == 0; };
-    if (p->option != 2 && p->option != 4 && p->option != 17) { why = "option must be 2, 4 or 17"; return 0; }
+    if (p->option != 2 && p->option != 4 && p->option != 10 && p->option != 17) {
+        why = "option must be 2, 4, 10 or 17";
+        return 0;
+    }
     if (!pow2(p->nx)) { why = "nx must be a power of two in [4,1024]"; return 0; }
     if (p->option == 17 && p->ny != 1) { why = "option 17 needs ny == 1"; return 0; }
     if (p->option != 17 && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
@@ -311,8 +186,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->zt, (size_t)ZT_COUNT * c->nz * es))) return bail(rc);
     if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
     if (c->f32) {
-        // the fused step covers the displacement forms (options 4, 17)
-        c->use_fused = fused_supported(c->nz) && p->option != 2 && getenv("SPARC_FP32_PER_STAGE") == nullptr;
+        // the fused step covers the quiet displacement forms (options 4, 17)
+        c->use_fused = fused_supported(c->nz) && (p->option == 4 || p->option == 17) &&
+                       getenv("SPARC_FP32_PER_STAGE") == nullptr;
         if (c->use_fused &&
             (rc = dalloc(c, (void**)&c->ftab, (size_t)FZ_COUNT * fused_nzp(c->nz) * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
@@ -332,8 +208,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     launch_set_time(c->d_time, 0, c->stream);
     c->t0.assign(c->S, 0);
     c->active_n = c->S;
-    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr;
+    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && p->option != 10;
     if (c->use_fused) fused_prepare(c->nz, c->nzpml);
+    if (p->option == 10 && (rc = mhd_create(c))) return bail(rc);
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
@@ -359,6 +236,7 @@ void sparc_gpu_destroy(sparc_ctx* c) {
     if (c->ev_done) cudaEventDestroy(c->ev_done);
     for (cudaEvent_t e : c->slot_ev) cudaEventDestroy(e);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    if (c->mhd) mhd_destroy(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -400,6 +278,9 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
         g[k] = gin[k] * c->diml / (c->dimc * c->dimc);
         graw[k] = g[k];
     }
+    c->zq = z;
+    c->cq.resize(nz); c->rhoq.resize(nz);
+    for (int k = 0; k < nz; ++k) { c->cq[k] = cin[k] / c->dimc; c->rhoq[k] = rhoin[k] / c->dimrho; }
     compact_coeffs(nz, c->cc64);
     Tri tri[4] = {tri_for(nz, 0), tri_for(nz, 1), tri_for(nz, 2), tri_for(nz, 3)};
     std::vector<double> unstretch, stretch(nz);
@@ -635,8 +516,24 @@ int sparc_gpu_info(sparc_ctx* c, double* out, double* ztab, double* ptab) {
 // ---------------------------------------------------------------------------
 // physical <-> spectral helpers
 // ---------------------------------------------------------------------------
+// Host planes into the context's representation: normalised half-spectra,
+// or (option 10) the dense physical planes themselves.
+// bytes between consecutive planes of a field: a spectral plane, or (option 10) a dense physical one
+static size_t plane_bytes(const sparc_ctx* c) { return c->mhd ? (size_t)c->NP * esz(c) : (size_t)c->M * csz(c); }
+
 static int to_spec(sparc_ctx* c, const double* host_field, void* spec_dst, int nplanes) {
     long long n = (long long)c->NP * nplanes;
+    if (c->mhd) {
+        if (c->f32) {
+            CK(cudaMemcpyAsync(c->phys64, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
+            launch_copy_convert<float>((float*)spec_dst, c->phys64, n, c->stream);
+            c->launches++;
+            CKL();
+        } else {
+            CK(cudaMemcpyAsync(spec_dst, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
+        }
+        return SPARC_OK;
+    }
     CK(cudaMemcpyAsync(c->phys64, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
     if (c->f32) {
         launch_copy_convert<float>((float*)c->phys, c->phys64, n, c->stream);
@@ -655,6 +552,16 @@ static int to_spec(sparc_ctx* c, const double* host_field, void* spec_dst, int n
 // spectral (device, T) -> physical FP64 on device (c->phys64)
 static int from_spec_dev(sparc_ctx* c, const void* spec_src, int nplanes) {
     long long n = (long long)c->NP * nplanes;
+    if (c->mhd) {
+        if (c->f32) {
+            launch_copy_back<float>(c->phys64, (const float*)spec_src, n, c->stream);
+            c->launches++;
+            CKL();
+        } else {
+            CK(cudaMemcpyAsync(c->phys64, spec_src, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        return SPARC_OK;
+    }
     if (c->f32) {
         fft_spec_to_phys<float>(CP<float>((void*)spec_src), (float*)c->phys, CP<float>(c->tmp), c->P.nx, c->P.ny,
                                 nplanes, c->tw_x, c->tw_y, c->stream);
@@ -689,6 +596,18 @@ int sparc_gpu_set_state(sparc_ctx* c, int src, const double* a, const double* pm
         int rc = to_spec(c, a + (long long)f * c->N, field_ptr(c, c->a, src, f, c->fs), c->nz);
         if (rc) return rc;
     }
+    if (c->mhd) {
+        // six PML auxiliaries of option 10, dense planes
+        const size_t pb = (size_t)6 * c->nzpml * c->NP * esz(c);
+        char* pbase = (char*)mhd_pml(c) + (size_t)src * pb;
+        if (pml && c->nzpml > 0) {
+            int rc = to_spec(c, pml, pbase, 6 * c->nzpml);
+            if (rc) return rc;
+        } else {
+            CK(cudaMemsetAsync(pbase, 0, pb, c->stream));
+        }
+        CK(cudaMemsetAsync((char*)mhd_spml(c) + (size_t)src * pb, 0, pb, c->stream));
+    } else {
     char* pbase = (char*)c->pml + (long long)src * 2 * c->ps * csz(c);
     if (pml && c->nzpml > 0) {
         for (int f = 0; f < 2; ++f) {
@@ -697,6 +616,7 @@ int sparc_gpu_set_state(sparc_ctx* c, int src, const double* a, const double* pm
         }
     } else {
         CK(cudaMemsetAsync(pbase, 0, 2 * c->ps * csz(c), c->stream));
+    }
     }
     CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * csz(c), c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -711,7 +631,11 @@ int sparc_gpu_get_state(sparc_ctx* c, int src, double* a, double* pml) {
         int rc = from_spec(c, field_ptr(c, c->a, src, f, c->fs), a + (long long)f * c->N, c->nz);
         if (rc) return rc;
     }
-    if (pml && c->nzpml > 0) {
+    if (pml && c->nzpml > 0 && c->mhd) {
+        const size_t pb = (size_t)6 * c->nzpml * c->NP * esz(c);
+        int rc = from_spec(c, (char*)mhd_pml(c) + (size_t)src * pb, pml, 6 * c->nzpml);
+        if (rc) return rc;
+    } else if (pml && c->nzpml > 0) {
         char* pbase = (char*)c->pml + (long long)src * 2 * c->ps * csz(c);
         for (int f = 0; f < 2; ++f) {
             int rc = from_spec(c, pbase + f * c->ps * csz(c), pml + (long long)f * c->NP * c->nzpml, c->nzpml);
@@ -728,7 +652,7 @@ int sparc_gpu_get_field(sparc_ctx* c, int src, int field, int k, double* host) {
         return fail(c, SPARC_EINVAL, "bad slot, field, plane or buffer");
     void* base = field < 6 ? c->a : c->scr;
     char* fp = field_ptr(c, base, src, field % 6, c->fs);
-    if (k > 0) return from_spec(c, fp + (long long)(k - 1) * c->M * csz(c), host, 1);
+    if (k > 0) return from_spec(c, fp + (long long)(k - 1) * plane_bytes(c), host, 1);
     return from_spec(c, fp, host, c->nz);
 }
 
@@ -771,12 +695,14 @@ int sparc_gpu_set_source(sparc_ctx* c, int src, int mode, const double* planes, 
         std::copy(series, series + nseries, ser.begin());
         if ((rc = upload(c, c->series + (long long)src * c->nseries, ser.data(), c->nseries * 8))) return rc;
     }
-    char* dst = (char*)c->planes + (long long)src * c->src_L * c->M * cs;
-    CK(cudaMemsetAsync(dst, 0, (size_t)c->src_L * c->M * cs, c->stream));
-    // planes are normalised spectra of the physical planes (ny,nx)
+    const size_t pbytes = plane_bytes(c);
+    char* dst = (char*)c->planes + (long long)src * c->src_L * pbytes;
+    CK(cudaMemsetAsync(dst, 0, (size_t)c->src_L * pbytes, c->stream));
+    // planes are normalised spectra of the physical planes (ny,nx), or the
+    // physical planes themselves (option 10)
     for (int l0 = 0; l0 < L; l0 += c->nz) {
         int nl = std::min(c->nz, L - l0);
-        if ((rc = to_spec(c, planes + (long long)l0 * c->NP, dst + (long long)l0 * c->M * cs, nl))) return rc;
+        if ((rc = to_spec(c, planes + (long long)l0 * c->NP, dst + (long long)l0 * pbytes, nl))) return rc;
     }
     CK(cudaStreamSynchronize(c->stream));
     if (c->src_mode != mode) c->epoch++;      // the step kernels' arguments changed
@@ -892,6 +818,7 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
 template <typename T>
 static int do_steps(sparc_ctx* c, int nsteps) {
     if (nsteps == 0) return SPARC_OK;
+    if (c->mhd) return mhd_steps(c, nsteps);
     if (c->use_graphs) {
         sparc_ctx::GraphEntry* ge = nullptr;
         for (auto& g : c->graphs)
@@ -948,9 +875,19 @@ int sparc_gpu_step(sparc_ctx* c, int nsteps) {
     return c->f32 ? do_steps<float>(c, nsteps) : do_steps<double>(c, nsteps);
 }
 
+int sparc_gpu_set_mhd_background(sparc_ctx* c, const double* rho, const double* cs, const double* p,
+                                 const double* bx, const double* by, const double* bz) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->mhd) return fail(c, SPARC_EINVAL, "the MHD background belongs to option 10");
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background (the quiet column) first");
+    if (!rho || !cs || !p || !bx || !by || !bz) return fail(c, SPARC_EINVAL, "null background array");
+    return mhd_set_background(c, rho, cs, p, bx, by, bz);
+}
+
 int sparc_gpu_autotune(sparc_ctx* c, int steps, int* choice, float* ms_per_step) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (c->mhd) return fail(c, SPARC_EINVAL, "option 10 has no launch variants to tune");
     if (steps < 1) return fail(c, SPARC_EINVAL, "steps < 1");
     const bool fused = c->use_fused && c->f32;
     const int cand[2] = {fused ? 4 : 128, fused ? 2 : 64};
@@ -1073,7 +1010,7 @@ int sparc_gpu_get_records(sparc_ctx* c, int src, double* host, int* nrec) {
     const char* base = (const char*)c->rec + (size_t)src * c->rec_max * c->M * csz(c);
     for (int r0 = 0; r0 < n_rec; r0 += c->nz) {
         int n = std::min(c->nz, n_rec - r0);
-        int rc = from_spec(c, base + (size_t)r0 * c->M * csz(c), host + (size_t)r0 * c->NP, n);
+        int rc = from_spec(c, base + (size_t)r0 * plane_bytes(c), host + (size_t)r0 * c->NP, n);
         if (rc) return rc;
     }
     return SPARC_OK;
@@ -1091,6 +1028,11 @@ int sparc_gpu_slot_reset(sparc_ctx* c, int src) {
     CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * cs, c->stream));
     CK(cudaMemsetAsync((char*)c->pml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
     CK(cudaMemsetAsync((char*)c->scrpml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
+    if (c->mhd) {
+        const size_t pb = (size_t)6 * c->nzpml * c->NP * esz(c);
+        CK(cudaMemsetAsync((char*)mhd_pml(c) + (size_t)src * pb, 0, pb, c->stream));
+        CK(cudaMemsetAsync((char*)mhd_spml(c) + (size_t)src * pb, 0, pb, c->stream));
+    }
     if (c->rec) CK(cudaMemsetAsync((char*)c->rec + (size_t)src * c->rec_max * c->M * cs, 0, (size_t)c->rec_max * c->M * cs, c->stream));
     c->t0[src] = c->time;
     CK(cudaMemcpyAsync(c->d_t0 + src, &c->t0[src], sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -1252,7 +1194,8 @@ extern "C" {
 int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (c->P.option == 2) return fail(c, SPARC_EINVAL, "sensitivity kernels need the displacement form");
+    if (c->P.option == 2 || c->P.option == 10)
+        return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the quiet displacement forms");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
         int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));
@@ -1360,6 +1303,7 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
 // ---------------------------------------------------------------------------
 int sparc_gpu_save_device(sparc_ctx* c, int idx, int capacity) {
     if (!c) return SPARC_EINVAL;
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     if (!c->dck) {
@@ -1379,6 +1323,7 @@ int sparc_gpu_save_device(sparc_ctx* c, int idx, int capacity) {
 
 int sparc_gpu_load_device(sparc_ctx* c, int idx) {
     if (!c) return SPARC_EINVAL;
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
     if (!c->dck || idx < 0 || idx >= c->dck_n || c->dck_time[idx] < 0)
         return fail(c, SPARC_EINVAL, "no such device checkpoint");
     size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
@@ -1408,6 +1353,7 @@ struct CkHeader {
 
 int sparc_gpu_checkpoint(sparc_ctx* c, const char* path) {
     if (!c || !path) return SPARC_EINVAL;
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     std::vector<unsigned char> buf(na + np);
@@ -1433,6 +1379,7 @@ int sparc_gpu_checkpoint(sparc_ctx* c, const char* path) {
 
 int sparc_gpu_restore(sparc_ctx* c, const char* path) {
     if (!c || !path) return SPARC_EINVAL;
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     FILE* f = fopen(path, "rb");
     if (!f) return fail(c, SPARC_EIO, std::string("cannot open ") + path);

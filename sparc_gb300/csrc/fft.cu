@@ -20,37 +20,6 @@ __device__ __forceinline__ long long grp_off(long long p, int ppg, long long gst
     return g * gstride + (p - g * ppg) * pe;
 }
 
-// Stockham radix-2 over `count` sequences of length n stored back to back in
-// src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
-// cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
-template <typename T, typename CT>
-__device__ CT* smem_fft(CT* src, CT* dst, int n, int count, T sign, const double* __restrict__ tw) {
-    const int half = n >> 1;
-    const int total = half * count;
-    for (int Ns = 1; Ns < n; Ns <<= 1) {
-        const int stride = n / (2 * Ns);
-        for (int t = threadIdx.x; t < total; t += blockDim.x) {
-            const int seq = t / half, j = t - seq * half;
-            CT* s = src + seq * n;
-            CT* d = dst + seq * n;
-            const int k = j & (Ns - 1);
-            CT v0 = s[j], v1 = s[j + half];
-            const int q = k * stride;
-            const T c = (T)__ldg(&tw[2 * q]);
-            const T sn = sign * (T)__ldg(&tw[2 * q + 1]);
-            CT w;
-            w.x = v1.x * c - v1.y * sn;
-            w.y = v1.x * sn + v1.y * c;
-            const int idx = ((j - k) << 1) + k;
-            d[idx] = v0 + w;
-            d[idx + Ns] = v0 - w;
-        }
-        __syncthreads();
-        CT* tmp = src; src = dst; dst = tmp;
-    }
-    return src;
-}
-
 // phys (nrows rows of nx reals) -> out (nrows rows of H = nx/2+1 complex), scaled by `scale`
 template <typename T>
 __global__ void rows_r2c_kernel(const T* __restrict__ phys, typename CplxOf<T>::type* __restrict__ out,
@@ -418,7 +387,7 @@ __global__ void spec_scale_z_kernel(typename CplxOf<T>::type* out, const typenam
     out[t] = in[t] * zt[row * nz + z];
 }
 
-// which: 0 -> i kx * in, 1 -> i ky * in, 2 -> damping rate * in
+// which: 0 -> i kx * in, 1 -> i ky * in, 2 -> damping rate * in, 3 -> horizontal filter * in
 template <typename T>
 __global__ void spec_dxdy_kernel(typename CplxOf<T>::type* out, const typename CplxOf<T>::type* in,
                                  const T* __restrict__ pt, int which, int M, long long n, long long out_ss,
@@ -430,7 +399,8 @@ __global__ void spec_dxdy_kernel(typename CplxOf<T>::type* out, const typename C
     int m = (int)(t % M);
     if (which == 0) out[t] = imul(pt[PT_KX * (long long)M + m], in[t]);
     else if (which == 1) out[t] = imul(pt[PT_KY * (long long)M + m], in[t]);
-    else out[t] = pt[PT_DAMP * (long long)M + m] * in[t];
+    else if (which == 2) out[t] = pt[PT_DAMP * (long long)M + m] * in[t];
+    else out[t] = pt[PT_HF * (long long)M + m] * in[t];
 }
 
 // Sensitivity-kernel accumulation, kernels.f90:276-311, for nsrc sources at

@@ -199,6 +199,37 @@ __device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, i
     return n;
 }
 
+// Stockham radix-2 over `count` sequences of length n stored back to back in
+// src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
+// cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
+template <typename T, typename CT>
+__device__ __forceinline__ CT* smem_fft(CT* src, CT* dst, int n, int count, T sign, const double* __restrict__ tw) {
+    const int half = n >> 1;
+    const int total = half * count;
+    for (int Ns = 1; Ns < n; Ns <<= 1) {
+        const int stride = n / (2 * Ns);
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int seq = t / half, j = t - seq * half;
+            CT* s = src + seq * n;
+            CT* d = dst + seq * n;
+            const int k = j & (Ns - 1);
+            CT v0 = s[j], v1 = s[j + half];
+            const int q = k * stride;
+            const T c = (T)__ldg(&tw[2 * q]);
+            const T sn = sign * (T)__ldg(&tw[2 * q + 1]);
+            CT w;
+            w.x = v1.x * c - v1.y * sn;
+            w.y = v1.x * sn + v1.y * c;
+            const int idx = ((j - k) << 1) + k;
+            d[idx] = v0 + w;
+            d[idx + Ns] = v0 - w;
+        }
+        __syncthreads();
+        CT* tmp = src; src = dst; dst = tmp;
+    }
+    return src;
+}
+
 // ---- argument blocks ----------------------------------------------------------
 template <typename T> struct StageArgs {
     typedef typename CplxOf<T>::type CT;

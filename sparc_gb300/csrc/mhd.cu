@@ -1,0 +1,860 @@
+// Linearised MHD in the displacement form, option 10 (MP_MHD_PML_3D_DISPL,
+// displacement.f90:663-849), on a background that varies in x and y (a
+// magnetic flux tube).  The background breaks the per-mode structure of the
+// quiet-Sun path, so here the state lives in physical space: each
+// [source][field] slot of the context holds one dense (nz, ny, nx) real
+// field, and a stage takes its 21 derivatives explicitly:
+//   d/dx  two real rows packed as one complex row, shared-memory FFT, times
+//         i k normx 2 pi stretchx (the reference's eyekx * stretchx, Nyquist
+//         dropped as its c2r does), inverse FFT  (derivatives.f90:28-58);
+//   d/dy  two adjacent x-columns packed as one complex column, the same
+//         along y (derivatives.f90:62-170); the derivative has a real kernel,
+//         so it acts on the packed real and imaginary parts separately;
+//   d/dz  DBYD2 on real pencils with the host-factorised MTRIDAG.
+// Point-wise kernels form the fluxes, div, p', rho', the induced field b,
+// curl b, the Lorentz forces, the sponge and gravity; DAMP_VELOCITY and the
+// horizontal filter go through the normalised 2-D transforms and the same
+// pencil multipliers as the quiet path.  The PML is bottom-only with six
+// auxiliaries (psi_vz, psi_p, psi_dzbx, psi_dzby, psi_induction_bx,
+// psi_induction_by; initialize.f90:487-490,560-566); the top has the sponge
+// over the last 36 planes.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+#include "ctx.cuh"
+
+namespace {
+
+// background fields (T, N values each)
+enum { MB_BOX, MB_BOY, MB_BOZ, MB_CBOX, MB_CBOY, MB_CBOZ, MB_GP0X, MB_GP0Y, MB_GP0Z, MB_GR0X, MB_GR0Y, MB_GR0Z,
+       MB_C2RHO0, MB_RHO0, MB_RHOINV, MB_COUNT };
+// stage scratch per source (T, N values each)
+enum { MW_T0, MW_T1, MW_T2, MW_T3, MW_T4, MW_T5, MW_F1, MW_F2, MW_F3, MW_DX, MW_DY, MW_DZ, MW_P, MW_R, MW_GPX,
+       MW_GPY, MW_GPZ, MW_BX, MW_BY, MW_BZ, MW_DZF1, MW_DZF2, MW_CBX, MW_CBY, MW_CBZ, MW_DZBX, MW_DZBY,
+       MW_COUNT };
+// PML auxiliaries of option 10 (scrpml / pmlvars index, initialize.f90:487-490,560-566)
+enum { PV_VZ, PV_P, PV_DZBX, PV_DZBY, PV_IBX, PV_IBY, PV_COUNT };
+
+}  // namespace
+
+struct MhdState {
+    void* bg = nullptr;        // [MB_COUNT][N] T
+    void* pab = nullptr;       // [2][nb*NP] T: a_z, b_z of the bottom PML planes
+    void* g = nullptr;         // [nz] T: gravity with the PML decay of the (1,1) column
+    void* sponge = nullptr;    // [nz] T: spongez (PERIODIC: spongexyz(:,:,k) = spongez(k))
+    int* plane = nullptr;      // [NP] 0-based source plane of each pixel
+    int* plane_obs = nullptr;  // [NP] 0-based observation plane of each pixel (surface records)
+    void* dw = nullptr;        // [NP] T: delta_width_2d
+    void* rx = nullptr;        // [nx] T: d/dx multipliers of the packed complex FFT
+    void* ry = nullptr;        // [ny] T
+    void* work = nullptr;      // [S][MW_COUNT][N] T
+    void* pml = nullptr;       // [S][6][nzpml*NP] T (pmlvars)
+    void* spml = nullptr;      // [S][6][nzpml*NP] T (scrpml)
+    void* spec = nullptr;      // one spectral field (nz*M complex T): damping / filter transforms
+    bool have_bg = false;
+};
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ typename CplxOf<T>::type imul_c(T k, typename CplxOf<T>::type z) {
+    typename CplxOf<T>::type r;
+    r.x = -k * z.y;
+    r.y = k * z.x;
+    return r;
+}
+
+// d/dx of nrows rows of nx reals (rows r = plane*ny + y, dense), two rows per CTA
+template <typename T>
+__global__ void rowderiv_kernel(const T* __restrict__ in, T* __restrict__ out, int nx, long long nrows,
+                                const T* __restrict__ rx, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* b0 = (CT*)smraw;
+    CT* b1 = b0 + nx;
+    const long long r0 = 2LL * blockIdx.x, r1 = r0 + 1;
+    const bool has1 = r1 < nrows;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        CT v;
+        v.x = in[r0 * nx + i];
+        v.y = has1 ? in[r1 * nx + i] : (T)0;
+        b0[i] = v;
+    }
+    __syncthreads();
+    CT* Z = smem_fft<T, CT>(b0, b1, nx, 1, (T)-1, tw);
+    for (int k = threadIdx.x; k < nx; k += blockDim.x) Z[k] = imul_c<T>(rx[k], Z[k]);
+    __syncthreads();
+    CT* Y = smem_fft<T, CT>(Z, Z == b0 ? b1 : b0, nx, 1, (T)1, tw);
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        out[r0 * nx + i] = Y[i].x;
+        if (has1) out[r1 * nx + i] = Y[i].y;
+    }
+}
+
+// d/dy of nplanes dense (ny, nx) planes: W complex columns (2W real x) per CTA
+template <typename T>
+__global__ void colderiv_kernel(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int W,
+                                const T* __restrict__ ry, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* b0 = (CT*)smraw;
+    CT* b1 = b0 + (long long)W * ny;
+    const int ntile = (nx / 2) / W;
+    const long long plane = blockIdx.x / ntile;
+    const int c0 = (blockIdx.x % ntile) * W;
+    const long long base = plane * (long long)ny * nx;
+    for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
+        const int y = t / W, c = t - y * W;
+        const long long o = base + (long long)y * nx + 2 * (c0 + c);
+        CT v;
+        v.x = in[o];
+        v.y = in[o + 1];
+        b0[c * ny + y] = v;
+    }
+    __syncthreads();
+    CT* Z = smem_fft<T, CT>(b0, b1, ny, W, (T)-1, tw);
+    for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
+        const int k = t % ny;
+        Z[t] = imul_c<T>(ry[k], Z[t]);
+    }
+    __syncthreads();
+    CT* Y = smem_fft<T, CT>(Z, Z == b0 ? b1 : b0, ny, W, (T)1, tw);
+    for (int t = threadIdx.x; t < W * ny; t += blockDim.x) {
+        const int y = t / W, c = t - y * W;
+        const long long o = base + (long long)y * nx + 2 * (c0 + c);
+        const CT v = Y[c * ny + y];
+        out[o] = v.x;
+        out[o + 1] = v.y;
+    }
+}
+
+// d/dz (DBYD2 with stretch, bc 0 or 1) of real pencils: npix pencils per
+// field, nfield fields with stride fstride (grid.y)
+template <typename T>
+__global__ void __launch_bounds__(128) zderiv_phys_kernel(const T* __restrict__ zt, Compact<T> cc,
+                                                          const T* __restrict__ in, T* __restrict__ out,
+                                                          long long npix, int nz, int bc, long long fstride) {
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= npix) return;
+    const T* b = in + blockIdx.y * fstride + m;
+    T* o = out + blockIdx.y * fstride + m;
+    compact_forward<T, T>(nz, bc, [&](int j) { return b[(long long)j * npix]; }, (T)0, (T)0,
+                          zt + (ZT_TH + 3 * bc) * nz, zt + (ZT_TH + 3 * bc + 1) * nz, cc, o, npix);
+    const T* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
+    T ud = o[(long long)(nz - 1) * npix];
+    o[(long long)(nz - 1) * npix] = ud * zt[ZT_STRETCH * nz + nz - 1];
+    for (int j = nz - 2; j >= 0; --j) {
+        ud = o[(long long)j * npix] - gam[j + 1] * ud;
+        o[(long long)j * npix] = ud * zt[ZT_STRETCH * nz + j];
+    }
+}
+
+// ---- set-up kernels (FP64) -------------------------------------------------
+
+// READ_IN_FIELD (all_modules.f90:491-505) and the reduction of the field
+// (physics.f90:116-129); taper[k] is the REAL*4 factor ((k-nz)/10.)**4 of the
+// top eleven planes (1 elsewhere), cq the quiet sound speed
+__global__ void mhd_read_kernel(double* rho0, double* c2, double* p0, double* bx, double* by, double* bz,
+                                const double* cq, const double* taper, long long NP, int nz, double dimrho,
+                                double dimc, double dimb) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NP * nz) return;
+    const int k = (int)(t / NP);
+    const double r = rho0[t] / dimrho;
+    const double cs = c2[t] / dimc;
+    rho0[t] = r;
+    c2[t] = pow(cs, 2.0);
+    p0[t] = p0[t] / (dimrho * pow(dimc, 2.0));
+    double x = bx[t] / dimb, y = by[t] / dimb, z = bz[t] / dimb;
+    double red = (pow(z, 2.0) + pow(x, 2.0) + pow(y, 2.0)) / (r * pow(cq[k], 2.0));
+    red = 8.0 / (8.0 + red);
+    red = red * taper[k];
+    const double s = pow(red, 0.5);
+    bx[t] = x * s; by[t] = y * s; bz[t] = z * s;
+}
+
+// a = s1 * b + s2 * c (element-wise)
+__global__ void axpby_kernel(double* a, const double* b, double s1, const double* c, double s2, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) a[t] = s1 * b[t] + (c ? s2 * c[t] : 0.0);
+}
+
+// PML decay of gradp0_z / gradrho0_z and the bottom a_z, b_z (physics.f90:255-297)
+__global__ void mhd_pml_kernel(double* gp0z, double* gr0z, double* az, double* bzp, const double* c2,
+                               const double* rho0, const double* bx, const double* by, const double* bz,
+                               const double* z, const double* alph, long long NP, int nz, int nb, int nt) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NP * nz) return;
+    const int k = (int)(t / NP);        // 0-based plane
+    const long long q = t - (long long)k * NP;
+    const bool bot = k < nb, top = k >= nz - nt;
+    if (!bot && !top) return;
+    auto tempin = [&](int kk) {
+        const long long i = q + NP * kk;
+        return pow(c2[i] + (pow(bx[i], 2.0) + pow(by[i], 2.0) + pow(bz[i], 2.0)) / rho0[i], 0.5);
+    };
+    double dampz, fdec;
+    if (bot) {
+        const double r = (z[nb - 1] - z[k]) / (z[nb - 1] - z[0]);
+        dampz = 2.0 * 3.0 * 3.0 * tempin(0) / (z[nb - 1] - z[0]) * (r * r);
+        fdec = alph[k] / (dampz + alph[k]);
+        gp0z[t] *= fdec; gr0z[t] *= fdec;
+        az[t] = -dampz;
+        bzp[t] = -alph[k] - dampz;
+    }
+    if (top) {
+        const double r = (z[nz - nt] - z[k]) / (z[nz - 1] - z[nz - nt]);
+        dampz = 3.0 * 3.0 * tempin(nz - 1) / (z[nz - 1] - z[nz - nt]) * (r * r);
+        fdec = alph[k] / (dampz + alph[k]);
+        gp0z[t] *= fdec; gr0z[t] *= fdec;
+    }
+}
+
+__global__ void rhoinv_kernel(double* rhoinv, double* c2rho0, const double* rho0, const double* c2, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    rhoinv[t] = 1.0 / rho0[t];
+    c2rho0[t] = c2[t] * rho0[t];
+}
+
+template <typename T>
+__global__ void to_t_kernel(T* dst, const double* src, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (T)src[t];
+}
+
+// ---- stage kernels (T) -------------------------------------------------------
+
+struct MhdArgs {
+    long long N, NP, FS;   // points per field, per plane; field stride of the state slots
+    int nz, nb, nzpml;
+    int S;
+};
+
+// temp = a + beta*scr (step.f90:52-71) into T0..T5, and the fluxes of xi x B0
+// (displacement.f90:672-674)
+template <typename T>
+__global__ void mhd_temp_kernel(const MhdArgs A, const T* __restrict__ a, const T* __restrict__ scr, T beta, int hs,
+                                const T* __restrict__ bg, T* __restrict__ work) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const T* as = a + (long long)s * 6 * A.FS;
+    const T* ss = scr + (long long)s * 6 * A.FS;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    T v[6];
+    #pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        v[f] = as[f * A.FS + t];
+        if (hs) v[f] = v[f] + beta * ss[f * A.FS + t];
+        w[(MW_T0 + f) * A.N + t] = v[f];
+    }
+    const T box = bg[MB_BOX * A.N + t], boy = bg[MB_BOY * A.N + t], boz = bg[MB_BOZ * A.N + t];
+    w[MW_F1 * A.N + t] = -(v[2] * boy - v[1] * boz);
+    w[MW_F2 * A.N + t] = -(v[0] * boz - v[2] * box);
+    w[MW_F3 * A.N + t] = -(v[1] * box - v[0] * boy);
+}
+
+// bottom-PML accounting (pml.f90:213-231 form; k <= npmlbot only in option 10):
+// rhs = a_z deriv + b_z psi, deriv += psi, with psi = pmlvars + beta*scrpml
+template <typename T>
+__device__ __forceinline__ T pml_bottom(const MhdArgs& A, long long t, int s, int aux, T deriv, const T* __restrict__ pab,
+                                        const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
+    const long long nbp = (long long)A.nb * A.NP;
+    if (t >= nbp) return deriv;
+    const long long o = ((long long)s * PV_COUNT + aux) * (A.nzpml * A.NP) + t;
+    T psi = pml[o];
+    if (hs) psi = psi + beta * spml[o];
+    spml[o] = pab[t] * deriv + pab[nbp + t] * psi;
+    return deriv + psi;
+}
+
+// div, p', rho' (displacement.f90:694-697) after the psi_vz accounting
+template <typename T>
+__global__ void mhd_div_kernel(const MhdArgs A, const T* __restrict__ bg, T* __restrict__ work, const T* __restrict__ pab,
+                               const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    const T dz = pml_bottom<T>(A, t, s, PV_VZ, w[MW_DZ * A.N + t], pab, pml, spml, beta, hs);
+    const T div = w[MW_DX * A.N + t] + w[MW_DY * A.N + t] + dz;
+    const T xx = w[MW_T0 * A.N + t], xy = w[MW_T1 * A.N + t], xz = w[MW_T2 * A.N + t];
+    w[MW_P * A.N + t] = -bg[MB_C2RHO0 * A.N + t] * div - xz * bg[MB_GP0Z * A.N + t] - xx * bg[MB_GP0X * A.N + t] -
+                        xy * bg[MB_GP0Y * A.N + t];
+    w[MW_R * A.N + t] = -bg[MB_RHO0 * A.N + t] * div - xz * bg[MB_GR0Z * A.N + t] - xx * bg[MB_GR0X * A.N + t] -
+                        xy * bg[MB_GR0Y * A.N + t];
+}
+
+// psi_p on gradp_z (displacement.f90:704-716), bottom planes only
+template <typename T>
+__global__ void mhd_pmlp_kernel(const MhdArgs A, T* __restrict__ work, const T* __restrict__ pab,
+                                const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)A.nb * A.NP) return;
+    const int s = blockIdx.y;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    w[MW_GPZ * A.N + t] = pml_bottom<T>(A, t, s, PV_P, w[MW_GPZ * A.N + t], pab, pml, spml, beta, hs);
+}
+
+// induced field b (displacement.f90:729-757): psi_induction_bx/by, then
+// bx = bx - dzflux2, by = -by + dzflux1, bz = bz - flux3
+template <typename T>
+__global__ void mhd_b_kernel(const MhdArgs A, T* __restrict__ work, const T* __restrict__ pab, const T* __restrict__ pml,
+                             T* __restrict__ spml, T beta, int hs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    const T dzf2 = pml_bottom<T>(A, t, s, PV_IBX, w[MW_DZF2 * A.N + t], pab, pml, spml, beta, hs);
+    const T dzf1 = pml_bottom<T>(A, t, s, PV_IBY, w[MW_DZF1 * A.N + t], pab, pml, spml, beta, hs);
+    w[MW_BX * A.N + t] = w[MW_BX * A.N + t] - dzf2;
+    w[MW_BY * A.N + t] = -w[MW_BY * A.N + t] + dzf1;
+    w[MW_BZ * A.N + t] = w[MW_BZ * A.N + t] - w[MW_F3 * A.N + t];
+}
+
+// curl b, the Lorentz forces, sponge, gravity and RHS xi = v
+// (displacement.f90:765-813) into scr
+template <typename T>
+__global__ void mhd_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __restrict__ work, const T* __restrict__ pab,
+                               const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs, const T* __restrict__ gz,
+                               const T* __restrict__ sponge, T* __restrict__ scr) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const int k = (int)(t / A.NP);
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    const T dzbx = pml_bottom<T>(A, t, s, PV_DZBX, w[MW_DZBX * A.N + t], pab, pml, spml, beta, hs);
+    const T dzby = pml_bottom<T>(A, t, s, PV_DZBY, w[MW_DZBY * A.N + t], pab, pml, spml, beta, hs);
+    const T cbx = w[MW_CBX * A.N + t] - dzby;
+    const T cby = -w[MW_CBY * A.N + t] + dzbx;
+    const T cbz = w[MW_CBZ * A.N + t] - w[MW_F1 * A.N + t];
+    const T box = bg[MB_BOX * A.N + t], boy = bg[MB_BOY * A.N + t], boz = bg[MB_BOZ * A.N + t];
+    const T ri = bg[MB_RHOINV * A.N + t];
+    // CROSS (derivatives.f90:471-480): c = a x b
+    T f1 = cby * boz - cbz * boy;
+    T f2 = box * cbz - cbx * boz;
+    T f3 = cbx * boy - cby * box;
+    T rvx = ri * (-w[MW_GPX * A.N + t] + f1);
+    T rvy = ri * (-w[MW_GPY * A.N + t] + f2);
+    T rvz = ri * (-w[MW_GPZ * A.N + t] + f3);
+    const T cbox = bg[MB_CBOX * A.N + t], cboy = bg[MB_CBOY * A.N + t], cboz = bg[MB_CBOZ * A.N + t];
+    const T bx = w[MW_BX * A.N + t], by = w[MW_BY * A.N + t], bz = w[MW_BZ * A.N + t];
+    f1 = cboy * bz - cboz * by;
+    f2 = bx * cboz - cbox * bz;
+    f3 = cbox * by - cboy * bx;
+    rvx = rvx + ri * f1;
+    rvy = rvy + ri * f2;
+    rvz = rvz + ri * f3;
+    const T vx = w[MW_T3 * A.N + t], vy = w[MW_T4 * A.N + t], vz = w[MW_T5 * A.N + t];
+    if (k >= A.nz - 36) {
+        const T sp = sponge[k];
+        rvx = rvx - sp * vx;
+        rvy = rvy - sp * vy;
+        rvz = rvz - sp * vz;
+    }
+    rvz = rvz - ri * w[MW_R * A.N + t] * gz[k];
+    T* ss = scr + (long long)s * 6 * A.FS;
+    ss[0 * A.FS + t] = vx;
+    ss[1 * A.FS + t] = vy;
+    ss[2 * A.FS + t] = vz;
+    ss[3 * A.FS + t] = rvx;
+    ss[4 * A.FS + t] = rvy;
+    ss[5 * A.FS + t] = rvz;
+}
+
+// DAMP_VELOCITY result (in DX, DY, DZ), the kernel-mode source on the source
+// plane of each pixel while the slot's clock is within the forcing gate
+// (displacement.f90:815-843), and the zero top and bottom rows (:845-848)
+template <typename T>
+__global__ void mhd_final_kernel(const MhdArgs A, const T* __restrict__ bg, const T* __restrict__ work, int damp,
+                                 T* __restrict__ scr, SlotClock clk, int src_mode, const T* __restrict__ planes,
+                                 long long plane_ss, int L, const double* __restrict__ series, int nseries,
+                                 const int* __restrict__ plane, const T* __restrict__ dw) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const int k = (int)(t / A.NP);
+    const long long q = t - (long long)k * A.NP;
+    const T* w = work + (long long)s * MW_COUNT * A.N;
+    T* ss = scr + (long long)s * 6 * A.FS;
+    if (damp) {
+        ss[3 * A.FS + t] = ss[3 * A.FS + t] - w[MW_DX * A.N + t];
+        ss[4 * A.FS + t] = ss[4 * A.FS + t] - w[MW_DY * A.N + t];
+        ss[5 * A.FS + t] = ss[5 * A.FS + t] - w[MW_DZ * A.N + t];
+    }
+    if (src_mode != 0 && k == plane[q]) {
+        const int tl = *clk.time - clk.t0[s];
+        if (tl >= 0 && tl <= clk.gate) {
+            const T* pl = planes + (long long)s * plane_ss + q;
+            T F = (T)0;
+            if (src_mode == 1) {
+                const T wt = (tl < nseries) ? (T)series[(long long)s * nseries + tl] : (T)0;
+                F = wt * pl[0];
+            } else {
+                for (int l = 0; l < 7; ++l) {
+                    int id;
+                    const double wl = lagrange_weight(clk, tl, L, l, &id);
+                    if (id >= 0) F = F + (T)wl * pl[(long long)id * A.NP];
+                }
+            }
+            ss[5 * A.FS + t] = ss[5 * A.FS + t] + F / bg[MB_RHO0 * A.N + t] * dw[q];
+        }
+    }
+    if (k == 0 || k == A.nz - 1) {
+        #pragma unroll
+        for (int f = 0; f < 6; ++f) ss[f * A.FS + t] = (T)0;
+    }
+}
+
+// a += dt*scr and FILTER_VARS_3D's z filter (physics.f90:755-783) on every
+// (source, field, pixel) column
+template <typename T>
+__global__ void __launch_bounds__(128) mhd_update_kernel(const MhdArgs A, T* __restrict__ a, const T* __restrict__ scr,
+                                                         T dt) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.NP) return;
+    const int s = blockIdx.y / 6, f = blockIdx.y % 6;
+    T* af = a + ((long long)s * 6 + f) * A.FS + q;
+    const T* sf = scr + ((long long)s * 6 + f) * A.FS + q;
+    zfilter_stream<T, T>(
+        A.nz, 0, [&](int j) { const long long o = (long long)j * A.NP; return af[o] + dt * sf[o]; },
+        [&](int j, T v) { af[(long long)j * A.NP] = v; });
+}
+
+template <typename T>
+__global__ void mhd_pml_update_kernel(T* pml, const T* spml, T dt, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) pml[t] = pml[t] + dt * spml[t];
+}
+
+// v_z of each slot on its source / observation plane into the record buffer
+// (dense planes) when the slot's clock is on the output cadence
+template <typename T>
+__global__ void mhd_record_kernel(const T* __restrict__ a, T* __restrict__ rec, const int* __restrict__ t0,
+                                  const int* __restrict__ time, int steps, int rec_max, long long FS, long long NP,
+                                  long long rec_ss, const int* __restrict__ plane) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (q >= NP) return;
+    const int tl = *time - t0[s];
+    if (tl < 0 || tl % steps != 0) return;
+    const int r = tl / steps;
+    if (r >= rec_max) return;
+    rec[(long long)s * rec_ss + (long long)r * NP + q] = a[((long long)s * 6 + 5) * FS + (long long)plane[q] * NP + q];
+}
+
+unsigned nb256(long long n) { return (unsigned)((n + 255) / 256); }
+
+template <typename T>
+int ddx_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
+    const int nx = c->P.nx;
+    const long long nrows = nplanes * c->P.ny;
+    const size_t sm = 2 * (size_t)nx * sizeof(typename CplxOf<T>::type);
+    const int thr = nx / 2 < 32 ? 32 : (nx / 2 > 256 ? 256 : nx / 2);
+    rowderiv_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, c->stream>>>(in, out, nx, nrows, (const T*)c->mhd->rx,
+                                                                           c->tw_x);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+template <typename T>
+int ddy_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
+    const int nx = c->P.nx, ny = c->P.ny;
+    const int W = std::max(1, std::min(nx / 2, 1024 / ny));
+    const size_t sm = 2 * (size_t)W * ny * sizeof(typename CplxOf<T>::type);
+    colderiv_kernel<T><<<(unsigned)(nplanes * ((nx / 2) / W)), 256, sm, c->stream>>>(in, out, nx, ny, W,
+                                                                                   (const T*)c->mhd->ry, c->tw_y);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+template <typename T>
+Compact<T> cc_of(const sparc_ctx* c) {
+    Compact<T> cc;
+    cc.C1 = (T)c->cc64.C1; cc.C2 = (T)c->cc64.C2;
+    for (int i = 0; i < 5; ++i) cc.Cb[i] = (T)c->cc64.Cb[i];
+    for (int i = 0; i < 4; ++i) cc.Cf[i] = (T)c->cc64.Cf[i];
+    cc.alpha2 = (T)c->cc64.alpha2; cc.beta1 = (T)c->cc64.beta1; cc.cnst = (T)c->cc64.cnst;
+    return cc;
+}
+
+// d/dz of nfield fields (stride fstride) with the context's T tables
+template <typename T>
+int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfield, long long fstride) {
+    dim3 grid((unsigned)((c->NP + 127) / 128), nfield);
+    zderiv_phys_kernel<T><<<grid, 128, 0, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc, fstride);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+}  // namespace
+
+int mhd_create(sparc_ctx* c) {
+    c->mhd = new MhdState();
+    MhdState& m = *c->mhd;
+    const size_t es = esz(c);
+    int rc;
+    if ((rc = dalloc(c, &m.bg, (size_t)MB_COUNT * c->N * es))) return rc;
+    if ((rc = dalloc(c, &m.pab, (size_t)2 * std::max(c->P.npmlbot, 1) * c->NP * es))) return rc;
+    if ((rc = dalloc(c, &m.g, (size_t)c->nz * es))) return rc;
+    if ((rc = dalloc(c, &m.sponge, (size_t)c->nz * es))) return rc;
+    if ((rc = dalloc(c, (void**)&m.plane, (size_t)c->NP * sizeof(int)))) return rc;
+    if ((rc = dalloc(c, (void**)&m.plane_obs, (size_t)c->NP * sizeof(int)))) return rc;
+    if ((rc = dalloc(c, &m.dw, (size_t)c->NP * es))) return rc;
+    if ((rc = dalloc(c, &m.rx, (size_t)c->P.nx * es))) return rc;
+    if ((rc = dalloc(c, &m.ry, (size_t)std::max(c->P.ny, 2) * es))) return rc;
+    if ((rc = dalloc(c, &m.work, (size_t)c->S * MW_COUNT * c->N * es))) return rc;
+    const size_t pv = (size_t)c->S * PV_COUNT * std::max(c->nzpml, 1) * c->NP * es;
+    if ((rc = dalloc(c, &m.pml, pv))) return rc;
+    if ((rc = dalloc(c, &m.spml, pv))) return rc;
+    if ((rc = dalloc(c, &m.spec, (size_t)c->fs * csz(c)))) return rc;
+    return SPARC_OK;
+}
+
+void mhd_destroy(sparc_ctx* c) {
+    delete c->mhd;
+    c->mhd = nullptr;
+}
+
+void* mhd_pml(sparc_ctx* c) { return c->mhd ? c->mhd->pml : nullptr; }
+void* mhd_spml(sparc_ctx* c) { return c->mhd ? c->mhd->spml : nullptr; }
+const int* mhd_planes(sparc_ctx* c) { return c->mhd ? c->mhd->plane : nullptr; }
+
+// The magnetic parts of mp_Initialize_RHS (physics.f90:62-161, 204-208,
+// 255-303, 356-363) in the reference's order; inputs are the 3-D cgs arrays
+// READ_IN_FIELD reads, (nz, ny, nx) C order.
+int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const double* p, const double* bx,
+                       const double* by, const double* bz) {
+    MhdState& m = *c->mhd;
+    const int nz = c->nz, nb = c->P.npmlbot, nt = c->P.npmltop;
+    const long long N = c->N, NP = c->NP;
+    const std::vector<double>& z = c->zq;
+    // FP64 work: 6 inputs, curl (3), horizontal gradients (4), z gradients (2), rhoinv, c2rho0, scratch
+    enum { W_RHO, W_C2, W_P, W_BX, W_BY, W_BZ, W_CBX, W_CBY, W_CBZ, W_GP0X, W_GP0Y, W_GR0X, W_GR0Y, W_GP0Z, W_GR0Z,
+           W_RI, W_C2R, W_TMP, W_AZ, W_BZP, W_N };
+    double* w64 = nullptr;
+    int rc = dalloc(c, (void**)&w64, (size_t)W_N * N * 8);
+    if (rc) return rc;
+    auto W = [&](int i) { return w64 + (size_t)i * N; };
+    const double* in[6] = {rho, cs, p, bx, by, bz};
+    for (int i = 0; i < 6; ++i)
+        if ((rc = upload(c, W(i), in[i], (size_t)N * 8))) return rc;
+    // erad_2d / orad_2d (physics.f90:62-87): searched before READ_IN_FIELD,
+    // on the density of solar_data (the quiet column) -- the same plane for
+    // every pixel; loop bounds clamped to the box
+    auto search = [&](int kc) {
+        double temp = 1.0;
+        int best = kc;
+        for (int k = std::max(1, kc - 50); k <= std::min(nz, kc + 10); ++k)
+            if (std::fabs(c->rhoq[kc - 1] - c->rhoq[k - 1]) <= temp) {
+                temp = std::fabs(c->rhoq[kc - 1] - c->rhoq[k - 1]);
+                best = k;
+            }
+        return best;
+    };
+    const int erad = search(c->e_rad), orad = search(c->o_rad);
+    const int k2 = c->P.compute_adjoint ? orad : erad;
+    const int ks = c->P.src_k > 0 ? c->P.src_k : k2;
+    std::vector<int> plane(NP, ks - 1), plane_obs(NP, orad - 1);
+    const double dw2 = 2.0 / (z[k2] - z[k2 - 2]);
+    // spongez (physics.f90:104-108)
+    std::vector<double> spz(nz), taper(nz, 1.0), alph(nz), gk(nz);
+    for (int k = 0; k < nz; ++k)
+        spz[k] = 200.0 / (1.0 + std::exp((R4(1.002) - z[k]) / R4(0.0001))) +
+                 300.0 / (1.0 + std::exp((z[k] - (z[0] + R4(0.005))) / R4(0.0005)));
+    // ((k-nz)/10.0)**4. in REAL*4 for k = nz-10..nz (physics.f90:123-125)
+    for (int k1 = std::max(1, nz - 10); k1 <= nz; ++k1) {
+        const float tt = (float)(k1 - nz) / 10.0f;
+        taper[k1 - 1] = (double)std::pow(tt, 4.0f);
+    }
+    // alphaz of the PML planes (physics.f90:269-285)
+    for (int k = 1; k <= nz; ++k) {
+        double a0 = c->pi * R4(0.005) * c->diml / c->dimc;
+        if (k < nb + 1) a0 = c->pi * R4(0.005) * c->diml / c->dimc * (z[k - 1] - z[0]) / (z[nb - 1] - z[0]);
+        if (k > nz - nt) a0 = c->pi * R4(0.005) * c->diml / c->dimc * (z[nz - 1] - z[k - 1]) / (z[nz - 1] - z[nz - nt]);
+        alph[k - 1] = a0;
+    }
+    // gravity with the decay of the (1,1) column (physics.f90:287,299), on the host
+    {
+        const double dimb = std::sqrt(4.0 * c->pi * c->dimc * c->dimc * c->dimrho);
+        auto tempin00 = [&](int k) {
+            const long long i = (long long)k * NP;
+            const double r = rho[i] / c->dimrho, css = cs[i] / c->dimc;
+            const double x = bx[i] / dimb, y = by[i] / dimb, zz = bz[i] / dimb;
+            double red = (std::pow(zz, 2.0) + std::pow(x, 2.0) + std::pow(y, 2.0)) / (r * std::pow(c->cq[k], 2.0));
+            red = 8.0 / (8.0 + red) * taper[k];
+            const double sc = std::pow(red, 0.5);
+            return std::pow(std::pow(css, 2.0) + (std::pow(x * sc, 2.0) + std::pow(y * sc, 2.0) +
+                                                   std::pow(zz * sc, 2.0)) / r, 0.5);
+        };
+        for (int k = 1; k <= nz; ++k) {
+            double fdec = 1.0;
+            if (k < nb + 1) {
+                const double r = (z[nb - 1] - z[k - 1]) / (z[nb - 1] - z[0]);
+                const double dampz = 2.0 * 3.0 * 3.0 * tempin00(0) / (z[nb - 1] - z[0]) * (r * r);
+                fdec = alph[k - 1] / (dampz + alph[k - 1]);
+            }
+            if (k > nz - nt) {
+                const double r = (z[nz - nt] - z[k - 1]) / (z[nz - 1] - z[nz - nt]);
+                const double dampz = 3.0 * 3.0 * tempin00(nz - 1) / (z[nz - 1] - z[nz - nt]) * (r * r);
+                fdec = alph[k - 1] / (dampz + alph[k - 1]);
+            }
+            gk[k - 1] = c->zt_host[(size_t)ZT_GRAW * nz + k - 1] * fdec;
+        }
+    }
+    double *d_cq = nullptr, *d_taper = nullptr, *d_z = nullptr, *d_alph = nullptr;
+    if ((rc = dalloc(c, (void**)&d_cq, nz * 8)) || (rc = dalloc(c, (void**)&d_taper, nz * 8)) ||
+        (rc = dalloc(c, (void**)&d_z, nz * 8)) || (rc = dalloc(c, (void**)&d_alph, nz * 8)))
+        return rc;
+    if ((rc = upload(c, d_cq, c->cq.data(), nz * 8)) || (rc = upload(c, d_taper, taper.data(), nz * 8)) ||
+        (rc = upload(c, d_z, z.data(), nz * 8)) || (rc = upload(c, d_alph, alph.data(), nz * 8)))
+        return rc;
+    const double dimb = std::sqrt(4.0 * c->pi * c->dimc * c->dimc * c->dimrho);
+    mhd_read_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_RHO), W(W_C2), W(W_P), W(W_BX), W(W_BY), W(W_BZ), d_cq,
+                                                     d_taper, NP, nz, c->dimrho, c->dimc, dimb);
+    CKL();
+    // FP64 derivative multipliers for the set-up, then the curl of B0 as the
+    // reference forms it (physics.f90:131-159: the d/dz parts are discarded)
+    // and the horizontal background gradients (physics.f90:356-363)
+    {
+        std::vector<double> rx(c->P.nx), ry(std::max(c->P.ny, 2), 0.0);
+        for (int k = 0; k < c->P.nx; ++k) {
+            const int kk = k < c->P.nx / 2 ? k : (k == c->P.nx / 2 ? 0 : k - c->P.nx);
+            rx[k] = (double)kk * c->normx * 2.0 * c->pi * c->stretchx;
+        }
+        for (int k = 0; k < c->P.ny; ++k) {
+            const int kk = k < c->P.ny / 2 ? k : (k == c->P.ny / 2 ? 0 : k - c->P.ny);
+            ry[k] = (double)kk * c->normy * 2.0 * c->pi * c->stretchy;
+        }
+        double *rx64 = nullptr, *ry64 = nullptr;
+        if ((rc = dalloc(c, (void**)&rx64, rx.size() * 8)) || (rc = dalloc(c, (void**)&ry64, ry.size() * 8))) return rc;
+        if ((rc = upload(c, rx64, rx.data(), rx.size() * 8)) || (rc = upload(c, ry64, ry.data(), ry.size() * 8))) return rc;
+        void* rx0 = m.rx; void* ry0 = m.ry;
+        m.rx = rx64; m.ry = ry64;                 // FP64 multipliers while setting up
+        if ((rc = ddx_launch<double>(c, W(W_BY), W(W_CBZ), nz)) || (rc = ddy_launch<double>(c, W(W_BX), W(W_TMP), nz)))
+            return rc;
+        axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_CBZ), W(W_CBZ), 1.0, W(W_TMP), -1.0, N);
+        if ((rc = ddy_launch<double>(c, W(W_BZ), W(W_CBX), nz)) || (rc = ddx_launch<double>(c, W(W_BZ), W(W_TMP), nz)))
+            return rc;
+        axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_CBY), W(W_TMP), -1.0, nullptr, 0.0, N);
+        if ((rc = ddx_launch<double>(c, W(W_RHO), W(W_GR0X), nz)) || (rc = ddy_launch<double>(c, W(W_RHO), W(W_GR0Y), nz)) ||
+            (rc = ddx_launch<double>(c, W(W_P), W(W_GP0X), nz)) || (rc = ddy_launch<double>(c, W(W_P), W(W_GP0Y), nz)))
+            return rc;
+        // d/dz of the background in FP64 (physics.f90:207-208)
+        if ((rc = ddz_launch<double>(c, c->zt64, W(W_RHO), W(W_GR0Z), 1, 1, 0)) ||
+            (rc = ddz_launch<double>(c, c->zt64, W(W_P), W(W_GP0Z), 1, 1, 0)))
+            return rc;
+        CKL();
+        // multipliers of the element type for the steps
+        std::vector<double> rxs = rx, rys = ry;
+        m.rx = rx0; m.ry = ry0;
+        if (c->f32) {
+            std::vector<float> fx(rx.begin(), rx.end()), fy(ry.begin(), ry.end());
+            if ((rc = upload(c, m.rx, fx.data(), fx.size() * 4)) || (rc = upload(c, m.ry, fy.data(), fy.size() * 4)))
+                return rc;
+        } else {
+            if ((rc = upload(c, m.rx, rx.data(), rx.size() * 8)) || (rc = upload(c, m.ry, ry.data(), ry.size() * 8)))
+                return rc;
+        }
+    }
+    rhoinv_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_RI), W(W_C2R), W(W_RHO), W(W_C2), N);
+    CKL();
+    mhd_pml_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_GP0Z), W(W_GR0Z), W(W_AZ), W(W_BZP), W(W_C2), W(W_RHO),
+                                                    W(W_BX), W(W_BY), W(W_BZ), d_z, d_alph, NP, nz, nb, nt);
+    CKL();
+    // to the element type: background fields, bottom PML coefficients, tables
+    const int src_of[MB_COUNT] = {W_BX, W_BY, W_BZ, W_CBX, W_CBY, W_CBZ, W_GP0X, W_GP0Y, W_GP0Z, W_GR0X,
+                                  W_GR0Y, W_GR0Z, W_C2R, W_RHO, W_RI};
+    const long long nbp = (long long)std::max(nb, 1) * NP;
+    for (int i = 0; i < MB_COUNT; ++i) {
+        if (c->f32) to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.bg + (size_t)i * N, W(src_of[i]), N);
+        else to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.bg + (size_t)i * N, W(src_of[i]), N);
+    }
+    if (c->f32) {
+        to_t_kernel<float><<<nb256(nbp), 256, 0, c->stream>>>((float*)m.pab, W(W_AZ), nbp);
+        to_t_kernel<float><<<nb256(nbp), 256, 0, c->stream>>>((float*)m.pab + nbp, W(W_BZP), nbp);
+    } else {
+        to_t_kernel<double><<<nb256(nbp), 256, 0, c->stream>>>((double*)m.pab, W(W_AZ), nbp);
+        to_t_kernel<double><<<nb256(nbp), 256, 0, c->stream>>>((double*)m.pab + nbp, W(W_BZP), nbp);
+    }
+    CKL();
+    std::vector<double> dwv(NP, dw2);
+    if (c->f32) {
+        std::vector<float> g32(gk.begin(), gk.end()), s32(spz.begin(), spz.end()), d32(dwv.begin(), dwv.end());
+        if ((rc = upload(c, m.g, g32.data(), nz * 4)) || (rc = upload(c, m.sponge, s32.data(), nz * 4)) ||
+            (rc = upload(c, m.dw, d32.data(), NP * 4)))
+            return rc;
+    } else {
+        if ((rc = upload(c, m.g, gk.data(), nz * 8)) || (rc = upload(c, m.sponge, spz.data(), nz * 8)) ||
+            (rc = upload(c, m.dw, dwv.data(), NP * 8)))
+            return rc;
+    }
+    if ((rc = upload(c, m.plane, plane.data(), NP * sizeof(int)))) return rc;
+    if ((rc = upload(c, m.plane_obs, plane_obs.data(), NP * sizeof(int)))) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    // release the FP64 set-up buffers
+    for (void* pp : {(void*)w64, (void*)d_cq, (void*)d_taper, (void*)d_z, (void*)d_alph}) {
+        auto it = std::find(c->allocs.begin(), c->allocs.end(), pp);
+        if (it != c->allocs.end()) c->allocs.erase(it);
+        cudaFree(pp);
+    }
+    c->dev_bytes -= (long long)W_N * N * 8 + 4LL * nz * 8;
+    m.have_bg = true;
+    return SPARC_OK;
+}
+
+namespace {
+
+template <typename T>
+int mhd_stage(sparc_ctx* c, T beta, int hs) {
+    MhdState& m = *c->mhd;
+    const int S = c->active_n, nz = c->nz;
+    MhdArgs A;
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nzpml = std::max(c->nzpml, 1);
+    A.S = S;
+    T* a = (T*)c->a;
+    T* scr = (T*)c->scr;
+    T* bg = (T*)m.bg;
+    T* work = (T*)m.work;
+    const T* pab = (const T*)m.pab;
+    T* pml = (T*)m.pml;
+    T* spml = (T*)m.spml;
+    const T* zt = (const T*)c->zt;
+    const long long N = c->N;
+    const dim3 g(nb256(N), S);
+    auto Wp = [&](int s, int f) { return work + ((size_t)s * MW_COUNT + f) * N; };
+    int rc;
+    mhd_temp_kernel<T><<<g, 256, 0, c->stream>>>(A, a, scr, beta, hs, bg, work);
+    c->launches++;
+    CKL();
+    // div: ddxyz(xi_x, xi_y, xi_z, bc 1)
+    for (int s = 0; s < S; ++s) {
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_T0), Wp(s, MW_DX), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_T1), Wp(s, MW_DY), nz)))
+            return rc;
+    }
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_T2), Wp(0, MW_DZ), 1, S, (long long)MW_COUNT * N))) return rc;
+    mhd_div_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // grad p: ddxyz(p, bc 0) and psi_p
+    for (int s = 0; s < S; ++s) {
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPX), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPY), nz)))
+            return rc;
+    }
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 0, S, (long long)MW_COUNT * N))) return rc;
+    mhd_pmlp_kernel<T><<<dim3(nb256((long long)A.nb * c->NP), S), 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // induction: ddxyz(flux3, by, flux3, bx, flux2, dzflux2); ddxyz(flux2, bz, flux1, flux3, flux1, dzflux1)
+    for (int s = 0; s < S; ++s) {
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BY), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BX), nz)) ||
+            (rc = ddx_launch<T>(c, Wp(s, MW_F2), Wp(s, MW_BZ), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_F1), Wp(s, MW_F3), nz)))
+            return rc;
+    }
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_F2), Wp(0, MW_DZF2), 1, S, (long long)MW_COUNT * N)) ||
+        (rc = ddz_launch<T>(c, zt, Wp(0, MW_F1), Wp(0, MW_DZF1), 1, S, (long long)MW_COUNT * N)))
+        return rc;
+    mhd_b_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // curl b: ddxyz(by, curlbz, bz, curlbx, bx, dzbx); ddxyz(bz, curlby, bx, flux1, by, dzby)
+    for (int s = 0; s < S; ++s) {
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_BY), Wp(s, MW_CBZ), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBX), nz)) ||
+            (rc = ddx_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBY), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_BX), Wp(s, MW_F1), nz)))
+            return rc;
+    }
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_BX), Wp(0, MW_DZBX), 1, S, (long long)MW_COUNT * N)) ||
+        (rc = ddz_launch<T>(c, zt, Wp(0, MW_BY), Wp(0, MW_DZBY), 1, S, (long long)MW_COUNT * N)))
+        return rc;
+    mhd_rhs_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs, (const T*)m.g,
+                                                 (const T*)m.sponge, scr);
+    c->launches++;
+    CKL();
+    // DAMP_VELOCITY (damping.f90:125-159) through the normalised 2-D transforms
+    const bool damp = c->P.damp_waves != 0;
+    if (damp) {
+        typedef typename CplxOf<T>::type CT;
+        for (int s = 0; s < S; ++s)
+            for (int q = 0; q < 3; ++q) {
+                fft_phys_to_spec<T>(Wp(s, MW_T3 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y,
+                                    c->stream);
+                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, MW_DX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
+                                    c->tw_y, c->stream);
+                c->launches += 5;
+            }
+        CKL();
+    }
+    SlotClock clk;
+    memset(&clk, 0, sizeof(clk));
+    clk.t0 = c->d_t0; clk.time = c->d_time; clk.freq = c->freq_filtering; clk.two_d = 0;
+    clk.gate = c->forcing_length * c->cadforcing_step; clk.num_steps = c->num_steps;
+    clk.ts = R4(c->P.timestep); clk.cad = R4(c->P.cadforcing);
+    mhd_final_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, damp ? 1 : 0, scr, clk, c->src_mode, (const T*)c->planes,
+                                                   (long long)c->src_L * c->NP, c->src_L, c->series, c->nseries,
+                                                   m.plane, (const T*)m.dw);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+template <typename T>
+int mhd_steps_t(sparc_ctx* c, int nsteps) {
+    MhdState& m = *c->mhd;
+    typedef typename CplxOf<T>::type CT;
+    MhdArgs A;
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = c->nz; A.nb = c->P.npmlbot; A.nzpml = std::max(c->nzpml, 1);
+    A.S = c->active_n;
+    const int S = c->active_n;
+    for (int it = 0; it < nsteps; ++it) {
+        int rc;
+        for (int rk = 0; rk < 5; ++rk)
+            if ((rc = mhd_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0))) return rc;
+        // update + z filter (step.f90:114-116, FILTER_VARS_3D)
+        mhd_update_kernel<T><<<dim3((unsigned)((c->NP + 127) / 128), 6 * S), 128, 0, c->stream>>>(
+            A, (T*)c->a, (const T*)c->scr, (T)c->deltat);
+        const long long npv = (long long)S * PV_COUNT * A.nzpml * c->NP;
+        mhd_pml_update_kernel<T><<<nb256(npv), 256, 0, c->stream>>>((T*)m.pml, (const T*)m.spml, (T)c->deltat, npv);
+        c->launches += 2;
+        CKL();
+        // horizontal filter every freq_filtering steps of each slot's clock on
+        // fields 1..5 (physics.f90:791-830)
+        for (int s = 0; s < S; ++s) {
+            const int tl = c->time - c->t0[s];
+            if (tl < 0 || tl % c->freq_filtering != 0) continue;
+            for (int f = 0; f < 5; ++f) {
+                T* fp = (T*)c->a + ((size_t)s * 6 + f) * 2 * c->fs;
+                fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
+                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 3, c->M, c->nz, 1, 0, 0, c->stream);
+                fft_spec_to_phys<T>((CT*)m.spec, fp, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
+                c->launches += 5;
+            }
+            CKL();
+        }
+        if (c->rec_on) {
+            mhd_record_kernel<T><<<dim3(nb256(c->NP), S), 256, 0, c->stream>>>(
+                (const T*)c->a, (T*)c->rec, c->d_t0, c->d_time, c->steps, c->rec_max, 2 * c->fs, c->NP,
+                (long long)c->rec_max * 2 * c->M, m.plane_obs);
+            c->launches++;
+            CKL();
+        }
+        launch_tick(c->d_time, c->stream);
+        c->launches++;
+        CKL();
+        c->time++;
+    }
+    return SPARC_OK;
+}
+
+}  // namespace
+
+int mhd_steps(sparc_ctx* c, int nsteps) {
+    if (!c->mhd || !c->mhd->have_bg) return fail(c, SPARC_ESTATE, "option 10 needs sparc_gpu_set_mhd_background");
+    return c->f32 ? mhd_steps_t<float>(c, nsteps) : mhd_steps_t<double>(c, nsteps);
+}

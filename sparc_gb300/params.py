@@ -21,8 +21,9 @@ import numpy as np
 #: option codes of step.f90:74-110 that this framework implements
 OPT_QUIET_PML_3D = 2           # pml.f90:12 (MP_QUIET_PML_3D), velocity form
 OPT_QUIET_PML_3D_DISPL = 4     # displacement.f90:482 (MP_QUIET_PML_3D_DISPL)
+OPT_MHD_PML_3D_DISPL = 10      # displacement.f90:663 (MP_MHD_PML_3D_DISPL)
 OPT_QUIET_PML_2D_DISPL = 17    # physics2d.f90:948 (MP_QUIET_PML_2D_DISPL)
-SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL)
+SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_MHD_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL)
 
 
 def r4(x: float) -> float:
@@ -128,9 +129,9 @@ class SparcParams:
     def from_params_i(cls, text: str, **overrides) -> "SparcParams":
         """Parse the ``parameter(name = value, ...)`` statements of a params.i
         file.  Logical switches map as PARSE_OPTIONS (initialize.f90:778-824)
-        does for the supported options: USE_PML must be true, DISPL selects
-        option 4 (true) or the velocity form, option 2 (false), and
-        MAGNETIC/FLOWS must be false."""
+        does for the supported options: USE_PML must be true; without
+        MAGNETIC, DISPL selects option 4 (true) or the velocity form, option 2
+        (false); MAGNETIC with DISPL selects option 10; FLOWS must be false."""
         vals: dict = {}
         body = re.sub(r"!.*", "", text)
         for m in re.finditer(r"parameter\s*\((.*?)\)\s*$", body, re.I | re.M | re.S):
@@ -144,12 +145,16 @@ class SparcParams:
         for m in re.finditer(r"logical[^:\n]*::\s*(\w+)\s*=\s*\.(\w+)\.", body, re.I):
             vals["_" + m.group(1).lower()] = m.group(2).lower() == "true"
         kw = {k: cls._KEYS[k](v) for k, v in vals.items() if not k.startswith("_")}
-        if vals.get("_magnetic") or vals.get("_flows"):
-            raise ValueError("MAGNETIC/FLOWS backgrounds are not supported by this framework")
+        if vals.get("_flows"):
+            raise ValueError("FLOWS backgrounds are not supported by this framework")
+        if vals.get("_magnetic") and vals.get("_displ") is False:
+            raise ValueError("the MHD velocity form (option 8) is not supported")
         if "_damp_waves" in vals:
             kw["damp_waves"] = vals["_damp_waves"]
         if vals.get("_displ") is False:
             kw["option"] = OPT_QUIET_PML_3D
+        if vals.get("_magnetic"):
+            kw["option"] = OPT_MHD_PML_3D_DISPL
         kw.update(overrides)
         p = cls(**kw)
         p.validate()
@@ -165,6 +170,8 @@ class SparcParams:
         if two_d:
             if self.option == OPT_QUIET_PML_3D:
                 raise ValueError("the 2-D velocity form (option 6) is not supported")
+            if self.option == OPT_MHD_PML_3D_DISPL:
+                raise ValueError("the 2-D MHD form (option 18) is not supported")
             p = p.replace(option=OPT_QUIET_PML_2D_DISPL, ny=1)
         return p
 

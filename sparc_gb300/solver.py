@@ -158,9 +158,21 @@ class Solver:
         self._ck(self.L.sparc_gpu_get_field(self.h, slot, f, k, _dp(out)))
         return out
 
+    @property
+    def npv(self) -> int:
+        """PML auxiliary fields: six for the MHD form (option 10), else two."""
+        return 6 if self.p.option == 10 else 2
+
+    def set_mhd_background(self, rho, c, p, bx, by, bz):
+        """3-D cgs background of option 10 (density, sound speed, pressure,
+        B_x, B_y, B_z), each (nz, ny, nx); set_background's quiet column is
+        the one the source planes are searched on."""
+        arrs = [_f64(np.asarray(v, dtype=np.float64).reshape(self.shape)) for v in (rho, c, p, bx, by, bz)]
+        self._ck(self.L.sparc_gpu_set_mhd_background(self.h, *[_dp(v) for v in arrs]))
+
     def state(self, slot: int = 0):
         a = np.zeros((6,) + self.shape)
-        pml = np.zeros((2, self.p.nzpml, self.p.ny, self.p.nx))
+        pml = np.zeros((self.npv, self.p.nzpml, self.p.ny, self.p.nx))
         self._ck(self.L.sparc_gpu_get_state(self.h, slot, _dp(a), _dp(pml)))
         return a, pml
 

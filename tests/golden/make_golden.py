@@ -1,7 +1,8 @@
 """Generates tests/golden/oracle_golden.npz: outputs of the CPU oracle on small
 seeded cases (compact derivative for every boundary code, spectral
 derivatives, damping, three 3-D time steps with a forward source, thirty-one
-2-D time steps, thirty-one velocity-form steps, one kernel accumulation).  Regenerate with
+2-D time steps, thirty-one velocity-form steps, five MHD steps on a flux
+tube, one kernel accumulation).  Regenerate with
     python tests/golden/make_golden.py
 The GPU parity tests compare the CUDA path against these fixtures as well as
 against the live oracle."""
@@ -31,6 +32,16 @@ def golden_params_vel():
     return small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4, option=2)
 
 
+def golden_params_mhd():
+    """MHD displacement form (option 10): bottom PML only, flux-tube background."""
+    return small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=0, option=10)
+
+
+def golden_mhd_background(p):
+    from sparc_gb300.background import flux_tube_background
+    return flux_tube_background(p, table_for(p), b_surf=800.0, r_surf_mm=8.0)
+
+
 def golden_inputs(p, seed):
     rng = np.random.default_rng(seed)
     a = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
@@ -43,7 +54,7 @@ def golden_inputs(p, seed):
         a[0] = 0.0
         a[4] = 0.0
         a[5] = 0.0
-    pml = rng.standard_normal((2, p.nzpml, p.ny, p.nx)) * 1e-5
+    pml = rng.standard_normal((6 if p.option == 10 else 2, p.nzpml, p.ny, p.nx)) * 1e-5
     pml[1, 0] = 0.0
     x = (np.arange(p.nx) / p.nx - 0.5) * p.xlength / 1e8
     if p.ny == 1:
@@ -95,6 +106,17 @@ def compute():
     st, _, pm = ov.state()
     out["step31_vel_a"] = st
     out["step31_vel_pml"] = pm
+    pm_ = golden_params_mhd()
+    om = O.Oracle(pm_, table_for(pm_))
+    om.set_mhd(*golden_mhd_background(pm_))
+    a, pml, plane, series = golden_inputs(pm_, 48)
+    a *= 1e-3                          # a small displacement on the strong-field background
+    om.set_state(a, pml)
+    om.set_source(1, plane[None].copy(), series)
+    om.step(5)
+    st, _, pm = om.state()
+    out["step5_mhd_a"] = st
+    out["step5_mhd_pml"] = pm
     # one kernel accumulation on seeded fields
     rng = np.random.default_rng(46)
     fwd = rng.standard_normal((6, p.nz, p.ny, p.nx))

@@ -40,18 +40,28 @@ def test_params_i_parsing_and_instruction():
     assert q2.option == 17 and q2.ny == 1 and q2.compute_forward
 
 
-def test_params_reject_magnetic():
+def test_params_magnetic_selects_option_10():
+    """PARSE_OPTIONS (initialize.f90:778-824): MAGNETIC + DISPL + USE_PML -> 10;
+    the 2-D MHD form (18), the MHD velocity form (8) and FLOWS are not built."""
+    mag = PARAMS_I.replace("magnetic = .false.", "magnetic = .true.")
+    assert SparcParams.from_params_i(mag).option == 10
     with pytest.raises(ValueError):
-        SparcParams.from_params_i(PARAMS_I.replace("magnetic = .false.", "magnetic = .true."))
+        SparcParams.from_params_i(mag).instruction("spectral\n2D\n")
+    with pytest.raises(ValueError):
+        SparcParams.from_params_i(mag + "logical, parameter :: DISPL = .false.\n")
+    with pytest.raises(ValueError):
+        SparcParams.from_params_i(PARAMS_I.replace("FLOWS = .FALSE.", "FLOWS = .TRUE."))
+    assert SparcParams.from_params_i(PARAMS_I + "logical, parameter :: DISPL = .false.\n").option == 2
 
 
 def test_params_validation():
     with pytest.raises(ValueError):
         SparcParams(nx=100).validate()
     with pytest.raises(ValueError):
-        SparcParams(option=10).validate()
+        SparcParams(option=8).validate()
     with pytest.raises(ValueError):
         SparcParams(option=17, ny=4).validate()
+    SparcParams(option=10).validate()
     SparcParams().validate()
 
 

@@ -214,3 +214,55 @@ def test_oracle_reproduces_golden_fixtures():
     now = compute()
     for k in g.files:
         assert rel_l2(now[k], g[k]) < 1e-12, k
+
+
+def _mhd_case(nx=16, ny=16, nz=32, b_surf=800.0):
+    from cases import small_params, table_for
+    from sparc_gb300.background import flux_tube_background
+    p = small_params(nx=nx, ny=ny, nz=nz, npmlbot=4, npmltop=0, option=10)
+    tab = table_for(p)
+    return p, tab, flux_tube_background(p, tab, b_surf=b_surf, r_surf_mm=8.0)
+
+
+def test_mhd_setup_follows_the_reference_order():
+    """READ_IN_FIELD, the field reduction with its REAL*4 top taper, and curl
+    B0 without its d/dz parts (physics.f90:116-159), against numpy twins."""
+    from oracle import oracle as O
+    p, tab, (rho, c, pr, bx, by, bz) = _mhd_case()
+    o = O.Oracle(p, tab)
+    o.set_mhd(rho, c, pr, bx, by, bz)
+    m = o.mhd_profiles()
+    info = o.info()
+    dimc, dimrho = info["dimc"], info["dimrho"]
+    dimb = np.sqrt(4.0 * info["pi"] * dimc ** 2 * dimrho)
+    cq = tab[:, 1] / dimc
+    red = ((bz / dimb) ** 2 + (bx / dimb) ** 2 + (by / dimb) ** 2) / ((rho / dimrho) * cq[:, None, None] ** 2)
+    red = 8.0 / (8.0 + red)
+    nz = p.nz
+    for k1 in range(nz - 10, nz + 1):
+        red[k1 - 1] *= float(np.float32(np.float32(k1 - nz) / np.float32(10.0)) ** np.float32(4.0))
+    assert rel_l2(m["boz"], bz / dimb * np.sqrt(red)) < 1e-14
+    assert np.abs(m["boz"][-1]).max() == 0.0                        # the taper zeroes the top plane
+    assert np.array_equal(m["curlboy"], -o.ddx(m["boz"]))
+    assert np.array_equal(m["curlbox"], o.ddy(m["boz"]))
+    assert rel_l2(m["curlboz"], o.ddx(m["boy"]) - o.ddy(m["box"])) < 1e-15
+    z = tab[:, 0]
+    spz = 200.0 / (1.0 + np.exp((float(np.float32(1.002)) - z) / float(np.float32(1e-4)))) + \
+        300.0 / (1.0 + np.exp((z - (z[0] + float(np.float32(0.005)))) / float(np.float32(5e-4))))
+    assert rel_l2(m["spongexyz"][:, 0, 0], spz) < 1e-14
+    assert np.array_equal(m["gradp0_x"], o.ddx(pr / (dimrho * dimc ** 2)))
+
+
+def test_mhd_runs_and_drives_the_induction_pml():
+    from oracle import oracle as O
+    p, tab, bg = _mhd_case()
+    o = O.Oracle(p, tab)
+    o.set_mhd(*bg)
+    a = np.zeros((6, p.nz, p.ny, p.nx))
+    a[0, 8:12] = 1e-6 * np.random.default_rng(0).standard_normal((4, p.ny, p.nx))
+    o.set_state(a)
+    o.step(3)
+    st, scr, pml = o.state()
+    assert np.isfinite(st).all() and np.isfinite(pml).all()
+    assert pml.shape[0] == 6
+    assert np.abs(pml[2:]).max() > 0          # psi_dzbx, psi_dzby, psi_induction_bx/by are driven
