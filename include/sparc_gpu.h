@@ -134,6 +134,19 @@ int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
 int sparc_gpu_set_mhd_background(sparc_ctx* ctx, const double* rho, const double* c, const double* p,
                                  const double* bx, const double* by, const double* bz);
 
+/* Option 18 (MP_MHD_PML_2D_DISPL, physics2d.f90:724-943; ny = 1): the 2-D
+ * cgs background -- density, sound speed, pressure and the vector potential
+ * psi (model_vectorpsi), each nx*nz values a(nx,nz) -- after
+ * sparc_gpu_set_background.  B_x = -d psi/dz and B_z = d psi/dx * stretchx
+ * (DBYD1 with ibc 0) as the magnetic part of mp_Initialize_RHS_2d forms them
+ * (physics2d.f90:106-195), then the gradients, the PML at both ends with the
+ * magnetic wave speed and the source planes e_rad / o_rad (:223-341).  The
+ * state is physical and the PML arrays of set_state / get_state hold six
+ * auxiliaries of nzpml planes (psi_vz, psi_p, psi_dzbx, unused, psi_induction_bx,
+ * unused). */
+int sparc_gpu_set_mhd2d_background(sparc_ctx* ctx, const double* rho, const double* c, const double* p,
+                                   const double* psi);
+
 /* Pick the fastest of the launch variants that give identical results (the
  * fused FP32 step's modes per CTA, 4 or 2; the per-stage kernels' threads per
  * CTA, 128 or 64) by timing real steps: the call advances the solution by

@@ -80,6 +80,7 @@ def lib():
             "oracle_kernel_finish": [P, D, ctypes.c_int],
             "oracle_plane_r2c": [P, D, D],
             "oracle_set_mhd": [P, D, D, D, D, D, D], "oracle_mhd_profiles": [P, D],
+            "oracle_set_mhd2d": [P, D, D, D, D],
         }.items():
             f = getattr(L, name)
             f.argtypes = args
@@ -186,20 +187,31 @@ class Oracle:
 
     def set_state(self, a: np.ndarray, pml: np.ndarray | None = None):
         a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != 6 * int(np.prod(self.shape)):
+            raise ValueError(f"state must hold 6 x {self.shape}")
         if pml is not None:
             pml = np.ascontiguousarray(pml, dtype=np.float64)
+            if pml.size != self.npv * self.p.nzpml * self.p.ny * self.p.nx:
+                raise ValueError(f"PML state must be ({self.npv}, {self.p.nzpml}, {self.p.ny}, {self.p.nx})")
         lib().oracle_set_state(self.h, _dp(a), _dp(pml) if pml is not None else None)
 
     @property
     def npv(self) -> int:
-        """PML auxiliary fields: 6 for the MHD displacement form (option 10), else 2."""
-        return 6 if self.p.option == 10 else 2
+        """PML auxiliary fields: 6 for the MHD displacement forms (options 10, 18), else 2."""
+        return 6 if self.p.option in (10, 18) else 2
 
     def set_mhd(self, rho, c, p, bx, by, bz):
         """3-D cgs background of option 10 (as READ_IN_FIELD reads it), (nz, ny, nx)."""
         arrs = [np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape) for v in (rho, c, p, bx, by, bz)]
         if lib().oracle_set_mhd(self.h, *[_dp(v) for v in arrs]) != 0:
             raise RuntimeError("oracle_set_mhd needs option 10")
+
+    def set_mhd2d(self, rho, c, p, psi):
+        """2-D MHD background of option 18, (nz, nx) cgs: density, sound speed,
+        pressure and the vector potential psi (G R_sun) whose curl is B."""
+        arrs = [np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape) for v in (p, rho, c, psi)]
+        if lib().oracle_set_mhd2d(self.h, *[_dp(v) for v in arrs]) != 0:
+            raise RuntimeError("oracle_set_mhd2d needs option 18")
 
     def mhd_profiles(self) -> dict:
         out = np.zeros((15,) + self.shape)

@@ -469,7 +469,7 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     m.num_steps = 2 * (m.num_steps / 2) + 2;
 
     // ---------------- mp_Initialize_RHS (physics.f90:34-404) / _2d ----------------
-    bool two_d = (P->option == 17);
+    bool two_d = (P->option == 17 || P->option == 18);
     {
         double temp2 = 1.0 + R4(P->excitdep) / m.rsun, temp = 1.0;
         for (int k = 0; k < nz; ++k)
@@ -565,7 +565,7 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     }
     // state
     m.a.assign(N * 6, 0); m.temp_step.assign(N * 6, 0); m.scr.assign(N * 6, 0);
-    m.npv = P->option == 10 ? 6 : 2;
+    m.npv = (P->option == 10 || P->option == 18) ? 6 : 2;
     long npml = (long)NP * std::max(m.nzpml, 1) * m.npv;
     m.scrpml.assign(npml, 0); m.pmlvars.assign(npml, 0); m.psipml.assign(npml, 0);
     m.gradp.assign(N * 3, 0); m.dvxdx.assign(N, 0); m.dvydy.assign(N, 0); m.gradvz.assign(N, 0);
@@ -979,6 +979,218 @@ static void rhs_option10(Model& m) {
 }
 
 // ----------------------------------------------------------------------------
+// DBYD1 (dbyd1.f) for ibc = 0: the compact first derivative of DBYD2 along
+// the first index, with the coefficients in default REAL (REAL*4) as that
+// file declares none, the end rows zero, solved by TRIDAG (tridag.f, the
+// Thomas algorithm with divisions).  a, b: (n2, n1) C order (n1 fastest).
+// ----------------------------------------------------------------------------
+static void dbyd1_ibc0(double* a, const double* b, int n1, long n2) {
+    const float d1i = (float)(n1 - 1);
+    const double C1 = (double)(d1i * 7.0f / 9.0f), C2 = (double)(d1i / 36.0f);
+    const double B1 = (double)(-43.0f / 96.0f * d1i), B2 = (double)(-5.0f / 6.0f * d1i);
+    const double B3 = (double)(9.0f / 8.0f * d1i), B4 = (double)(1.0f / 6.0f * d1i), B5 = (double)(-1.0f / 96.0f * d1i);
+    std::vector<double> uppr(n1 + 1, 0.0), lowr(n1 + 1, 0.0), diag(n1 + 1, 1.0);
+    for (int J = 3; J <= n1 - 2; ++J) uppr[J] = (double)(1.0f / 3.0f);
+    uppr[1] = 0.0;                                  // mod(ibc,2) == 0
+    uppr[2] = (double)(3.0f / 4.0f);
+    uppr[n1 - 1] = (double)(1.0f / 8.0f);
+    for (int I = 1; I <= n1; ++I) lowr[I] = uppr[n1 - I + 1];
+    lowr[n1] = 0.0;                                 // ibc /= 1, 2
+    std::vector<double> gam(n1 + 1), ud(n1 + 1), r(n1 + 1);
+    for (long i = 0; i < n2; ++i) {
+        const double* B = b + i * n1 - 1;           // 1-based
+        double* A = a + i * n1 - 1;
+        for (int J = 3; J <= n1 - 2; ++J) r[J] = C1 * (B[J + 1] - B[J - 1]) + C2 * (B[J + 2] - B[J - 2]);
+        r[2] = B1 * B[1] + B2 * B[2] + B3 * B[3] + B4 * B[4] + B5 * B[5];
+        r[n1 - 1] = -(B1 * B[n1] + B2 * B[n1 - 1] + B3 * B[n1 - 2] + B4 * B[n1 - 3] + B5 * B[n1 - 4]);
+        r[1] = 0.0;
+        r[n1] = 0.0;
+        // TRIDAG(LOWR, DIAG, UPPR, A, A, N1, 0)
+        double bet = diag[1];
+        ud[1] = r[1] / bet;
+        for (int J = 2; J <= n1; ++J) {
+            gam[J] = uppr[J - 1] / bet;
+            bet = diag[J] - lowr[J] * gam[J];
+            ud[J] = (r[J] - lowr[J] * ud[J - 1]) / bet;
+        }
+        for (int J = n1 - 1; J >= 1; --J) ud[J] = ud[J] - gam[J + 1] * ud[J + 1];
+        for (int J = 1; J <= n1; ++J) A[J] = ud[J];
+    }
+}
+
+// ----------------------------------------------------------------------------
+// 2-D MHD background (option 18, kernel mode): the magnetic part of
+// mp_Initialize_RHS_2d (physics2d.f90:106-195) and the rest of it in order
+// (:223-226 gradients, :262-297 PML with the magnetic wave speed, :318-341
+// horizontal gradients and source planes).  Inputs (nz, nx) cgs: pressure,
+// density, sound speed (model_c) and the vector potential psi
+// (model_vectorpsi): B_x = -d psi/dz, B_z = DBYD1(psi) * stretchx.
+// ----------------------------------------------------------------------------
+static void setup_mhd2d(Model& m, const double* pr, const double* rho, const double* cs, const double* psi) {
+    long N = m.N, NP = m.NP; int nx = m.nx, nz = m.nz;
+    m.box.assign(N, 0); m.boy.assign(N, 0); m.boz.assign(N, 0);
+    ddz(m, psi, m.box.data(), 1);
+    for (long q = 0; q < N; ++q) m.box[q] = -m.box[q];
+    dbyd1_ibc0(m.boz.data(), psi, nx, (long)nz);
+    for (long q = 0; q < N; ++q) m.boz[q] = m.boz[q] * m.stretchx;
+    for (long q = 0; q < N; ++q) {
+        m.box[q] = m.box[q] / m.dimb;
+        m.boz[q] = m.boz[q] / m.dimb;
+        m.p0[q] = pr[q] / (m.dimrho * std::pow(m.dimc, 2.0));
+        m.rho0[q] = rho[q] / m.dimrho;
+        m.c_speed[q] = cs[q] / m.dimc;
+        m.c2[q] = std::pow(m.c_speed[q], 2.0);
+    }
+    for (int k = 0; k < nz; ++k) { m.cq[k] = m.c_speed[NP * k]; m.rhoq[k] = m.rho0[NP * k]; }
+    // curl B0 (physics2d.f90:180-183; the reduction is computed, then reset to 1)
+    std::vector<double> tmp(N);
+    m.curlbox.assign(N, 0); m.curlboy.assign(N, 0); m.curlboz.assign(N, 0);
+    ddz(m, m.box.data(), m.curlboy.data(), 1);
+    ddx(m, m.boz.data(), tmp.data());
+    for (long q = 0; q < N; ++q) m.curlboy[q] = m.curlboy[q] - tmp[q];
+    // physics2d.f90:223-226
+    for (long q = 0; q < N; ++q) { m.rhoinv[q] = 1.0 / m.rho0[q]; m.c2rho0[q] = m.c2[q] * m.rho0[q]; }
+    ddz(m, m.rho0.data(), m.gradrho0_z.data(), 1);
+    ddz(m, m.p0.data(), m.gradp0_z.data(), 1);
+    // PML (physics2d.f90:262-297): tempin at k = 1 (bottom) and nz-5 (top), factor 3*3 at both ends
+    {
+        int nb = m.P.npmlbot, nt = m.P.npmltop;
+        std::vector<double> tempin(N);
+        for (long q = 0; q < N; ++q)
+            tempin[q] = std::pow(m.c2[q] + (std::pow(m.box[q], 2.0) + std::pow(m.boz[q], 2.0)) / m.rho0[q], 0.5);
+        for (int k = 1; k <= nz; ++k) {
+            double alphaz = m.pi * R4(0.005) * m.diml / m.dimc;
+            if (k < nb + 1) alphaz = m.pi * R4(0.005) * m.diml / m.dimc * (m.z[k - 1] - m.z[0]) / (m.z[nb - 1] - m.z[0]);
+            if (k > nz - nt) alphaz = m.pi * R4(0.005) * m.diml / m.dimc * (m.z[nz - 1] - m.z[k - 1]) / (m.z[nz - 1] - m.z[nz - nt]);
+            double fdec00 = 1.0;
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1);
+                double dampz = 0.0, fdec = 1.0;
+                if (k < nb + 1) {
+                    double r = (m.z[nb - 1] - m.z[k - 1]) / (m.z[nb - 1] - m.z[0]);
+                    dampz = 3.0 * 3.0 * tempin[q] / (m.z[nb - 1] - m.z[0]) * (r * r);
+                    fdec = alphaz / (dampz + alphaz);
+                    m.gradp0_z[id] *= fdec; m.gradrho0_z[id] *= fdec;
+                }
+                if (k > nz - nt) {
+                    double r = (m.z[nz - nt] - m.z[k - 1]) / (m.z[nz - 1] - m.z[nz - nt]);
+                    dampz = 3.0 * 3.0 * tempin[q + NP * (long)(nz - 6)] / (m.z[nz - 1] - m.z[nz - nt]) * (r * r);
+                    fdec = alphaz / (dampz + alphaz);
+                    m.gradp0_z[id] *= fdec; m.gradrho0_z[id] *= fdec;
+                }
+                if (q == 0) fdec00 = fdec;
+                m.bzpml[id] = -alphaz - dampz;
+                m.az[id] = -dampz;
+            }
+            m.g[k - 1] = (k < nb + 1 || k > nz - nt) ? m.graw[k - 1] * fdec00 : m.graw[k - 1];
+        }
+    }
+    m.gradrho0_x.assign(N, 0); m.gradp0_x.assign(N, 0); m.gradrho0_y.assign(N, 0); m.gradp0_y.assign(N, 0);
+    ddx(m, m.rho0.data(), m.gradrho0_x.data());
+    ddx(m, m.p0.data(), m.gradp0_x.data());
+    // source planes: erad_2d = e_rad, orad_2d = o_rad (physics2d.f90:334-335)
+    m.erad_2d.assign(NP, m.e_rad); m.orad_2d.assign(NP, m.o_rad); m.delta_width_2d.assign(NP, 0.0);
+    for (long q = 0; q < NP; ++q) {
+        const int k2 = m.P.compute_adjoint ? m.orad_2d[q] : m.erad_2d[q];
+        m.delta_width_2d[q] = 2.0 / (m.z[k2] - m.z[k2 - 2]);
+    }
+    m.spongexyz.assign(N, 0.0);
+}
+
+// ----------------------------------------------------------------------------
+// MP_MHD_PML_2D_DISPL (physics2d.f90:724-943), option 18 (ny = 1): PML at
+// both ends with psi_vz, psi_p, psi_induction_bx, psi_dzbx; only the bottom
+// row is zeroed
+// ----------------------------------------------------------------------------
+static void rhs_option18(Model& m) {
+    long N = m.N, NP = m.NP; int nz = m.nz;
+    double* xi_x = &m.temp_step[0]; double* xi_z = &m.temp_step[2 * N];
+    double* v_x = &m.temp_step[3 * N]; double* v_z = &m.temp_step[5 * N];
+    double* RHSxi_x = &m.scr[0]; double* RHSxi_z = &m.scr[2 * N];
+    double* RHSv_x = &m.scr[3 * N]; double* RHSv_z = &m.scr[5 * N];
+    long PS = NP * m.nzpml;
+    double* psivz = &m.psipml[0]; double* psip = &m.psipml[PS];
+    double* psidzbx = &m.psipml[2 * PS]; double* psiibx = &m.psipml[4 * PS];
+    double* RHSpsivz = &m.scrpml[0]; double* RHSpsip = &m.scrpml[PS];
+    double* RHSpsidzbx = &m.scrpml[2 * PS]; double* RHSpsiibx = &m.scrpml[4 * PS];
+    int nb = m.P.npmlbot, nt = m.P.npmltop;
+    std::vector<double> dxixdx(N), dxizdz(N, 0.0), p(N), rho(N), gradp_x(N), gradp_z(N, 0.0), flux2(N);
+    std::vector<double> bx(N), bz(N), dzbx(N), curlby(N);
+    auto pml = [&](double* deriv, double* psi, double* rhs) {
+        int pmlindex = 0;
+        for (int k = 1; k <= nz; ++k) {
+            if (k <= nb || k >= nz - nt + 1) {
+                pmlindex++;
+                for (long q = 0; q < NP; ++q) {
+                    long id = q + NP * (k - 1), ip = q + NP * (pmlindex - 1);
+                    rhs[ip] = m.az[id] * deriv[id] + m.bzpml[id] * psi[ip];
+                    deriv[id] = deriv[id] + psi[ip];
+                }
+            }
+        }
+    };
+    ddx(m, xi_x, dxixdx.data());
+    for (long q = 0; q < NP; ++q) dxizdz[q + NP * (nz - 1)] = -dxixdx[q + NP * (nz - 1)] * m.unstretch[nz - 1];
+    oracle_dbyd2(dxizdz.data(), xi_z, NP, nz, 3);
+    for (int k = 0; k < nz; ++k)
+        for (long q = 0; q < NP; ++q) dxizdz[q + NP * k] *= m.stretch[k];
+    pml(dxizdz.data(), psivz, RHSpsivz);
+    for (long q = 0; q < N; ++q) {
+        const double div = dxixdx[q] + dxizdz[q];
+        p[q] = -m.c2rho0[q] * div - xi_z[q] * m.gradp0_z[q] - xi_x[q] * m.gradp0_x[q];
+        rho[q] = -m.rho0[q] * div - xi_z[q] * m.gradrho0_z[q] - xi_x[q] * m.gradrho0_x[q];
+    }
+    ddx(m, p.data(), gradp_x.data());
+    // ddz(p, gradp_z, 2): the caller-set bottom value is the previous
+    // gradp_z(:,:,1), zero in every reachable state
+    oracle_dbyd2(gradp_z.data(), p.data(), NP, nz, 2);
+    for (int k = 0; k < nz; ++k)
+        for (long q = 0; q < NP; ++q) gradp_z[q + NP * k] *= m.stretch[k];
+    pml(gradp_z.data(), psip, RHSpsip);
+    for (long q = 0; q < N; ++q) flux2[q] = -(xi_x[q] * m.boz[q] - xi_z[q] * m.box[q]);
+    ddz(m, flux2.data(), bx.data(), 0);
+    ddx(m, flux2.data(), bz.data());
+    pml(bx.data(), psiibx, RHSpsiibx);
+    for (long q = 0; q < N; ++q) bx[q] = -bx[q];
+    ddz(m, bx.data(), dzbx.data(), 0);
+    ddx(m, bz.data(), curlby.data());
+    pml(dzbx.data(), psidzbx, RHSpsidzbx);
+    for (long q = 0; q < N; ++q) {
+        curlby[q] = -curlby[q] + dzbx[q];
+        double flux1 = curlby[q] * m.boz[q];
+        double flux3 = -curlby[q] * m.box[q];
+        RHSv_x[q] = m.rhoinv[q] * (-gradp_x[q] + flux1);
+        RHSv_z[q] = m.rhoinv[q] * (-gradp_z[q] + flux3);
+        flux1 = m.curlboy[q] * bz[q];
+        flux3 = -m.curlboy[q] * bx[q];
+        RHSv_x[q] = RHSv_x[q] + m.rhoinv[q] * flux1;
+        RHSv_z[q] = RHSv_z[q] + m.rhoinv[q] * flux3;
+    }
+    for (int k = 0; k < nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * k;
+            RHSv_z[id] = RHSv_z[id] - m.rhoinv[id] * rho[id] * m.g[k];
+        }
+    for (long q = 0; q < N; ++q) { RHSxi_x[q] = v_x[q]; RHSxi_z[q] = v_z[q]; }
+    if (m.P.damp_waves) {
+        damp_velocity(m, v_x, RHSv_x);
+        damp_velocity(m, v_z, RHSv_z);
+    }
+    if (m.src_mode != 0 && m.time <= m.forcing_length * m.cadforcing_step) {
+        for (long q = 0; q < NP; ++q) {
+            const int k2 = m.P.src_k > 0 ? m.P.src_k : (m.P.compute_adjoint ? m.orad_2d[q] : m.erad_2d[q]);
+            long id = q + NP * (k2 - 1);
+            if (m.P.compute_adjoint)
+                RHSv_z[id] = RHSv_z[id] + m.forcing[q] * m.delta_width_2d[q] / m.rho0[id];
+            else
+                RHSv_z[id] = RHSv_z[id] + m.forcing[q] / m.rho0[id] * m.delta_width_2d[q];
+        }
+    }
+    for (int l = 0; l < 6; ++l)
+        for (long q = 0; q < NP; ++q) m.scr[l * N + q] = 0.0;
+}
+
+// ----------------------------------------------------------------------------
 // MP_QUIET_PML_2D_DISPL (physics2d.f90:948-1105), option 17 (ny = 1)
 // ----------------------------------------------------------------------------
 static void rhs_option17(Model& m) {
@@ -1203,12 +1415,13 @@ static void step(Model& m) {
         if (m.P.option == 4) rhs_option4(m);
         else if (m.P.option == 2) rhs_option2(m);
         else if (m.P.option == 10) rhs_option10(m);
+        else if (m.P.option == 18) rhs_option18(m);
         else rhs_option17(m);
     }
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < N6; ++q) m.a[q] = m.a[q] + m.deltat * m.scr[q];
     for (long q = 0; q < NPML; ++q) m.pmlvars[q] = m.pmlvars[q] + m.deltat * m.scrpml[q];
-    if (m.P.option == 17) filter_vars_2d(m);
+    if (m.P.option == 17 || m.P.option == 18) filter_vars_2d(m);
     else filter_vars_3d(m);
 }
 
@@ -1325,6 +1538,14 @@ int oracle_set_mhd(void* h, const double* rho, const double* c, const double* p,
     Model& m = *(Model*)h;
     if (m.P.option != 10) return -1;
     setup_mhd(m, rho, c, p, bx, by, bz);
+    return 0;
+}
+
+// 2-D MHD background of option 18 ((nz, nx) cgs: pressure, density, sound speed, vector potential)
+int oracle_set_mhd2d(void* h, const double* p, const double* rho, const double* c, const double* psi) {
+    Model& m = *(Model*)h;
+    if (m.P.option != 18) return -1;
+    setup_mhd2d(m, p, rho, c, psi);
     return 0;
 }
 

@@ -129,3 +129,47 @@ def flux_tube_background(p, table: np.ndarray, b_surf: float = 2000.0, r_surf_mm
     rho = rho_q[:, None, None] * pres / pq
     c = np.broadcast_to(c_q[:, None, None], (nz, ny, nx)).copy()
     return rho, c, pres, bx, by, bz
+
+
+def flux_sheet_background(p, table: np.ndarray, b_surf: float = 300.0, w_mm: float = 10.0,
+                          z_fade_mm: float = 0.0, fade_mm: float = 0.2, x0_mm: float = 0.0,
+                          p_floor: float = 0.2):
+    """2-D (ny = 1) magnetic flux sheet on the quiet column, as the cgs arrays
+    the reference reads for the 2-D MHD run (density, sound speed, pressure
+    and the vector potential psi of model_vectorpsi, physics2d.f90:106-146),
+    each (nz, 1, nx).
+
+    The reference forms B_x = -d psi/dz and B_z = d psi/dx * stretchx with x
+    and z in solar radii, so psi is in G R_sun.  Here
+        psi(x, z) = (sqrt(pi)/2) b(z) W erf((x - x0) / W),
+        b(z) = b_surf / (1 + exp((z - z_fade) / fade)),
+    a sheet of constant half-width W (a few pixels: DBYD1 rings on a sheet
+    narrower than the grid): B_z = b(z) exp(-(x-x0)^2/W^2), and a
+    horizontal B_x = -(sqrt(pi)/2) W b'(z) erf(.) only in the fade layer.
+    The field fades out of the low-density atmosphere: a sheet that spread
+    with height there (flux conservation over ~140 km pressure scale heights)
+    carries a strong horizontal field in which this linear system grows
+    exponentially (the reference notes the form fails at very small
+    densities).  Pressure p = p_quiet - B^2/8pi floored at p_floor * p_quiet,
+    density scaled with p, c unchanged: a synthetic test background in
+    approximate horizontal pressure balance.
+    """
+    from math import erf
+    nx, nz = p.nx, p.nz
+    z_r = table[:, 0]
+    z_cm = (z_r - 1.0) * RSUN_CM
+    c_q, rho_q, p_q = table[:, 1], table[:, 2], table[:, 3]
+    W = w_mm * 1e8 / RSUN_CM
+    prof = 1.0 / (1.0 + np.exp((z_cm - z_fade_mm * 1e8) / (fade_mm * 1e8)))
+    dprof = np.gradient(prof, z_r)
+    x = ((np.arange(nx) / nx - 0.5) * p.xlength - x0_mm * 1e8) / RSUN_CM
+    E = np.vectorize(erf)(x / W)
+    amp = 0.5 * np.sqrt(np.pi) * b_surf * W
+    psi = (amp * prof)[:, None, None] * E[None, None, :]
+    bz = (b_surf * prof)[:, None, None] * np.exp(-(x / W) ** 2)[None, None, :]
+    bx = -(amp * dprof)[:, None, None] * E[None, None, :]
+    pq = p_q[:, None, None]
+    pres = np.maximum(pq - (bx ** 2 + bz ** 2) / (8.0 * np.pi), p_floor * pq)
+    rho = rho_q[:, None, None] * pres / pq
+    c = np.broadcast_to(c_q[:, None, None], (nz, 1, nx)).copy()
+    return rho, c, pres, psi

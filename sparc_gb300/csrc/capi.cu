@@ -127,13 +127,14 @@ const char* sparc_gpu_last_error(const sparc_ctx* c) { return c ? c->err.c_str()
 
 static int validate(const sparc_params* p, std::string& why) {
     auto pow2 = [](int n) { return n >= 4 && n <= 1024 && (n & (n - 1)) == 0; };
-    if (p->option != 2 && p->option != 4 && p->option != 10 && p->option != 17) {
-        why = "option must be 2, 4, 10 or 17";
+    if (p->option != 2 && p->option != 4 && p->option != 10 && p->option != 17 && p->option != 18) {
+        why = "option must be 2, 4, 10, 17 or 18";
         return 0;
     }
     if (!pow2(p->nx)) { why = "nx must be a power of two in [4,1024]"; return 0; }
-    if (p->option == 17 && p->ny != 1) { why = "option 17 needs ny == 1"; return 0; }
-    if (p->option != 17 && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
+    const bool is2d = (p->option == 17 || p->option == 18);
+    if (is2d && p->ny != 1) { why = "the 2-D options (17, 18) need ny == 1"; return 0; }
+    if (!is2d && !pow2(p->ny)) { why = "ny must be a power of two in [4,1024]"; return 0; }
     if (p->nz < 16 || p->nz > 1024) { why = "nz must be in [16,1024]"; return 0; }
     if (p->npmlbot < 2 || p->npmlbot > p->nz / 4 || p->npmltop < 0 || p->npmltop > p->nz / 4) {
         why = "PML widths out of range"; return 0;
@@ -208,9 +209,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     launch_set_time(c->d_time, 0, c->stream);
     c->t0.assign(c->S, 0);
     c->active_n = c->S;
-    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && p->option != 10;
+    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && p->option != 10 && p->option != 18;
     if (c->use_fused) fused_prepare(c->nz, c->nzpml);
-    if (p->option == 10 && (rc = mhd_create(c))) return bail(rc);
+    if ((p->option == 10 || p->option == 18) && (rc = mhd_create(c))) return bail(rc);
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
@@ -255,7 +256,7 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     if (!zin || !cin || !rhoin || !pin || !gin || !gamin) return fail(c, SPARC_EINVAL, "null background array");
     const sparc_params& P = c->P;
     const int nz = c->nz, nx = P.nx, ny = P.ny;
-    const bool two_d = (P.option == 17);
+    const bool two_d = (P.option == 17 || P.option == 18);
     for (int k = 0; k < nz; ++k) {
         if (!std::isfinite(zin[k]) || !(cin[k] > 0) || !(rhoin[k] > 0) || !std::isfinite(pin[k]) || !std::isfinite(gin[k]))
             return fail(c, SPARC_EINVAL, "background row " + std::to_string(k + 1) + " is not finite/positive");
@@ -417,7 +418,8 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
                 }
                 c->pt_host[PT_KX * (size_t)c->M + m] = kxm;
                 c->pt_host[PT_KY * (size_t)c->M + m] = kym;
-                c->pt_host[PT_DAMP * (size_t)c->M + m] = P.damp_waves && !two_d ? gam : 0.0;
+                // the quiet 2-D form does not damp; the 2-D MHD form does (physics2d.f90:897)
+                c->pt_host[PT_DAMP * (size_t)c->M + m] = P.damp_waves && P.option != 17 ? gam : 0.0;
                 c->pt_host[PT_HF * (size_t)c->M + m] = hf;
             }
         }
@@ -525,15 +527,22 @@ static int to_spec(sparc_ctx* c, const double* host_field, void* spec_dst, int n
     long long n = (long long)c->NP * nplanes;
     if (c->mhd) {
         if (c->f32) {
-            CK(cudaMemcpyAsync(c->phys64, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
-            launch_copy_convert<float>((float*)spec_dst, c->phys64, n, c->stream);
-            c->launches++;
-            CKL();
+            // staged through phys64 (nz planes) in chunks: the six PML
+            // auxiliaries can hold more planes than one field
+            for (int off = 0; off < nplanes; off += c->nz) {
+                const long long nc = (long long)c->NP * std::min(c->nz, nplanes - off);
+                CK(cudaMemcpyAsync(c->phys64, host_field + (long long)off * c->NP, nc * 8, cudaMemcpyHostToDevice,
+                                   c->stream));
+                launch_copy_convert<float>((float*)spec_dst + (long long)off * c->NP, c->phys64, nc, c->stream);
+                c->launches++;
+                CKL();
+            }
         } else {
             CK(cudaMemcpyAsync(spec_dst, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
         }
         return SPARC_OK;
     }
+    if (nplanes > c->nz) return fail(c, SPARC_EINVAL, "staging of more planes than phys64 holds");
     CK(cudaMemcpyAsync(c->phys64, host_field, n * 8, cudaMemcpyHostToDevice, c->stream));
     if (c->f32) {
         launch_copy_convert<float>((float*)c->phys, c->phys64, n, c->stream);
@@ -552,6 +561,7 @@ static int to_spec(sparc_ctx* c, const double* host_field, void* spec_dst, int n
 // spectral (device, T) -> physical FP64 on device (c->phys64)
 static int from_spec_dev(sparc_ctx* c, const void* spec_src, int nplanes) {
     long long n = (long long)c->NP * nplanes;
+    if (nplanes > c->nz) return fail(c, SPARC_EINVAL, "staging of more planes than phys64 holds");
     if (c->mhd) {
         if (c->f32) {
             launch_copy_back<float>(c->phys64, (const float*)spec_src, n, c->stream);
@@ -577,10 +587,16 @@ static int from_spec_dev(sparc_ctx* c, const void* spec_src, int nplanes) {
 }
 
 static int from_spec(sparc_ctx* c, const void* spec_src, double* host_field, int nplanes) {
-    int rc = from_spec_dev(c, spec_src, nplanes);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(host_field, c->phys64, (size_t)c->NP * nplanes * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    // dense planes (MHD) go through phys64 at most nz planes at a time
+    const int chunk = c->mhd ? c->nz : nplanes;
+    for (int off = 0; off < nplanes; off += chunk) {
+        const int np = std::min(chunk, nplanes - off);
+        int rc = from_spec_dev(c, (const char*)spec_src + (size_t)off * plane_bytes(c), np);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(host_field + (long long)off * c->NP, c->phys64, (size_t)c->NP * np * 8,
+                           cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
     return SPARC_OK;
 }
 
@@ -739,7 +755,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.clk.t0 = c->d_t0;
     A.clk.time = c->d_time;
     A.clk.freq = c->freq_filtering;
-    A.clk.two_d = (P.option == 17);
+    A.clk.two_d = (P.option == 17 || P.option == 18);
     A.clk.gate = c->forcing_length * c->cadforcing_step;
     A.clk.num_steps = c->num_steps;
     A.clk.ts = R4(P.timestep);
@@ -875,10 +891,19 @@ int sparc_gpu_step(sparc_ctx* c, int nsteps) {
     return c->f32 ? do_steps<float>(c, nsteps) : do_steps<double>(c, nsteps);
 }
 
+int sparc_gpu_set_mhd2d_background(sparc_ctx* c, const double* rho, const double* cs, const double* p,
+                                   const double* psi) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->mhd || c->P.option != 18) return fail(c, SPARC_EINVAL, "the 2-D MHD background belongs to option 18");
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background (the quiet column) first");
+    if (!p || !rho || !cs || !psi) return fail(c, SPARC_EINVAL, "null background array");
+    return mhd2d_set_background(c, p, rho, cs, psi);
+}
+
 int sparc_gpu_set_mhd_background(sparc_ctx* c, const double* rho, const double* cs, const double* p,
                                  const double* bx, const double* by, const double* bz) {
     if (!c) return SPARC_EINVAL;
-    if (!c->mhd) return fail(c, SPARC_EINVAL, "the MHD background belongs to option 10");
+    if (!c->mhd || c->P.option != 10) return fail(c, SPARC_EINVAL, "the MHD background belongs to option 10");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background (the quiet column) first");
     if (!rho || !cs || !p || !bx || !by || !bz) return fail(c, SPARC_EINVAL, "null background array");
     return mhd_set_background(c, rho, cs, p, bx, by, bz);
@@ -1194,7 +1219,7 @@ extern "C" {
 int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (c->P.option == 2 || c->P.option == 10)
+    if (c->P.option == 2 || c->P.option == 10 || c->P.option == 18)
         return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the quiet displacement forms");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");

@@ -139,6 +139,7 @@ int mhd_create(sparc_ctx* c);
 void mhd_destroy(sparc_ctx* c);
 int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const double* p, const double* bx,
                        const double* by, const double* bz);
+int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const double* cs, const double* psi);
 int mhd_steps(sparc_ctx* c, int nsteps);
 void* mhd_pml(sparc_ctx* c);      // [S][6][nzpml*NP] T pmlvars of option 10
 void* mhd_spml(sparc_ctx* c);     // scrpml

@@ -41,7 +41,7 @@ enum { PV_VZ, PV_P, PV_DZBX, PV_DZBY, PV_IBX, PV_IBY, PV_COUNT };
 
 struct MhdState {
     void* bg = nullptr;        // [MB_COUNT][N] T
-    void* pab = nullptr;       // [2][nb*NP] T: a_z, b_z of the bottom PML planes
+    void* pab = nullptr;       // [2][nzpml*NP] T: a_z, b_z of the PML planes (pmlindex order)
     void* g = nullptr;         // [nz] T: gravity with the PML decay of the (1,1) column
     void* sponge = nullptr;    // [nz] T: spongez (PERIODIC: spongexyz(:,:,k) = spongez(k))
     int* plane = nullptr;      // [NP] 0-based source plane of each pixel
@@ -132,15 +132,19 @@ __global__ void colderiv_kernel(const T* __restrict__ in, T* __restrict__ out, i
 
 // d/dz (DBYD2 with stretch, bc 0 or 1) of real pencils: npix pencils per
 // field, nfield fields with stride fstride (grid.y)
+// bc 2: the caller-set bottom value is 0; bc 3: the caller-set top value is
+// topscale * topsrc(plane nz-1) of the same field index
 template <typename T>
 __global__ void __launch_bounds__(128) zderiv_phys_kernel(const T* __restrict__ zt, Compact<T> cc,
                                                           const T* __restrict__ in, T* __restrict__ out,
-                                                          long long npix, int nz, int bc, long long fstride) {
+                                                          long long npix, int nz, int bc, long long fstride,
+                                                          const T* __restrict__ topsrc, T topscale) {
     const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= npix) return;
     const T* b = in + blockIdx.y * fstride + m;
     T* o = out + blockIdx.y * fstride + m;
-    compact_forward<T, T>(nz, bc, [&](int j) { return b[(long long)j * npix]; }, (T)0, (T)0,
+    const T top = topsrc ? topscale * topsrc[blockIdx.y * fstride + (long long)(nz - 1) * npix + m] : (T)0;
+    compact_forward<T, T>(nz, bc, [&](int j) { return b[(long long)j * npix]; }, (T)0, top,
                           zt + (ZT_TH + 3 * bc) * nz, zt + (ZT_TH + 3 * bc + 1) * nz, cc, o, npix);
     const T* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
     T ud = o[(long long)(nz - 1) * npix];
@@ -229,9 +233,17 @@ __global__ void to_t_kernel(T* dst, const double* src, long long n) {
 
 struct MhdArgs {
     long long N, NP, FS;   // points per field, per plane; field stride of the state slots
-    int nz, nb, nzpml;
+    int nz, nb, nt, nzpml;
     int S;
+    int both;              // PML at both ends (option 18) or at the bottom only (option 10)
 };
+
+// pmlindex of 0-based plane k (PML_BOUNDARY_ACCOUNTING order), -1 outside
+__device__ __forceinline__ int pml_plane(const MhdArgs& A, int k) {
+    if (k < A.nb) return k;
+    if (A.both && k >= A.nz - A.nt) return A.nb + (k - (A.nz - A.nt));
+    return -1;
+}
 
 // temp = a + beta*scr (step.f90:52-71) into T0..T5, and the fluxes of xi x B0
 // (displacement.f90:672-674)
@@ -257,17 +269,21 @@ __global__ void mhd_temp_kernel(const MhdArgs A, const T* __restrict__ a, const 
     w[MW_F3 * A.N + t] = -(v[1] * box - v[0] * boy);
 }
 
-// bottom-PML accounting (pml.f90:213-231 form; k <= npmlbot only in option 10):
-// rhs = a_z deriv + b_z psi, deriv += psi, with psi = pmlvars + beta*scrpml
+// PML accounting (pml.f90:213-231 form; the bottom planes only in option 10,
+// both ends in option 18): rhs = a_z deriv + b_z psi, deriv += psi, with
+// psi = pmlvars + beta*scrpml
 template <typename T>
 __device__ __forceinline__ T pml_bottom(const MhdArgs& A, long long t, int s, int aux, T deriv, const T* __restrict__ pab,
                                         const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
-    const long long nbp = (long long)A.nb * A.NP;
-    if (t >= nbp) return deriv;
-    const long long o = ((long long)s * PV_COUNT + aux) * (A.nzpml * A.NP) + t;
+    const int k = (int)(t / A.NP);
+    const int ip = pml_plane(A, k);
+    if (ip < 0) return deriv;
+    const long long q = t - (long long)k * A.NP;
+    const long long np = (long long)A.nzpml * A.NP, ipq = (long long)ip * A.NP + q;
+    const long long o = ((long long)s * PV_COUNT + aux) * np + ipq;
     T psi = pml[o];
     if (hs) psi = psi + beta * spml[o];
-    spml[o] = pab[t] * deriv + pab[nbp + t] * psi;
+    spml[o] = pab[ipq] * deriv + pab[np + ipq] * psi;
     return deriv + psi;
 }
 
@@ -293,7 +309,7 @@ template <typename T>
 __global__ void mhd_pmlp_kernel(const MhdArgs A, T* __restrict__ work, const T* __restrict__ pab,
                                 const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)A.nb * A.NP) return;
+    if (t >= A.N) return;
     const int s = blockIdx.y;
     T* w = work + (long long)s * MW_COUNT * A.N;
     w[MW_GPZ * A.N + t] = pml_bottom<T>(A, t, s, PV_P, w[MW_GPZ * A.N + t], pab, pml, spml, beta, hs);
@@ -413,14 +429,14 @@ __global__ void mhd_final_kernel(const MhdArgs A, const T* __restrict__ bg, cons
 // (source, field, pixel) column
 template <typename T>
 __global__ void __launch_bounds__(128) mhd_update_kernel(const MhdArgs A, T* __restrict__ a, const T* __restrict__ scr,
-                                                         T dt) {
+                                                         T dt, int mode) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= A.NP) return;
     const int s = blockIdx.y / 6, f = blockIdx.y % 6;
     T* af = a + ((long long)s * 6 + f) * A.FS + q;
     const T* sf = scr + ((long long)s * 6 + f) * A.FS + q;
     zfilter_stream<T, T>(
-        A.nz, 0, [&](int j) { const long long o = (long long)j * A.NP; return af[o] + dt * sf[o]; },
+        A.nz, mode, [&](int j) { const long long o = (long long)j * A.NP; return af[o] + dt * sf[o]; },
         [&](int j, T v) { af[(long long)j * A.NP] = v; });
 }
 
@@ -485,9 +501,11 @@ Compact<T> cc_of(const sparc_ctx* c) {
 
 // d/dz of nfield fields (stride fstride) with the context's T tables
 template <typename T>
-int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfield, long long fstride) {
+int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfield, long long fstride,
+               const T* topsrc = nullptr, T topscale = (T)0) {
     dim3 grid((unsigned)((c->NP + 127) / 128), nfield);
-    zderiv_phys_kernel<T><<<grid, 128, 0, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc, fstride);
+    zderiv_phys_kernel<T><<<grid, 128, 0, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc, fstride, topsrc,
+                                                       topscale);
     c->launches++;
     CKL();
     return SPARC_OK;
@@ -501,7 +519,8 @@ int mhd_create(sparc_ctx* c) {
     const size_t es = esz(c);
     int rc;
     if ((rc = dalloc(c, &m.bg, (size_t)MB_COUNT * c->N * es))) return rc;
-    if ((rc = dalloc(c, &m.pab, (size_t)2 * std::max(c->P.npmlbot, 1) * c->NP * es))) return rc;
+    CK(cudaMemsetAsync(m.bg, 0, (size_t)MB_COUNT * c->N * es, c->stream));   // 2-D leaves the y rows at 0
+    if ((rc = dalloc(c, &m.pab, (size_t)2 * std::max(c->nzpml, 1) * c->NP * es))) return rc;
     if ((rc = dalloc(c, &m.g, (size_t)c->nz * es))) return rc;
     if ((rc = dalloc(c, &m.sponge, (size_t)c->nz * es))) return rc;
     if ((rc = dalloc(c, (void**)&m.plane, (size_t)c->NP * sizeof(int)))) return rc;
@@ -513,6 +532,8 @@ int mhd_create(sparc_ctx* c) {
     const size_t pv = (size_t)c->S * PV_COUNT * std::max(c->nzpml, 1) * c->NP * es;
     if ((rc = dalloc(c, &m.pml, pv))) return rc;
     if ((rc = dalloc(c, &m.spml, pv))) return rc;
+    CK(cudaMemsetAsync(m.pml, 0, pv, c->stream));
+    CK(cudaMemsetAsync(m.spml, 0, pv, c->stream));   // 2-D never writes psi_dzby, psi_induction_by
     if ((rc = dalloc(c, &m.spec, (size_t)c->fs * csz(c)))) return rc;
     return SPARC_OK;
 }
@@ -671,17 +692,17 @@ int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const 
     // to the element type: background fields, bottom PML coefficients, tables
     const int src_of[MB_COUNT] = {W_BX, W_BY, W_BZ, W_CBX, W_CBY, W_CBZ, W_GP0X, W_GP0Y, W_GP0Z, W_GR0X,
                                   W_GR0Y, W_GR0Z, W_C2R, W_RHO, W_RI};
-    const long long nbp = (long long)std::max(nb, 1) * NP;
+    const long long nbp = (long long)std::max(nb, 1) * NP, npz = (long long)std::max(c->nzpml, 1) * NP;
     for (int i = 0; i < MB_COUNT; ++i) {
         if (c->f32) to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.bg + (size_t)i * N, W(src_of[i]), N);
         else to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.bg + (size_t)i * N, W(src_of[i]), N);
     }
     if (c->f32) {
         to_t_kernel<float><<<nb256(nbp), 256, 0, c->stream>>>((float*)m.pab, W(W_AZ), nbp);
-        to_t_kernel<float><<<nb256(nbp), 256, 0, c->stream>>>((float*)m.pab + nbp, W(W_BZP), nbp);
+        to_t_kernel<float><<<nb256(nbp), 256, 0, c->stream>>>((float*)m.pab + npz, W(W_BZP), nbp);
     } else {
         to_t_kernel<double><<<nb256(nbp), 256, 0, c->stream>>>((double*)m.pab, W(W_AZ), nbp);
-        to_t_kernel<double><<<nb256(nbp), 256, 0, c->stream>>>((double*)m.pab + nbp, W(W_BZP), nbp);
+        to_t_kernel<double><<<nb256(nbp), 256, 0, c->stream>>>((double*)m.pab + npz, W(W_BZP), nbp);
     }
     CKL();
     std::vector<double> dwv(NP, dw2);
@@ -709,6 +730,388 @@ int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const 
     return SPARC_OK;
 }
 
+// ---- option 18 (2-D, ny = 1) ---------------------------------------------------
+
+namespace {
+
+// DBYD1 (dbyd1.f) with ibc = 0 along x for n2 rows of n1: the DBYD2 compact
+// scheme with its coefficients in default REAL (the file declares no
+// kinds), zero end rows, solved by TRIDAG (tridag.f: Thomas with divisions)
+void host_dbyd1_ibc0(std::vector<double>& a, const double* b, int n1, long n2) {
+    const float d1i = (float)(n1 - 1);
+    const double C1 = (double)(d1i * 7.0f / 9.0f), C2 = (double)(d1i / 36.0f);
+    const double B1 = (double)(-43.0f / 96.0f * d1i), B2 = (double)(-5.0f / 6.0f * d1i);
+    const double B3 = (double)(9.0f / 8.0f * d1i), B4 = (double)(1.0f / 6.0f * d1i), B5 = (double)(-1.0f / 96.0f * d1i);
+    std::vector<double> uppr(n1 + 1, 0.0), lowr(n1 + 1, 0.0), diag(n1 + 1, 1.0), gam(n1 + 1), ud(n1 + 1), r(n1 + 1);
+    for (int J = 3; J <= n1 - 2; ++J) uppr[J] = (double)(1.0f / 3.0f);
+    uppr[2] = (double)(3.0f / 4.0f);
+    uppr[n1 - 1] = (double)(1.0f / 8.0f);
+    for (int I = 1; I <= n1; ++I) lowr[I] = uppr[n1 - I + 1];
+    lowr[n1] = 0.0;
+    a.assign((size_t)n1 * n2, 0.0);
+    for (long i = 0; i < n2; ++i) {
+        const double* B = b + i * n1 - 1;
+        for (int J = 3; J <= n1 - 2; ++J) r[J] = C1 * (B[J + 1] - B[J - 1]) + C2 * (B[J + 2] - B[J - 2]);
+        r[2] = B1 * B[1] + B2 * B[2] + B3 * B[3] + B4 * B[4] + B5 * B[5];
+        r[n1 - 1] = -(B1 * B[n1] + B2 * B[n1 - 1] + B3 * B[n1 - 2] + B4 * B[n1 - 3] + B5 * B[n1 - 4]);
+        r[1] = 0.0;
+        r[n1] = 0.0;
+        double bet = diag[1];
+        ud[1] = r[1] / bet;
+        for (int J = 2; J <= n1; ++J) {
+            gam[J] = uppr[J - 1] / bet;
+            bet = diag[J] - lowr[J] * gam[J];
+            ud[J] = (r[J] - lowr[J] * ud[J - 1]) / bet;
+        }
+        for (int J = n1 - 1; J >= 1; --J) ud[J] = ud[J] - gam[J + 1] * ud[J + 1];
+        for (int J = 1; J <= n1; ++J) a[(size_t)i * n1 + J - 1] = ud[J];
+    }
+}
+
+// physics2d.f90:154-172: non-dimensional background, B = (B_x, B_z) / dimb
+__global__ void mhd2d_read_kernel(double* p0, double* rho0, double* c2, double* bx, double* bz, long long n,
+                                  double dimrho, double dimc, double dimb) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    bx[t] = bx[t] / dimb;
+    bz[t] = bz[t] / dimb;
+    p0[t] = p0[t] / (dimrho * pow(dimc, 2.0));
+    rho0[t] = rho0[t] / dimrho;
+    c2[t] = pow(c2[t] / dimc, 2.0);
+}
+
+// PML of physics2d.f90:262-297 with the magnetic wave speed: tempin at
+// plane 1 (bottom) and nz-5 (top), factor 3*3 at both ends; a_z, b_z stored
+// in pmlindex order; g(k) decayed with the (1,1) column
+__global__ void mhd2d_pml_kernel(double* gp0z, double* gr0z, double* az, double* bzp, double* gk, const double* graw,
+                                 const double* c2, const double* rho0, const double* bx, const double* bz,
+                                 const double* z, const double* alph, long long NP, int nz, int nb, int nt) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NP * nz) return;
+    const int k = (int)(t / NP);
+    const long long q = t - (long long)k * NP;
+    const bool bot = k < nb, top = k >= nz - nt;
+    auto tempin = [&](int kk) {
+        const long long i = q + NP * kk;
+        return pow(c2[i] + (pow(bx[i], 2.0) + pow(bz[i], 2.0)) / rho0[i], 0.5);
+    };
+    double fdec = 1.0, dampz = 0.0;
+    if (bot) {
+        const double r = (z[nb - 1] - z[k]) / (z[nb - 1] - z[0]);
+        dampz = 3.0 * 3.0 * tempin(0) / (z[nb - 1] - z[0]) * (r * r);
+        fdec = alph[k] / (dampz + alph[k]);
+        gp0z[t] *= fdec; gr0z[t] *= fdec;
+        az[(long long)k * NP + q] = -dampz;
+        bzp[(long long)k * NP + q] = -alph[k] - dampz;
+    }
+    if (top) {
+        const double r = (z[nz - nt] - z[k]) / (z[nz - 1] - z[nz - nt]);
+        dampz = 3.0 * 3.0 * tempin(nz - 6) / (z[nz - 1] - z[nz - nt]) * (r * r);
+        fdec = alph[k] / (dampz + alph[k]);
+        gp0z[t] *= fdec; gr0z[t] *= fdec;
+        const long long ip = nb + (k - (nz - nt));
+        az[ip * NP + q] = -dampz;
+        bzp[ip * NP + q] = -alph[k] - dampz;
+    }
+    if (q == 0) gk[k] = (bot || top) ? graw[k] * fdec : graw[k];
+}
+
+}  // namespace
+
+int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const double* cs, const double* psi) {
+    MhdState& m = *c->mhd;
+    const int nz = c->nz, nb = c->P.npmlbot, nt = c->P.npmltop, nx = c->P.nx;
+    const long long N = c->N, NP = c->NP;
+    const std::vector<double>& z = c->zq;
+    enum { W_P, W_RHO, W_C2, W_PSI, W_BX, W_BZ, W_CBY, W_TMP, W_RI, W_C2R, W_GR0Z, W_GP0Z, W_GR0X, W_GP0X, W_AZ,
+           W_BZP, W_N };
+    double* w64 = nullptr;
+    int rc = dalloc(c, (void**)&w64, (size_t)W_N * N * 8);
+    if (rc) return rc;
+    auto W = [&](int i) { return w64 + (size_t)i * N; };
+    if ((rc = upload(c, W(W_P), p, N * 8)) || (rc = upload(c, W(W_RHO), rho, N * 8)) ||
+        (rc = upload(c, W(W_C2), cs, N * 8)) || (rc = upload(c, W(W_PSI), psi, N * 8)))
+        return rc;
+    // B_x = -d psi/dz (ddz, bc 1); B_z = DBYD1(psi) * stretchx (physics2d.f90:140-146)
+    if ((rc = ddz_launch<double>(c, c->zt64, W(W_PSI), W(W_BX), 1, 1, 0))) return rc;
+    axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_BX), W(W_BX), -1.0, nullptr, 0.0, N);
+    std::vector<double> bzh;
+    host_dbyd1_ibc0(bzh, psi, nx, (long)nz);
+    for (double& v : bzh) v = v * c->stretchx;
+    if ((rc = upload(c, W(W_BZ), bzh.data(), N * 8))) return rc;
+    const double dimb = std::sqrt(4.0 * c->pi * c->dimc * c->dimc * c->dimrho);
+    mhd2d_read_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_P), W(W_RHO), W(W_C2), W(W_BX), W(W_BZ), N, c->dimrho,
+                                                       c->dimc, dimb);
+    CKL();
+    // curl_y B0 = dBx/dz - dBz/dx (physics2d.f90:180-183), then the gradients
+    std::vector<double> rx(nx);
+    for (int k = 0; k < nx; ++k) {
+        const int kk = k < nx / 2 ? k : (k == nx / 2 ? 0 : k - nx);
+        rx[k] = (double)kk * c->normx * 2.0 * c->pi * c->stretchx;
+    }
+    double* rx64 = nullptr;
+    if ((rc = dalloc(c, (void**)&rx64, nx * 8)) || (rc = upload(c, rx64, rx.data(), nx * 8))) return rc;
+    void* rx0 = m.rx;
+    m.rx = rx64;
+    if ((rc = ddz_launch<double>(c, c->zt64, W(W_BX), W(W_CBY), 1, 1, 0)) ||
+        (rc = ddx_launch<double>(c, W(W_BZ), W(W_TMP), nz)))
+        return rc;
+    axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_CBY), W(W_CBY), 1.0, W(W_TMP), -1.0, N);
+    rhoinv_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_RI), W(W_C2R), W(W_RHO), W(W_C2), N);
+    if ((rc = ddz_launch<double>(c, c->zt64, W(W_RHO), W(W_GR0Z), 1, 1, 0)) ||
+        (rc = ddz_launch<double>(c, c->zt64, W(W_P), W(W_GP0Z), 1, 1, 0)))
+        return rc;
+    // PML and gravity
+    std::vector<double> alph(nz);
+    for (int k = 1; k <= nz; ++k) {
+        double a0 = c->pi * R4(0.005) * c->diml / c->dimc;
+        if (k < nb + 1) a0 = c->pi * R4(0.005) * c->diml / c->dimc * (z[k - 1] - z[0]) / (z[nb - 1] - z[0]);
+        if (k > nz - nt) a0 = c->pi * R4(0.005) * c->diml / c->dimc * (z[nz - 1] - z[k - 1]) / (z[nz - 1] - z[nz - nt]);
+        alph[k - 1] = a0;
+    }
+    double *d_z = nullptr, *d_alph = nullptr, *d_g = nullptr;
+    if ((rc = dalloc(c, (void**)&d_z, nz * 8)) || (rc = dalloc(c, (void**)&d_alph, nz * 8)) ||
+        (rc = dalloc(c, (void**)&d_g, nz * 8)))
+        return rc;
+    if ((rc = upload(c, d_z, z.data(), nz * 8)) || (rc = upload(c, d_alph, alph.data(), nz * 8))) return rc;
+    mhd2d_pml_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_GP0Z), W(W_GR0Z), W(W_AZ), W(W_BZP), d_g,
+                                                      c->zt64 + (size_t)ZT_GRAW * nz, W(W_C2), W(W_RHO), W(W_BX),
+                                                      W(W_BZ), d_z, d_alph, NP, nz, nb, nt);
+    CKL();
+    // horizontal gradients (physics2d.f90:318-321)
+    if ((rc = ddx_launch<double>(c, W(W_RHO), W(W_GR0X), nz)) || (rc = ddx_launch<double>(c, W(W_P), W(W_GP0X), nz)))
+        return rc;
+    m.rx = rx0;
+    {
+        std::vector<double> rxs(rx);
+        if (c->f32) {
+            std::vector<float> fx(rxs.begin(), rxs.end());
+            if ((rc = upload(c, m.rx, fx.data(), nx * 4))) return rc;
+        } else if ((rc = upload(c, m.rx, rxs.data(), nx * 8))) {
+            return rc;
+        }
+    }
+    // to the element type (the y components and the other curl components stay 0)
+    const int dst_of[] = {MB_BOX, MB_BOZ, MB_CBOY, MB_GP0X, MB_GP0Z, MB_GR0X, MB_GR0Z, MB_C2RHO0, MB_RHO0, MB_RHOINV};
+    const int src_of[] = {W_BX, W_BZ, W_CBY, W_GP0X, W_GP0Z, W_GR0X, W_GR0Z, W_C2R, W_RHO, W_RI};
+    const long long npz = (long long)std::max(c->nzpml, 1) * NP;
+    for (int i = 0; i < 10; ++i) {
+        if (c->f32) to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.bg + (size_t)dst_of[i] * N, W(src_of[i]), N);
+        else to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.bg + (size_t)dst_of[i] * N, W(src_of[i]), N);
+    }
+    if (c->f32) {
+        to_t_kernel<float><<<nb256(npz), 256, 0, c->stream>>>((float*)m.pab, W(W_AZ), npz);
+        to_t_kernel<float><<<nb256(npz), 256, 0, c->stream>>>((float*)m.pab + npz, W(W_BZP), npz);
+        to_t_kernel<float><<<1, 256, 0, c->stream>>>((float*)m.g, d_g, nz);
+    } else {
+        to_t_kernel<double><<<nb256(npz), 256, 0, c->stream>>>((double*)m.pab, W(W_AZ), npz);
+        to_t_kernel<double><<<nb256(npz), 256, 0, c->stream>>>((double*)m.pab + npz, W(W_BZP), npz);
+        to_t_kernel<double><<<1, 256, 0, c->stream>>>((double*)m.g, d_g, nz);
+    }
+    CKL();
+    // source planes: erad_2d = e_rad, orad_2d = o_rad (physics2d.f90:334-341)
+    const int k2 = c->P.compute_adjoint ? c->o_rad : c->e_rad;
+    const int ks = c->P.src_k > 0 ? c->P.src_k : k2;
+    std::vector<int> plane(NP, ks - 1), plane_obs(NP, c->o_rad - 1);
+    std::vector<double> dwv(NP, 2.0 / (z[k2] - z[k2 - 2]));
+    if (c->f32) {
+        std::vector<float> d32(dwv.begin(), dwv.end());
+        if ((rc = upload(c, m.dw, d32.data(), NP * 4))) return rc;
+    } else if ((rc = upload(c, m.dw, dwv.data(), NP * 8))) {
+        return rc;
+    }
+    if ((rc = upload(c, m.plane, plane.data(), NP * sizeof(int))) ||
+        (rc = upload(c, m.plane_obs, plane_obs.data(), NP * sizeof(int))))
+        return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    for (void* pp : {(void*)w64, (void*)d_z, (void*)d_alph, (void*)d_g}) {
+        auto it = std::find(c->allocs.begin(), c->allocs.end(), pp);
+        if (it != c->allocs.end()) c->allocs.erase(it);
+        cudaFree(pp);
+    }
+    c->dev_bytes -= (long long)W_N * N * 8 + 3LL * nz * 8;
+    m.have_bg = true;
+    return SPARC_OK;
+}
+
+namespace {
+
+// 2-D stage kernels (MP_MHD_PML_2D_DISPL, physics2d.f90:724-943)
+template <typename T>
+__global__ void mhd2d_div_kernel(const MhdArgs A, const T* __restrict__ bg, T* __restrict__ work, const T* __restrict__ pab,
+                                 const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    const T dz = pml_bottom<T>(A, t, s, PV_VZ, w[MW_DZ * A.N + t], pab, pml, spml, beta, hs);
+    const T div = w[MW_DX * A.N + t] + dz;
+    const T xx = w[MW_T0 * A.N + t], xz = w[MW_T2 * A.N + t];
+    w[MW_P * A.N + t] = -bg[MB_C2RHO0 * A.N + t] * div - xz * bg[MB_GP0Z * A.N + t] - xx * bg[MB_GP0X * A.N + t];
+    w[MW_R * A.N + t] = -bg[MB_RHO0 * A.N + t] * div - xz * bg[MB_GR0Z * A.N + t] - xx * bg[MB_GR0X * A.N + t];
+}
+
+template <typename T>
+__global__ void mhd2d_b_kernel(const MhdArgs A, T* __restrict__ work, const T* __restrict__ pab, const T* __restrict__ pml,
+                               T* __restrict__ spml, T beta, int hs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    w[MW_BX * A.N + t] = -pml_bottom<T>(A, t, s, PV_IBX, w[MW_BX * A.N + t], pab, pml, spml, beta, hs);
+}
+
+template <typename T>
+__global__ void mhd2d_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __restrict__ work, const T* __restrict__ pab,
+                                 const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs, const T* __restrict__ gz,
+                                 T* __restrict__ scr) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const int k = (int)(t / A.NP);
+    T* w = work + (long long)s * MW_COUNT * A.N;
+    const T dzbx = pml_bottom<T>(A, t, s, PV_DZBX, w[MW_DZBX * A.N + t], pab, pml, spml, beta, hs);
+    const T cby = -w[MW_CBY * A.N + t] + dzbx;
+    const T box = bg[MB_BOX * A.N + t], boz = bg[MB_BOZ * A.N + t], cboy = bg[MB_CBOY * A.N + t];
+    const T ri = bg[MB_RHOINV * A.N + t];
+    T rvx = ri * (-w[MW_GPX * A.N + t] + cby * boz);
+    T rvz = ri * (-w[MW_GPZ * A.N + t] + (-cby * box));
+    rvx = rvx + ri * (cboy * w[MW_BZ * A.N + t]);
+    rvz = rvz + ri * (-cboy * w[MW_BX * A.N + t]);
+    rvz = rvz - ri * w[MW_R * A.N + t] * gz[k];
+    T* ss = scr + (long long)s * 6 * A.FS;
+    ss[0 * A.FS + t] = w[MW_T3 * A.N + t];
+    ss[1 * A.FS + t] = (T)0;
+    ss[2 * A.FS + t] = w[MW_T5 * A.N + t];
+    ss[3 * A.FS + t] = rvx;
+    ss[4 * A.FS + t] = (T)0;
+    ss[5 * A.FS + t] = rvz;
+}
+
+// damping of v_x, v_z (DX, DZ), the source while time <= forcing_length *
+// cadforcing_step (forward: vr * fwdsource / rho0 * dw; adjoint: forcing * dw
+// / rho0), and the zero bottom row (physics2d.f90:897-938)
+template <typename T>
+__global__ void mhd2d_final_kernel(const MhdArgs A, const T* __restrict__ bg, const T* __restrict__ work, int damp,
+                                   T* __restrict__ scr, SlotClock clk, int src_mode, const T* __restrict__ planes,
+                                   long long plane_ss, int L, const double* __restrict__ series, int nseries,
+                                   const int* __restrict__ plane, const T* __restrict__ dw, int adjoint) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const int k = (int)(t / A.NP);
+    const long long q = t - (long long)k * A.NP;
+    const T* w = work + (long long)s * MW_COUNT * A.N;
+    T* ss = scr + (long long)s * 6 * A.FS;
+    if (damp) {
+        ss[3 * A.FS + t] = ss[3 * A.FS + t] - w[MW_DX * A.N + t];
+        ss[5 * A.FS + t] = ss[5 * A.FS + t] - w[MW_DZ * A.N + t];
+    }
+    if (src_mode != 0 && k == plane[q]) {
+        const int tl = *clk.time - clk.t0[s];
+        if (tl >= 0 && tl <= clk.gate) {
+            const T* pl = planes + (long long)s * plane_ss + q;
+            T F = (T)0;
+            if (src_mode == 1) {
+                const T wt = (tl < nseries) ? (T)series[(long long)s * nseries + tl] : (T)0;
+                F = wt * pl[0];
+            } else {
+                for (int l = 0; l < 7; ++l) {
+                    int id;
+                    const double wl = lagrange_weight(clk, tl, L, l, &id);
+                    if (id >= 0) F = F + (T)wl * pl[(long long)id * A.NP];
+                }
+            }
+            const T r0 = bg[MB_RHO0 * A.N + t];
+            ss[5 * A.FS + t] = ss[5 * A.FS + t] + (adjoint ? F * dw[q] / r0 : F / r0 * dw[q]);
+        }
+    }
+    if (k == 0) {
+        #pragma unroll
+        for (int f = 0; f < 6; ++f) ss[f * A.FS + t] = (T)0;
+    }
+}
+
+template <typename T>
+int mhd2d_stage(sparc_ctx* c, T beta, int hs) {
+    MhdState& m = *c->mhd;
+    const int S = c->active_n, nz = c->nz;
+    MhdArgs A;
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
+    A.nzpml = std::max(c->nzpml, 1);
+    A.S = S;
+    A.both = 1;
+    T* bg = (T*)m.bg;
+    T* work = (T*)m.work;
+    const T* pab = (const T*)m.pab;
+    T* pml = (T*)m.pml;
+    T* spml = (T*)m.spml;
+    const T* zt = (const T*)c->zt;
+    const long long N = c->N, fst = (long long)MW_COUNT * N;
+    const dim3 g(nb256(N), S);
+    auto Wp = [&](int s, int f) { return work + ((size_t)s * MW_COUNT + f) * N; };
+    int rc;
+    mhd_temp_kernel<T><<<g, 256, 0, c->stream>>>(A, (const T*)c->a, (const T*)c->scr, beta, hs, bg, work);
+    c->launches++;
+    CKL();
+    // d(xi_x)/dx; d(xi_z)/dz with bc 3, the top value -dxixdx(nz) * unstretch(nz) (physics2d.f90:731-733)
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_T0), Wp(s, MW_DX), nz))) return rc;
+    const T unstr = (T)c->zt_host[(size_t)ZT_UNSTRETCH * nz + nz - 1];
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_T2), Wp(0, MW_DZ), 3, S, fst, Wp(0, MW_DX), -unstr))) return rc;
+    mhd2d_div_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // grad p: ddx(p); ddz(p, bc 2) with the caller-set bottom value 0 (every reachable state)
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPX), nz))) return rc;
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 2, S, fst))) return rc;
+    mhd_pmlp_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // induction: bx = -(d flux2/dz + psi), bz = d flux2/dx
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_F2), Wp(s, MW_BZ), nz))) return rc;
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_F2), Wp(0, MW_BX), 0, S, fst))) return rc;
+    mhd2d_b_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
+    c->launches++;
+    CKL();
+    // curl_y b = -d bz/dx + (d bx/dz + psi)
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBY), nz))) return rc;
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_BX), Wp(0, MW_DZBX), 0, S, fst))) return rc;
+    mhd2d_rhs_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs, (const T*)m.g, (T*)c->scr);
+    c->launches++;
+    CKL();
+    const bool damp = c->P.damp_waves != 0;
+    if (damp) {
+        typedef typename CplxOf<T>::type CT;
+        for (int s = 0; s < S; ++s)
+            for (int q = 0; q < 2; ++q) {
+                const int src = q == 0 ? MW_T3 : MW_T5, dst = q == 0 ? MW_DX : MW_DZ;
+                fft_phys_to_spec<T>(Wp(s, src), (CT*)m.spec, (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream);
+                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, dst), (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream);
+                c->launches += 5;
+            }
+        CKL();
+    }
+    SlotClock clk;
+    memset(&clk, 0, sizeof(clk));
+    clk.t0 = c->d_t0; clk.time = c->d_time; clk.freq = c->freq_filtering; clk.two_d = 1;
+    clk.gate = c->forcing_length * c->cadforcing_step; clk.num_steps = c->num_steps;
+    clk.ts = R4(c->P.timestep); clk.cad = R4(c->P.cadforcing);
+    mhd2d_final_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, damp ? 1 : 0, (T*)c->scr, clk, c->src_mode,
+                                                     (const T*)c->planes, (long long)c->src_L * c->NP, c->src_L,
+                                                     c->series, c->nseries, m.plane, (const T*)m.dw,
+                                                     c->P.compute_adjoint ? 1 : 0);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+}  // namespace
+
 namespace {
 
 template <typename T>
@@ -716,8 +1119,10 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
     MhdState& m = *c->mhd;
     const int S = c->active_n, nz = c->nz;
     MhdArgs A;
-    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nzpml = std::max(c->nzpml, 1);
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
+    A.nzpml = std::max(c->nzpml, 1);
     A.S = S;
+    A.both = (c->P.option == 18);
     T* a = (T*)c->a;
     T* scr = (T*)c->scr;
     T* bg = (T*)m.bg;
@@ -748,7 +1153,7 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
             return rc;
     }
     if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 0, S, (long long)MW_COUNT * N))) return rc;
-    mhd_pmlp_kernel<T><<<dim3(nb256((long long)A.nb * c->NP), S), 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
+    mhd_pmlp_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
     c->launches++;
     CKL();
     // induction: ddxyz(flux3, by, flux3, bx, flux2, dzflux2); ddxyz(flux2, bz, flux1, flux3, flux1, dzflux1)
@@ -809,26 +1214,33 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
     MhdState& m = *c->mhd;
     typedef typename CplxOf<T>::type CT;
     MhdArgs A;
-    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = c->nz; A.nb = c->P.npmlbot; A.nzpml = std::max(c->nzpml, 1);
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = c->nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
+    A.nzpml = std::max(c->nzpml, 1);
     A.S = c->active_n;
+    A.both = (c->P.option == 18);
     const int S = c->active_n;
     for (int it = 0; it < nsteps; ++it) {
         int rc;
-        for (int rk = 0; rk < 5; ++rk)
-            if ((rc = mhd_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0))) return rc;
+        const bool two_d = (c->P.option == 18);
+        for (int rk = 0; rk < 5; ++rk) {
+            rc = two_d ? mhd2d_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0)
+                       : mhd_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0);
+            if (rc) return rc;
+        }
         // update + z filter (step.f90:114-116, FILTER_VARS_3D)
         mhd_update_kernel<T><<<dim3((unsigned)((c->NP + 127) / 128), 6 * S), 128, 0, c->stream>>>(
-            A, (T*)c->a, (const T*)c->scr, (T)c->deltat);
+            A, (T*)c->a, (const T*)c->scr, (T)c->deltat, two_d ? 1 : 0);
         const long long npv = (long long)S * PV_COUNT * A.nzpml * c->NP;
         mhd_pml_update_kernel<T><<<nb256(npv), 256, 0, c->stream>>>((T*)m.pml, (const T*)m.spml, (T)c->deltat, npv);
         c->launches += 2;
         CKL();
-        // horizontal filter every freq_filtering steps of each slot's clock on
-        // fields 1..5 (physics.f90:791-830)
+        // horizontal filter every freq_filtering steps of each slot's clock:
+        // 3-D on fields 1..5 when mod(time, 30) = 0 (physics.f90:791-830),
+        // 2-D on all six when mod(time+1, 30) = 0 (physics2d.f90:566-584)
         for (int s = 0; s < S; ++s) {
             const int tl = c->time - c->t0[s];
-            if (tl < 0 || tl % c->freq_filtering != 0) continue;
-            for (int f = 0; f < 5; ++f) {
+            if (tl < 0 || (two_d ? (tl + 1) : tl) % c->freq_filtering != 0) continue;
+            for (int f = 0; f < (two_d ? 6 : 5); ++f) {
                 T* fp = (T*)c->a + ((size_t)s * 6 + f) * 2 * c->fs;
                 fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
                 launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 3, c->M, c->nz, 1, 0, 0, c->stream);
@@ -855,6 +1267,8 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
 }  // namespace
 
 int mhd_steps(sparc_ctx* c, int nsteps) {
-    if (!c->mhd || !c->mhd->have_bg) return fail(c, SPARC_ESTATE, "option 10 needs sparc_gpu_set_mhd_background");
+    if (!c->mhd || !c->mhd->have_bg)
+        return fail(c, SPARC_ESTATE, c->P.option == 18 ? "option 18 needs sparc_gpu_set_mhd2d_background"
+                                                        : "option 10 needs sparc_gpu_set_mhd_background");
     return c->f32 ? mhd_steps_t<float>(c, nsteps) : mhd_steps_t<double>(c, nsteps);
 }

@@ -40,6 +40,7 @@ EXPORTS = [
     "sparc_gpu_kernels", "sparc_gpu_ddx", "sparc_gpu_ddy", "sparc_gpu_ddz", "sparc_gpu_damp",
     "sparc_gpu_stream", "sparc_gpu_launch_count", "sparc_gpu_device_bytes", "sparc_gpu_info",
     "sparc_gpu_sync", "sparc_gpu_spec_to_phys_noalloc", "sparc_gpu_autotune", "sparc_gpu_set_mhd_background",
+    "sparc_gpu_set_mhd2d_background",
 ]
 
 
@@ -119,6 +120,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_spec_to_phys_noalloc": ([P, P, P, I, P], I),
         "sparc_gpu_autotune": ([P, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)], I),
         "sparc_gpu_set_mhd_background": ([P, D, D, D, D, D, D], I),
+        "sparc_gpu_set_mhd2d_background": ([P, D, D, D, D], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

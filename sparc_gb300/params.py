@@ -23,7 +23,9 @@ OPT_QUIET_PML_3D = 2           # pml.f90:12 (MP_QUIET_PML_3D), velocity form
 OPT_QUIET_PML_3D_DISPL = 4     # displacement.f90:482 (MP_QUIET_PML_3D_DISPL)
 OPT_MHD_PML_3D_DISPL = 10      # displacement.f90:663 (MP_MHD_PML_3D_DISPL)
 OPT_QUIET_PML_2D_DISPL = 17    # physics2d.f90:948 (MP_QUIET_PML_2D_DISPL)
-SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_MHD_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL)
+OPT_MHD_PML_2D_DISPL = 18      # physics2d.f90:724 (MP_MHD_PML_2D_DISPL)
+SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_MHD_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL,
+                     OPT_MHD_PML_2D_DISPL)
 
 
 def r4(x: float) -> float:
@@ -61,8 +63,8 @@ class SparcParams:
     def validate(self) -> None:
         if self.option not in SUPPORTED_OPTIONS:
             raise ValueError(f"option {self.option} not supported (have {SUPPORTED_OPTIONS})")
-        if self.option == OPT_QUIET_PML_2D_DISPL and self.ny != 1:
-            raise ValueError("option 17 (2-D) needs ny == 1")
+        if self.option in (OPT_QUIET_PML_2D_DISPL, OPT_MHD_PML_2D_DISPL) and self.ny != 1:
+            raise ValueError(f"option {self.option} (2-D) needs ny == 1")
         for n in (self.nx,) + ((self.ny,) if self.ny > 1 else ()):
             if n < 4 or (n & (n - 1)) != 0 or n > 1024:
                 raise ValueError(f"horizontal size {n} must be a power of two in [4, 1024]")
@@ -162,7 +164,8 @@ class SparcParams:
 
     def instruction(self, text: str) -> "SparcParams":
         """Apply an Instruction file (initialize.f90:1006-1051): line 1
-        'spectral' | 'adjoint', line 2 '2D' or not."""
+        'spectral' | 'adjoint', line 2 '2D' or not; 2D turns option 4 into 17
+        and option 10 into 18 (PARSE_OPTIONS, initialize.f90:778-824)."""
         lines = [l.strip() for l in text.strip().splitlines()]
         kind = lines[0].lower() if lines else "spectral"
         two_d = len(lines) > 1 and lines[1].upper() == "2D"
@@ -170,9 +173,8 @@ class SparcParams:
         if two_d:
             if self.option == OPT_QUIET_PML_3D:
                 raise ValueError("the 2-D velocity form (option 6) is not supported")
-            if self.option == OPT_MHD_PML_3D_DISPL:
-                raise ValueError("the 2-D MHD form (option 18) is not supported")
-            p = p.replace(option=OPT_QUIET_PML_2D_DISPL, ny=1)
+            two_d_of = {OPT_QUIET_PML_3D_DISPL: OPT_QUIET_PML_2D_DISPL, OPT_MHD_PML_3D_DISPL: OPT_MHD_PML_2D_DISPL}
+            p = p.replace(option=two_d_of.get(self.option, self.option), ny=1)
         return p
 
 

@@ -160,8 +160,8 @@ class Solver:
 
     @property
     def npv(self) -> int:
-        """PML auxiliary fields: six for the MHD form (option 10), else two."""
-        return 6 if self.p.option == 10 else 2
+        """PML auxiliary fields: six for the MHD forms (options 10, 18), else two."""
+        return 6 if self.p.option in (10, 18) else 2
 
     def set_mhd_background(self, rho, c, p, bx, by, bz):
         """3-D cgs background of option 10 (density, sound speed, pressure,
@@ -169,6 +169,12 @@ class Solver:
         the one the source planes are searched on."""
         arrs = [_f64(np.asarray(v, dtype=np.float64).reshape(self.shape)) for v in (rho, c, p, bx, by, bz)]
         self._ck(self.L.sparc_gpu_set_mhd_background(self.h, *[_dp(v) for v in arrs]))
+
+    def set_mhd2d_background(self, rho, c, p, psi):
+        """2-D cgs background of option 18 (density, sound speed, pressure and
+        the vector potential psi), each (nz, 1, nx) or (nz, nx)."""
+        arrs = [_f64(np.asarray(v, dtype=np.float64).reshape(self.shape)) for v in (rho, c, p, psi)]
+        self._ck(self.L.sparc_gpu_set_mhd2d_background(self.h, *[_dp(v) for v in arrs]))
 
     def state(self, slot: int = 0):
         a = np.zeros((6,) + self.shape)
@@ -183,6 +189,8 @@ class Solver:
         pp = None
         if pml is not None:
             pml = _f64(pml)
+            if pml.shape != (self.npv, self.p.nzpml, self.p.ny, self.p.nx):
+                raise ValueError(f"PML state must be ({self.npv}, {self.p.nzpml}, {self.p.ny}, {self.p.nx})")
             pp = _dp(pml)
         self._ck(self.L.sparc_gpu_set_state(self.h, slot, _dp(a), pp))
 

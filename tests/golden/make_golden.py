@@ -2,7 +2,7 @@
 seeded cases (compact derivative for every boundary code, spectral
 derivatives, damping, three 3-D time steps with a forward source, thirty-one
 2-D time steps, thirty-one velocity-form steps, five MHD steps on a flux
-tube, one kernel accumulation).  Regenerate with
+tube, thirty-one 2-D MHD steps on a flux sheet, one kernel accumulation).  Regenerate with
     python tests/golden/make_golden.py
 The GPU parity tests compare the CUDA path against these fixtures as well as
 against the live oracle."""
@@ -42,6 +42,16 @@ def golden_mhd_background(p):
     return flux_tube_background(p, table_for(p), b_surf=800.0, r_surf_mm=8.0)
 
 
+def golden_params_mhd2d():
+    """2-D MHD displacement form (option 18): PML at both ends, flux sheet."""
+    return small_params_2d(nx=32, nz=32, npmlbot=4, npmltop=4, option=18)
+
+
+def golden_mhd2d_background(p):
+    from sparc_gb300.background import flux_sheet_background
+    return flux_sheet_background(p, table_for(p), b_surf=300.0, w_mm=10.0)
+
+
 def golden_inputs(p, seed):
     rng = np.random.default_rng(seed)
     a = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
@@ -54,8 +64,11 @@ def golden_inputs(p, seed):
         a[0] = 0.0
         a[4] = 0.0
         a[5] = 0.0
-    pml = rng.standard_normal((6 if p.option == 10 else 2, p.nzpml, p.ny, p.nx)) * 1e-5
+    pml = rng.standard_normal((6 if p.option in (10, 18) else 2, p.nzpml, p.ny, p.nx)) * 1e-5
     pml[1, 0] = 0.0
+    if p.option == 18:
+        pml[3] = 0.0                   # psi_dzby, psi_induction_by: not in the 2-D form
+        pml[5] = 0.0
     x = (np.arange(p.nx) / p.nx - 0.5) * p.xlength / 1e8
     if p.ny == 1:
         plane = np.exp(-x ** 2 / 2.0)[None, :]
@@ -117,6 +130,17 @@ def compute():
     st, _, pm = om.state()
     out["step5_mhd_a"] = st
     out["step5_mhd_pml"] = pm
+    # 2-D MHD: 31 steps cover the horizontal filter at mod(time+1, 30) = 0
+    p18 = golden_params_mhd2d()
+    o18 = O.Oracle(p18, table_for(p18))
+    o18.set_mhd2d(*golden_mhd2d_background(p18))
+    a, pml, plane, series = golden_inputs(p18, 49)
+    o18.set_state(a * 1e-3, pml)
+    o18.set_source(1, plane[None].copy(), series)
+    o18.step(31)
+    st, _, pm = o18.state()
+    out["step31_mhd2d_a"] = st
+    out["step31_mhd2d_pml"] = pm
     # one kernel accumulation on seeded fields
     rng = np.random.default_rng(46)
     fwd = rng.standard_normal((6, p.nz, p.ny, p.nx))

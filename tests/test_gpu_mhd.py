@@ -102,3 +102,107 @@ def test_mhd_fp32_and_records(gpu_lib, oracle_mod):
     assert rel_l2(r32, r64) < 1e-4
     assert np.abs(r64[1]).max() > 0
     assert rel_l2(r64[1], a64[5, int(orad) - 1]) < 1e-15     # record 1 = v_z after the step at time 15
+
+
+# ---- option 18: MP_MHD_PML_2D_DISPL (physics2d.f90:724-943) on a flux sheet ----
+
+def _case2d(prec="f64", **kw):
+    sys.path.insert(0, os.path.dirname(__file__))
+    from golden.make_golden import golden_mhd2d_background, golden_params_mhd2d
+    p = golden_params_mhd2d().replace(precision=prec, **kw)
+    return p, table_for(p), golden_mhd2d_background(p)
+
+
+def _state2d(p, seed):
+    """A state the reference can reach: no y components, psi_p zero on the
+    bottom plane (ddz's bc 2 reads it as the caller-set value, which the
+    reference leaves at 0), the 3-D-only auxiliaries zero."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((6, p.nz, 1, p.nx)) * 1e-6
+    a[1] = 0.0
+    a[4] = 0.0
+    pml = rng.standard_normal((6, p.nzpml, 1, p.nx)) * 1e-8
+    pml[1, 0] = 0.0
+    pml[3] = 0.0
+    pml[5] = 0.0
+    return a, pml
+
+
+@pytest.mark.parametrize("nsteps,mode,adjoint", [(1, 1, False), (31, 1, False), (31, 2, True)])
+def test_mhd2d_matches_oracle(gpu_lib, oracle_mod, nsteps, mode, adjoint):
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case2d(compute_adjoint=adjoint, compute_forward=not adjoint)
+    g, o = Solver(p, tab), oracle_mod.Oracle(p, tab)
+    g.set_mhd2d_background(*bg)
+    o.set_mhd2d(*bg)
+    a0, pml0 = _state2d(p, 33)
+    g.set_state(a0, pml0)
+    o.set_state(a0, pml0)
+    if mode == 1:
+        plane = gaussian_plane(p, sigma_mm=8.0)
+        series = oracle_mod.forward_source(p, 200) * 1e3
+        g.set_source_series(plane, series)
+        o.set_source(1, plane[None].copy(), series)
+    else:
+        planes = np.random.default_rng(7).standard_normal((12, 1, p.nx)) * 1e-4
+        g.set_source_lagrange(planes)
+        o.set_source(2, planes, None)
+    g.step(nsteps)
+    o.step(nsteps)
+    ag, pg = g.state()
+    ao, _, po = o.state()
+    for f in (0, 2, 3, 5):
+        assert rel_l2(ag[f], ao[f]) < TOL64, (f, rel_l2(ag[f], ao[f]))
+    assert np.abs(ag[1]).max() == 0 and np.abs(ag[4]).max() == 0
+    for f in (0, 1, 2, 4):
+        assert rel_l2(pg[f], po[f]) < TOL64, ("pml", f, rel_l2(pg[f], po[f]))
+    assert np.abs(pg[3]).max() == 0 and np.abs(pg[5]).max() == 0
+
+
+def test_mhd2d_matches_committed_fixture(gpu_lib):
+    from sparc_gb300.solver import Solver
+    from golden.make_golden import golden_inputs
+    p, tab, bg = _case2d()
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_golden.npz"))
+    s = Solver(p, tab)
+    s.set_mhd2d_background(*bg)
+    a, pml, plane, series = golden_inputs(p, 49)
+    s.set_state(a * 1e-3, pml)
+    s.set_source_series(plane, series)
+    s.step(31)
+    st, pm = s.state()
+    for f in (0, 2, 3, 5):
+        assert rel_l2(st[f], g["step31_mhd2d_a"][f]) < TOL64, f
+    assert rel_l2(pm, g["step31_mhd2d_pml"]) < TOL64
+
+
+def test_mhd2d_fp32_and_records(gpu_lib, oracle_mod):
+    from sparc_gb300.solver import Solver
+    out = []
+    for prec in ("f64", "f32"):
+        p, tab, bg = _case2d(prec)
+        s = Solver(p, tab)
+        s.set_mhd2d_background(*bg)
+        a0, pml0 = _state2d(p, 34)
+        s.set_state(a0, pml0)
+        s.set_source_series(gaussian_plane(p, sigma_mm=8.0), oracle_mod.forward_source(p, 200) * 1e3)
+        s.record_surface(4)
+        s.step(31)
+        out.append((s.state()[0], s.records(), s.info()["o_rad"]))
+    (a64, r64, orad), (a32, r32, _) = out
+    for f in (0, 2, 3, 5):
+        assert rel_l2(a32[f], a64[f]) < 1e-4, (f, rel_l2(a32[f], a64[f]))
+    assert r64.shape[0] == 3                                    # times 0, 15, 30
+    assert rel_l2(r32, r64) < 1e-4
+    assert rel_l2(r64[2], a64[5, int(orad) - 1]) < 1e-15     # record 2 = v_z after the step at time 30
+
+
+def test_mhd2d_needs_its_background(gpu_lib):
+    from sparc_gb300.native import SparcError
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case2d()
+    s = Solver(p, tab)
+    with pytest.raises(SparcError):
+        s.step(1)
+    with pytest.raises(SparcError):
+        s.set_mhd_background(*bg[:3], bg[3], bg[3], bg[3])      # the 3-D call belongs to option 10

@@ -41,12 +41,14 @@ def test_params_i_parsing_and_instruction():
 
 
 def test_params_magnetic_selects_option_10():
-    """PARSE_OPTIONS (initialize.f90:778-824): MAGNETIC + DISPL + USE_PML -> 10;
-    the 2-D MHD form (18), the MHD velocity form (8) and FLOWS are not built."""
+    """PARSE_OPTIONS (initialize.f90:778-824): MAGNETIC + DISPL + USE_PML -> 10,
+    and 18 with a 2D instruction; the MHD velocity form (8) and FLOWS are not built."""
     mag = PARAMS_I.replace("magnetic = .false.", "magnetic = .true.")
     assert SparcParams.from_params_i(mag).option == 10
+    q = SparcParams.from_params_i(mag).instruction("adjoint\n2D\n")
+    assert q.option == 18 and q.ny == 1 and q.compute_adjoint
     with pytest.raises(ValueError):
-        SparcParams.from_params_i(mag).instruction("spectral\n2D\n")
+        SparcParams(option=18, ny=4).validate()
     with pytest.raises(ValueError):
         SparcParams.from_params_i(mag + "logical, parameter :: DISPL = .false.\n")
     with pytest.raises(ValueError):

@@ -266,3 +266,113 @@ def test_mhd_runs_and_drives_the_induction_pml():
     assert np.isfinite(st).all() and np.isfinite(pml).all()
     assert pml.shape[0] == 6
     assert np.abs(pml[2:]).max() > 0          # psi_dzbx, psi_dzby, psi_induction_bx/by are driven
+
+
+def _mhd2d_case(nx=32, nz=32, b_surf=300.0):
+    from cases import small_params_2d, table_for
+    from sparc_gb300.background import flux_sheet_background
+    p = small_params_2d(nx=nx, nz=nz, npmlbot=4, npmltop=4, option=18)
+    tab = table_for(p)
+    return p, tab, flux_sheet_background(p, tab, b_surf=b_surf)
+
+
+def _dbyd1_ibc0_dense(b, n1):
+    """DBYD1 (dbyd1.f) with ibc 0 as a dense solve: REAL*4 coefficients,
+    rows 1 and n1 of the right side zero, the tridiagonal system with
+    diagonal 1, upper (0, 3/4, 1/3 ..., 1/8, 0) and its mirror below."""
+    f = np.float32
+    d1i = f(n1 - 1)
+    c1, c2 = float(d1i * f(7) / f(9)), float(d1i / f(36))
+    bc = [float(f(-43) / f(96) * d1i), float(f(-5) / f(6) * d1i), float(f(9) / f(8) * d1i),
+          float(f(1) / f(6) * d1i), float(f(-1) / f(96) * d1i)]
+    up = np.zeros(n1)
+    up[2:n1 - 2] = float(f(1) / f(3))
+    up[1] = float(f(3) / f(4))
+    up[n1 - 2] = float(f(1) / f(8))
+    lo = up[::-1].copy()
+    lo[n1 - 1] = 0.0
+    M = np.eye(n1) + np.diag(up[:-1], 1) + np.diag(lo[1:], -1)
+    r = np.zeros(b.shape)
+    r[..., 2:n1 - 2] = c1 * (b[..., 3:n1 - 1] - b[..., 1:n1 - 3]) + c2 * (b[..., 4:] - b[..., :n1 - 4])
+    r[..., 1] = sum(bc[i] * b[..., i] for i in range(5))
+    r[..., n1 - 2] = -sum(bc[i] * b[..., n1 - 1 - i] for i in range(5))
+    return np.linalg.solve(M, r.reshape(-1, n1).T).T.reshape(b.shape)
+
+
+def test_mhd2d_setup_follows_the_reference_order():
+    """mp_Initialize_RHS_2d's magnetic part (physics2d.f90:106-195): B_x =
+    -d psi/dz, B_z = DBYD1(psi) stretchx, curl_y B0 = dBx/dz - dBz/dx, the
+    PML at both ends, against numpy twins."""
+    from oracle import oracle as O
+    p, tab, (rho, c, pr, psi) = _mhd2d_case()
+    o = O.Oracle(p, tab)
+    o.set_mhd2d(rho, c, pr, psi)
+    m = o.mhd_profiles()
+    info = o.info()
+    dimc, dimrho = info["dimc"], info["dimrho"]
+    dimb = np.sqrt(4.0 * info["pi"] * dimc ** 2 * dimrho)
+    stretchx = info["rsun"] / float(np.float32(p.xlength))
+    assert rel_l2(m["box"], -o.ddz(psi, 1) / dimb) < 1e-14
+    assert rel_l2(m["boz"], _dbyd1_ibc0_dense(psi, p.nx) * stretchx / dimb) < 1e-12
+    assert np.abs(m["boy"]).max() == 0.0 and np.abs(m["curlbox"]).max() == 0.0
+    assert rel_l2(m["curlboy"], o.ddz(m["box"], 1) - o.ddx(m["boz"])) < 1e-14
+    # B_z a plane below the fade is close to the generator's field (DBYD1
+    # spans the box with n-1 intervals, so the scale is n/(n-1) off)
+    z_cm = (tab[:, 0] - 1.0) * 69598946770.0
+    k0 = int(np.argmin(np.abs(z_cm + 1.0e8)))
+    bz_cgs = m["boz"][k0, 0] * dimb
+    assert abs(bz_cgs.max() / 300.0 - 1.0) < 0.1, bz_cgs.max()
+    # PML: a_z = -dampz in both layers, zero on each layer's inner plane and
+    # growing towards the edge
+    az = m["az"][:, 0, p.nx // 2]
+    assert (az[:3] < 0).all() and (az[-3:] < 0).all() and np.all(az[3:-3] == 0)
+    assert az[0] < az[1] < az[2] and az[-1] < az[-2] < az[-3]
+    assert np.array_equal(m["gradp0_x"], o.ddx(pr / (dimrho * dimc ** 2)))
+
+
+def test_mhd2d_without_field_is_the_quiet_2d_form():
+    """With psi = 0 every magnetic term vanishes and option 18 steps as
+    option 17 does (physics2d.f90:724-943 against :948-1105, same filter
+    cadence) once damping is off: option 18 calls DAMP_VELOCITY, option 17
+    never does."""
+    from oracle import oracle as O
+    from cases import random_state
+    p, tab, (rho, c, pr, psi) = _mhd2d_case()
+    p = p.replace(damp_waves=False)
+    p17 = p.replace(option=17)
+    o18, o17 = O.Oracle(p, tab), O.Oracle(p17, tab)
+    o18.set_mhd2d(tab[:, 2][:, None, None] * np.ones_like(rho), c, tab[:, 3][:, None, None] * np.ones_like(pr),
+                  np.zeros_like(psi))
+    a, pml = random_state(p17, 5, 1e-6)
+    pml6 = np.zeros((6,) + pml.shape[1:])
+    pml6[:2] = pml
+    pml6[1, 0] = 0.0
+    pml[1, 0] = 0.0
+    o18.set_state(a, pml6)
+    o17.set_state(a, pml)
+    o18.step(31)
+    o17.step(31)
+    s18, _, q18 = o18.state()
+    s17, _, q17 = o17.state()
+    assert rel_l2(s18, s17) < 1e-12
+    assert rel_l2(q18[:2], q17) < 1e-12
+
+
+def test_mhd2d_runs_and_drives_both_pml_layers():
+    from oracle import oracle as O
+    p, tab, bg = _mhd2d_case()
+    o = O.Oracle(p, tab)
+    o.set_mhd2d(*bg)
+    a = np.zeros((6, p.nz, 1, p.nx))
+    rng = np.random.default_rng(0)
+    a[0, 2:6] = 1e-6 * rng.standard_normal((4, 1, p.nx))
+    a[2, -6:-2] = 1e-6 * rng.standard_normal((4, 1, p.nx))
+    o.set_state(a)
+    o.step(3)
+    st, scr, pml = o.state()
+    assert np.isfinite(st).all() and np.isfinite(pml).all()
+    assert pml.shape[0] == 6
+    for i in (0, 1, 2, 4):                 # psi_vz, psi_p, psi_dzbx, psi_induction_bx
+        assert np.abs(pml[i, :4]).max() > 0 and np.abs(pml[i, 4:]).max() > 0, i
+    assert np.abs(pml[3]).max() == 0 and np.abs(pml[5]).max() == 0
+    assert np.abs(st[1]).max() == 0 and np.abs(st[4]).max() == 0
