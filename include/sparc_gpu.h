@@ -60,9 +60,11 @@ extern "C" {
 /* Mirror of params.i (params.i:25-150) plus the Instruction-file flags
  * (initialize.f90:1006-1051).  Lengths in cm, times in s, frequencies in Hz. */
 typedef struct sparc_params {
-    int nx, ny, nz;            /* params.i:25  (nx, ny powers of two; ny = 1 for option 17) */
+    int nx, ny, nz;            /* params.i:25  (nx, ny powers of two; ny = 1 for options 17, 18) */
     int npmlbot, npmltop;      /* params.i:108 */
-    int option;                /* 4 = MP_QUIET_PML_3D_DISPL, 17 = MP_QUIET_PML_2D_DISPL (step.f90:74-110) */
+    int option;                /* step.f90:74-110: 2 = MP_QUIET_PML_3D, 4 = MP_QUIET_PML_3D_DISPL,
+                                  8 = MP_MHD_PML_3D, 10 = MP_MHD_PML_3D_DISPL,
+                                  17 = MP_QUIET_PML_2D_DISPL, 18 = MP_MHD_PML_2D_DISPL */
     int compute_forward;       /* Instruction 'spectral' */
     int compute_adjoint;       /* Instruction 'adjoint' */
     int damp_waves;            /* params.i:38 */
@@ -121,16 +123,19 @@ int sparc_gpu_set_source(sparc_ctx* ctx, int src_idx, int mode, const double* pl
  * (driver.f90:455-476). */
 int sparc_gpu_step(sparc_ctx* ctx, int nsteps);
 
-/* Option 10 (MP_MHD_PML_3D_DISPL, displacement.f90:663-849): the 3-D cgs
- * background that READ_IN_FIELD reads (all_modules.f90:486-513) -- density,
+/* Options 10 (MP_MHD_PML_3D_DISPL, displacement.f90:663-849) and 8
+ * (MP_MHD_PML_3D, pml.f90:80-208): the 3-D cgs background that READ_IN_FIELD reads (all_modules.f90:486-513) -- density,
  * sound speed, pressure and B_x, B_y, B_z, each nx*ny*nz values in the
  * Fortran order a(nx,ny,nz) -- after sparc_gpu_set_background has set the
  * quiet column (z grid, gravity, Gamma_1, and the column the source planes
  * are searched on).  Replaces the magnetic parts of mp_Initialize_RHS
- * (physics.f90:62-161, 204-208, 255-303, 356-363).  For option 10 the state
- * is physical (get_field / get_state return it without transforms) and the
- * PML arrays of set_state / get_state hold six auxiliaries (psi_vz, psi_p,
- * psi_dzbx, psi_dzby, psi_induction_bx, psi_induction_by) of nzpml planes. */
+ * (physics.f90:62-161, 204-208, 255-303, 356-363).  For both options the
+ * state is physical (get_field / get_state return it without transforms) and
+ * the PML arrays of set_state / get_state hold six auxiliaries (psi_vz,
+ * psi_p, psi_dzbx, psi_dzby, psi_induction_bx, psi_induction_by) of nzpml
+ * planes: option 10 accounts for the bottom layer only, option 8 for both.
+ * Option 8 holds eight fields per state (rho, v_x, v_y, v_z, p, b_x, b_y,
+ * b_z; initialize.f90:498-510,545-551). */
 int sparc_gpu_set_mhd_background(sparc_ctx* ctx, const double* rho, const double* c, const double* p,
                                  const double* bx, const double* by, const double* bz);
 
@@ -168,14 +173,16 @@ int sparc_gpu_set_time(sparc_ctx* ctx, int time);
 /* ---- state in and out ------------------------------------------------------ */
 
 /* Field `field` (SPARC_XI_X..SPARC_V_Z) of slot src_idx into host (nz,ny,nx),
- * or only plane k (1-based) into host (ny,nx) when k > 0.
- * field 6..11 return the last RK-stage right-hand side scr(:,:,:,1..6), whose
- * components 4..6 are the 'acc' fields of WRITE_OUT_PARTIAL_STATE
+ * or only plane k (1-based) into host (ny,nx) when k > 0.  With nf fields
+ * per state (6; 8 in option 8), field nf..2nf-1 return the last RK-stage
+ * right-hand side scr(:,:,:,1..nf); in the displacement forms components
+ * 4..6 of it are the 'acc' fields of WRITE_OUT_PARTIAL_STATE
  * (all_modules.f90:771-778). */
 int sparc_gpu_get_field(sparc_ctx* ctx, int src_idx, int field, int k, double* host);
 
-/* Whole state of one slot: a (6,nz,ny,nx) and the PML auxiliaries
- * pmlvars (2,nzpml,ny,nx); pml may be NULL.  Replaces READ_IN_INITIAL_CONDITION /
+/* Whole state of one slot: a (nf,nz,ny,nx) -- nf = 6, or 8 in option 8 --
+ * and the PML auxiliaries pmlvars (2,nzpml,ny,nx), or (6,nzpml,ny,nx) in the
+ * MHD forms; pml may be NULL.  Replaces READ_IN_INITIAL_CONDITION /
  * WRITE_OUT_FULL_STATE (all_modules.f90:533-694) in memory. */
 int sparc_gpu_set_state(sparc_ctx* ctx, int src_idx, const double* a, const double* pml);
 int sparc_gpu_get_state(sparc_ctx* ctx, int src_idx, double* a, double* pml);

@@ -146,6 +146,7 @@ class Oracle:
         if not self.h:
             raise RuntimeError("oracle_create failed")
         self.shape = (p.nz, p.ny, p.nx)
+        self.nf = 8 if p.option == 8 else 6          # fields of the state (dimfive, at least 6)
 
     def close(self):
         if self.h:
@@ -187,8 +188,8 @@ class Oracle:
 
     def set_state(self, a: np.ndarray, pml: np.ndarray | None = None):
         a = np.ascontiguousarray(a, dtype=np.float64)
-        if a.size != 6 * int(np.prod(self.shape)):
-            raise ValueError(f"state must hold 6 x {self.shape}")
+        if a.size != self.nf * int(np.prod(self.shape)):
+            raise ValueError(f"state must hold {self.nf} x {self.shape}")
         if pml is not None:
             pml = np.ascontiguousarray(pml, dtype=np.float64)
             if pml.size != self.npv * self.p.nzpml * self.p.ny * self.p.nx:
@@ -197,14 +198,14 @@ class Oracle:
 
     @property
     def npv(self) -> int:
-        """PML auxiliary fields: 6 for the MHD displacement forms (options 10, 18), else 2."""
-        return 6 if self.p.option in (10, 18) else 2
+        """PML auxiliary fields: 6 for the MHD forms (options 8, 10, 18), else 2."""
+        return 6 if self.p.option in (8, 10, 18) else 2
 
     def set_mhd(self, rho, c, p, bx, by, bz):
-        """3-D cgs background of option 10 (as READ_IN_FIELD reads it), (nz, ny, nx)."""
+        """3-D cgs background of options 8 and 10 (as READ_IN_FIELD reads it), (nz, ny, nx)."""
         arrs = [np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape) for v in (rho, c, p, bx, by, bz)]
         if lib().oracle_set_mhd(self.h, *[_dp(v) for v in arrs]) != 0:
-            raise RuntimeError("oracle_set_mhd needs option 10")
+            raise RuntimeError("oracle_set_mhd needs option 8 or 10")
 
     def set_mhd2d(self, rho, c, p, psi):
         """2-D MHD background of option 18, (nz, nx) cgs: density, sound speed,
@@ -223,8 +224,8 @@ class Oracle:
 
     def state(self):
         p = self.p
-        a = np.zeros((6,) + self.shape)
-        scr = np.zeros((6,) + self.shape)
+        a = np.zeros((self.nf,) + self.shape)
+        scr = np.zeros((self.nf,) + self.shape)
         pml = np.zeros((self.npv, max(p.npmlbot + p.npmltop, 1), p.ny, p.nx))
         lib().oracle_get_state(self.h, _dp(a), _dp(pml), _dp(scr))
         return a, scr, pml

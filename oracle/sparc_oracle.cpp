@@ -264,7 +264,7 @@ extern "C" int oracle_dbyd2(double* A, const double* B, long N1, int N2, int ibc
 // ----------------------------------------------------------------------------
 struct Model {
     oracle_params P;
-    int nx, ny, nz, nzpml, dimfive;
+    int nx, ny, nz, nzpml, dimfive, nf;
     long N;            // nx*ny*nz
     long NP;           // nx*ny
     double pi, rsun, normx, normy, dimc, dimrho, diml, dimb, deltat;
@@ -399,7 +399,9 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
     m.nx = P->nx; m.ny = P->ny; m.nz = P->nz;
     m.NP = (long)m.nx * m.ny; m.N = m.NP * m.nz;
     m.nzpml = P->npmlbot + P->npmltop;
-    m.dimfive = P->option == 2 ? 5 : 6;              // velocity / displacement form (initialize.f90:310-312)
+    // velocity / MHD velocity / displacement form (initialize.f90:310-312)
+    m.dimfive = P->option == 2 ? 5 : (P->option == 8 ? 8 : 6);
+    m.nf = std::max(m.dimfive, 6);                   // fields held per state (a, temp_step, scr)
     m.pi = R4(3.14159265358979);                     // initialize.f90:38 (REAL*4 literal)
     m.rsun = R4(69598946770.0);
     m.normx = 1.0 / (double)m.nx; m.normy = 1.0 / (double)m.ny;
@@ -564,8 +566,8 @@ static void setup(Model& m, const oracle_params* P, const double* table /* (nz,6
         for (int i = 0; i < 5; ++i) m.betas[i] = b[i + 1] * m.deltat;
     }
     // state
-    m.a.assign(N * 6, 0); m.temp_step.assign(N * 6, 0); m.scr.assign(N * 6, 0);
-    m.npv = (P->option == 10 || P->option == 18) ? 6 : 2;
+    m.a.assign(N * m.nf, 0); m.temp_step.assign(N * m.nf, 0); m.scr.assign(N * m.nf, 0);
+    m.npv = (P->option == 8 || P->option == 10 || P->option == 18) ? 6 : 2;
     long npml = (long)NP * std::max(m.nzpml, 1) * m.npv;
     m.scrpml.assign(npml, 0); m.pmlvars.assign(npml, 0); m.psipml.assign(npml, 0);
     m.gradp.assign(N * 3, 0); m.dvxdx.assign(N, 0); m.dvydy.assign(N, 0); m.gradvz.assign(N, 0);
@@ -847,6 +849,118 @@ static inline void cross3(double ax, double ay, double az, double bx, double by,
     cx = ay * bz - az * by;
     cy = az * bx - ax * bz;
     cz = ax * by - ay * bx;
+}
+
+// ----------------------------------------------------------------------------
+// MP_MHD_PML_3D (pml.f90:80-208), option 8: the MHD velocity form, fields
+// rho, v_x, v_y, v_z, p, b_x, b_y, b_z (initialize.f90:498-510, 545-551);
+// PML_BOUNDARY_ACCOUNTING_3D (pml.f90:213-285) at both ends with psi_p,
+// psi_vz, psi_induction_bx (on d flux2/dz), psi_induction_by (on d flux1/dz),
+// psi_dzbx, psi_dzby; source forcing*source_dep(k) for |k - e_rad| <= 4
+// ----------------------------------------------------------------------------
+static void rhs_option8(Model& m) {
+    long N = m.N, NP = m.NP; int nz = m.nz;
+    double* rho = &m.temp_step[0];
+    double* v_x = &m.temp_step[N]; double* v_y = &m.temp_step[2 * N]; double* v_z = &m.temp_step[3 * N];
+    double* p = &m.temp_step[4 * N];
+    double* bx = &m.temp_step[5 * N]; double* by = &m.temp_step[6 * N]; double* bz = &m.temp_step[7 * N];
+    double* RHScont = &m.scr[0];
+    double* RHSv_x = &m.scr[N]; double* RHSv_y = &m.scr[2 * N]; double* RHSv_z = &m.scr[3 * N];
+    double* RHSp = &m.scr[4 * N];
+    double* RHSb_x = &m.scr[5 * N]; double* RHSb_y = &m.scr[6 * N]; double* RHSb_z = &m.scr[7 * N];
+    long PS = NP * m.nzpml;
+    double* psivz = &m.psipml[0]; double* psip = &m.psipml[PS];
+    double* psidzbx = &m.psipml[2 * PS]; double* psidzby = &m.psipml[3 * PS];
+    double* psiibx = &m.psipml[4 * PS]; double* psiiby = &m.psipml[5 * PS];
+    double* RHSpsivz = &m.scrpml[0]; double* RHSpsip = &m.scrpml[PS];
+    double* RHSpsidzbx = &m.scrpml[2 * PS]; double* RHSpsidzby = &m.scrpml[3 * PS];
+    double* RHSpsiibx = &m.scrpml[4 * PS]; double* RHSpsiiby = &m.scrpml[5 * PS];
+    int nb = m.P.npmlbot, nt = m.P.npmltop;
+    std::vector<double> flux1(N), flux2(N), flux3(N), dvxdx(N), dvydy(N), dvzdz(N);
+    std::vector<double> gradp_x(N), gradp_y(N), gradp_z(N), dzflux1(N), dzflux2(N);
+    std::vector<double> curlbx(N), curlby(N), curlbz(N), dzbx(N), dzby(N);
+    for (long q = 0; q < N; ++q) {
+        flux1[q] = -(v_z[q] * m.boy[q] - v_y[q] * m.boz[q]);
+        flux2[q] = -(v_x[q] * m.boz[q] - v_z[q] * m.box[q]);
+        flux3[q] = -(v_y[q] * m.box[q] - v_x[q] * m.boy[q]);
+    }
+    // the six ddxyz calls of pml.f90:106-116, in order (flux2 and flux3 are
+    // reused as outputs once their derivatives are taken)
+    ddxyz(m, v_x, dvxdx.data(), v_y, dvydy.data(), v_z, dvzdz.data(), 1);
+    ddxyz(m, flux3.data(), RHSb_y, p, gradp_y.data(), flux1.data(), dzflux1.data(), 1);
+    ddxyz(m, p, gradp_x.data(), flux3.data(), RHSb_x, flux2.data(), dzflux2.data(), 1);
+    ddxyz(m, flux2.data(), RHSb_z, bz, curlbx.data(), bx, dzbx.data(), 1);
+    ddxyz(m, by, curlbz.data(), bx, flux2.data(), p, gradp_z.data(), 1);
+    ddxyz(m, bz, curlby.data(), flux1.data(), flux3.data(), by, dzby.data(), 1);
+    // PML_BOUNDARY_ACCOUNTING_3D
+    int pmlindex = 0;
+    for (int k = 1; k <= nz; ++k) {
+        if (k <= nb || k >= nz - nt + 1) {
+            pmlindex++;
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1), ip = q + NP * (pmlindex - 1);
+                RHSpsip[ip] = m.az[id] * gradp_z[id] + m.bzpml[id] * psip[ip];
+                gradp_z[id] = gradp_z[id] + psip[ip];
+                RHSpsivz[ip] = m.az[id] * dvzdz[id] + m.bzpml[id] * psivz[ip];
+                dvzdz[id] = dvzdz[id] + psivz[ip];
+            }
+        }
+    }
+    pmlindex = 0;
+    for (int k = 1; k <= nz; ++k) {
+        if (k <= nb || k >= nz - nt + 1) {
+            pmlindex++;
+            for (long q = 0; q < NP; ++q) {
+                long id = q + NP * (k - 1), ip = q + NP * (pmlindex - 1);
+                RHSpsiibx[ip] = m.az[id] * dzflux2[id] + m.bzpml[id] * psiibx[ip];
+                dzflux2[id] = dzflux2[id] + psiibx[ip];
+                RHSpsiiby[ip] = m.az[id] * dzflux1[id] + m.bzpml[id] * psiiby[ip];
+                dzflux1[id] = dzflux1[id] + psiiby[ip];
+                RHSpsidzbx[ip] = m.az[id] * dzbx[id] + m.bzpml[id] * psidzbx[ip];
+                dzbx[id] = dzbx[id] + psidzbx[ip];
+                RHSpsidzby[ip] = m.az[id] * dzby[id] + m.bzpml[id] * psidzby[ip];
+                dzby[id] = dzby[id] + psidzby[ip];
+            }
+        }
+    }
+    for (long q = 0; q < N; ++q) {
+        RHSb_x[q] = RHSb_x[q] - dzflux2[q];
+        RHSb_y[q] = -RHSb_y[q] + dzflux1[q];
+        RHSb_z[q] = RHSb_z[q] - flux3[q];
+        const double div = dvxdx[q] + dvydy[q] + dvzdz[q];
+        curlbx[q] = curlbx[q] - dzby[q];
+        curlby[q] = -curlby[q] + dzbx[q];
+        curlbz[q] = curlbz[q] - flux2[q];
+        RHScont[q] = -m.gradrho0_x[q] * v_x[q] - m.gradrho0_y[q] * v_y[q] - m.gradrho0_z[q] * v_z[q] - m.rho0[q] * div;
+        RHSp[q] = -m.c2rho0[q] * div - v_x[q] * m.gradp0_x[q] - v_y[q] * m.gradp0_y[q] - v_z[q] * m.gradp0_z[q];
+        double f1, f2, f3;
+        cross3(curlbx[q], curlby[q], curlbz[q], m.box[q], m.boy[q], m.boz[q], f1, f2, f3);
+        RHSv_x[q] = -m.rhoinv[q] * (gradp_x[q] - f1);
+        RHSv_y[q] = -m.rhoinv[q] * (gradp_y[q] - f2);
+        RHSv_z[q] = -m.rhoinv[q] * (gradp_z[q] - f3);
+        cross3(m.curlbox[q], m.curlboy[q], m.curlboz[q], bx[q], by[q], bz[q], f1, f2, f3);
+        RHSv_x[q] = RHSv_x[q] + m.rhoinv[q] * f1;
+        RHSv_y[q] = RHSv_y[q] + m.rhoinv[q] * f2;
+        RHSv_z[q] = RHSv_z[q] + m.rhoinv[q] * f3;
+    }
+    int kc = m.P.src_k > 0 ? m.P.src_k : m.e_rad;
+    for (int k = 1; k <= nz; ++k)
+        for (long q = 0; q < NP; ++q) {
+            long id = q + NP * (k - 1);
+            RHSv_z[id] = RHSv_z[id] - m.rhoinv[id] * rho[id] * m.g[k - 1];
+            if (std::abs(k - kc) <= 4 && m.src_mode != 0)
+                RHSv_z[id] = RHSv_z[id] + m.forcing[q] * m.source_dep[k - 1];
+        }
+    for (int l = 0; l < 8; ++l)
+        for (long q = 0; q < NP; ++q) {
+            m.scr[l * N + q + NP * (nz - 1)] = 0.0;
+            m.scr[l * N + q] = 0.0;
+        }
+    if (m.P.damp_waves) {
+        damp_velocity(m, v_x, RHSv_x);
+        damp_velocity(m, v_y, RHSv_y);
+        damp_velocity(m, v_z, RHSv_z);
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -1401,7 +1515,7 @@ static void lagrange_interp(Model& m) {
 // STEP (step.f90:43-128) for options 2, 4 and 17 (USE_PML, no horizontal PML);
 // in the velocity form the sixth field is unused and stays zero
 static void step(Model& m) {
-    long N6 = m.N * 6, NPML = (long)m.NP * m.nzpml * m.npv;
+    long N6 = m.N * m.nf, NPML = (long)m.NP * m.nzpml * m.npv;
     for (int rk = 1; rk <= 5; ++rk) {
         if (rk == 1) {
             m.temp_step = m.a;
@@ -1414,6 +1528,7 @@ static void step(Model& m) {
         }
         if (m.P.option == 4) rhs_option4(m);
         else if (m.P.option == 2) rhs_option2(m);
+        else if (m.P.option == 8) rhs_option8(m);
         else if (m.P.option == 10) rhs_option10(m);
         else if (m.P.option == 18) rhs_option18(m);
         else rhs_option17(m);
@@ -1499,7 +1614,7 @@ int oracle_set_source(void* h, int mode, const double* planes, int L, const doub
 
 int oracle_set_state(void* h, const double* a, const double* pml) {
     Model& m = *(Model*)h;
-    std::copy(a, a + m.N * 6, m.a.begin());
+    std::copy(a, a + m.N * m.nf, m.a.begin());
     if (pml) std::copy(pml, pml + (long)m.NP * m.nzpml * m.npv, m.pmlvars.begin());
     return 0;
 }
@@ -1536,7 +1651,7 @@ int oracle_set_time(void* h, int t) { ((Model*)h)->time = t; return 0; }
 int oracle_set_mhd(void* h, const double* rho, const double* c, const double* p, const double* bx,
                    const double* by, const double* bz) {
     Model& m = *(Model*)h;
-    if (m.P.option != 10) return -1;
+    if (m.P.option != 10 && m.P.option != 8) return -1;
     setup_mhd(m, rho, c, p, bx, by, bz);
     return 0;
 }

@@ -127,8 +127,8 @@ const char* sparc_gpu_last_error(const sparc_ctx* c) { return c ? c->err.c_str()
 
 static int validate(const sparc_params* p, std::string& why) {
     auto pow2 = [](int n) { return n >= 4 && n <= 1024 && (n & (n - 1)) == 0; };
-    if (p->option != 2 && p->option != 4 && p->option != 10 && p->option != 17 && p->option != 18) {
-        why = "option must be 2, 4, 10, 17 or 18";
+    if (p->option != 2 && p->option != 4 && p->option != 8 && p->option != 10 && p->option != 17 && p->option != 18) {
+        why = "option must be 2, 4, 8, 10, 17 or 18";
         return 0;
     }
     if (!pow2(p->nx)) { why = "nx must be a power of two in [4,1024]"; return 0; }
@@ -166,6 +166,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     c->NP = (long long)p->nx * p->ny;
     c->N = c->NP * c->nz;
     c->f32 = (p->precision == SPARC_FP32);
+    c->nf = (p->option == 8) ? 8 : 6;            // dimfive: rho, v, p, b in the MHD velocity form
+    const bool mhd_form = (p->option == 8 || p->option == 10 || p->option == 18);
     int rc = SPARC_OK;
     auto bail = [&](int code) { sparc_gpu_destroy(c); return code; };
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -177,8 +179,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     }
     size_t cs = csz(c), es = esz(c);
     long long S = c->S;
-    if ((rc = dalloc(c, &c->a, (size_t)S * 6 * c->fs * cs))) return bail(rc);
-    if ((rc = dalloc(c, &c->scr, (size_t)S * 6 * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->a, (size_t)S * c->nf * c->fs * cs))) return bail(rc);
+    if ((rc = dalloc(c, &c->scr, (size_t)S * c->nf * c->fs * cs))) return bail(rc);
     if ((rc = dalloc(c, &c->pml, (size_t)S * 2 * c->ps * cs))) return bail(rc);
     if ((rc = dalloc(c, &c->scrpml, (size_t)S * 2 * c->ps * cs))) return bail(rc);
     if ((rc = dalloc(c, &c->ybuf, (size_t)S * c->fs * cs))) return bail(rc);
@@ -209,9 +211,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     launch_set_time(c->d_time, 0, c->stream);
     c->t0.assign(c->S, 0);
     c->active_n = c->S;
-    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && p->option != 10 && p->option != 18;
+    c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && !mhd_form;
     if (c->use_fused) fused_prepare(c->nz, c->nzpml);
-    if ((p->option == 10 || p->option == 18) && (rc = mhd_create(c))) return bail(rc);
+    if (mhd_form && (rc = mhd_create(c))) return bail(rc);
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
@@ -483,8 +485,8 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
         if ((rc = upload(c, c->pt, c->pt_host.data(), c->pt_host.size() * 8))) return rc;
     }
     size_t cs = csz(c);
-    CK(cudaMemsetAsync(c->a, 0, (size_t)c->S * 6 * c->fs * cs, c->stream));
-    CK(cudaMemsetAsync(c->scr, 0, (size_t)c->S * 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(c->a, 0, (size_t)c->S * c->nf * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(c->scr, 0, (size_t)c->S * c->nf * c->fs * cs, c->stream));
     CK(cudaMemsetAsync(c->pml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
     CK(cudaMemsetAsync(c->scrpml, 0, (size_t)c->S * 2 * c->ps * cs, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -601,14 +603,14 @@ static int from_spec(sparc_ctx* c, const void* spec_src, double* host_field, int
 }
 
 static char* field_ptr(sparc_ctx* c, void* base, int src, int field, long long fstride_elems) {
-    return (char*)base + ((long long)src * 6 + field) * fstride_elems * csz(c);
+    return (char*)base + ((long long)src * c->nf + field) * fstride_elems * csz(c);
 }
 
 int sparc_gpu_set_state(sparc_ctx* c, int src, const double* a, const double* pml) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     if (src < 0 || src >= c->S || !a) return fail(c, SPARC_EINVAL, "bad slot or null state");
-    for (int f = 0; f < 6; ++f) {
+    for (int f = 0; f < c->nf; ++f) {
         int rc = to_spec(c, a + (long long)f * c->N, field_ptr(c, c->a, src, f, c->fs), c->nz);
         if (rc) return rc;
     }
@@ -634,7 +636,7 @@ int sparc_gpu_set_state(sparc_ctx* c, int src, const double* a, const double* pm
         CK(cudaMemsetAsync(pbase, 0, 2 * c->ps * csz(c), c->stream));
     }
     }
-    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * csz(c), c->stream));
+    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, c->nf * c->fs * csz(c), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SPARC_OK;
 }
@@ -643,7 +645,7 @@ int sparc_gpu_get_state(sparc_ctx* c, int src, double* a, double* pml) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     if (src < 0 || src >= c->S || !a) return fail(c, SPARC_EINVAL, "bad slot or null buffer");
-    for (int f = 0; f < 6; ++f) {
+    for (int f = 0; f < c->nf; ++f) {
         int rc = from_spec(c, field_ptr(c, c->a, src, f, c->fs), a + (long long)f * c->N, c->nz);
         if (rc) return rc;
     }
@@ -664,10 +666,10 @@ int sparc_gpu_get_state(sparc_ctx* c, int src, double* a, double* pml) {
 int sparc_gpu_get_field(sparc_ctx* c, int src, int field, int k, double* host) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (src < 0 || src >= c->S || field < 0 || field > 11 || k < 0 || k > c->nz || !host)
+    if (src < 0 || src >= c->S || field < 0 || field >= 2 * c->nf || k < 0 || k > c->nz || !host)
         return fail(c, SPARC_EINVAL, "bad slot, field, plane or buffer");
-    void* base = field < 6 ? c->a : c->scr;
-    char* fp = field_ptr(c, base, src, field % 6, c->fs);
+    void* base = field < c->nf ? c->a : c->scr;
+    char* fp = field_ptr(c, base, src, field % c->nf, c->fs);
     if (k > 0) return from_spec(c, fp + (long long)(k - 1) * plane_bytes(c), host, 1);
     return from_spec(c, fp, host, c->nz);
 }
@@ -903,7 +905,8 @@ int sparc_gpu_set_mhd2d_background(sparc_ctx* c, const double* rho, const double
 int sparc_gpu_set_mhd_background(sparc_ctx* c, const double* rho, const double* cs, const double* p,
                                  const double* bx, const double* by, const double* bz) {
     if (!c) return SPARC_EINVAL;
-    if (!c->mhd || c->P.option != 10) return fail(c, SPARC_EINVAL, "the MHD background belongs to option 10");
+    if (!c->mhd || (c->P.option != 10 && c->P.option != 8))
+        return fail(c, SPARC_EINVAL, "the 3-D MHD background belongs to options 8 and 10");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background (the quiet column) first");
     if (!rho || !cs || !p || !bx || !by || !bz) return fail(c, SPARC_EINVAL, "null background array");
     return mhd_set_background(c, rho, cs, p, bx, by, bz);
@@ -988,7 +991,7 @@ int sparc_gpu_sync(sparc_ctx* c, int check_finite) {
     CK(cudaStreamSynchronize(c->stream));
     if (check_finite && c->have_bg) {
         CK(cudaMemsetAsync(c->d_flag, 0, 4, c->stream));
-        long long n = (long long)c->S * 6 * c->fs * 2;
+        long long n = (long long)c->S * c->nf * c->fs * 2;
         if (c->f32) launch_check_finite_f32((const float*)c->a, n, c->d_flag, c->stream);
         else launch_check_finite_f64((const double*)c->a, n, c->d_flag, c->stream);
         c->launches++;
@@ -1049,8 +1052,8 @@ int sparc_gpu_slot_reset(sparc_ctx* c, int src) {
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
     const size_t cs = csz(c);
-    CK(cudaMemsetAsync(field_ptr(c, c->a, src, 0, c->fs), 0, 6 * c->fs * cs, c->stream));
-    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, 6 * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(field_ptr(c, c->a, src, 0, c->fs), 0, c->nf * c->fs * cs, c->stream));
+    CK(cudaMemsetAsync(field_ptr(c, c->scr, src, 0, c->fs), 0, c->nf * c->fs * cs, c->stream));
     CK(cudaMemsetAsync((char*)c->pml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
     CK(cudaMemsetAsync((char*)c->scrpml + (size_t)src * 2 * c->ps * cs, 0, 2 * c->ps * cs, c->stream));
     if (c->mhd) {
@@ -1219,7 +1222,7 @@ extern "C" {
 int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (c->P.option == 2 || c->P.option == 10 || c->P.option == 18)
+    if (c->P.option == 2 || c->mhd)
         return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the quiet displacement forms");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
@@ -1328,9 +1331,9 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
 // ---------------------------------------------------------------------------
 int sparc_gpu_save_device(sparc_ctx* c, int idx, int capacity) {
     if (!c) return SPARC_EINVAL;
-    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not the MHD forms)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    size_t na = (size_t)c->S * c->nf * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     if (!c->dck) {
         if (capacity < 1) return fail(c, SPARC_EINVAL, "capacity < 1");
         int rc = dalloc(c, &c->dck, (size_t)capacity * (na + np));
@@ -1348,10 +1351,10 @@ int sparc_gpu_save_device(sparc_ctx* c, int idx, int capacity) {
 
 int sparc_gpu_load_device(sparc_ctx* c, int idx) {
     if (!c) return SPARC_EINVAL;
-    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not the MHD forms)");
     if (!c->dck || idx < 0 || idx >= c->dck_n || c->dck_time[idx] < 0)
         return fail(c, SPARC_EINVAL, "no such device checkpoint");
-    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    size_t na = (size_t)c->S * c->nf * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     const char* src = (const char*)c->dck + (size_t)idx * (na + np);
     CK(cudaMemcpyAsync(c->a, src, na, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(c->pml, src + na, np, cudaMemcpyDeviceToDevice, c->stream));
@@ -1378,9 +1381,9 @@ struct CkHeader {
 
 int sparc_gpu_checkpoint(sparc_ctx* c, const char* path) {
     if (!c || !path) return SPARC_EINVAL;
-    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not the MHD forms)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    size_t na = (size_t)c->S * c->nf * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     std::vector<unsigned char> buf(na + np);
     CK(cudaMemcpyAsync(buf.data(), c->a, na, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(buf.data() + na, c->pml, np, cudaMemcpyDeviceToHost, c->stream));
@@ -1404,7 +1407,7 @@ int sparc_gpu_checkpoint(sparc_ctx* c, const char* path) {
 
 int sparc_gpu_restore(sparc_ctx* c, const char* path) {
     if (!c || !path) return SPARC_EINVAL;
-    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not option 10)");
+    if (c->mhd) return fail(c, SPARC_EINVAL, "checkpoints hold the quiet-Sun state layout (not the MHD forms)");
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     FILE* f = fopen(path, "rb");
     if (!f) return fail(c, SPARC_EIO, std::string("cannot open ") + path);
@@ -1413,7 +1416,7 @@ int sparc_gpu_restore(sparc_ctx* c, const char* path) {
         fclose(f);
         return fail(c, SPARC_EIO, "not a checkpoint file");
     }
-    size_t na = (size_t)c->S * 6 * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
+    size_t na = (size_t)c->S * c->nf * c->fs * csz(c), np = (size_t)c->S * 2 * c->ps * csz(c);
     if (h.abi != SPARC_GPU_ABI_VERSION || h.nx != c->P.nx || h.ny != c->P.ny || h.nz != c->nz ||
         h.npmlbot != c->P.npmlbot || h.npmltop != c->P.npmltop || h.option != c->P.option ||
         h.precision != c->P.precision || h.nsrc != c->S || h.payload_bytes != na + np || h.time < 0) {

@@ -15,6 +15,7 @@ struct sparc_ctx {
     int H, M, nz, S, nzpml;
     long long fs, ps, NP, N;
     int f32;
+    int nf;                 // fields per state slot: 6, or 8 in the MHD velocity form (option 8)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_done = nullptr;     // last cross-context hand-off on this stream
     std::string err;

@@ -37,6 +37,14 @@ enum { MW_T0, MW_T1, MW_T2, MW_T3, MW_T4, MW_T5, MW_F1, MW_F2, MW_F3, MW_DX, MW_
 // PML auxiliaries of option 10 (scrpml / pmlvars index, initialize.f90:487-490,560-566)
 enum { PV_VZ, PV_P, PV_DZBX, PV_DZBY, PV_IBX, PV_IBY, PV_COUNT };
 
+// work fields of a stage of the MHD velocity form (option 8): the eight
+// temporaries, the fluxes of v x B0, the eighteen derivatives of the six
+// ddxyz calls of pml.f90:106-116 (named for the derivative they hold) and
+// the three damping terms
+enum { V8_T0, V8_T1, V8_T2, V8_T3, V8_T4, V8_T5, V8_T6, V8_T7, V8_F1, V8_F2, V8_F3,
+       V8_DVXDX, V8_DVYDY, V8_DVZDZ, V8_DXF3, V8_GPY, V8_DZF1, V8_GPX, V8_DYF3, V8_DZF2, V8_DXF2, V8_DYBZ,
+       V8_DZBX, V8_DXBY, V8_DYBX, V8_GPZ, V8_DXBZ, V8_DYF1, V8_DZBY, V8_DMX, V8_DMY, V8_DMZ, V8_COUNT };
+
 }  // namespace
 
 struct MhdState {
@@ -49,7 +57,7 @@ struct MhdState {
     void* dw = nullptr;        // [NP] T: delta_width_2d
     void* rx = nullptr;        // [nx] T: d/dx multipliers of the packed complex FFT
     void* ry = nullptr;        // [ny] T
-    void* work = nullptr;      // [S][MW_COUNT][N] T
+    void* work = nullptr;      // [S][MW_COUNT][N] T ([S][V8_COUNT][N] in option 8)
     void* pml = nullptr;       // [S][6][nzpml*NP] T (pmlvars)
     void* spml = nullptr;      // [S][6][nzpml*NP] T (scrpml)
     void* spec = nullptr;      // one spectral field (nz*M complex T): damping / filter transforms
@@ -213,6 +221,11 @@ __global__ void mhd_pml_kernel(double* gp0z, double* gr0z, double* az, double* b
         dampz = 3.0 * 3.0 * tempin(nz - 1) / (z[nz - 1] - z[nz - nt]) * (r * r);
         fdec = alph[k] / (dampz + alph[k]);
         gp0z[t] *= fdec; gr0z[t] *= fdec;
+        // pmlindex order: the top planes follow the nb bottom ones (read by
+        // option 8; option 10 accounts for the bottom only)
+        const long long ip = nb + (k - (nz - nt));
+        az[ip * NP + q] = -dampz;
+        bzp[ip * NP + q] = -alph[k] - dampz;
     }
 }
 
@@ -235,7 +248,8 @@ struct MhdArgs {
     long long N, NP, FS;   // points per field, per plane; field stride of the state slots
     int nz, nb, nt, nzpml;
     int S;
-    int both;              // PML at both ends (option 18) or at the bottom only (option 10)
+    int both;              // PML at both ends (options 8, 18) or at the bottom only (option 10)
+    int nf;                // fields per state slot (8 in option 8, else 6)
 };
 
 // pmlindex of 0-based plane k (PML_BOUNDARY_ACCOUNTING order), -1 outside
@@ -432,9 +446,9 @@ __global__ void __launch_bounds__(128) mhd_update_kernel(const MhdArgs A, T* __r
                                                          T dt, int mode) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= A.NP) return;
-    const int s = blockIdx.y / 6, f = blockIdx.y % 6;
-    T* af = a + ((long long)s * 6 + f) * A.FS + q;
-    const T* sf = scr + ((long long)s * 6 + f) * A.FS + q;
+    const int s = blockIdx.y / A.nf, f = blockIdx.y % A.nf;
+    T* af = a + ((long long)s * A.nf + f) * A.FS + q;
+    const T* sf = scr + ((long long)s * A.nf + f) * A.FS + q;
     zfilter_stream<T, T>(
         A.nz, mode, [&](int j) { const long long o = (long long)j * A.NP; return af[o] + dt * sf[o]; },
         [&](int j, T v) { af[(long long)j * A.NP] = v; });
@@ -446,12 +460,12 @@ __global__ void mhd_pml_update_kernel(T* pml, const T* spml, T dt, long long n) 
     if (t < n) pml[t] = pml[t] + dt * spml[t];
 }
 
-// v_z of each slot on its source / observation plane into the record buffer
-// (dense planes) when the slot's clock is on the output cadence
+// v_z (field fz of nf per slot) of each slot on its observation plane into
+// the record buffer (dense planes) when the slot's clock is on the output cadence
 template <typename T>
 __global__ void mhd_record_kernel(const T* __restrict__ a, T* __restrict__ rec, const int* __restrict__ t0,
                                   const int* __restrict__ time, int steps, int rec_max, long long FS, long long NP,
-                                  long long rec_ss, const int* __restrict__ plane) {
+                                  long long rec_ss, const int* __restrict__ plane, int nf, int fz) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int s = blockIdx.y;
     if (q >= NP) return;
@@ -459,7 +473,7 @@ __global__ void mhd_record_kernel(const T* __restrict__ a, T* __restrict__ rec, 
     if (tl < 0 || tl % steps != 0) return;
     const int r = tl / steps;
     if (r >= rec_max) return;
-    rec[(long long)s * rec_ss + (long long)r * NP + q] = a[((long long)s * 6 + 5) * FS + (long long)plane[q] * NP + q];
+    rec[(long long)s * rec_ss + (long long)r * NP + q] = a[((long long)s * nf + fz) * FS + (long long)plane[q] * NP + q];
 }
 
 unsigned nb256(long long n) { return (unsigned)((n + 255) / 256); }
@@ -528,7 +542,8 @@ int mhd_create(sparc_ctx* c) {
     if ((rc = dalloc(c, &m.dw, (size_t)c->NP * es))) return rc;
     if ((rc = dalloc(c, &m.rx, (size_t)c->P.nx * es))) return rc;
     if ((rc = dalloc(c, &m.ry, (size_t)std::max(c->P.ny, 2) * es))) return rc;
-    if ((rc = dalloc(c, &m.work, (size_t)c->S * MW_COUNT * c->N * es))) return rc;
+    const int nwork = c->P.option == 8 ? (int)V8_COUNT : (int)MW_COUNT;
+    if ((rc = dalloc(c, &m.work, (size_t)c->S * nwork * c->N * es))) return rc;
     const size_t pv = (size_t)c->S * PV_COUNT * std::max(c->nzpml, 1) * c->NP * es;
     if ((rc = dalloc(c, &m.pml, pv))) return rc;
     if ((rc = dalloc(c, &m.spml, pv))) return rc;
@@ -692,7 +707,8 @@ int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const 
     // to the element type: background fields, bottom PML coefficients, tables
     const int src_of[MB_COUNT] = {W_BX, W_BY, W_BZ, W_CBX, W_CBY, W_CBZ, W_GP0X, W_GP0Y, W_GP0Z, W_GR0X,
                                   W_GR0Y, W_GR0Z, W_C2R, W_RHO, W_RI};
-    const long long nbp = (long long)std::max(nb, 1) * NP, npz = (long long)std::max(c->nzpml, 1) * NP;
+    // a_z, b_z of all nzpml PML planes in pmlindex order (option 10 reads the bottom nb)
+    const long long nbp = (long long)std::max(c->nzpml, 1) * NP, npz = nbp;
     for (int i = 0; i < MB_COUNT; ++i) {
         if (c->f32) to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.bg + (size_t)i * N, W(src_of[i]), N);
         else to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.bg + (size_t)i * N, W(src_of[i]), N);
@@ -1041,6 +1057,7 @@ int mhd2d_stage(sparc_ctx* c, T beta, int hs) {
     A.nzpml = std::max(c->nzpml, 1);
     A.S = S;
     A.both = 1;
+    A.nf = 6;
     T* bg = (T*)m.bg;
     T* work = (T*)m.work;
     const T* pab = (const T*)m.pab;
@@ -1114,6 +1131,182 @@ int mhd2d_stage(sparc_ctx* c, T beta, int hs) {
 
 namespace {
 
+// ---- option 8: MP_MHD_PML_3D (pml.f90:80-208), the MHD velocity form -----------
+// fields rho, v_x, v_y, v_z, p, b_x, b_y, b_z
+
+// temp = a + beta*scr (step.f90:52-71) into T0..T7 and the fluxes of v x B0
+// (pml.f90:93-95)
+template <typename T>
+__global__ void mhd8_temp_kernel(const MhdArgs A, const T* __restrict__ a, const T* __restrict__ scr, T beta, int hs,
+                                 const T* __restrict__ bg, T* __restrict__ work) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const T* as = a + (long long)s * 8 * A.FS;
+    const T* ss = scr + (long long)s * 8 * A.FS;
+    T* w = work + (long long)s * V8_COUNT * A.N;
+    T v[8];
+    #pragma unroll
+    for (int f = 0; f < 8; ++f) {
+        v[f] = as[f * A.FS + t];
+        if (hs) v[f] = v[f] + beta * ss[f * A.FS + t];
+        w[(V8_T0 + f) * A.N + t] = v[f];
+    }
+    const T box = bg[MB_BOX * A.N + t], boy = bg[MB_BOY * A.N + t], boz = bg[MB_BOZ * A.N + t];
+    w[V8_F1 * A.N + t] = -(v[3] * boy - v[2] * boz);
+    w[V8_F2 * A.N + t] = -(v[1] * boz - v[3] * box);
+    w[V8_F3 * A.N + t] = -(v[2] * box - v[1] * boy);
+}
+
+// everything after the derivatives, point-wise: PML_BOUNDARY_ACCOUNTING_3D
+// at both ends (pml.f90:213-285), the induction RHS, div, curl b, continuity,
+// pressure, the two Lorentz terms (CROSS, derivatives.f90:471-480), gravity,
+// the source forcing * source_dep(k) for |k - e_rad| <= 4 (pml.f90:175-181),
+// the zero top and bottom rows of all eight fields, then DAMP_VELOCITY
+template <typename T>
+__global__ void mhd8_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, const T* __restrict__ work,
+                                const T* __restrict__ pab, const T* __restrict__ pml, T* __restrict__ spml, T beta,
+                                int hs, const T* __restrict__ gz, const T* __restrict__ zt, int damp,
+                                T* __restrict__ scr, SlotClock clk, int src_mode, const T* __restrict__ planes,
+                                long long plane_ss, int L, const double* __restrict__ series, int nseries, int ksrc) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.N) return;
+    const int s = blockIdx.y;
+    const int k = (int)(t / A.NP);
+    const long long q = t - (long long)k * A.NP;
+    const T* w = work + (long long)s * V8_COUNT * A.N;
+    auto W = [&](int f) { return w[(long long)f * A.N + t]; };
+    auto B = [&](int f) { return bg[(long long)f * A.N + t]; };
+    const T gpz = pml_bottom<T>(A, t, s, PV_P, W(V8_GPZ), pab, pml, spml, beta, hs);
+    const T dvzdz = pml_bottom<T>(A, t, s, PV_VZ, W(V8_DVZDZ), pab, pml, spml, beta, hs);
+    const T dzf2 = pml_bottom<T>(A, t, s, PV_IBX, W(V8_DZF2), pab, pml, spml, beta, hs);
+    const T dzf1 = pml_bottom<T>(A, t, s, PV_IBY, W(V8_DZF1), pab, pml, spml, beta, hs);
+    const T dzbx = pml_bottom<T>(A, t, s, PV_DZBX, W(V8_DZBX), pab, pml, spml, beta, hs);
+    const T dzby = pml_bottom<T>(A, t, s, PV_DZBY, W(V8_DZBY), pab, pml, spml, beta, hs);
+    const T rbx = W(V8_DYF3) - dzf2;
+    const T rby = -W(V8_DXF3) + dzf1;
+    const T rbz = W(V8_DXF2) - W(V8_DYF1);
+    const T div = W(V8_DVXDX) + W(V8_DVYDY) + dvzdz;
+    const T cbx = W(V8_DYBZ) - dzby;
+    const T cby = -W(V8_DXBZ) + dzbx;
+    const T cbz = W(V8_DXBY) - W(V8_DYBX);
+    const T rho = W(V8_T0), vx = W(V8_T1), vy = W(V8_T2), vz = W(V8_T3);
+    const T bx = W(V8_T5), by = W(V8_T6), bz = W(V8_T7);
+    const T rcont = -B(MB_GR0X) * vx - B(MB_GR0Y) * vy - B(MB_GR0Z) * vz - B(MB_RHO0) * div;
+    const T rp = -B(MB_C2RHO0) * div - vx * B(MB_GP0X) - vy * B(MB_GP0Y) - vz * B(MB_GP0Z);
+    const T box = B(MB_BOX), boy = B(MB_BOY), boz = B(MB_BOZ), ri = B(MB_RHOINV);
+    T f1 = cby * boz - cbz * boy, f2 = cbz * box - cbx * boz, f3 = cbx * boy - cby * box;
+    T rvx = -ri * (W(V8_GPX) - f1);
+    T rvy = -ri * (W(V8_GPY) - f2);
+    T rvz = -ri * (gpz - f3);
+    const T cbox = B(MB_CBOX), cboy = B(MB_CBOY), cboz = B(MB_CBOZ);
+    f1 = cboy * bz - cboz * by; f2 = cboz * bx - cbox * bz; f3 = cbox * by - cboy * bx;
+    rvx = rvx + ri * f1;
+    rvy = rvy + ri * f2;
+    rvz = rvz + ri * f3;
+    rvz = rvz - ri * rho * gz[k];
+    if (src_mode != 0 && abs(k - ksrc) <= 4) {
+        const int tl = *clk.time - clk.t0[s];
+        if (slot_src_on(clk, tl)) {
+            const T* pl = planes + (long long)s * plane_ss + q;
+            T F = (T)0;
+            if (src_mode == 1) {
+                const T wt = (tl < nseries) ? (T)series[(long long)s * nseries + tl] : (T)0;
+                F = wt * pl[0];
+            } else {
+                for (int l = 0; l < 7; ++l) {
+                    int id;
+                    const double wl = lagrange_weight(clk, tl, L, l, &id);
+                    if (id >= 0) F = F + (T)wl * pl[(long long)id * A.NP];
+                }
+            }
+            rvz = rvz + F * zt[ZT_SRCDEP * A.nz + k];
+        }
+    }
+    T out[8] = {rcont, rvx, rvy, rvz, rp, rbx, rby, rbz};
+    if (k == 0 || k == A.nz - 1) {
+        #pragma unroll
+        for (int f = 0; f < 8; ++f) out[f] = (T)0;
+    }
+    if (damp) {
+        out[1] = out[1] - W(V8_DMX);
+        out[2] = out[2] - W(V8_DMY);
+        out[3] = out[3] - W(V8_DMZ);
+    }
+    T* ss = scr + (long long)s * 8 * A.FS;
+    #pragma unroll
+    for (int f = 0; f < 8; ++f) ss[f * A.FS + t] = out[f];
+}
+
+template <typename T>
+int mhd8_stage(sparc_ctx* c, T beta, int hs) {
+    MhdState& m = *c->mhd;
+    const int S = c->active_n, nz = c->nz;
+    MhdArgs A;
+    A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
+    A.nzpml = std::max(c->nzpml, 1);
+    A.S = S;
+    A.both = 1;
+    A.nf = 8;
+    T* work = (T*)m.work;
+    const T* zt = (const T*)c->zt;
+    const long long N = c->N, fst = (long long)V8_COUNT * N;
+    const dim3 g(nb256(N), S);
+    auto Wp = [&](int s, int f) { return work + ((size_t)s * V8_COUNT + f) * N; };
+    int rc;
+    mhd8_temp_kernel<T><<<g, 256, 0, c->stream>>>(A, (const T*)c->a, (const T*)c->scr, beta, hs, (const T*)m.bg, work);
+    c->launches++;
+    CKL();
+    // the six ddxyz calls (pml.f90:106-116), all with bc 1; x and y per
+    // source, z batched over the sources
+    static const int xs[6][2] = {{V8_T1, V8_DVXDX}, {V8_F3, V8_DXF3}, {V8_T4, V8_GPX},
+                                 {V8_F2, V8_DXF2}, {V8_T6, V8_DXBY}, {V8_T7, V8_DXBZ}};
+    static const int ys[6][2] = {{V8_T2, V8_DVYDY}, {V8_T4, V8_GPY}, {V8_F3, V8_DYF3},
+                                 {V8_T7, V8_DYBZ}, {V8_T5, V8_DYBX}, {V8_F1, V8_DYF1}};
+    static const int zs[6][2] = {{V8_T3, V8_DVZDZ}, {V8_F1, V8_DZF1}, {V8_F2, V8_DZF2},
+                                 {V8_T5, V8_DZBX}, {V8_T4, V8_GPZ}, {V8_T6, V8_DZBY}};
+    for (int d = 0; d < 6; ++d) {
+        for (int s = 0; s < S; ++s)
+            if ((rc = ddx_launch<T>(c, Wp(s, xs[d][0]), Wp(s, xs[d][1]), nz)) ||
+                (rc = ddy_launch<T>(c, Wp(s, ys[d][0]), Wp(s, ys[d][1]), nz)))
+                return rc;
+        if ((rc = ddz_launch<T>(c, zt, Wp(0, zs[d][0]), Wp(0, zs[d][1]), 1, S, fst))) return rc;
+    }
+    // DAMP_VELOCITY (damping.f90:125-159) of v_x, v_y, v_z
+    const bool damp = c->P.damp_waves != 0;
+    if (damp) {
+        typedef typename CplxOf<T>::type CT;
+        for (int s = 0; s < S; ++s)
+            for (int q = 0; q < 3; ++q) {
+                fft_phys_to_spec<T>(Wp(s, V8_T1 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
+                                    c->tw_y, c->stream);
+                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, V8_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
+                                    c->tw_y, c->stream);
+                c->launches += 5;
+            }
+        CKL();
+    }
+    SlotClock clk;
+    memset(&clk, 0, sizeof(clk));
+    clk.t0 = c->d_t0; clk.time = c->d_time; clk.freq = c->freq_filtering; clk.two_d = 0;
+    clk.gate = c->forcing_length * c->cadforcing_step; clk.num_steps = c->num_steps;
+    clk.ts = R4(c->P.timestep); clk.cad = R4(c->P.cadforcing);
+    const int ksrc = (c->P.src_k > 0 ? c->P.src_k : c->e_rad) - 1;
+    mhd8_rhs_kernel<T><<<g, 256, 0, c->stream>>>(A, (const T*)m.bg, work, (const T*)m.pab, (const T*)m.pml,
+                                                  (T*)m.spml, beta, hs, (const T*)m.g, zt, damp ? 1 : 0,
+                                                  (T*)c->scr, clk, c->src_mode, (const T*)c->planes,
+                                                  (long long)c->src_L * c->NP, c->src_L, c->series, c->nseries,
+                                                  ksrc);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+}  // namespace
+
+namespace {
+
 template <typename T>
 int mhd_stage(sparc_ctx* c, T beta, int hs) {
     MhdState& m = *c->mhd;
@@ -1122,7 +1315,8 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
     A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
     A.nzpml = std::max(c->nzpml, 1);
     A.S = S;
-    A.both = (c->P.option == 18);
+    A.both = 0;
+    A.nf = 6;
     T* a = (T*)c->a;
     T* scr = (T*)c->scr;
     T* bg = (T*)m.bg;
@@ -1217,18 +1411,21 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
     A.N = c->N; A.NP = c->NP; A.FS = 2 * c->fs; A.nz = c->nz; A.nb = c->P.npmlbot; A.nt = c->P.npmltop;
     A.nzpml = std::max(c->nzpml, 1);
     A.S = c->active_n;
-    A.both = (c->P.option == 18);
+    A.both = (c->P.option == 18 || c->P.option == 8);
+    A.nf = c->nf;
     const int S = c->active_n;
     for (int it = 0; it < nsteps; ++it) {
         int rc;
         const bool two_d = (c->P.option == 18);
         for (int rk = 0; rk < 5; ++rk) {
-            rc = two_d ? mhd2d_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0)
-                       : mhd_stage<T>(c, (T)c->betas[rk], rk > 0 ? 1 : 0);
+            const T beta = (T)c->betas[rk];
+            const int hs = rk > 0 ? 1 : 0;
+            rc = two_d ? mhd2d_stage<T>(c, beta, hs)
+                       : (c->P.option == 8 ? mhd8_stage<T>(c, beta, hs) : mhd_stage<T>(c, beta, hs));
             if (rc) return rc;
         }
-        // update + z filter (step.f90:114-116, FILTER_VARS_3D)
-        mhd_update_kernel<T><<<dim3((unsigned)((c->NP + 127) / 128), 6 * S), 128, 0, c->stream>>>(
+        // update + z filter on all dimfive fields (step.f90:114-116, FILTER_VARS_3D)
+        mhd_update_kernel<T><<<dim3((unsigned)((c->NP + 127) / 128), c->nf * S), 128, 0, c->stream>>>(
             A, (T*)c->a, (const T*)c->scr, (T)c->deltat, two_d ? 1 : 0);
         const long long npv = (long long)S * PV_COUNT * A.nzpml * c->NP;
         mhd_pml_update_kernel<T><<<nb256(npv), 256, 0, c->stream>>>((T*)m.pml, (const T*)m.spml, (T)c->deltat, npv);
@@ -1241,7 +1438,7 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
             const int tl = c->time - c->t0[s];
             if (tl < 0 || (two_d ? (tl + 1) : tl) % c->freq_filtering != 0) continue;
             for (int f = 0; f < (two_d ? 6 : 5); ++f) {
-                T* fp = (T*)c->a + ((size_t)s * 6 + f) * 2 * c->fs;
+                T* fp = (T*)c->a + ((size_t)s * c->nf + f) * 2 * c->fs;
                 fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
                 launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 3, c->M, c->nz, 1, 0, 0, c->stream);
                 fft_spec_to_phys<T>((CT*)m.spec, fp, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
@@ -1252,7 +1449,7 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
         if (c->rec_on) {
             mhd_record_kernel<T><<<dim3(nb256(c->NP), S), 256, 0, c->stream>>>(
                 (const T*)c->a, (T*)c->rec, c->d_t0, c->d_time, c->steps, c->rec_max, 2 * c->fs, c->NP,
-                (long long)c->rec_max * 2 * c->M, m.plane_obs);
+                (long long)c->rec_max * 2 * c->M, m.plane_obs, c->nf, c->P.option == 8 ? 3 : 5);
             c->launches++;
             CKL();
         }
@@ -1269,6 +1466,6 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
 int mhd_steps(sparc_ctx* c, int nsteps) {
     if (!c->mhd || !c->mhd->have_bg)
         return fail(c, SPARC_ESTATE, c->P.option == 18 ? "option 18 needs sparc_gpu_set_mhd2d_background"
-                                                        : "option 10 needs sparc_gpu_set_mhd_background");
+                                                        : "options 8 and 10 need sparc_gpu_set_mhd_background");
     return c->f32 ? mhd_steps_t<float>(c, nsteps) : mhd_steps_t<double>(c, nsteps);
 }

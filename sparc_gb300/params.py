@@ -21,11 +21,12 @@ import numpy as np
 #: option codes of step.f90:74-110 that this framework implements
 OPT_QUIET_PML_3D = 2           # pml.f90:12 (MP_QUIET_PML_3D), velocity form
 OPT_QUIET_PML_3D_DISPL = 4     # displacement.f90:482 (MP_QUIET_PML_3D_DISPL)
+OPT_MHD_PML_3D = 8             # pml.f90:80 (MP_MHD_PML_3D), MHD velocity form
 OPT_MHD_PML_3D_DISPL = 10      # displacement.f90:663 (MP_MHD_PML_3D_DISPL)
 OPT_QUIET_PML_2D_DISPL = 17    # physics2d.f90:948 (MP_QUIET_PML_2D_DISPL)
 OPT_MHD_PML_2D_DISPL = 18      # physics2d.f90:724 (MP_MHD_PML_2D_DISPL)
-SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_MHD_PML_3D_DISPL, OPT_QUIET_PML_2D_DISPL,
-                     OPT_MHD_PML_2D_DISPL)
+SUPPORTED_OPTIONS = (OPT_QUIET_PML_3D, OPT_QUIET_PML_3D_DISPL, OPT_MHD_PML_3D, OPT_MHD_PML_3D_DISPL,
+                     OPT_QUIET_PML_2D_DISPL, OPT_MHD_PML_2D_DISPL)
 
 
 def r4(x: float) -> float:
@@ -133,7 +134,8 @@ class SparcParams:
         file.  Logical switches map as PARSE_OPTIONS (initialize.f90:778-824)
         does for the supported options: USE_PML must be true; without
         MAGNETIC, DISPL selects option 4 (true) or the velocity form, option 2
-        (false); MAGNETIC with DISPL selects option 10; FLOWS must be false."""
+        (false); MAGNETIC selects option 10 with DISPL, option 8 without; FLOWS
+        must be false."""
         vals: dict = {}
         body = re.sub(r"!.*", "", text)
         for m in re.finditer(r"parameter\s*\((.*?)\)\s*$", body, re.I | re.M | re.S):
@@ -149,14 +151,12 @@ class SparcParams:
         kw = {k: cls._KEYS[k](v) for k, v in vals.items() if not k.startswith("_")}
         if vals.get("_flows"):
             raise ValueError("FLOWS backgrounds are not supported by this framework")
-        if vals.get("_magnetic") and vals.get("_displ") is False:
-            raise ValueError("the MHD velocity form (option 8) is not supported")
         if "_damp_waves" in vals:
             kw["damp_waves"] = vals["_damp_waves"]
         if vals.get("_displ") is False:
             kw["option"] = OPT_QUIET_PML_3D
         if vals.get("_magnetic"):
-            kw["option"] = OPT_MHD_PML_3D_DISPL
+            kw["option"] = OPT_MHD_PML_3D if vals.get("_displ") is False else OPT_MHD_PML_3D_DISPL
         kw.update(overrides)
         p = cls(**kw)
         p.validate()
@@ -173,6 +173,8 @@ class SparcParams:
         if two_d:
             if self.option == OPT_QUIET_PML_3D:
                 raise ValueError("the 2-D velocity form (option 6) is not supported")
+            if self.option == OPT_MHD_PML_3D:
+                raise ValueError("the 2-D MHD velocity form (option 12) is not supported")
             two_d_of = {OPT_QUIET_PML_3D_DISPL: OPT_QUIET_PML_2D_DISPL, OPT_MHD_PML_3D_DISPL: OPT_MHD_PML_2D_DISPL}
             p = p.replace(option=two_d_of.get(self.option, self.option), ny=1)
         return p

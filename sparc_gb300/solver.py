@@ -160,13 +160,19 @@ class Solver:
 
     @property
     def npv(self) -> int:
-        """PML auxiliary fields: six for the MHD forms (options 10, 18), else two."""
-        return 6 if self.p.option in (10, 18) else 2
+        """PML auxiliary fields: six for the MHD forms (options 8, 10, 18), else two."""
+        return 6 if self.p.option in (8, 10, 18) else 2
+
+    @property
+    def nf(self) -> int:
+        """Fields of the state: eight in the MHD velocity form (option 8:
+        rho, v_x, v_y, v_z, p, b_x, b_y, b_z), else six."""
+        return 8 if self.p.option == 8 else 6
 
     def set_mhd_background(self, rho, c, p, bx, by, bz):
-        """3-D cgs background of option 10 (density, sound speed, pressure,
-        B_x, B_y, B_z), each (nz, ny, nx); set_background's quiet column is
-        the one the source planes are searched on."""
+        """3-D cgs background of options 8 and 10 (density, sound speed,
+        pressure, B_x, B_y, B_z), each (nz, ny, nx); set_background's quiet
+        column is the one the source planes are searched on."""
         arrs = [_f64(np.asarray(v, dtype=np.float64).reshape(self.shape)) for v in (rho, c, p, bx, by, bz)]
         self._ck(self.L.sparc_gpu_set_mhd_background(self.h, *[_dp(v) for v in arrs]))
 
@@ -177,15 +183,15 @@ class Solver:
         self._ck(self.L.sparc_gpu_set_mhd2d_background(self.h, *[_dp(v) for v in arrs]))
 
     def state(self, slot: int = 0):
-        a = np.zeros((6,) + self.shape)
+        a = np.zeros((self.nf,) + self.shape)
         pml = np.zeros((self.npv, self.p.nzpml, self.p.ny, self.p.nx))
         self._ck(self.L.sparc_gpu_get_state(self.h, slot, _dp(a), _dp(pml)))
         return a, pml
 
     def set_state(self, a: np.ndarray, pml: np.ndarray | None = None, slot: int = 0):
         a = _f64(a)
-        if a.shape != (6,) + self.shape:
-            raise ValueError("state must be (6, nz, ny, nx)")
+        if a.shape != (self.nf,) + self.shape:
+            raise ValueError(f"state must be ({self.nf}, nz, ny, nx)")
         pp = None
         if pml is not None:
             pml = _f64(pml)

@@ -2,7 +2,8 @@
 seeded cases (compact derivative for every boundary code, spectral
 derivatives, damping, three 3-D time steps with a forward source, thirty-one
 2-D time steps, thirty-one velocity-form steps, five MHD steps on a flux
-tube, thirty-one 2-D MHD steps on a flux sheet, one kernel accumulation).  Regenerate with
+tube, thirty-one MHD velocity-form steps on a flux tube, thirty-one 2-D MHD
+steps on a flux sheet, one kernel accumulation).  Regenerate with
     python tests/golden/make_golden.py
 The GPU parity tests compare the CUDA path against these fixtures as well as
 against the live oracle."""
@@ -42,6 +43,11 @@ def golden_mhd_background(p):
     return flux_tube_background(p, table_for(p), b_surf=800.0, r_surf_mm=8.0)
 
 
+def golden_params_mhd8():
+    """MHD velocity form (option 8): PML at both ends, flux-tube background."""
+    return small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4, option=8)
+
+
 def golden_params_mhd2d():
     """2-D MHD displacement form (option 18): PML at both ends, flux sheet."""
     return small_params_2d(nx=32, nz=32, npmlbot=4, npmltop=4, option=18)
@@ -54,6 +60,17 @@ def golden_mhd2d_background(p):
 
 def golden_inputs(p, seed):
     rng = np.random.default_rng(seed)
+    if p.option == 8:
+        # rho, v, p, b: a velocity perturbation at rest density, pressure
+        # and field; the induction drives b
+        a = rng.standard_normal((8, p.nz, p.ny, p.nx)) * 1e-3
+        a[0] = 0.0
+        a[4:] = 0.0
+        pml = rng.standard_normal((6, p.nzpml, p.ny, p.nx)) * 1e-5
+        pml[1, 0] = 0.0
+        X, Y = np.meshgrid(*(2 * [(np.arange(p.nx) / p.nx - 0.5) * p.xlength / 1e8]))
+        plane = np.exp(-(X ** 2 + Y ** 2) / 2.0)
+        return a, pml, plane, O.forward_source(p, 200) * 1e3
     a = rng.standard_normal((6, p.nz, p.ny, p.nx)) * 1e-3
     if p.ny == 1:
         a[1] = 0.0
@@ -130,6 +147,17 @@ def compute():
     st, _, pm = om.state()
     out["step5_mhd_a"] = st
     out["step5_mhd_pml"] = pm
+    # MHD velocity form: 31 steps cover the horizontal filter at time 30
+    p8 = golden_params_mhd8()
+    o8 = O.Oracle(p8, table_for(p8))
+    o8.set_mhd(*golden_mhd_background(p8))
+    a, pml, plane, series = golden_inputs(p8, 50)
+    o8.set_state(a * 1e-3, pml)
+    o8.set_source(1, plane[None].copy(), series)
+    o8.step(31)
+    st, _, pm = o8.state()
+    out["step31_mhd8_a"] = st
+    out["step31_mhd8_pml"] = pm
     # 2-D MHD: 31 steps cover the horizontal filter at mod(time+1, 30) = 0
     p18 = golden_params_mhd2d()
     o18 = O.Oracle(p18, table_for(p18))

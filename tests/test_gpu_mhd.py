@@ -206,3 +206,108 @@ def test_mhd2d_needs_its_background(gpu_lib):
         s.step(1)
     with pytest.raises(SparcError):
         s.set_mhd_background(*bg[:3], bg[3], bg[3], bg[3])      # the 3-D call belongs to option 10
+
+
+# ---- option 8: MP_MHD_PML_3D (pml.f90:80-208), the MHD velocity form ----------
+
+def _case8(prec="f64", **kw):
+    sys.path.insert(0, os.path.dirname(__file__))
+    from golden.make_golden import golden_mhd_background, golden_params_mhd8
+    p = golden_params_mhd8().replace(precision=prec, **kw)
+    return p, table_for(p), golden_mhd_background(p)
+
+
+def _state8(p, seed):
+    rng = np.random.default_rng(seed)
+    a = np.zeros((8, p.nz, p.ny, p.nx))
+    a[1:4] = rng.standard_normal((3, p.nz, p.ny, p.nx)) * 1e-6
+    a[5:] = rng.standard_normal((3, p.nz, p.ny, p.nx)) * 1e-9
+    pml = rng.standard_normal((6, p.nzpml, p.ny, p.nx)) * 1e-8
+    return a, pml
+
+
+@pytest.mark.parametrize("nsteps,mode", [(1, 1), (31, 1), (31, 2)])
+def test_mhd8_matches_oracle(gpu_lib, oracle_mod, nsteps, mode):
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case8()
+    g, o = Solver(p, tab), oracle_mod.Oracle(p, tab)
+    g.set_mhd_background(*bg)
+    o.set_mhd(*bg)
+    a0, pml0 = _state8(p, 35)
+    g.set_state(a0, pml0)
+    o.set_state(a0, pml0)
+    if mode == 1:
+        plane = gaussian_plane(p)
+        series = oracle_mod.forward_source(p, 200) * 1e3
+        g.set_source_series(plane, series)
+        o.set_source(1, plane[None].copy(), series)
+    else:
+        planes = np.random.default_rng(8).standard_normal((12, p.ny, p.nx)) * 1e-4
+        g.set_source_lagrange(planes)
+        o.set_source(2, planes, None)
+    g.step(nsteps)
+    o.step(nsteps)
+    ag, pg = g.state()
+    ao, _, po = o.state()
+    assert ag.shape[0] == 8
+    for f in range(8):
+        assert rel_l2(ag[f], ao[f]) < TOL64, (f, rel_l2(ag[f], ao[f]))
+    for f in range(6):
+        assert rel_l2(pg[f], po[f]) < TOL64, ("pml", f, rel_l2(pg[f], po[f]))
+
+
+def test_mhd8_matches_committed_fixture(gpu_lib):
+    from sparc_gb300.solver import Solver
+    from golden.make_golden import golden_inputs
+    p, tab, bg = _case8()
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_golden.npz"))
+    s = Solver(p, tab)
+    s.set_mhd_background(*bg)
+    a, pml, plane, series = golden_inputs(p, 50)
+    s.set_state(a * 1e-3, pml)
+    s.set_source_series(plane, series)
+    s.step(31)
+    st, pm = s.state()
+    for f in range(8):
+        assert rel_l2(st[f], g["step31_mhd8_a"][f]) < TOL64, f
+    assert rel_l2(pm, g["step31_mhd8_pml"]) < TOL64
+
+
+def test_mhd8_fp32_and_records(gpu_lib, oracle_mod):
+    """FP32 against FP64, and the surface records: v_z (field 4 of the
+    velocity form) on the observation plane."""
+    from sparc_gb300.solver import Solver
+    out = []
+    for prec in ("f64", "f32"):
+        p, tab, bg = _case8(prec)
+        s = Solver(p, tab)
+        s.set_mhd_background(*bg)
+        a0, pml0 = _state8(p, 36)
+        s.set_state(a0, pml0)
+        s.set_source_series(gaussian_plane(p), oracle_mod.forward_source(p, 200) * 1e3)
+        s.record_surface(3)
+        s.step(16)
+        out.append((s.state()[0], s.records(), s.info()["o_rad"]))
+    (a64, r64, orad), (a32, r32, _) = out
+    for f in range(8):
+        assert rel_l2(a32[f], a64[f]) < 1e-4, (f, rel_l2(a32[f], a64[f]))
+    assert r64.shape[0] == 2
+    assert rel_l2(r32, r64) < 1e-4
+    assert rel_l2(r64[1], a64[3, int(orad) - 1]) < 1e-15
+
+
+def test_mhd8_state_shape_and_fields(gpu_lib):
+    from sparc_gb300.native import SparcError
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case8()
+    s = Solver(p, tab)
+    with pytest.raises(SparcError):
+        s.step(1)                                       # no magnetic background yet
+    s.set_mhd_background(*bg)
+    a0, pml0 = _state8(p, 37)
+    s.set_state(a0, pml0)
+    assert np.array_equal(s.field(7), a0[7])           # b_z, the eighth field
+    with pytest.raises(ValueError):
+        s.set_state(a0[:6], pml0)
+    with pytest.raises(SparcError):
+        s.field(16)

@@ -42,15 +42,18 @@ def test_params_i_parsing_and_instruction():
 
 def test_params_magnetic_selects_option_10():
     """PARSE_OPTIONS (initialize.f90:778-824): MAGNETIC + DISPL + USE_PML -> 10,
-    and 18 with a 2D instruction; the MHD velocity form (8) and FLOWS are not built."""
+    and 18 with a 2D instruction; MAGNETIC without DISPL -> 8 (its 2-D form,
+    12, and FLOWS are not built)."""
     mag = PARAMS_I.replace("magnetic = .false.", "magnetic = .true.")
     assert SparcParams.from_params_i(mag).option == 10
     q = SparcParams.from_params_i(mag).instruction("adjoint\n2D\n")
     assert q.option == 18 and q.ny == 1 and q.compute_adjoint
     with pytest.raises(ValueError):
         SparcParams(option=18, ny=4).validate()
+    q8 = SparcParams.from_params_i(mag + "logical, parameter :: DISPL = .false.\n")
+    assert q8.option == 8
     with pytest.raises(ValueError):
-        SparcParams.from_params_i(mag + "logical, parameter :: DISPL = .false.\n")
+        q8.instruction("spectral\n2D\n")
     with pytest.raises(ValueError):
         SparcParams.from_params_i(PARAMS_I.replace("FLOWS = .FALSE.", "FLOWS = .TRUE."))
     assert SparcParams.from_params_i(PARAMS_I + "logical, parameter :: DISPL = .false.\n").option == 2
@@ -60,9 +63,10 @@ def test_params_validation():
     with pytest.raises(ValueError):
         SparcParams(nx=100).validate()
     with pytest.raises(ValueError):
-        SparcParams(option=8).validate()
+        SparcParams(option=12).validate()            # the 2-D MHD velocity form is not built
     with pytest.raises(ValueError):
         SparcParams(option=17, ny=4).validate()
+    SparcParams(option=8).validate()
     SparcParams(option=10).validate()
     SparcParams().validate()
 

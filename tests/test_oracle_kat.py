@@ -376,3 +376,44 @@ def test_mhd2d_runs_and_drives_both_pml_layers():
         assert np.abs(pml[i, :4]).max() > 0 and np.abs(pml[i, 4:]).max() > 0, i
     assert np.abs(pml[3]).max() == 0 and np.abs(pml[5]).max() == 0
     assert np.abs(st[1]).max() == 0 and np.abs(st[4]).max() == 0
+
+
+def test_mhd8_without_field_keeps_b_at_zero():
+    """MP_MHD_PML_3D (pml.f90:80-208) with B0 = 0: the fluxes of v x B0
+    vanish, so b and the four magnetic PML auxiliaries stay exactly zero
+    while the hydrodynamic fields evolve."""
+    from oracle import oracle as O
+    from cases import small_params, table_for
+    p = small_params(nx=16, ny=16, nz=32, npmlbot=4, npmltop=4, option=8)
+    tab = table_for(p)
+    o = O.Oracle(p, tab)
+    rho = np.broadcast_to(tab[:, 2][:, None, None], o.shape).copy()
+    c = np.broadcast_to(tab[:, 1][:, None, None], o.shape).copy()
+    pr = np.broadcast_to(tab[:, 3][:, None, None], o.shape).copy()
+    z = np.zeros(o.shape)
+    o.set_mhd(rho, c, pr, z, z, z)
+    a = np.zeros((8,) + o.shape)
+    a[1:4] = np.random.default_rng(3).standard_normal((3,) + o.shape) * 1e-6
+    o.set_state(a)
+    o.step(31)
+    st, _, pml = o.state()
+    assert np.abs(st[5:]).max() == 0.0
+    assert np.abs(pml[2:]).max() == 0.0
+    assert np.isfinite(st).all() and np.abs(st[1:4]).max() > 0 and np.abs(pml[:2]).max() > 0
+
+
+def test_mhd8_drives_induction_and_both_pml_layers():
+    from oracle import oracle as O
+    p, tab, bg = _mhd_case()
+    p = p.replace(option=8, npmltop=4)
+    o = O.Oracle(p, tab)
+    o.set_mhd(*bg)
+    a = np.zeros((8,) + o.shape)
+    a[1:4] = np.random.default_rng(4).standard_normal((3,) + o.shape) * 1e-6
+    o.set_state(a)
+    o.step(5)
+    st, _, pml = o.state()
+    assert np.isfinite(st).all()
+    assert np.abs(st[5:]).max() > 0                       # b from the induction equation
+    for i in range(6):
+        assert np.abs(pml[i, :4]).max() > 0 and np.abs(pml[i, 4:]).max() > 0, i
