@@ -171,10 +171,13 @@ class SparcParams:
         two_d = len(lines) > 1 and lines[1].upper() == "2D"
         p = self.replace(compute_forward=(kind == "spectral"), compute_adjoint=(kind == "adjoint"))
         if two_d:
-            if self.option == OPT_QUIET_PML_3D:
-                raise ValueError("the 2-D velocity form (option 6) is not supported")
-            if self.option == OPT_MHD_PML_3D:
-                raise ValueError("the 2-D MHD velocity form (option 12) is not supported")
+            # READ_PARAMETERS turns every 2-D kernel-mode run into option 17
+            # or 18 (initialize.f90:315,1081-1084), both displacement forms;
+            # with DISPL = .false. the reference has sized the state for the
+            # velocity form by then (initialize.f90:310-312)
+            if self.option in (OPT_QUIET_PML_3D, OPT_MHD_PML_3D):
+                raise ValueError("a 2D instruction selects the displacement forms 17/18; "
+                                 "DISPL = .false. has no consistent 2-D run")
             two_d_of = {OPT_QUIET_PML_3D_DISPL: OPT_QUIET_PML_2D_DISPL, OPT_MHD_PML_3D_DISPL: OPT_MHD_PML_2D_DISPL}
             p = p.replace(option=two_d_of.get(self.option, self.option), ny=1)
         return p
