@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--small", action="store_true", help="128x128x150 smoke-size workload")
     ap.add_argument("--skip-mhd", action="store_true", help="skip the flux-tube (option 10) line")
+    ap.add_argument("--mhd-only", action="store_true",
+                    help="only the flux-tube line (--steps timed, --warmup untimed), for profiling")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
     return ap.parse_args()
@@ -385,6 +387,10 @@ def main():
     b.build()
     from sparc_gb300 import bytes_model
     p0, tab = workload(args.small)
+    if args.mhd_only:
+        print(json.dumps({"mhd": mhd_section(p0, tab, steps=max(1, args.steps), warmup=max(1, args.warmup))}),
+              flush=True)
+        return 0
     K, W = max(1, args.steps), max(3, args.warmup)
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")

@@ -124,48 +124,6 @@ __global__ void cols_fft_kernel(const typename CplxOf<T>::type* __restrict__ in,
 // CTA.  W_m^j = exp(sign 2 pi i j / m) comes from the FP64 table tw
 // (cos, sin of 2 pi q / n for q < n/2).
 
-template <typename T, typename CT>
-__device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, T sign) {
-    // W_n^q for 0 <= q < n
-    const int h = n >> 1;
-    const bool flip = q >= h;
-    const int r = flip ? q - h : q;
-    T c = (T)__ldg(&tw[2 * r]), sn = sign * (T)__ldg(&tw[2 * r + 1]);
-    if (flip) { c = -c; sn = -sn; }
-    CT w;
-    w.x = c;
-    w.y = sn;
-    return w;
-}
-
-// in-register DFT of length R (decimation in frequency): on return v[brev(k)]
-// holds X[k]; w[j] = W_R^j for j < R/2
-template <typename CT, int R>
-__device__ __forceinline__ void reg_dft(CT (&v)[R], const CT (&w)[R / 2]) {
-    #pragma unroll
-    for (int len = R; len >= 2; len >>= 1) {
-        const int half = len >> 1, step = R / len;
-        #pragma unroll
-        for (int b = 0; b < R; b += len) {
-            #pragma unroll
-            for (int k = 0; k < half; ++k) {
-                const CT a = v[b + k], c = v[b + k + half];
-                v[b + k] = a + c;
-                const CT d = a - c;
-                v[b + k + half] = (k == 0) ? d : cmul(d, w[k * step]);
-            }
-        }
-    }
-}
-
-template <int R>
-__host__ __device__ constexpr int brev(int k) {
-    int r = 0;
-    for (int b = 1, m = R >> 1; b < R; b <<= 1, m >>= 1)
-        if (k & b) r |= m;
-    return r;
-}
-
 // complex FFT along y (length ny = R*R) for NC = 256/R kx-columns per CTA;
 // data [plane][y][kx] with H columns per row
 template <typename T, int R>
@@ -265,6 +223,57 @@ __global__ void __launch_bounds__(256) rows_c2r_sq_kernel(const typename CplxOf<
     }
 }
 
+// forward real transform along x (length nx = R*R) of two rows packed as one
+// complex FFT, split by Hermitian symmetry and scaled as rows_r2c_kernel;
+// NP = 256/R row pairs per CTA
+template <typename T, int R>
+__global__ void __launch_bounds__(256) rows_r2c_sq_kernel(const T* __restrict__ phys,
+                                                          typename CplxOf<T>::type* __restrict__ out,
+                                                          long long nrows, T scale, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int nx = R * R, H = nx / 2 + 1, NP = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int r = threadIdx.x % R, pp = threadIdx.x / R;
+    CT* Zp = (CT*)smraw + pp * R * (R + 1);              // [k1][R+1], then the spectrum [k]
+    const long long r0 = 2LL * ((long long)blockIdx.x * NP + pp), r1 = r0 + 1;
+    const bool has0 = r0 < nrows, has1 = r1 < nrows;
+    CT w[R / 2];
+    #pragma unroll
+    for (int j = 0; j < R / 2; ++j) w[j] = tw_n<T, CT>(tw, j * R, nx, (T)-1);
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) {
+        v[n1].x = has0 ? phys[r0 * nx + R * n1 + r] : (T)0;
+        v[n1].y = has1 ? phys[r1 * nx + R * n1 + r] : (T)0;
+    }
+    reg_dft<CT, R>(v, w);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = v[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, nx, (T)-1));
+        Zp[k1 * (R + 1) + r] = y;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) v[n2] = Zp[r * (R + 1) + n2];
+    reg_dft<CT, R>(v, w);
+    __syncthreads();                                     // the tile now takes the spectrum
+    #pragma unroll
+    for (int k2 = 0; k2 < R; ++k2) Zp[r + R * k2] = v[brev<R>(k2)];
+    __syncthreads();
+    const T hs = (T)0.5 * scale;
+    for (int k = r; k < H; k += R) {
+        const CT zk = Zp[k], zn = Zp[(nx - k) & (nx - 1)];
+        CT x1, x2;
+        x1.x = (zk.x + zn.x) * hs;
+        x1.y = (zk.y - zn.y) * hs;
+        x2.x = (zk.y + zn.y) * hs;
+        x2.y = -(zk.x - zn.x) * hs;
+        if (has0) out[r0 * H + k] = x1;
+        if (has1) out[r1 * H + k] = x2;
+    }
+}
+
 static int sq_radix(int n) { return n == 256 ? 16 : (n == 64 ? 8 : 0); }
 
 static int col_tile(int ny) { return ny >= 1024 ? 4 : (ny >= 512 ? 8 : 16); }
@@ -282,13 +291,40 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
     typedef typename CplxOf<T>::type CT;
     const int H = nx / 2 + 1;
     const long long nrows = (long long)ny * nplanes;
-    size_t sm = 2 * (size_t)nx * sizeof(CT);
-    int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
-    set_smem<T>((const void*)rows_r2c_kernel<T>, sm);
     CT* dst = (ny == 1) ? spec : tmp;
-    rows_r2c_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(phys, dst, nx, nrows,
-                                                                     (T)(1.0 / ((double)nx * ny)), tw_x);
-    if (ny > 1) {
+    const T scale = (T)(1.0 / ((double)nx * ny));
+    const int Rx = sq_radix(nx);
+    if (Rx) {
+        const long long rows_per_cta = 2LL * (256 / Rx);
+        const unsigned grid = (unsigned)((nrows + rows_per_cta - 1) / rows_per_cta);
+        const size_t smr = (size_t)(256 / Rx) * Rx * (Rx + 1) * sizeof(CT);
+        if (Rx == 16) {
+            set_smem<T>((const void*)rows_r2c_sq_kernel<T, 16>, smr);
+            rows_r2c_sq_kernel<T, 16><<<grid, 256, smr, s>>>(phys, dst, nrows, scale, tw_x);
+        } else {
+            set_smem<T>((const void*)rows_r2c_sq_kernel<T, 8>, smr);
+            rows_r2c_sq_kernel<T, 8><<<grid, 256, smr, s>>>(phys, dst, nrows, scale, tw_x);
+        }
+    } else {
+        size_t sm = 2 * (size_t)nx * sizeof(CT);
+        int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
+        set_smem<T>((const void*)rows_r2c_kernel<T>, sm);
+        rows_r2c_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(phys, dst, nx, nrows, scale, tw_x);
+    }
+    const int Ry = sq_radix(ny);
+    if (ny > 1 && Ry) {
+        const int NC = 256 / Ry, ntile = (H + NC - 1) / NC;
+        const size_t smc = (size_t)ny * NC * sizeof(CT);
+        if (Ry == 16) {
+            set_smem<T>((const void*)cols_fft_sq_kernel<T, 16>, smc);
+            cols_fft_sq_kernel<T, 16><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, spec, H, (T)-1,
+                                                                                             tw_y, nplanes, 0LL);
+        } else {
+            set_smem<T>((const void*)cols_fft_sq_kernel<T, 8>, smc);
+            cols_fft_sq_kernel<T, 8><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, spec, H, (T)-1,
+                                                                                            tw_y, nplanes, 0LL);
+        }
+    } else if (ny > 1) {
         int W = col_tile(ny);
         size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
         set_smem<T>((const void*)cols_fft_kernel<T>, sm2);

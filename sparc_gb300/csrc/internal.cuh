@@ -202,6 +202,50 @@ __device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, i
 // Stockham radix-2 over `count` sequences of length n stored back to back in
 // src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
 // cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
+// ---- register DFTs of the two-pass transforms (n = R*R) -----------------------
+template <typename T, typename CT>
+__device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, T sign) {
+    // W_n^q for 0 <= q < n
+    const int h = n >> 1;
+    const bool flip = q >= h;
+    const int r = flip ? q - h : q;
+    T c = (T)__ldg(&tw[2 * r]), sn = sign * (T)__ldg(&tw[2 * r + 1]);
+    if (flip) { c = -c; sn = -sn; }
+    CT w;
+    w.x = c;
+    w.y = sn;
+    return w;
+}
+
+// in-register DFT of length R (decimation in frequency): on return v[brev(k)]
+// holds X[k]; w[j] = W_R^j for j < R/2
+template <typename CT, int R>
+__device__ __forceinline__ void reg_dft(CT (&v)[R], const CT (&w)[R / 2]) {
+    #pragma unroll
+    for (int len = R; len >= 2; len >>= 1) {
+        const int half = len >> 1, step = R / len;
+        #pragma unroll
+        for (int b = 0; b < R; b += len) {
+            #pragma unroll
+            for (int k = 0; k < half; ++k) {
+                const CT a = v[b + k], c = v[b + k + half];
+                v[b + k] = a + c;
+                const CT d = a - c;
+                v[b + k + half] = (k == 0) ? d : cmul(d, w[k * step]);
+            }
+        }
+    }
+}
+
+template <int R>
+__host__ __device__ constexpr int brev(int k) {
+    int r = 0;
+    for (int b = 1, m = R >> 1; b < R; b <<= 1, m >>= 1)
+        if (k & b) r |= m;
+    return r;
+}
+
+
 template <typename T, typename CT>
 __device__ __forceinline__ CT* smem_fft(CT* src, CT* dst, int n, int count, T sign, const double* __restrict__ tw) {
     const int half = n >> 1;

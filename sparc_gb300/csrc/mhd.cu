@@ -101,6 +101,113 @@ __global__ void rowderiv_kernel(const T* __restrict__ in, T* __restrict__ out, i
     }
 }
 
+// ---- spectral derivative of packed lines of length n = R*R (R = 8, 16) ------
+// Thread r holds v[n1] = z[R n1 + r] of one packed line z (two real lines as
+// real and imaginary parts).  Forward two-pass DFT (n = R n1 + n2, k = k1 +
+// R k2: thread n2 does the DFT over n1, twiddle W^(n2 k1), exchange, thread k1
+// the DFT over n2), times i*mul[k], then the inverse in the mirrored order
+// (thread k1: DFT over k2, twiddle W^-(n2 k1), exchange, thread n2: DFT over
+// k1), so that on return v[n1] holds the derivative at R n1 + r again.  The
+// derivative operator is real, so the two packed lines stay separate.
+// zs(a, b) is the exchange cell (row a, column b) of this line's R x R tile.
+template <typename T, typename CT, int R, typename ZS>
+__device__ __forceinline__ void deriv_sq(CT (&v)[R], int r, ZS zs, const T* __restrict__ mul,
+                                         const double* __restrict__ tw) {
+    constexpr int n = R * R;
+    CT wf[R / 2], wi[R / 2];
+    #pragma unroll
+    for (int j = 0; j < R / 2; ++j) {
+        wf[j] = tw_n<T, CT>(tw, j * R, n, (T)-1);
+        wi[j] = tw_n<T, CT>(tw, j * R, n, (T)1);
+    }
+    reg_dft<CT, R>(v, wf);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = v[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, n, (T)-1));
+        zs(k1, r) = y;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) v[n2] = zs(r, n2);
+    __syncthreads();                                   // the tile is rewritten below
+    reg_dft<CT, R>(v, wf);
+    CT u[R];
+    #pragma unroll
+    for (int k2 = 0; k2 < R; ++k2) {
+        const CT X = v[brev<R>(k2)];
+        const T m = __ldg(&mul[r + R * k2]);
+        u[k2].x = -m * X.y;
+        u[k2].y = m * X.x;
+    }
+    reg_dft<CT, R>(u, wi);
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) {
+        CT y = u[brev<R>(n2)];
+        if (n2 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * n2, n, (T)1));
+        zs(n2, r) = y;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) u[k1] = zs(r, k1);
+    reg_dft<CT, R>(u, wi);
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) v[n1] = u[brev<R>(n1)];
+}
+
+// d/dx of nrows dense rows of nx = R*R reals: 256/R row pairs per CTA, R
+// threads per pair
+template <typename T, int R>
+__global__ void __launch_bounds__(256) rowderiv_sq_kernel(const T* __restrict__ in, T* __restrict__ out,
+                                                          long long nrows, const T* __restrict__ mul,
+                                                          const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int nx = R * R, NPR = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int r = threadIdx.x % R, pp = threadIdx.x / R;
+    CT* Zp = (CT*)smraw + pp * R * (R + 1);
+    const long long r0 = 2LL * ((long long)blockIdx.x * NPR + pp), r1 = r0 + 1;
+    const bool has0 = r0 < nrows, has1 = r1 < nrows;
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) {
+        v[n1].x = has0 ? in[r0 * nx + R * n1 + r] : (T)0;
+        v[n1].y = has1 ? in[r1 * nx + R * n1 + r] : (T)0;
+    }
+    deriv_sq<T, CT, R>(v, r, [&](int a, int b) -> CT& { return Zp[a * (R + 1) + b]; }, mul, tw);
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) {
+        if (has0) out[r0 * nx + R * n1 + r] = v[n1].x;
+        if (has1) out[r1 * nx + R * n1 + r] = v[n1].y;
+    }
+}
+
+// d/dy of nplanes dense (ny, nx) planes, ny = R*R: 256/R pairs of adjacent
+// x-columns per CTA (read and written as one complex value), R threads per pair
+template <typename T, int R>
+__global__ void __launch_bounds__(256) colderiv_sq_kernel(const T* __restrict__ in, T* __restrict__ out, int nx,
+                                                          const T* __restrict__ mul, const double* __restrict__ tw) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int ny = R * R, NC = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* Z = (CT*)smraw;
+    const int npair = nx / 2, ntile = (npair + NC - 1) / NC;
+    const long long plane = blockIdx.x / ntile;
+    const int c = threadIdx.x % NC, r = threadIdx.x / NC;
+    const int cp = (blockIdx.x % ntile) * NC + c;
+    const bool cv = cp < npair;
+    const CT* src = (const CT*)(in + plane * (long long)ny * nx) + cp;
+    CT* dst = (CT*)(out + plane * (long long)ny * nx) + cp;
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) v[n1] = cv ? src[(long long)(R * n1 + r) * npair] : czero<CT>();
+    deriv_sq<T, CT, R>(v, r, [&](int a, int b) -> CT& { return Z[(a * R + b) * NC + c]; }, mul, tw);
+    if (cv) {
+        #pragma unroll
+        for (int n1 = 0; n1 < R; ++n1) dst[(long long)(R * n1 + r) * npair] = v[n1];
+    }
+}
+
 // d/dy of nplanes dense (ny, nx) planes: W complex columns (2W real x) per CTA
 template <typename T>
 __global__ void colderiv_kernel(const T* __restrict__ in, T* __restrict__ out, int nx, int ny, int W,
@@ -160,6 +267,128 @@ __global__ void __launch_bounds__(128) zderiv_phys_kernel(const T* __restrict__ 
     for (int j = nz - 2; j >= 0; --j) {
         ud = o[(long long)j * npix] - gam[j + 1] * ud;
         o[(long long)j * npix] = ud * zt[ZT_STRETCH * nz + j];
+    }
+}
+
+// DBYD2's right-hand side of row j (0-based) for boundary code bc (the rows of
+// compact_forward): interior 6th-order stencil, 5th-order rows 1 and nz-2,
+// the bc-dependent closures of rows 0 and nz-1 (caller-set bot / top for bc 2 / 3)
+template <typename T, typename Ld>
+__device__ __forceinline__ T compact_rhs_row(int j, int nz, int bc, Ld B, T bot, T top, const Compact<T>& c) {
+    if (j >= 2 && j <= nz - 3) return c.C1 * (B(j + 1) - B(j - 1)) + c.C2 * (B(j + 2) - B(j - 2));
+    if (j == 1 || j == 0) {
+        const T R1 = c.Cb[0] * B(0) + c.Cb[1] * B(1) + c.Cb[2] * B(2) + c.Cb[3] * B(3) + c.Cb[4] * B(4);
+        if (j == 1) return R1;
+        if (bc == 0) return (T)0;
+        if (bc == 2) return bot;
+        const T R0 = c.Cf[0] * B(0) + c.Cf[1] * B(1) + c.Cf[2] * B(2) + c.Cf[3] * B(3);
+        return (c.alpha2 * R0 - c.beta1 * R1) * c.cnst;
+    }
+    const T Rn2 = -(c.Cb[0] * B(nz - 1) + c.Cb[1] * B(nz - 2) + c.Cb[2] * B(nz - 3) + c.Cb[3] * B(nz - 4) +
+                    c.Cb[4] * B(nz - 5));
+    if (j == nz - 2) return Rn2;
+    if (bc == 0) return (T)0;
+    if (bc == 3) return top;
+    const T Rn1 = -(c.Cf[0] * B(nz - 1) + c.Cf[1] * B(nz - 2) + c.Cf[2] * B(nz - 3) + c.Cf[3] * B(nz - 4));
+    return (c.alpha2 * Rn1 - c.beta1 * Rn2) * c.cnst;
+}
+
+// d/dz of dense fields (DBYD2 * stretch) by chunks: 32 pencils per CTA (one
+// per lane), NCH warps, warp w owning planes [w*cs, w*cs + cs).  Forward
+// elimination y_j = (R_j - low_j y_{j-1}) ibd_j is affine in y_{j-1}: each
+// warp eliminates its chunk from zero (y'), keeping the product of the
+// multipliers -low_j ibd_j, and after one barrier adds the carry-in composed
+// from the chunks below.  The back substitution x_j = y_j - gam_{j+1} x_{j+1}
+// runs the same way from the top.  y and x stay in shared memory; each
+// element is read once and written once.
+template <typename T, int NCH>
+__global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restrict__ zt, Compact<T> cc,
+                                                                const T* __restrict__ in, T* __restrict__ out,
+                                                                long long npix, int nz, int bc, long long fstride,
+                                                                const T* __restrict__ topsrc, T topscale) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* Y = (T*)smraw;                        // [nz][32]
+    T* Cy = Y + (long long)nz * 32;          // [NCH][32] chunk-end value
+    T* Cp = Cy + NCH * 32;                   // [NCH][32] chunk multiplier product
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long m = (long long)blockIdx.x * 32 + lane;
+    const bool on = m < npix;
+    const T* b = in + blockIdx.y * fstride + (on ? m : 0);
+    T* o = out + blockIdx.y * fstride + m;
+    const T* low = zt + (ZT_TH + 3 * bc) * nz;
+    const T* ibd = zt + (ZT_TH + 3 * bc + 1) * nz;
+    const T* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
+    const T* str = zt + ZT_STRETCH * nz;
+    const int cs = (nz + NCH - 1) / NCH;
+    const int s = w * cs, e = min(nz, s + cs) - 1;   // empty chunk when s > e
+    auto B = [&](int j) -> T { return b[(long long)j * npix]; };
+    const T top = (topsrc && on) ? topscale * topsrc[blockIdx.y * fstride + (long long)(nz - 1) * npix + m] : (T)0;
+    // stage the chunk's input in its own rows of Y (independent loads), the
+    // two planes either side in registers
+    T h0 = (T)0, h1 = (T)0, h2 = (T)0, h3 = (T)0;
+    if (s <= e) {
+        #pragma unroll 8
+        for (int j = s; j <= e; ++j) Y[j * 32 + lane] = B(j);
+        h0 = s >= 2 ? B(s - 2) : (T)0;
+        h1 = s >= 1 ? B(s - 1) : (T)0;
+        h2 = e + 1 < nz ? B(e + 1) : (T)0;
+        h3 = e + 2 < nz ? B(e + 2) : (T)0;
+    }
+    __syncwarp();
+    auto V = [&](int j) -> T {             // b_j for j in [s-2, e+2]
+        return j < s ? (j == s - 2 ? h0 : h1) : (j > e ? (j == e + 1 ? h2 : h3) : Y[j * 32 + lane]);
+    };
+    // forward, local; row j of Y is overwritten with y'_j after its last use
+    T y = (T)0, pr = (T)1;
+    if (s <= e) {
+        T wm2 = V(s - 2), wm1 = V(s - 1), w0 = V(s), w1 = V(s + 1), w2 = V(s + 2);
+        for (int j = s; j <= e; ++j) {
+            T R;
+            if (j >= 2 && j <= nz - 3) R = cc.C1 * (w1 - wm1) + cc.C2 * (w2 - wm2);
+            else R = compact_rhs_row<T>(j, nz, bc, B, (T)0, top, cc);
+            const T l = j > 0 ? __ldg(&low[j]) : (T)0, ib = __ldg(&ibd[j]);
+            y = (R - l * y) * ib;
+            pr = pr * (-l * ib);
+            wm2 = wm1; wm1 = w0; w0 = w1; w1 = w2;
+            w2 = V(j + 3);
+            Y[j * 32 + lane] = y;
+        }
+    }
+    Cy[w * 32 + lane] = y;
+    Cp[w * 32 + lane] = pr;
+    __syncthreads();
+    T cin = (T)0;
+    for (int q = 0; q < w; ++q) cin = Cy[q * 32 + lane] + Cp[q * 32 + lane] * cin;
+    // forward fix-up, then backward, local
+    T x = (T)0;
+    pr = (T)1;
+    if (s <= e) {
+        if (w > 0) {
+            T pj = (T)1;
+            for (int j = s; j <= e; ++j) {
+                pj = pj * (-__ldg(&low[j]) * __ldg(&ibd[j]));
+                Y[j * 32 + lane] = Y[j * 32 + lane] + pj * cin;
+            }
+        }
+        for (int j = e; j >= s; --j) {
+            const T g = j + 1 < nz ? __ldg(&gam[j + 1]) : (T)0;
+            x = Y[j * 32 + lane] - g * x;
+            pr = pr * (-g);
+            Y[j * 32 + lane] = x;
+        }
+    }
+    __syncthreads();                         // all chunk-end values of the forward pass are read
+    Cy[w * 32 + lane] = x;                   // x' at the chunk's first plane
+    Cp[w * 32 + lane] = pr;
+    __syncthreads();
+    T xin = (T)0;
+    for (int q = NCH - 1; q > w; --q) xin = Cy[q * 32 + lane] + Cp[q * 32 + lane] * xin;
+    if (s <= e && on) {
+        T pj = (T)1;
+        for (int j = e; j >= s; --j) {
+            pj = pj * (j + 1 < nz ? -__ldg(&gam[j + 1]) : (T)0);
+            o[(long long)j * npix] = (Y[j * 32 + lane] + pj * xin) * __ldg(&str[j]);
+        }
     }
 }
 
@@ -482,6 +711,22 @@ template <typename T>
 int ddx_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
     const int nx = c->P.nx;
     const long long nrows = nplanes * c->P.ny;
+    typedef typename CplxOf<T>::type CT;
+    if (nx == 256 || nx == 64) {
+        const long long rows_per_cta = 2LL * (256 / (nx == 256 ? 16 : 8));
+        const unsigned grid = (unsigned)((nrows + rows_per_cta - 1) / rows_per_cta);
+        if (nx == 256) {
+            const size_t sm = (size_t)16 * 16 * 17 * sizeof(CT);
+            cudaFuncSetAttribute((const void*)rowderiv_sq_kernel<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            rowderiv_sq_kernel<T, 16><<<grid, 256, sm, c->stream>>>(in, out, nrows, (const T*)c->mhd->rx, c->tw_x);
+        } else {
+            const size_t sm = (size_t)32 * 8 * 9 * sizeof(CT);
+            rowderiv_sq_kernel<T, 8><<<grid, 256, sm, c->stream>>>(in, out, nrows, (const T*)c->mhd->rx, c->tw_x);
+        }
+        c->launches++;
+        CKL();
+        return SPARC_OK;
+    }
     const size_t sm = 2 * (size_t)nx * sizeof(typename CplxOf<T>::type);
     const int thr = nx / 2 < 32 ? 32 : (nx / 2 > 256 ? 256 : nx / 2);
     rowderiv_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, c->stream>>>(in, out, nx, nrows, (const T*)c->mhd->rx,
@@ -494,6 +739,24 @@ int ddx_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
 template <typename T>
 int ddy_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
     const int nx = c->P.nx, ny = c->P.ny;
+    typedef typename CplxOf<T>::type CT;
+    if (ny == 256 || ny == 64) {
+        const int R = ny == 256 ? 16 : 8, NC = 256 / R;
+        const long long ntile = (nx / 2 + NC - 1) / NC;
+        const size_t sm = (size_t)R * R * NC * sizeof(CT);
+        if (ny == 256) {
+            cudaFuncSetAttribute((const void*)colderiv_sq_kernel<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            colderiv_sq_kernel<T, 16><<<(unsigned)(nplanes * ntile), 256, sm, c->stream>>>(in, out, nx, (const T*)c->mhd->ry,
+                                                                                        c->tw_y);
+        } else {
+            cudaFuncSetAttribute((const void*)colderiv_sq_kernel<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            colderiv_sq_kernel<T, 8><<<(unsigned)(nplanes * ntile), 256, sm, c->stream>>>(in, out, nx, (const T*)c->mhd->ry,
+                                                                                       c->tw_y);
+        }
+        c->launches++;
+        CKL();
+        return SPARC_OK;
+    }
     const int W = std::max(1, std::min(nx / 2, 1024 / ny));
     const size_t sm = 2 * (size_t)W * ny * sizeof(typename CplxOf<T>::type);
     colderiv_kernel<T><<<(unsigned)(nplanes * ((nx / 2) / W)), 256, sm, c->stream>>>(in, out, nx, ny, W,
@@ -517,6 +780,20 @@ Compact<T> cc_of(const sparc_ctx* c) {
 template <typename T>
 int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfield, long long fstride,
                const T* topsrc = nullptr, T topscale = (T)0) {
+    // FP32: chunked solve; FP64: one thread per pencil (the chunked form's
+    // extra multiplications cost more on the FP64 pipe than it saves)
+    constexpr int NCH = 8;
+    const size_t sm = ((size_t)c->nz * 32 + 2 * NCH * 32) * sizeof(T);
+    if (sizeof(T) == 4 && sm <= 200 * 1024) {
+        cudaFuncSetAttribute((const void*)zderiv_chunk_kernel<T, NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
+        dim3 g((unsigned)((c->NP + 31) / 32), nfield);
+        zderiv_chunk_kernel<T, NCH><<<g, 32 * NCH, sm, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc,
+                                                                   fstride, topsrc, topscale);
+        c->launches++;
+        CKL();
+        return SPARC_OK;
+    }
     dim3 grid((unsigned)((c->NP + 127) / 128), nfield);
     zderiv_phys_kernel<T><<<grid, 128, 0, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc, fstride, topsrc,
                                                        topscale);

@@ -311,3 +311,52 @@ def test_mhd8_state_shape_and_fields(gpu_lib):
         s.set_state(a0[:6], pml0)
     with pytest.raises(SparcError):
         s.field(16)
+
+
+# ---- the register-FFT derivative kernels (horizontal sizes 64 and 256) ------
+
+@pytest.mark.parametrize("option,nx,ny,nz,nsteps", [(10, 64, 64, 32, 5), (8, 64, 64, 32, 3),
+                                                     (10, 256, 256, 24, 1), (18, 64, 1, 32, 31),
+                                                     (18, 256, 1, 32, 5)])
+def test_mhd_register_fft_derivatives(gpu_lib, oracle_mod, option, nx, ny, nz, nsteps):
+    """The x and y derivatives of the physical-space path at nx, ny = 64 and
+    256 (R x R two-pass register DFTs) against the oracle's FFTs, through
+    whole steps of each MHD form, FP64 <= 1e-10."""
+    from cases import small_params, small_params_2d
+    from sparc_gb300.background import flux_sheet_background, flux_tube_background
+    from sparc_gb300.solver import Solver
+    if option == 18:
+        p = small_params_2d(nx=nx, nz=nz, npmlbot=4, npmltop=4, option=18)
+    else:
+        p = small_params(nx=nx, ny=ny, nz=nz, npmlbot=4, npmltop=4 if option == 8 else 0, option=option,
+                         xlength=200e8, ylength=200e8)
+    tab = table_for(p)
+    g, o = Solver(p, tab), oracle_mod.Oracle(p, tab)
+    if option == 18:
+        bg = flux_sheet_background(p, tab)
+        g.set_mhd2d_background(*bg)
+        o.set_mhd2d(*bg)
+        a0, pml0 = _state2d(p, 41)
+    else:
+        bg = flux_tube_background(p, tab, b_surf=800.0, r_surf_mm=8.0)
+        g.set_mhd_background(*bg)
+        o.set_mhd(*bg)
+        a0, pml0 = (_state8 if option == 8 else _state)(p, 41)
+    g.set_state(a0, pml0)
+    o.set_state(a0, pml0)
+    plane = gaussian_plane(p, sigma_mm=8.0)
+    series = oracle_mod.forward_source(p, 200) * 1e3
+    g.set_source_series(plane, series)
+    o.set_source(1, plane[None].copy(), series)
+    g.step(nsteps)
+    o.step(nsteps)
+    ag, pg = g.state()
+    ao, _, po = o.state()
+    for f in range(ag.shape[0]):
+        if np.abs(ao[f]).max() == 0:
+            assert np.abs(ag[f]).max() == 0, f
+            continue
+        assert rel_l2(ag[f], ao[f]) < TOL64, (f, rel_l2(ag[f], ao[f]))
+    for f in range(6):
+        if np.abs(po[f]).max() > 0:
+            assert rel_l2(pg[f], po[f]) < TOL64, ("pml", f, rel_l2(pg[f], po[f]))

@@ -458,3 +458,30 @@ def test_fused_fp32_lagrange_source_matches_fp64(gpu_lib):
     for f in range(6):
         assert rel_l2(res[1][0][f], res[0][0][f]) < 2e-5, f
         assert rel_l2(res[1][1][f], 2 * res[0][0][f]) < 2e-5, f
+
+
+@pytest.mark.parametrize("nx,nz,prec", [(64, 32, "f64"), (256, 24, "f64"), (64, 32, "f32")])
+def test_register_fft_sizes_round_trip_and_steps(gpu_lib, oracle_mod, nx, nz, prec):
+    """The R x R register transforms (horizontal sizes 64 and 256) between
+    physical planes and the spectral state: set_state -> get_state returns the
+    fields, and three steps with the damping match the oracle."""
+    p = small_params(nx=nx, ny=nx, nz=nz, npmlbot=4, npmltop=4, xlength=200e8, ylength=200e8, precision=prec)
+    g, o = make_pair(p, oracle_mod, gpu_lib)
+    a0, pml0 = random_state(p, seed=9)
+    g.set_state(a0, pml0)
+    a1, p1 = g.state()
+    tol_rt = 1e-14 if prec == "f64" else 1e-6
+    assert rel_l2(a1, a0) < tol_rt and rel_l2(p1, pml0) < tol_rt
+    o.set_state(a0, pml0)
+    plane = gaussian_plane(p, sigma_mm=8.0)
+    series = oracle_mod.forward_source(p, 200) * 1e3
+    g.set_source_series(plane, series)
+    o.set_source(1, plane[None].copy(), series)
+    g.step(3)
+    o.step(3)
+    ag, pg = g.state()
+    ao, _, po = o.state()
+    tol = TOL64 if prec == "f64" else 1e-4
+    for f in range(6):
+        assert rel_l2(ag[f], ao[f]) < tol, (f, rel_l2(ag[f], ao[f]))
+    assert rel_l2(pg, po) < tol
