@@ -200,8 +200,9 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
         c->zt64 = (double*)c->zt;
         c->pt64 = (double*)c->pt;
     }
-    if ((rc = dalloc(c, (void**)&c->tw_x, (size_t)p->nx * 8))) return bail(rc);
-    if ((rc = dalloc(c, (void**)&c->tw_y, (size_t)std::max(p->ny, 2) * 8))) return bail(rc);
+    // twiddle tables: n FP64 values, then the same n values in FP32
+    if ((rc = dalloc(c, (void**)&c->tw_x, (size_t)p->nx * 12))) return bail(rc);
+    if ((rc = dalloc(c, (void**)&c->tw_y, (size_t)std::max(p->ny, 2) * 12))) return bail(rc);
     if ((rc = dalloc(c, &c->tmp, (size_t)c->fs * cs))) return bail(rc);
     if ((rc = dalloc(c, &c->phys, (size_t)c->N * es))) return bail(rc);
     if ((rc = dalloc(c, (void**)&c->phys64, (size_t)c->N * 8))) return bail(rc);
@@ -214,17 +215,21 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && !mhd_form;
     if (c->use_fused) fused_prepare(c->nz, c->nzpml);
     if (mhd_form && (rc = mhd_create(c))) return bail(rc);
-    // twiddles cos/sin(2 pi q / n), q < n/2, exact pi
+    // twiddles cos/sin(2 pi q / n), q < n/2, exact pi; the FP32 copy (rounded
+    // from FP64) follows the FP64 table in the same allocation
     for (int dir = 0; dir < 2; ++dir) {
         int n = dir == 0 ? p->nx : p->ny;
         if (n < 2) continue;
         std::vector<double> tw(n);
+        std::vector<float> tw32(n);
         for (int q = 0; q < n / 2; ++q) {
             double ang = 2.0 * M_PI * (double)q / (double)n;
             tw[2 * q] = std::cos(ang);
             tw[2 * q + 1] = std::sin(ang);
         }
-        if ((rc = upload(c, dir == 0 ? c->tw_x : c->tw_y, tw.data(), n * 8))) return bail(rc);
+        for (int q = 0; q < n; ++q) tw32[q] = (float)tw[q];
+        double* dst = dir == 0 ? c->tw_x : c->tw_y;
+        if ((rc = upload(c, dst, tw.data(), n * 8)) || (rc = upload(c, dst + n, tw32.data(), n * 4))) return bail(rc);
     }
     c->src_set.assign(c->S, 0);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(SPARC_ECUDA);

@@ -199,17 +199,23 @@ __device__ __forceinline__ int lagrange_dev(const SlotClock& k, int tl, int L, i
     return n;
 }
 
-// Stockham radix-2 over `count` sequences of length n stored back to back in
-// src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
-// cos, sin(2 pi q / n) for q < n/2 (FP64 table computed on the host).
 // ---- register DFTs of the two-pass transforms (n = R*R) -----------------------
+// W_n^q = exp(sign 2 pi i q / n) for 0 <= q < n from a table of n values
+// (cos, sin of 2 pi q / n for q < n/2) in FP64, followed by the same n values
+// in FP32 (read by the FP32 kernels, so no conversion on the FP64 pipe)
+template <typename T> __device__ __forceinline__ T tw_val(const double* __restrict__ tw, int n, int i);
+template <> __device__ __forceinline__ double tw_val<double>(const double* __restrict__ tw, int, int i) {
+    return __ldg(&tw[i]);
+}
+template <> __device__ __forceinline__ float tw_val<float>(const double* __restrict__ tw, int n, int i) {
+    return __ldg(&reinterpret_cast<const float*>(tw + n)[i]);
+}
 template <typename T, typename CT>
 __device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, T sign) {
-    // W_n^q for 0 <= q < n
     const int h = n >> 1;
     const bool flip = q >= h;
     const int r = flip ? q - h : q;
-    T c = (T)__ldg(&tw[2 * r]), sn = sign * (T)__ldg(&tw[2 * r + 1]);
+    T c = tw_val<T>(tw, n, 2 * r), sn = sign * tw_val<T>(tw, n, 2 * r + 1);
     if (flip) { c = -c; sn = -sn; }
     CT w;
     w.x = c;
@@ -246,6 +252,9 @@ __host__ __device__ constexpr int brev(int k) {
 }
 
 
+// Stockham radix-2 over `count` sequences of length n stored back to back in
+// src; returns the buffer that holds the result.  tw[2q], tw[2q+1] =
+// cos, sin(2 pi q / n) for q < n/2 (the twiddle table of tw_val, computed on the host).
 template <typename T, typename CT>
 __device__ __forceinline__ CT* smem_fft(CT* src, CT* dst, int n, int count, T sign, const double* __restrict__ tw) {
     const int half = n >> 1;
@@ -259,8 +268,8 @@ __device__ __forceinline__ CT* smem_fft(CT* src, CT* dst, int n, int count, T si
             const int k = j & (Ns - 1);
             CT v0 = s[j], v1 = s[j + half];
             const int q = k * stride;
-            const T c = (T)__ldg(&tw[2 * q]);
-            const T sn = sign * (T)__ldg(&tw[2 * q + 1]);
+            const T c = tw_val<T>(tw, n, 2 * q);
+            const T sn = sign * tw_val<T>(tw, n, 2 * q + 1);
             CT w;
             w.x = v1.x * c - v1.y * sn;
             w.y = v1.x * sn + v1.y * c;

@@ -33,7 +33,7 @@ enum { MB_BOX, MB_BOY, MB_BOZ, MB_CBOX, MB_CBOY, MB_CBOZ, MB_GP0X, MB_GP0Y, MB_G
 // stage scratch per source (T, N values each)
 enum { MW_T0, MW_T1, MW_T2, MW_T3, MW_T4, MW_T5, MW_F1, MW_F2, MW_F3, MW_DX, MW_DY, MW_DZ, MW_P, MW_R, MW_GPX,
        MW_GPY, MW_GPZ, MW_BX, MW_BY, MW_BZ, MW_DZF1, MW_DZF2, MW_CBX, MW_CBY, MW_CBZ, MW_DZBX, MW_DZBY,
-       MW_COUNT };
+       MW_DMX, MW_DMY, MW_DMZ, MW_COUNT };
 // PML auxiliaries of option 10 (scrpml / pmlvars index, initialize.f90:487-490,560-566)
 enum { PV_VZ, PV_P, PV_DZBX, PV_DZBY, PV_IBX, PV_IBY, PV_COUNT };
 
@@ -576,15 +576,27 @@ __global__ void mhd_b_kernel(const MhdArgs A, T* __restrict__ work, const T* __r
 
 // curl b, the Lorentz forces, sponge, gravity and RHS xi = v
 // (displacement.f90:765-813) into scr
+// the rest of a stage of MP_MHD_PML_3D_DISPL, point-wise (displacement.f90:
+// 759-848): psi_p on d p'/dz and psi_dzbx, psi_dzby (bottom PML), curl b,
+// the two Lorentz terms (CROSS, derivatives.f90:471-480), the sponge on the
+// top 36 planes, gravity, RHSxi = v, DAMP_VELOCITY (its terms DMX..DMZ were
+// transformed after the temporaries), the kernel-mode source on each pixel's
+// source plane while the slot's clock is within the forcing gate, and the
+// zero top and bottom rows
 template <typename T>
 __global__ void mhd_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __restrict__ work, const T* __restrict__ pab,
                                const T* __restrict__ pml, T* __restrict__ spml, T beta, int hs, const T* __restrict__ gz,
-                               const T* __restrict__ sponge, T* __restrict__ scr) {
+                               const T* __restrict__ sponge, T* __restrict__ scr, int damp, SlotClock clk,
+                               int src_mode, const T* __restrict__ planes, long long plane_ss, int L,
+                               const double* __restrict__ series, int nseries, const int* __restrict__ plane,
+                               const T* __restrict__ dw) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.N) return;
     const int s = blockIdx.y;
     const int k = (int)(t / A.NP);
+    const long long q = t - (long long)k * A.NP;
     T* w = work + (long long)s * MW_COUNT * A.N;
+    const T gpz = pml_bottom<T>(A, t, s, PV_P, w[MW_GPZ * A.N + t], pab, pml, spml, beta, hs);
     const T dzbx = pml_bottom<T>(A, t, s, PV_DZBX, w[MW_DZBX * A.N + t], pab, pml, spml, beta, hs);
     const T dzby = pml_bottom<T>(A, t, s, PV_DZBY, w[MW_DZBY * A.N + t], pab, pml, spml, beta, hs);
     const T cbx = w[MW_CBX * A.N + t] - dzby;
@@ -598,7 +610,7 @@ __global__ void mhd_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __r
     T f3 = cbx * boy - cby * box;
     T rvx = ri * (-w[MW_GPX * A.N + t] + f1);
     T rvy = ri * (-w[MW_GPY * A.N + t] + f2);
-    T rvz = ri * (-w[MW_GPZ * A.N + t] + f3);
+    T rvz = ri * (-gpz + f3);
     const T cbox = bg[MB_CBOX * A.N + t], cboy = bg[MB_CBOY * A.N + t], cboz = bg[MB_CBOZ * A.N + t];
     const T bx = w[MW_BX * A.N + t], by = w[MW_BY * A.N + t], bz = w[MW_BZ * A.N + t];
     f1 = cboy * bz - cboz * by;
@@ -607,7 +619,7 @@ __global__ void mhd_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __r
     rvx = rvx + ri * f1;
     rvy = rvy + ri * f2;
     rvz = rvz + ri * f3;
-    const T vx = w[MW_T3 * A.N + t], vy = w[MW_T4 * A.N + t], vz = w[MW_T5 * A.N + t];
+    T vx = w[MW_T3 * A.N + t], vy = w[MW_T4 * A.N + t], vz = w[MW_T5 * A.N + t];
     if (k >= A.nz - 36) {
         const T sp = sponge[k];
         rvx = rvx - sp * vx;
@@ -615,34 +627,10 @@ __global__ void mhd_rhs_kernel(const MhdArgs A, const T* __restrict__ bg, T* __r
         rvz = rvz - sp * vz;
     }
     rvz = rvz - ri * w[MW_R * A.N + t] * gz[k];
-    T* ss = scr + (long long)s * 6 * A.FS;
-    ss[0 * A.FS + t] = vx;
-    ss[1 * A.FS + t] = vy;
-    ss[2 * A.FS + t] = vz;
-    ss[3 * A.FS + t] = rvx;
-    ss[4 * A.FS + t] = rvy;
-    ss[5 * A.FS + t] = rvz;
-}
-
-// DAMP_VELOCITY result (in DX, DY, DZ), the kernel-mode source on the source
-// plane of each pixel while the slot's clock is within the forcing gate
-// (displacement.f90:815-843), and the zero top and bottom rows (:845-848)
-template <typename T>
-__global__ void mhd_final_kernel(const MhdArgs A, const T* __restrict__ bg, const T* __restrict__ work, int damp,
-                                 T* __restrict__ scr, SlotClock clk, int src_mode, const T* __restrict__ planes,
-                                 long long plane_ss, int L, const double* __restrict__ series, int nseries,
-                                 const int* __restrict__ plane, const T* __restrict__ dw) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.N) return;
-    const int s = blockIdx.y;
-    const int k = (int)(t / A.NP);
-    const long long q = t - (long long)k * A.NP;
-    const T* w = work + (long long)s * MW_COUNT * A.N;
-    T* ss = scr + (long long)s * 6 * A.FS;
     if (damp) {
-        ss[3 * A.FS + t] = ss[3 * A.FS + t] - w[MW_DX * A.N + t];
-        ss[4 * A.FS + t] = ss[4 * A.FS + t] - w[MW_DY * A.N + t];
-        ss[5 * A.FS + t] = ss[5 * A.FS + t] - w[MW_DZ * A.N + t];
+        rvx = rvx - w[MW_DMX * A.N + t];
+        rvy = rvy - w[MW_DMY * A.N + t];
+        rvz = rvz - w[MW_DMZ * A.N + t];
     }
     if (src_mode != 0 && k == plane[q]) {
         const int tl = *clk.time - clk.t0[s];
@@ -659,13 +647,19 @@ __global__ void mhd_final_kernel(const MhdArgs A, const T* __restrict__ bg, cons
                     if (id >= 0) F = F + (T)wl * pl[(long long)id * A.NP];
                 }
             }
-            ss[5 * A.FS + t] = ss[5 * A.FS + t] + F / bg[MB_RHO0 * A.N + t] * dw[q];
+            rvz = rvz + F / bg[MB_RHO0 * A.N + t] * dw[q];
         }
     }
     if (k == 0 || k == A.nz - 1) {
-        #pragma unroll
-        for (int f = 0; f < 6; ++f) ss[f * A.FS + t] = (T)0;
+        vx = vy = vz = rvx = rvy = rvz = (T)0;
     }
+    T* ss = scr + (long long)s * 6 * A.FS;
+    ss[0 * A.FS + t] = vx;
+    ss[1 * A.FS + t] = vy;
+    ss[2 * A.FS + t] = vz;
+    ss[3 * A.FS + t] = rvx;
+    ss[4 * A.FS + t] = rvy;
+    ss[5 * A.FS + t] = rvz;
 }
 
 // a += dt*scr and FILTER_VARS_3D's z filter (physics.f90:755-783) on every
@@ -1609,6 +1603,22 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
     mhd_temp_kernel<T><<<g, 256, 0, c->stream>>>(A, a, scr, beta, hs, bg, work);
     c->launches++;
     CKL();
+    // DAMP_VELOCITY (damping.f90:125-159) through the normalised 2-D transforms;
+    // it needs only the temporaries, so its terms are ready for the RHS kernel
+    const bool damp = c->P.damp_waves != 0;
+    if (damp) {
+        typedef typename CplxOf<T>::type CT;
+        for (int s = 0; s < S; ++s)
+            for (int q = 0; q < 3; ++q) {
+                fft_phys_to_spec<T>(Wp(s, MW_T3 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y,
+                                    c->stream);
+                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, MW_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
+                                    c->tw_y, c->stream);
+                c->launches += 5;
+            }
+        CKL();
+    }
     // div: ddxyz(xi_x, xi_y, xi_z, bc 1)
     for (int s = 0; s < S; ++s) {
         if ((rc = ddx_launch<T>(c, Wp(s, MW_T0), Wp(s, MW_DX), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_T1), Wp(s, MW_DY), nz)))
@@ -1624,9 +1634,6 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
             return rc;
     }
     if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 0, S, (long long)MW_COUNT * N))) return rc;
-    mhd_pmlp_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
-    c->launches++;
-    CKL();
     // induction: ddxyz(flux3, by, flux3, bx, flux2, dzflux2); ddxyz(flux2, bz, flux1, flux3, flux1, dzflux1)
     for (int s = 0; s < S; ++s) {
         if ((rc = ddx_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BY), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BX), nz)) ||
@@ -1648,33 +1655,15 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
     if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_BX), Wp(0, MW_DZBX), 1, S, (long long)MW_COUNT * N)) ||
         (rc = ddz_launch<T>(c, zt, Wp(0, MW_BY), Wp(0, MW_DZBY), 1, S, (long long)MW_COUNT * N)))
         return rc;
-    mhd_rhs_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs, (const T*)m.g,
-                                                 (const T*)m.sponge, scr);
-    c->launches++;
-    CKL();
-    // DAMP_VELOCITY (damping.f90:125-159) through the normalised 2-D transforms
-    const bool damp = c->P.damp_waves != 0;
-    if (damp) {
-        typedef typename CplxOf<T>::type CT;
-        for (int s = 0; s < S; ++s)
-            for (int q = 0; q < 3; ++q) {
-                fft_phys_to_spec<T>(Wp(s, MW_T3 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y,
-                                    c->stream);
-                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
-                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, MW_DX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
-                                    c->tw_y, c->stream);
-                c->launches += 5;
-            }
-        CKL();
-    }
     SlotClock clk;
     memset(&clk, 0, sizeof(clk));
     clk.t0 = c->d_t0; clk.time = c->d_time; clk.freq = c->freq_filtering; clk.two_d = 0;
     clk.gate = c->forcing_length * c->cadforcing_step; clk.num_steps = c->num_steps;
     clk.ts = R4(c->P.timestep); clk.cad = R4(c->P.cadforcing);
-    mhd_final_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, damp ? 1 : 0, scr, clk, c->src_mode, (const T*)c->planes,
-                                                   (long long)c->src_L * c->NP, c->src_L, c->series, c->nseries,
-                                                   m.plane, (const T*)m.dw);
+    mhd_rhs_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs, (const T*)m.g,
+                                                 (const T*)m.sponge, scr, damp ? 1 : 0, clk, c->src_mode,
+                                                 (const T*)c->planes, (long long)c->src_L * c->NP, c->src_L,
+                                                 c->series, c->nseries, m.plane, (const T*)m.dw);
     c->launches++;
     CKL();
     return SPARC_OK;
