@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--skip-mhd", action="store_true", help="skip the flux-tube (option 10) line")
     ap.add_argument("--mhd-only", action="store_true",
                     help="only the flux-tube line (--steps timed, --warmup untimed), for profiling")
+    ap.add_argument("--mhd-prec", default="f64,f32", help="precisions of the flux-tube line")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
     return ap.parse_args()
@@ -283,7 +284,7 @@ def small_step_latency(n=60):
     return out
 
 
-def mhd_section(p0, tab, steps=5, warmup=2):
+def mhd_section(p0, tab, steps=5, warmup=2, precs=("f64", "f32")):
     """The flux-tube configuration: linearised MHD (option 10) at the bench
     grid on a 2 kG, 3 Mm self-similar tube, one source, forward steps in FP64
     and FP32 (device time per step, CUDA events on the context's stream)."""
@@ -294,7 +295,7 @@ def mhd_section(p0, tab, steps=5, warmup=2):
     pm = p0.replace(option=10, npmltop=0, nsrc=1)
     bg = flux_tube_background(pm, tab)
     out = {"grid": [pm.nx, pm.ny, pm.nz], "background": "self-similar flux tube, 2 kG, 3 Mm at z = 0"}
-    for prec in ("f64", "f32"):
+    for prec in precs:
         s = Solver(pm.replace(precision=prec), tab)
         s.set_mhd_background(*bg)
         s.set_source_series(sources.gaussian_plane(pm, 1.0, 20.0, 0.0), sources.ricker_series(pm, 4000))
@@ -388,8 +389,8 @@ def main():
     from sparc_gb300 import bytes_model
     p0, tab = workload(args.small)
     if args.mhd_only:
-        print(json.dumps({"mhd": mhd_section(p0, tab, steps=max(1, args.steps), warmup=max(1, args.warmup))}),
-              flush=True)
+        print(json.dumps({"mhd": mhd_section(p0, tab, steps=max(1, args.steps), warmup=max(1, args.warmup),
+                                             precs=tuple(args.mhd_prec.split(",")))}), flush=True)
         return 0
     K, W = max(1, args.steps), max(3, args.warmup)
     peaks = {}

@@ -299,59 +299,95 @@ __device__ __forceinline__ T compact_rhs_row(int j, int nz, int bc, Ld B, T bot,
 // warp eliminates its chunk from zero (y'), keeping the product of the
 // multipliers -low_j ibd_j, and after one barrier adds the carry-in composed
 // from the chunks below.  The back substitution x_j = y_j - gam_{j+1} x_{j+1}
-// runs the same way from the top.  y and x stay in shared memory; each
-// element is read once and written once.
+// runs the same way from the top.  Each warp stages its chunk and two halo
+// planes either side in its own rows of shared memory (row i = plane s-2+i);
+// the input is read once and the result written once.  The coefficient
+// tables are copied to shared memory first.
 template <typename T, int NCH>
 __global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restrict__ zt, Compact<T> cc,
                                                                 const T* __restrict__ in, T* __restrict__ out,
                                                                 long long npix, int nz, int bc, long long fstride,
                                                                 const T* __restrict__ topsrc, T topscale) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    T* Y = (T*)smraw;                        // [nz][32]
-    T* Cy = Y + (long long)nz * 32;          // [NCH][32] chunk-end value
+    const int cs = (nz + NCH - 1) / NCH, rows = cs + 4;
+    T* tmf = (T*)smraw;                      // [nz] -low_j ibd_j
+    T* tib = tmf + nz;                       // [nz] ibd_j
+    T* tlo = tib + nz;                       // [nz] low_j
+    T* tga = tlo + nz;                       // [nz+1] gam_j (gam_nz = 0)
+    T* tst = tga + nz + 1;                   // [nz] stretch_j
+    T* Cy = tst + nz;                        // [NCH][32] chunk-end value
     T* Cp = Cy + NCH * 32;                   // [NCH][32] chunk multiplier product
+    T* Yall = Cp + NCH * 32;                 // [NCH][rows][32]
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    {
+        const T* low = zt + (ZT_TH + 3 * bc) * nz;
+        const T* ibd = zt + (ZT_TH + 3 * bc + 1) * nz;
+        const T* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
+        for (int j = threadIdx.x; j <= nz; j += blockDim.x) {
+            if (j < nz) {
+                const T l = j > 0 ? low[j] : (T)0, ib = ibd[j];
+                tlo[j] = l;
+                tib[j] = ib;
+                tmf[j] = -l * ib;
+                tst[j] = zt[ZT_STRETCH * nz + j];
+            }
+            tga[j] = (j > 0 && j < nz) ? gam[j] : (T)0;
+        }
+    }
+    T* Y = Yall + (long long)w * rows * 32 + lane;   // Y[i * 32] = plane s - 2 + i
     const long long m = (long long)blockIdx.x * 32 + lane;
     const bool on = m < npix;
     const T* b = in + blockIdx.y * fstride + (on ? m : 0);
     T* o = out + blockIdx.y * fstride + m;
-    const T* low = zt + (ZT_TH + 3 * bc) * nz;
-    const T* ibd = zt + (ZT_TH + 3 * bc + 1) * nz;
-    const T* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
-    const T* str = zt + ZT_STRETCH * nz;
-    const int cs = (nz + NCH - 1) / NCH;
     const int s = w * cs, e = min(nz, s + cs) - 1;   // empty chunk when s > e
     auto B = [&](int j) -> T { return b[(long long)j * npix]; };
     const T top = (topsrc && on) ? topscale * topsrc[blockIdx.y * fstride + (long long)(nz - 1) * npix + m] : (T)0;
-    // stage the chunk's input in its own rows of Y (independent loads), the
-    // two planes either side in registers
-    T h0 = (T)0, h1 = (T)0, h2 = (T)0, h3 = (T)0;
     if (s <= e) {
-        #pragma unroll 8
-        for (int j = s; j <= e; ++j) Y[j * 32 + lane] = B(j);
-        h0 = s >= 2 ? B(s - 2) : (T)0;
-        h1 = s >= 1 ? B(s - 1) : (T)0;
-        h2 = e + 1 < nz ? B(e + 1) : (T)0;
-        h3 = e + 2 < nz ? B(e + 2) : (T)0;
+        // asynchronous copies (cp.async): every plane of the chunk in flight at once
+        for (int i = 0; i < e - s + 5; ++i) {
+            const int j = s - 2 + i;
+            if (j >= 0 && j < nz) {
+                const unsigned dst = (unsigned)__cvta_generic_to_shared(Y + i * 32);
+                const T* src = b + (long long)j * npix;
+                if (sizeof(T) == 4)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+                else
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+            } else {
+                Y[i * 32] = (T)0;
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
-    __syncwarp();
-    auto V = [&](int j) -> T {             // b_j for j in [s-2, e+2]
-        return j < s ? (j == s - 2 ? h0 : h1) : (j > e ? (j == e + 1 ? h2 : h3) : Y[j * 32 + lane]);
-    };
-    // forward, local; row j of Y is overwritten with y'_j after its last use
+    __syncthreads();                         // tables
+    // the closures of rows 0, 1 and nz-2, nz-1 from the staged planes (before
+    // the forward pass overwrites them), global reads only for planes
+    // outside this chunk's staged range
+    auto Bs = [&](int j) -> T { return (j >= s - 2 && j <= e + 2) ? Y[(j - s + 2) * 32] : B(j); };
+    T Rlo0 = (T)0, Rlo1 = (T)0, Rhi2 = (T)0, Rhi1 = (T)0;
+    if (s <= e && s <= 1) {
+        Rlo0 = compact_rhs_row<T>(0, nz, bc, Bs, (T)0, top, cc);
+        Rlo1 = compact_rhs_row<T>(1, nz, bc, Bs, (T)0, top, cc);
+    }
+    if (s <= e && e >= nz - 2) {
+        Rhi2 = compact_rhs_row<T>(nz - 2, nz, bc, Bs, (T)0, top, cc);
+        Rhi1 = compact_rhs_row<T>(nz - 1, nz, bc, Bs, (T)0, top, cc);
+    }
+    // forward, local; row i of plane j is overwritten with y'_j once the
+    // register window holds b_j
     T y = (T)0, pr = (T)1;
     if (s <= e) {
-        T wm2 = V(s - 2), wm1 = V(s - 1), w0 = V(s), w1 = V(s + 1), w2 = V(s + 2);
-        for (int j = s; j <= e; ++j) {
+        T wm2 = Y[0], wm1 = Y[32], w0 = Y[64], w1 = Y[96], w2 = Y[128];
+        for (int j = s, i = 2; j <= e; ++j, ++i) {
             T R;
             if (j >= 2 && j <= nz - 3) R = cc.C1 * (w1 - wm1) + cc.C2 * (w2 - wm2);
-            else R = compact_rhs_row<T>(j, nz, bc, B, (T)0, top, cc);
-            const T l = j > 0 ? __ldg(&low[j]) : (T)0, ib = __ldg(&ibd[j]);
-            y = (R - l * y) * ib;
-            pr = pr * (-l * ib);
+            else R = j == 0 ? Rlo0 : (j == 1 ? Rlo1 : (j == nz - 2 ? Rhi2 : Rhi1));
+            y = (R - tlo[j] * y) * tib[j];
+            pr = pr * tmf[j];
             wm2 = wm1; wm1 = w0; w0 = w1; w1 = w2;
-            w2 = V(j + 3);
-            Y[j * 32 + lane] = y;
+            if (j < e) w2 = Y[(i + 3) * 32];
+            Y[i * 32] = y;
         }
     }
     Cy[w * 32 + lane] = y;
@@ -365,16 +401,16 @@ __global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restr
     if (s <= e) {
         if (w > 0) {
             T pj = (T)1;
-            for (int j = s; j <= e; ++j) {
-                pj = pj * (-__ldg(&low[j]) * __ldg(&ibd[j]));
-                Y[j * 32 + lane] = Y[j * 32 + lane] + pj * cin;
+            for (int j = s, i = 2; j <= e; ++j, ++i) {
+                pj = pj * tmf[j];
+                Y[i * 32] = Y[i * 32] + pj * cin;
             }
         }
-        for (int j = e; j >= s; --j) {
-            const T g = j + 1 < nz ? __ldg(&gam[j + 1]) : (T)0;
-            x = Y[j * 32 + lane] - g * x;
+        for (int j = e, i = e - s + 2; j >= s; --j, --i) {
+            const T g = tga[j + 1];
+            x = Y[i * 32] - g * x;
             pr = pr * (-g);
-            Y[j * 32 + lane] = x;
+            Y[i * 32] = x;
         }
     }
     __syncthreads();                         // all chunk-end values of the forward pass are read
@@ -385,9 +421,9 @@ __global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restr
     for (int q = NCH - 1; q > w; --q) xin = Cy[q * 32 + lane] + Cp[q * 32 + lane] * xin;
     if (s <= e && on) {
         T pj = (T)1;
-        for (int j = e; j >= s; --j) {
-            pj = pj * (j + 1 < nz ? -__ldg(&gam[j + 1]) : (T)0);
-            o[(long long)j * npix] = (Y[j * 32 + lane] + pj * xin) * __ldg(&str[j]);
+        for (int j = e, i = e - s + 2; j >= s; --j, --i) {
+            pj = pj * (-tga[j + 1]);
+            o[(long long)j * npix] = (Y[i * 32] + pj * xin) * tst[j];
         }
     }
 }
@@ -777,7 +813,8 @@ int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfiel
     // FP32: chunked solve; FP64: one thread per pencil (the chunked form's
     // extra multiplications cost more on the FP64 pipe than it saves)
     constexpr int NCH = 8;
-    const size_t sm = ((size_t)c->nz * 32 + 2 * NCH * 32) * sizeof(T);
+    const int cs = (c->nz + NCH - 1) / NCH;
+    const size_t sm = ((size_t)5 * c->nz + 1 + 2 * NCH * 32 + (size_t)NCH * (cs + 4) * 32) * sizeof(T);
     if (sizeof(T) == 4 && sm <= 200 * 1024) {
         cudaFuncSetAttribute((const void*)zderiv_chunk_kernel<T, NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
