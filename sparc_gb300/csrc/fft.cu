@@ -130,7 +130,7 @@ template <typename T, int R>
 __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<T>::type* __restrict__ in,
                                                           typename CplxOf<T>::type* __restrict__ out, int H,
                                                           T sign, const double* __restrict__ tw, int ppg,
-                                                          long long gstride) {
+                                                          long long gstride, const T* __restrict__ mul) {
     typedef typename CplxOf<T>::type CT;
     constexpr int n = R * R, NC = 256 / R;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -163,7 +163,11 @@ __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<
     reg_dft<CT, R>(v, w);
     if (cv) {
         #pragma unroll
-        for (int k2 = 0; k2 < R; ++k2) out[base + (long long)(r + R * k2) * H] = v[brev<R>(k2)];
+        for (int k2 = 0; k2 < R; ++k2) {
+            CT val = v[brev<R>(k2)];
+            if (mul) val = __ldg(&mul[(long long)(r + R * k2) * H + kx0 + c]) * val;   // a real pencil multiplier
+            out[base + (long long)(r + R * k2) * H] = val;
+        }
     }
 }
 
@@ -285,9 +289,20 @@ static void set_smem(const void* fn, size_t bytes) {
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// spec[plane][m] *= mul[m] (a real pencil multiplier, m < M)
+template <typename T>
+__global__ void spec_mul_kernel(typename CplxOf<T>::type* spec, const T* __restrict__ mul, int M, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) spec[t] = mul[t % M] * spec[t];
+}
+
+// phys -> normalised half-spectrum; with mul, each spectral plane is also
+// multiplied by the real pencil multiplier mul[m] (in the column pass when
+// there is one)
 template <typename T>
 void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
-                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s) {
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s,
+                      const T* mul) {
     typedef typename CplxOf<T>::type CT;
     const int H = nx / 2 + 1;
     const long long nrows = (long long)ny * nplanes;
@@ -318,11 +333,11 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
         if (Ry == 16) {
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 16>, smc);
             cols_fft_sq_kernel<T, 16><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, spec, H, (T)-1,
-                                                                                             tw_y, nplanes, 0LL);
+                                                                                             tw_y, nplanes, 0LL, mul);
         } else {
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 8>, smc);
             cols_fft_sq_kernel<T, 8><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, spec, H, (T)-1,
-                                                                                            tw_y, nplanes, 0LL);
+                                                                                            tw_y, nplanes, 0LL, mul);
         }
     } else if (ny > 1) {
         int W = col_tile(ny);
@@ -331,6 +346,10 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
         int ntile = (H + W - 1) / W;
         cols_fft_kernel<T><<<(unsigned)(ntile * (long long)nplanes), 256, sm2, s>>>(tmp, spec, ny, H, W, (T)-1, tw_y,
                                                                                    nplanes, 0LL);
+    }
+    if (mul && !(ny > 1 && Ry)) {
+        const long long n = (long long)nplanes * ny * H;
+        spec_mul_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(spec, mul, ny * H, n);
     }
 }
 
@@ -351,11 +370,11 @@ void fft_spec_to_phys_g(const typename CplxOf<T>::type* spec, int ppg, long long
         if (Ry == 16) {
             const size_t sm2 = (size_t)16 * 16 * 16 * sizeof(CT);
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 16>, sm2);
-            cols_fft_sq_kernel<T, 16><<<blocks16, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride);
+            cols_fft_sq_kernel<T, 16><<<blocks16, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride, nullptr);
         } else if (Ry == 8) {
             const size_t sm2 = (size_t)8 * 8 * 32 * sizeof(CT);
             set_smem<T>((const void*)cols_fft_sq_kernel<T, 8>, sm2);
-            cols_fft_sq_kernel<T, 8><<<blocks8, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride);
+            cols_fft_sq_kernel<T, 8><<<blocks8, 256, sm2, s>>>(spec, tmp, H, (T)1, tw_y, ppg, gstride, nullptr);
         } else {
             int W = col_tile(ny);
             size_t sm2 = 2 * (size_t)W * ny * sizeof(CT);
@@ -566,7 +585,7 @@ int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t
 
 #define INST(T)                                                                                                   \
     template void fft_phys_to_spec<T>(const T*, CplxOf<T>::type*, CplxOf<T>::type*, int, int, int, const double*, \
-                                      const double*, cudaStream_t);                                               \
+                                      const double*, cudaStream_t, const T*);                                     \
     template void fft_spec_to_phys<T>(const CplxOf<T>::type*, T*, CplxOf<T>::type*, int, int, int, const double*, \
                                       const double*, cudaStream_t);                                               \
     template void fft_spec_to_phys_g<T>(const CplxOf<T>::type*, int, long long, T*, CplxOf<T>::type*, int, int, \

@@ -378,7 +378,8 @@ __attribute__((visibility("hidden"))) void sparc_internal_count_launches(sparc_c
 // transforms (fft.cu)
 template <typename T>
 void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
-                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s,
+                      const T* mul = nullptr);
 template <typename T>
 void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
                       int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);

@@ -737,6 +737,13 @@ __global__ void mhd_record_kernel(const T* __restrict__ a, T* __restrict__ rec, 
 
 unsigned nb256(long long n) { return (unsigned)((n + 255) / 256); }
 
+// launches of one filtered transform pair (phys -> spec x multiplier -> phys):
+// rows, columns (which apply the multiplier on the register path) and back
+int filter_pair_launches(const sparc_ctx* c) {
+    const bool sq_y = c->P.ny == 64 || c->P.ny == 256;
+    return c->P.ny > 1 ? (sq_y ? 4 : 5) : 3;
+}
+
 template <typename T>
 int ddx_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
     const int nx = c->P.nx;
@@ -1414,10 +1421,10 @@ int mhd2d_stage(sparc_ctx* c, T beta, int hs) {
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 2; ++q) {
                 const int src = q == 0 ? MW_T3 : MW_T5, dst = q == 0 ? MW_DX : MW_DZ;
-                fft_phys_to_spec<T>(Wp(s, src), (CT*)m.spec, (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream);
-                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                fft_phys_to_spec<T>(Wp(s, src), (CT*)m.spec, (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream,
+                                    (const T*)c->pt + (size_t)PT_DAMP * c->M);
                 fft_spec_to_phys<T>((CT*)m.spec, Wp(s, dst), (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream);
-                c->launches += 5;
+                c->launches += filter_pair_launches(c);
             }
         CKL();
     }
@@ -1587,11 +1594,10 @@ int mhd8_stage(sparc_ctx* c, T beta, int hs) {
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 3; ++q) {
                 fft_phys_to_spec<T>(Wp(s, V8_T1 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
-                                    c->tw_y, c->stream);
-                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                                    c->tw_y, c->stream, (const T*)c->pt + (size_t)PT_DAMP * c->M);
                 fft_spec_to_phys<T>((CT*)m.spec, Wp(s, V8_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
                                     c->tw_y, c->stream);
-                c->launches += 5;
+                c->launches += filter_pair_launches(c);
             }
         CKL();
     }
@@ -1648,11 +1654,10 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 3; ++q) {
                 fft_phys_to_spec<T>(Wp(s, MW_T3 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y,
-                                    c->stream);
-                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 2, c->M, nz, 1, 0, 0, c->stream);
+                                    c->stream, (const T*)c->pt + (size_t)PT_DAMP * c->M);
                 fft_spec_to_phys<T>((CT*)m.spec, Wp(s, MW_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
                                     c->tw_y, c->stream);
-                c->launches += 5;
+                c->launches += filter_pair_launches(c);
             }
         CKL();
     }
@@ -1742,10 +1747,10 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
             if (tl < 0 || (two_d ? (tl + 1) : tl) % c->freq_filtering != 0) continue;
             for (int f = 0; f < (two_d ? 6 : 5); ++f) {
                 T* fp = (T*)c->a + ((size_t)s * c->nf + f) * 2 * c->fs;
-                fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
-                launch_spec_dxdy<T>((CT*)m.spec, (CT*)m.spec, (const T*)c->pt, 3, c->M, c->nz, 1, 0, 0, c->stream);
+                fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream,
+                                    (const T*)c->pt + (size_t)PT_HF * c->M);
                 fft_spec_to_phys<T>((CT*)m.spec, fp, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
-                c->launches += 5;
+                c->launches += filter_pair_launches(c);
             }
             CKL();
         }
