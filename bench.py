@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--mhd-only", action="store_true",
                     help="only the flux-tube line (--steps timed, --warmup untimed), for profiling")
     ap.add_argument("--mhd-prec", default="f64,f32", help="precisions of the flux-tube line")
+    ap.add_argument("--mhd-grid", default="", help="NXxNYxNZ of the flux-tube line (default: the bench grid)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
     return ap.parse_args()
@@ -389,6 +390,11 @@ def main():
     from sparc_gb300 import bytes_model
     p0, tab = workload(args.small)
     if args.mhd_only:
+        if args.mhd_grid:
+            from sparc_gb300.background import polytrope_table
+            nx, ny, nz = (int(v) for v in args.mhd_grid.lower().split("x"))
+            p0 = p0.replace(nx=nx, ny=ny, nz=nz)
+            tab = polytrope_table(nz, z_bot_mm=-25.0, z_top_mm=1.2)
         print(json.dumps({"mhd": mhd_section(p0, tab, steps=max(1, args.steps), warmup=max(1, args.warmup),
                                              precs=tuple(args.mhd_prec.split(",")))}), flush=True)
         return 0
