@@ -247,6 +247,14 @@ int sparc_gpu_kernel_reset(sparc_ctx* adj);
 int sparc_gpu_kernels(sparc_ctx* adj, int src_idx, int sum_slots, double* kc, double* krho,
                       double* hessian);
 
+/* Option 18 (2-D MHD): the B-field kernels of the MAGNETIC_KERNELS block
+ * (kernels.f90:337-453) accumulated beside K_c, K_rho and the hessian, with
+ * B0 and curl B0 formed as kernel mode forms them from the vector potential
+ * (kernels.f90:99-133), scaled as kernels.f90:498-514 into host arrays
+ * (nz,1,nx): kernel_bx, kernel_bz and kernel_vectorpsi (the y component of
+ * the curl of (kernel_bx, 0, kernel_bz)).  Any of the three may be NULL. */
+int sparc_gpu_kernels_b(sparc_ctx* adj, int src_idx, int sum_slots, double* kbx, double* kbz, double* kpsi);
+
 /* ---- primitives (the reference's derivative routines) ---------------------- */
 
 /* ddx / ddy (derivatives.f90:28-170) and ddz (derivatives.f90:10-24 with

@@ -78,6 +78,7 @@ def lib():
             "oracle_ddz": [P, D, D, ctypes.c_int], "oracle_damp": [P, D, D],
             "oracle_kernel_reset": [P], "oracle_kernel_accumulate": [P, D, D, D],
             "oracle_kernel_finish": [P, D, ctypes.c_int],
+            "oracle_kernel_accumulate_b": [P, D, D], "oracle_kernel_finish_b": [P, D, ctypes.c_int],
             "oracle_plane_r2c": [P, D, D],
             "oracle_set_mhd": [P, D, D, D, D, D, D], "oracle_mhd_profiles": [P, D],
             "oracle_set_mhd2d": [P, D, D, D, D],
@@ -161,7 +162,7 @@ class Oracle:
         keys = ["e_rad", "o_rad", "delta_width", "deltat", "steps", "freq_filtering",
                 "maxtime", "forcing_length", "cadforcing_step", "num_steps",
                 "beta1", "beta2", "beta3", "beta4", "beta5", "stretchx", "stretchy",
-                "pi", "rsun", "dimc", "dimrho"]
+                "pi", "rsun", "dimc", "dimrho", "diml"]
         return dict(zip(keys, out[:n].tolist()))
 
     def profiles(self) -> dict:
@@ -266,6 +267,21 @@ class Oracle:
     def kernel_finish(self, stepskern: int) -> np.ndarray:
         out = np.zeros((3,) + self.shape)
         lib().oracle_kernel_finish(self.h, _dp(out), int(stepskern))
+        return out
+
+    def kernel_accumulate_b(self, fxi: np.ndarray, av: np.ndarray):
+        """One pass of the B-field kernel (kernels.f90:337-453) of the 2-D MHD
+        form: forward displacement and adjoint velocity, each (3, nz, ny, nx)."""
+        fxi = np.ascontiguousarray(fxi, dtype=np.float64)
+        av = np.ascontiguousarray(av, dtype=np.float64)
+        if lib().oracle_kernel_accumulate_b(self.h, _dp(fxi), _dp(av)) != 0:
+            raise RuntimeError("B-field kernels need the 2-D MHD background (option 18)")
+
+    def kernel_finish_b(self, stepskern: int) -> np.ndarray:
+        """(kernel_bx, kernel_bz, kernel_vectorpsi), kernels.f90:498-514."""
+        out = np.zeros((3,) + self.shape)
+        if lib().oracle_kernel_finish_b(self.h, _dp(out), int(stepskern)) != 0:
+            raise RuntimeError("no B-field kernel accumulation")
         return out
 
 

@@ -295,6 +295,9 @@ struct Model {
     std::vector<double> series;   // forward time series, indexed by time (0-based)
     // kernels
     std::vector<double> kernelc2, kernelrho, hessian;
+    // kernel mode of the 2-D MHD form (kernels.f90:99-133): B from the vector
+    // potential as PRODUCE_KERNELS forms it, curl B0, and the B-field kernel
+    std::vector<double> kbox, kboz, kcurlbox, kcurlboy, kcurlboz, kernelb;   // kernelb: (x, y, z) x N
     double* F(int l) { return &a[(long)l * N]; }
 };
 
@@ -1573,7 +1576,7 @@ int oracle_info(void* h, double* out) {
     out[n++] = m.cadforcing_step; out[n++] = m.num_steps;
     for (int i = 0; i < 5; ++i) out[n++] = m.betas[i];
     out[n++] = m.stretchx; out[n++] = m.stretchy; out[n++] = m.pi; out[n++] = m.rsun;
-    out[n++] = m.dimc; out[n++] = m.dimrho;
+    out[n++] = m.dimc; out[n++] = m.dimrho; out[n++] = m.diml;
     return n;
 }
 
@@ -1657,10 +1660,13 @@ int oracle_set_mhd(void* h, const double* rho, const double* c, const double* p,
 }
 
 // 2-D MHD background of option 18 ((nz, nx) cgs: pressure, density, sound speed, vector potential)
+static void setup_kernel_b2d(Model& m, const double* psi);
+
 int oracle_set_mhd2d(void* h, const double* p, const double* rho, const double* c, const double* psi) {
     Model& m = *(Model*)h;
     if (m.P.option != 18) return -1;
     setup_mhd2d(m, p, rho, c, psi);
+    setup_kernel_b2d(m, psi);
     return 0;
 }
 
@@ -1750,6 +1756,142 @@ static void compute_div(Model& m, const double* fx, const double* fy, const doub
 int oracle_kernel_reset(void* h) {
     Model& m = *(Model*)h;
     m.kernelc2.assign(m.N, 0.0); m.kernelrho.assign(m.N, 0.0); m.hessian.assign(m.N, 0.0);
+    m.kernelb.assign(3 * m.N, 0.0);
+    return 0;
+}
+
+// ---- magnetic kernels (kernels.f90:337-453, scaling :498-514) ---------------
+// CROSS_KERN (kernels.f90:757-766): c = a x b on whole fields
+static void cross_kern(const double* const a[3], const double* const b[3], double* const c[3], long N) {
+    for (long q = 0; q < N; ++q) {
+        const double cx = a[1][q] * b[2][q] - a[2][q] * b[1][q];
+        const double cy = b[0][q] * a[2][q] - a[0][q] * b[2][q];
+        const double cz = a[0][q] * b[1][q] - a[1][q] * b[0][q];
+        c[0][q] = cx; c[1][q] = cy; c[2][q] = cz;
+    }
+}
+
+// CURL_KERN (kernels.f90:770-793).  The boundary codes bcx, bcy, bcz are
+// declared (initialize.f90:145) and never assigned; as module variables they
+// are zero, so ddzkern takes bc 0.  ddykern of a 2-D box (ny = 1) multiplies
+// by eyeky(1) = 0.
+static void curl_kern(Model& m, const double* const f[3], double* const c[3]) {
+    const long N = m.N;
+    std::vector<double> temp(N);
+    auto dy = [&](const double* v, double* d) {
+        if (m.ny > 1) ddy(m, v, d);
+        else std::fill(d, d + N, 0.0);
+    };
+    ddx(m, f[1], c[2]);
+    dy(f[0], temp.data());
+    for (long q = 0; q < N; ++q) c[2][q] = c[2][q] - temp[q];
+    dy(f[2], c[0]);
+    ddzkern(m, f[1], temp.data(), 0);
+    for (long q = 0; q < N; ++q) c[0][q] = c[0][q] - temp[q];
+    ddzkern(m, f[0], c[1], 0);
+    ddx(m, f[2], temp.data());
+    for (long q = 0; q < N; ++q) c[1][q] = c[1][q] - temp[q];
+}
+
+// B0 of kernel mode (kernels.f90:99-133): box = -ddzkern(psi, 0), boz =
+// DBYD1(psi) stretchx (the solve's), both / dimb, boy = 0; curl B0 by CURL_KERN
+static void setup_kernel_b2d(Model& m, const double* psi) {
+    const long N = m.N;
+    m.kbox.assign(N, 0.0);
+    ddzkern(m, psi, m.kbox.data(), 0);
+    for (long q = 0; q < N; ++q) m.kbox[q] = -m.kbox[q];
+    for (long q = 0; q < N; ++q) m.kbox[q] = m.kbox[q] / m.dimb;
+    m.kboz = m.boz;
+    std::vector<double> zero(N, 0.0);
+    m.kcurlbox.assign(N, 0.0); m.kcurlboy.assign(N, 0.0); m.kcurlboz.assign(N, 0.0);
+    const double* f[3] = {m.kbox.data(), zero.data(), m.kboz.data()};
+    double* c[3] = {m.kcurlbox.data(), m.kcurlboy.data(), m.kcurlboz.data()};
+    curl_kern(m, f, c);
+}
+
+// One pass of the MAGNETIC_KERNELS block (kernels.f90:337-453): fxi = forward
+// displacement (x, y, z), av = adjoint velocity (x, y, z), each N.
+int oracle_kernel_accumulate_b(void* h, const double* fxi, const double* av) {
+    Model& m = *(Model*)h;
+    if (m.kbox.empty()) return -1;
+    const long N = m.N;
+    if (m.kernelb.size() != (size_t)(3 * N)) m.kernelb.assign(3 * N, 0.0);
+    std::vector<double> buf(15 * N, 0.0);
+    auto F = [&](int i) { return buf.data() + (long)i * N; };
+    double* tx = F(0); double* ty = F(1); double* tz = F(2);
+    double* fbx = F(3); double* fby = F(4); double* fbz = F(5);
+    double* t1 = F(6); double* t2 = F(7); double* t3 = F(8);
+    double* abx = F(9); double* aby = F(10); double* abz = F(11);
+    std::vector<double> zero(N, 0.0);
+    const double* xi[3] = {fxi, fxi + N, fxi + 2 * N};
+    const double* va[3] = {av, av + N, av + 2 * N};
+    const double* B0[3] = {m.kbox.data(), zero.data(), m.kboz.data()};
+    const double* CB0[3] = {m.kcurlbox.data(), m.kcurlboy.data(), m.kcurlboz.data()};
+    double* T[3] = {tx, ty, tz};
+    double* T123[3] = {t1, t2, t3};
+    double* FB[3] = {fbx, fby, fbz};
+    double* AB[3] = {abx, aby, abz};
+    const double* cT[3] = {tx, ty, tz};
+    const double* cT123[3] = {t1, t2, t3};
+    const double* cFB[3] = {fbx, fby, fbz};
+    const double* cAB[3] = {abx, aby, abz};
+    auto add = [&](const double* const v[3]) {
+        for (int i = 0; i < 3; ++i)
+            for (long q = 0; q < N; ++q) m.kernelb[(long)i * N + q] = m.kernelb[(long)i * N + q] + v[i][q];
+    };
+    cross_kern(xi, B0, T, N);
+    curl_kern(m, cT, FB);
+    curl_kern(m, cFB, T);
+    cross_kern(va, cT, T123, N);
+    add(cT123);
+    // the first term
+    cross_kern(cFB, va, T, N);
+    curl_kern(m, cT, T123);
+    add(cT123);
+    // the third term
+    cross_kern(va, B0, T, N);
+    curl_kern(m, cT, AB);
+    curl_kern(m, cAB, T);
+    cross_kern(xi, cT, T123, N);
+    add(cT123);
+    // the second term
+    cross_kern(va, CB0, T123, N);
+    curl_kern(m, cT123, T);
+    cross_kern(cT, xi, T123, N);
+    add(cT123);
+    // the fourth term: div(av) (COMPUTE_DIV), then (xi x curl B0) div(av)
+    std::vector<double> dv(N);
+    compute_div(m, va[0], va[1], va[2], dv.data());
+    cross_kern(xi, CB0, T, N);
+    for (int i = 0; i < 3; ++i)
+        for (long q = 0; q < N; ++q) m.kernelb[(long)i * N + q] = m.kernelb[(long)i * N + q] + T[i][q] * dv[q];
+    // equilibrium term 2: curl(B0 x (xi div(av)))
+    for (int i = 0; i < 3; ++i)
+        for (long q = 0; q < N; ++q) T[i][q] = xi[i][q] * dv[q];
+    cross_kern(B0, cT, T123, N);
+    curl_kern(m, cT123, T);
+    add(cT);
+    return 0;
+}
+
+// Scaling of the B-field kernels (kernels.f90:498-514): out = (kernel_bx,
+// kernel_bz, kernel_vectorpsi), the last the y component of CURL_KERN of
+// (kernel_bx, 0, kernel_bz).  2-D dimensions (test_in_2d).
+int oracle_kernel_finish_b(void* h, double* out, int stepskern) {
+    Model& m = *(Model*)h;
+    if (m.kernelb.size() != (size_t)(3 * m.N)) return -1;
+    const long N = m.N;
+    const double ts = R4(m.P.timestep);
+    const double dimen = 1.0 / (m.diml * (double)1.0e-8f * R4(m.P.xlength) * (double)1.0e-8f * m.dimb);
+    std::vector<double> kb(3 * N);
+    for (long q = 0; q < 3 * N; ++q) kb[q] = m.kernelb[q] * stepskern * ts * dimen;
+    std::vector<double> zero(N, 0.0), cx(N), cy(N), cz(N);
+    const double* f[3] = {kb.data(), zero.data(), kb.data() + 2 * N};
+    double* c[3] = {cx.data(), cy.data(), cz.data()};
+    curl_kern(m, f, c);
+    std::copy(kb.begin(), kb.begin() + N, out);
+    std::copy(kb.begin() + 2 * N, kb.end(), out + N);
+    std::copy(cy.begin(), cy.end(), out + 2 * N);
     return 0;
 }
 

@@ -1227,8 +1227,9 @@ extern "C" {
 int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (c->P.option == 2 || c->mhd)
-        return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the quiet displacement forms");
+    if (c->P.option == 2 || (c->mhd && c->P.option != 18))
+        return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the displacement forms 4, 17 and 18 "
+                                     "(the reference computes kernels in 2-D)");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
         int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));
@@ -1248,8 +1249,9 @@ int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     for (int s0 = 0; s0 < c->S; s0 += G) {
         const int g = std::min(G, c->S - s0);
         char* dst = (char*)c->store + ((size_t)snap * 7 * c->S + s0) * c->N * esz(c);
-        int rc = c->f32 ? derive_to_phys<float>(c, s0, g, false, (float*)dst, ofs)
-                        : derive_to_phys<double>(c, s0, g, false, (double*)dst, ofs);
+        int rc = c->mhd ? mhd2d_derive(c, s0, g, false, dst, ofs)
+                        : (c->f32 ? derive_to_phys<float>(c, s0, g, false, (float*)dst, ofs)
+                                  : derive_to_phys<double>(c, s0, g, false, (double*)dst, ofs));
         if (rc) return rc;
     }
     return SPARC_OK;
@@ -1262,6 +1264,7 @@ int sparc_gpu_kernel_reset(sparc_ctx* c) {
         if (rc) return rc;
     }
     CK(cudaMemsetAsync(c->kacc, 0, (size_t)c->S * 3 * c->N * 8, c->stream));
+    if (c->mhd && c->P.option == 18) return mhd2d_kernel_b_reset(c);
     return SPARC_OK;
 }
 
@@ -1269,7 +1272,9 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
     if (!fwd || !c) return SPARC_EINVAL;
     if (!c->have_bg || !fwd->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
     if (!fwd->store || snap < 0 || snap >= fwd->store_n) return fail(c, SPARC_EINVAL, "no such forward snapshot");
-    if (fwd->S != c->S || fwd->N != c->N || fwd->f32 != c->f32) return fail(c, SPARC_EINVAL, "forward/adjoint contexts differ");
+    if (fwd->S != c->S || fwd->N != c->N || fwd->f32 != c->f32 || fwd->P.option != c->P.option)
+        return fail(c, SPARC_EINVAL, "forward/adjoint contexts differ");
+    if (c->mhd && c->P.option != 18) return fail(c, SPARC_EINVAL, "kernels of the 3-D MHD forms are not built");
     if (!c->kacc) { int rc = sparc_gpu_kernel_reset(c); if (rc) return rc; }
     const int G = kernel_group(c->S);
     if (!c->ktemp) { int rc = dalloc(c, &c->ktemp, (size_t)7 * G * c->N * esz(c)); if (rc) return rc; }
@@ -1283,16 +1288,25 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
         const size_t f7 = ((size_t)snap * 7 * c->S + s0) * N;  // element offset of field 0, source s0
         double* acc = c->kacc + (size_t)s0 * 3 * N;
         int rc;
+        const double* c2f = mhd_kernel_c2(c);           // a 2-D MHD background varies in x
         if (c->f32) {
-            rc = derive_to_phys<float>(c, s0, g, true, (float*)c->ktemp, (long long)g * N);
+            rc = c->mhd ? mhd2d_derive(c, s0, g, true, c->ktemp, (long long)g * N)
+                        : derive_to_phys<float>(c, s0, g, true, (float*)c->ktemp, (long long)g * N);
             if (rc) return rc;
             launch_kernel_accum<float>(acc, (const float*)fwd->store + f7, sfs, (const float*)c->ktemp,
-                                       (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream);
+                                       (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream, c2f);
+            if (c->mhd && (rc = mhd2d_kernel_b_accumulate(c, (const float*)fwd->store + f7, sfs, c->ktemp,
+                                                          (long long)g * N, s0, g)))
+                return rc;
         } else {
-            rc = derive_to_phys<double>(c, s0, g, true, (double*)c->ktemp, (long long)g * N);
+            rc = c->mhd ? mhd2d_derive(c, s0, g, true, c->ktemp, (long long)g * N)
+                        : derive_to_phys<double>(c, s0, g, true, (double*)c->ktemp, (long long)g * N);
             if (rc) return rc;
             launch_kernel_accum<double>(acc, (const double*)fwd->store + f7, sfs, (const double*)c->ktemp,
-                                        (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream);
+                                        (long long)g * N, c->zt64, c->NP, c->nz, c->P.ny > 4, g, c->stream, c2f);
+            if (c->mhd && (rc = mhd2d_kernel_b_accumulate(c, (const double*)fwd->store + f7, sfs, c->ktemp,
+                                                          (long long)g * N, s0, g)))
+                return rc;
         }
         c->launches++;
         CKL();
@@ -1317,7 +1331,8 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     int rc = dalloc(c, (void**)&out, (size_t)3 * c->N * 8);
     if (rc) return rc;
     const double* acc = c->kacc + (sum_slots ? 0 : (size_t)src * 3 * c->N);
-    launch_kernel_finish(out, acc, c->zt64, c->NP, c->nz, sc, sr, sum_slots ? c->S : 1, 3 * c->N, c->stream);
+    launch_kernel_finish(out, acc, c->zt64, c->NP, c->nz, sc, sr, sum_slots ? c->S : 1, 3 * c->N, c->stream,
+                         mhd_kernel_rho0(c), mhd_kernel_c2(c));
     c->launches++;
     CKL();
     if (kc) CK(cudaMemcpyAsync(kc, out, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1329,6 +1344,13 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)out), c->allocs.end());
     c->dev_bytes -= (long long)3 * c->N * 8;
     return SPARC_OK;
+}
+
+int sparc_gpu_kernels_b(sparc_ctx* c, int src, int sum_slots, double* kbx, double* kbz, double* kpsi) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->mhd || c->P.option != 18) return fail(c, SPARC_EINVAL, "B-field kernels belong to option 18");
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
+    return mhd2d_kernels_b(c, src, sum_slots, kbx, kbz, kpsi);
 }
 
 // ---------------------------------------------------------------------------

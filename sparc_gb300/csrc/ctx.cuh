@@ -142,5 +142,13 @@ int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const 
                        const double* by, const double* bz);
 int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const double* cs, const double* psi);
 int mhd_steps(sparc_ctx* c, int nsteps);
+// sensitivity kernels of option 18 (mhd.cu)
+int mhd2d_derive(sparc_ctx* c, int s0, int G, bool adjoint, void* out, long long ofs);
+int mhd2d_kernel_b_reset(sparc_ctx* c);
+int mhd2d_kernel_b_accumulate(sparc_ctx* c, const void* fst, long long sfs, const void* adj, long long afs, int s0,
+                              int G);
+int mhd2d_kernels_b(sparc_ctx* c, int src, int sum_slots, double* kbx, double* kbz, double* kpsi);
+const double* mhd_kernel_c2(const sparc_ctx* c);    // per-point c^2 and rho0 of a 2-D MHD context, or null
+const double* mhd_kernel_rho0(const sparc_ctx* c);
 void* mhd_pml(sparc_ctx* c);      // [S][6][nzpml*NP] T pmlvars of option 10
 void* mhd_spml(sparc_ctx* c);     // scrpml

@@ -467,7 +467,7 @@ __global__ void spec_dxdy_kernel(typename CplxOf<T>::type* out, const typename C
 template <typename T>
 __global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restrict__ fwd, long long fwd_fs,
                                     const T* __restrict__ adj, long long adj_fs, const double* __restrict__ zt64,
-                                    long long NP, int nz, int use_y, int nsrc) {
+                                    long long NP, int nz, int use_y, int nsrc, const double* __restrict__ c2f) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long N = NP * nz;
     if (t >= N * nsrc) return;
@@ -480,7 +480,7 @@ __global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restric
     const T a1 = adj[t], avx = adj[adj_fs + t], avy = use_y ? adj[2 * adj_fs + t] : zero, avz = adj[3 * adj_fs + t];
     const T d31 = adj[4 * adj_fs + t], d32 = use_y ? adj[5 * adj_fs + t] : zero, d33 = adj[6 * adj_fs + t];
     if constexpr (sizeof(T) == 8) {
-        const double c2 = zt64[ZT_C2 * nz + z], gr = zt64[ZT_GRAW * nz + z];
+        const double c2 = c2f ? c2f[i] : zt64[ZT_C2 * nz + z], gr = zt64[ZT_GRAW * nz + z];
         A[2 * N + i] = A[2 * N + i] + faz * faz + fax * fax + fay * fay;
         const double t1 = f1 * a1;
         A[i] = A[i] + t1;
@@ -488,7 +488,7 @@ __global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restric
         kr = kr - gr * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
         A[N + i] = kr;
     } else {
-        const T c2 = (T)zt64[ZT_C2 * nz + z], gr = (T)zt64[ZT_GRAW * nz + z];
+        const T c2 = (T)(c2f ? c2f[i] : zt64[ZT_C2 * nz + z]), gr = (T)zt64[ZT_GRAW * nz + z];
         const T h = faz * faz + fax * fax + fay * fay;
         const T t1 = f1 * a1;
         const T kr = t1 * c2 + faz * avz + fax * avx + fay * avy - gr * fxz * a1 + (fxx * d31 + fxy * d32 + fxz * d33);
@@ -501,12 +501,13 @@ __global__ void kernel_accum_kernel(double* __restrict__ acc, const T* __restric
 // Final scaling kernels.f90:523-539, optionally summed over nsum slots
 __global__ void kernel_finish_kernel(double* __restrict__ out, const double* __restrict__ acc,
                                      const double* __restrict__ zt64, long long NP, int nz, double scale_c,
-                                     double scale_r, int nsum, long long acc_ss) {
+                                     double scale_r, int nsum, long long acc_ss, const double* __restrict__ r0f,
+                                     const double* __restrict__ c2f) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long N = NP * nz;
     if (t >= N) return;
     const int z = (int)(t / NP);
-    const double r0 = zt64[ZT_RHO0 * nz + z], c2 = zt64[ZT_C2 * nz + z];
+    const double r0 = r0f ? r0f[t] : zt64[ZT_RHO0 * nz + z], c2 = c2f ? c2f[t] : zt64[ZT_C2 * nz + z];
     double kc = 0, kr = 0, h = 0;
     for (int s = 0; s < nsum; ++s) {
         const double* A = acc + s * acc_ss;
@@ -560,13 +561,16 @@ void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::t
 }
 template <typename T>
 void launch_kernel_accum(double* acc, const T* fwd, long long fwd_fs, const T* adj, long long adj_fs,
-                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s) {
+                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s,
+                         const double* c2f) {
     kernel_accum_kernel<T><<<nblk(NP * nz * nsrc), 256, 0, s>>>(acc, fwd, fwd_fs, adj, adj_fs, zt64, NP, nz, use_y,
-                                                                nsrc);
+                                                                nsrc, c2f);
 }
 void launch_kernel_finish(double* out, const double* acc, const double* zt64, long long NP, int nz, double scale_c,
-                          double scale_r, int nsum, long long acc_ss, cudaStream_t s) {
-    kernel_finish_kernel<<<nblk(NP * nz), 256, 0, s>>>(out, acc, zt64, NP, nz, scale_c, scale_r, nsum, acc_ss);
+                          double scale_r, int nsum, long long acc_ss, cudaStream_t s, const double* r0f,
+                          const double* c2f) {
+    kernel_finish_kernel<<<nblk(NP * nz), 256, 0, s>>>(out, acc, zt64, NP, nz, scale_c, scale_r, nsum, acc_ss, r0f,
+                                                       c2f);
 }
 template <typename T> void launch_copy_convert(T* dst, const double* src, long long n, cudaStream_t s) {
     copy_convert_kernel<T><<<nblk(n), 256, 0, s>>>(dst, src, n);
@@ -597,7 +601,7 @@ int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t
     template void launch_spec_dxdy<T>(CplxOf<T>::type*, const CplxOf<T>::type*, const T*, int, int, int, int,    \
                                       long long, long long, cudaStream_t);                                        \
     template void launch_kernel_accum<T>(double*, const T*, long long, const T*, long long, const double*,       \
-                                         long long, int, int, int, cudaStream_t);                                 \
+                                         long long, int, int, int, cudaStream_t, const double*);                  \
     template void launch_copy_convert<T>(T*, const double*, long long, cudaStream_t);                             \
     template void launch_copy_back<T>(double*, const T*, long long, cudaStream_t);
 INST(double)

@@ -407,8 +407,10 @@ void launch_spec_dxdy(typename CplxOf<T>::type* out, const typename CplxOf<T>::t
                       cudaStream_t s);
 // acc [nsrc][3][N]; fwd field f of source g at fwd + f*fwd_fs + g*N, adj likewise
 template <typename T>
+// c2f: per-point c^2 (a 2-D background) instead of the z profile, or null
 void launch_kernel_accum(double* acc, const T* fwd, long long fwd_fs, const T* adj, long long adj_fs,
-                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s);
+                         const double* zt64, long long NP, int nz, int use_y, int nsrc, cudaStream_t s,
+                         const double* c2f = nullptr);
 template <typename T>
 void launch_copy_convert(T* dst, const double* src, long long n, cudaStream_t s);
 template <typename T>
@@ -417,4 +419,5 @@ void launch_spec_mult(double2* spec, const double* mult, long long M, int nplane
 int launch_check_finite_f64(const double* p, long long n, int* flag, cudaStream_t s);
 int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t s);
 void launch_kernel_finish(double* out, const double* acc, const double* zt64, long long NP, int nz,
-                          double scale_c, double scale_r, int nsum, long long acc_ss, cudaStream_t s);
+                          double scale_c, double scale_r, int nsum, long long acc_ss, cudaStream_t s,
+                          const double* r0f = nullptr, const double* c2f = nullptr);

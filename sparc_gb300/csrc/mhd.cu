@@ -62,6 +62,13 @@ struct MhdState {
     void* spml = nullptr;      // [S][6][nzpml*NP] T (scrpml)
     void* spec = nullptr;      // one spectral field (nz*M complex T): damping / filter transforms
     bool have_bg = false;
+    // sensitivity kernels of the 2-D form (kernels.f90:99-133, 337-453)
+    void* kbox = nullptr;      // [N] T: B_x of kernel mode, -ddzkern(psi, 0) / dimb
+    void* kcby = nullptr;      // [N] T: (curl B0)_y of kernel mode (CURL_KERN)
+    double* kc2 = nullptr;     // [N] c^2 (non-dimensional) for the kernel products and scaling
+    double* krho = nullptr;    // [N] rho0 (non-dimensional)
+    double* rx64 = nullptr;    // [nx] FP64 d/dx multipliers (kernel scaling in FP64)
+    double* kbacc = nullptr;   // [S][2][N] B-field kernel sums (x, z)
 };
 
 namespace {
@@ -428,6 +435,32 @@ __global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restr
     }
 }
 
+// FILTER_VAR_Z (kernels.f90:845-881) of nfield dense fields in place, one
+// thread per pencil: rows 2..nz-1 written (the same stencil as FILTER_VARS_3D)
+template <typename T>
+__global__ void zfilter_phys_kernel(T* __restrict__ f, long long npix, int nz, long long fstride) {
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= npix) return;
+    T* p = f + blockIdx.y * fstride + m;
+    zfilter_stream<T, T>(
+        nz, 0, [&](int j) { return p[(long long)j * npix]; }, [&](int j, T v) { p[(long long)j * npix] = v; });
+}
+
+// a += b
+template <typename T>
+__global__ void add_kernel(T* __restrict__ a, const T* __restrict__ b, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) a[t] = a[t] + b[t];
+}
+
+// out = in * prof[plane]
+template <typename T>
+__global__ void zscale_kernel(T* __restrict__ out, const T* __restrict__ in, const T* __restrict__ prof,
+                              long long npix, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = in[t] * prof[t / npix];
+}
+
 // ---- set-up kernels (FP64) -------------------------------------------------
 
 // READ_IN_FIELD (all_modules.f90:491-505) and the reduction of the field
@@ -450,6 +483,12 @@ __global__ void mhd_read_kernel(double* rho0, double* c2, double* p0, double* bx
     red = red * taper[k];
     const double s = pow(red, 0.5);
     bx[t] = x * s; by[t] = y * s; bz[t] = z * s;
+}
+
+// a = -a / d (element-wise)
+__global__ void neg_div_kernel(double* a, double d, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) a[t] = -a[t] / d;
 }
 
 // a = s1 * b + s2 * c (element-wise)
@@ -1155,7 +1194,7 @@ int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const
     const long long N = c->N, NP = c->NP;
     const std::vector<double>& z = c->zq;
     enum { W_P, W_RHO, W_C2, W_PSI, W_BX, W_BZ, W_CBY, W_TMP, W_RI, W_C2R, W_GR0Z, W_GP0Z, W_GR0X, W_GP0X, W_AZ,
-           W_BZP, W_N };
+           W_BZP, W_KBX, W_KCY, W_N };
     double* w64 = nullptr;
     int rc = dalloc(c, (void**)&w64, (size_t)W_N * N * 8);
     if (rc) return rc;
@@ -1212,6 +1251,32 @@ int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const
     // horizontal gradients (physics2d.f90:318-321)
     if ((rc = ddx_launch<double>(c, W(W_RHO), W(W_GR0X), nz)) || (rc = ddx_launch<double>(c, W(W_P), W(W_GP0X), nz)))
         return rc;
+    // B0 of kernel mode (kernels.f90:99-133): box = -ddzkern(psi, 0) / dimb
+    // (bc 0 and FILTER_VAR_Z, unlike the solve's ddz bc 1), boz as the
+    // solve's, curl_y B0 = ddzkern(box, 0) - d boz/dx (CURL_KERN with bcz = 0)
+    if ((rc = ddz_launch<double>(c, c->zt64, W(W_PSI), W(W_KBX), 0, 1, 0))) return rc;
+    zfilter_phys_kernel<double><<<dim3(nb256(NP), 1), 256, 0, c->stream>>>(W(W_KBX), NP, nz, 0);
+    neg_div_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_KBX), dimb, N);
+    if ((rc = ddz_launch<double>(c, c->zt64, W(W_KBX), W(W_KCY), 0, 1, 0))) return rc;
+    zfilter_phys_kernel<double><<<dim3(nb256(NP), 1), 256, 0, c->stream>>>(W(W_KCY), NP, nz, 0);
+    if ((rc = ddx_launch<double>(c, W(W_BZ), W(W_TMP), nz))) return rc;
+    axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(W(W_KCY), W(W_KCY), 1.0, W(W_TMP), -1.0, N);
+    CKL();
+    if (!m.kc2) {
+        if ((rc = dalloc(c, (void**)&m.kc2, N * 8)) || (rc = dalloc(c, (void**)&m.krho, N * 8)) ||
+            (rc = dalloc(c, &m.kbox, N * esz(c))) || (rc = dalloc(c, &m.kcby, N * esz(c))))
+            return rc;
+    }
+    CK(cudaMemcpyAsync(m.kc2, W(W_C2), N * 8, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(m.krho, W(W_RHO), N * 8, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->f32) {
+        to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.kbox, W(W_KBX), N);
+        to_t_kernel<float><<<nb256(N), 256, 0, c->stream>>>((float*)m.kcby, W(W_KCY), N);
+    } else {
+        to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.kbox, W(W_KBX), N);
+        to_t_kernel<double><<<nb256(N), 256, 0, c->stream>>>((double*)m.kcby, W(W_KCY), N);
+    }
+    m.rx64 = rx64;                           // kept for the kernel scaling in FP64
     m.rx = rx0;
     {
         std::vector<double> rxs(rx);
@@ -1777,3 +1842,233 @@ int mhd_steps(sparc_ctx* c, int nsteps) {
                                                         : "options 8 and 10 need sparc_gpu_set_mhd_background");
     return c->f32 ? mhd_steps_t<float>(c, nsteps) : mhd_steps_t<double>(c, nsteps);
 }
+
+// ---- sensitivity kernels of the 2-D MHD form (option 18) ---------------------
+
+namespace {
+
+// ddzkern: DBYD2 * stretch, then FILTER_VAR_Z (kernels.f90:609-621)
+template <typename T>
+int ddzk_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc) {
+    int rc = ddz_launch<T>(c, zt, in, out, bc, 1, 0);
+    if (rc) return rc;
+    zfilter_phys_kernel<T><<<dim3(nb256(c->NP), 1), 256, 0, c->stream>>>(out, c->NP, c->nz, 0);
+    c->launches++;
+    CKL();
+    return SPARC_OK;
+}
+
+// the seven physical fields of a kernel snapshot of sources s0..s0+G-1 (the
+// layout of the quiet path's store): forward div(xi) (COMPUTE_DIV), acc =
+// scr(v) (3), xi (3); adjoint div(v), v (3), grad(v_z grav) (3)
+template <typename T>
+int mhd2d_derive_t(sparc_ctx* c, int s0, int G, bool adjoint, T* out, long long ofs) {
+    MhdState& m = *c->mhd;
+    const long long N = c->N, fs2 = 2 * c->fs;
+    const T* zt = (const T*)c->zt;
+    T* sc = (T*)m.work + (size_t)MW_P * N;      // scratch: work fields of slot 0
+    T* sc2 = (T*)m.work + (size_t)MW_R * N;
+    int rc;
+    for (int g = 0; g < G; ++g) {
+        const int s = s0 + g;
+        auto A = [&](int f) { return (T*)c->a + ((size_t)s * c->nf + f) * fs2; };
+        auto S = [&](int f) { return (T*)c->scr + ((size_t)s * c->nf + f) * fs2; };
+        auto O = [&](int f) { return out + (size_t)f * ofs + (size_t)g * N; };
+        const int fx = adjoint ? 3 : 0;
+        if ((rc = ddx_launch<T>(c, A(fx), O(0), c->nz)) || (rc = ddzk_launch<T>(c, zt, A(fx + 2), sc, 1))) return rc;
+        add_kernel<T><<<nb256(N), 256, 0, c->stream>>>(O(0), sc, N);
+        for (int q = 0; q < 3; ++q) {
+            CK(cudaMemcpyAsync(O(1 + q), adjoint ? A(3 + q) : S(3 + q), N * sizeof(T), cudaMemcpyDeviceToDevice,
+                               c->stream));
+            if (!adjoint) CK(cudaMemcpyAsync(O(4 + q), A(q), N * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
+        }
+        if (adjoint) {
+            // grad(v_z grav) (kernels.f90:299-304)
+            zscale_kernel<T><<<nb256(N), 256, 0, c->stream>>>(sc2, A(5), zt + (size_t)ZT_GRAW * c->nz, c->NP, N);
+            if ((rc = ddx_launch<T>(c, sc2, O(4), c->nz)) || (rc = ddzk_launch<T>(c, zt, sc2, O(6), 1))) return rc;
+            CK(cudaMemsetAsync(O(5), 0, N * sizeof(T), c->stream));
+        }
+        c->launches += adjoint ? 3 : 1;
+        CKL();
+    }
+    return SPARC_OK;
+}
+
+// the y-only products of the MAGNETIC_KERNELS block in 2-D (B0 = (Bx, 0, Bz),
+// curl B0 = (0, cby, 0), d/dy = 0): ty = (xi x B0)_y, uy = (v x B0)_y,
+// (wx, wz) = v x curl B0, vy = (B0 x xi div v)_y
+template <typename T>
+__global__ void kb_products_kernel(const T* __restrict__ fxx, const T* __restrict__ fxz, const T* __restrict__ avx,
+                                   const T* __restrict__ avz, const T* __restrict__ dA, const T* __restrict__ box,
+                                   const T* __restrict__ boz, const T* __restrict__ cby, T* __restrict__ ty,
+                                   T* __restrict__ uy, T* __restrict__ wx, T* __restrict__ wz, T* __restrict__ vy,
+                                   long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    ty[t] = box[t] * fxz[t] - fxx[t] * boz[t];
+    uy[t] = box[t] * avz[t] - avx[t] * boz[t];
+    wx[t] = -(avz[t] * cby[t]);
+    wz[t] = avx[t] * cby[t];
+    const T tx = fxx[t] * dA[t], tz = fxz[t] * dA[t];
+    vy[t] = tx * boz[t] - box[t] * tz;
+}
+
+// fb = curl(0, ty, 0) = (-ddzk ty, 0, d ty/dx); ab likewise from uy; t3y = (fb x v)_y
+template <typename T>
+__global__ void kb_curls_kernel(T* __restrict__ fbx, const T* __restrict__ fbz, T* __restrict__ abx,
+                                const T* __restrict__ avx, const T* __restrict__ avz, T* __restrict__ t3y,
+                                long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const T bx = -fbx[t];
+    fbx[t] = bx;
+    abx[t] = -abx[t];
+    t3y[t] = avx[t] * fbz[t] - bx * avz[t];
+}
+
+// kernelb += the six terms in the reference's order (kernels.f90:337-453)
+template <typename T>
+__global__ void kb_accum_kernel(double* __restrict__ kbx, double* __restrict__ kbz, const T* __restrict__ fxx,
+                                const T* __restrict__ fxz, const T* __restrict__ avx, const T* __restrict__ avz,
+                                const T* __restrict__ dA, const T* __restrict__ cby, const T* __restrict__ r1,
+                                const T* __restrict__ r2, const T* __restrict__ u1, const T* __restrict__ u2,
+                                const T* __restrict__ s1, const T* __restrict__ s2, const T* __restrict__ p1,
+                                const T* __restrict__ p2, const T* __restrict__ q1, const T* __restrict__ q2,
+                                long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const T t2y = r1[t] - r2[t];                    // curl(curl(xi x B0))_y
+    const T t4y = s1[t] - s2[t];                    // curl(curl(v x B0))_y
+    const T sy = p1[t] - p2[t];                     // curl(v x curl B0)_y
+    double x = kbx[t], z = kbz[t];
+    x = x + (double)(-(avz[t] * t2y)); z = z + (double)(avx[t] * t2y);
+    x = x + (double)(-u1[t]);          z = z + (double)u2[t];
+    x = x + (double)(-(fxz[t] * t4y)); z = z + (double)(fxx[t] * t4y);
+    x = x + (double)(sy * fxz[t]);     z = z + (double)(-(sy * fxx[t]));
+    x = x + (double)(-(fxz[t] * cby[t]) * dA[t]);
+    z = z + (double)((fxx[t] * cby[t]) * dA[t]);
+    x = x + (double)(-q1[t]);          z = z + (double)q2[t];
+    kbx[t] = x;
+    kbz[t] = z;
+}
+
+template <typename T>
+int mhd2d_kernel_b_t(sparc_ctx* c, const T* fst, long long sfs, const T* adj, long long afs, int s0, int G) {
+    MhdState& m = *c->mhd;
+    const long long N = c->N;
+    const T* zt = (const T*)c->zt;
+    T* w = (T*)m.work;                               // work fields of slot 0 as scratch
+    auto Wf = [&](int i) { return w + (size_t)i * N; };
+    T *ty = Wf(0), *uy = Wf(1), *wx = Wf(2), *wz = Wf(3), *vy = Wf(4), *fbx = Wf(5), *fbz = Wf(6), *abx = Wf(7);
+    T *abz = Wf(8), *p1 = Wf(9), *p2 = Wf(10), *q1 = Wf(11), *q2 = Wf(12), *t3y = Wf(13), *r1 = Wf(14);
+    T *r2 = Wf(15), *s1 = Wf(16), *s2 = Wf(17), *u1 = Wf(18), *u2 = Wf(19);
+    const unsigned nb = nb256(N);
+    int rc;
+    for (int g = 0; g < G; ++g) {
+        const T* fxx = fst + 4 * sfs + (size_t)g * N;
+        const T* fxz = fst + 6 * sfs + (size_t)g * N;
+        const T* dA = adj + (size_t)g * N;
+        const T* avx = adj + afs + (size_t)g * N;
+        const T* avz = adj + 3 * afs + (size_t)g * N;
+        double* kb = m.kbacc + (size_t)(s0 + g) * 2 * N;
+        kb_products_kernel<T><<<nb, 256, 0, c->stream>>>(fxx, fxz, avx, avz, dA, (const T*)m.kbox,
+                                                         (const T*)m.bg + (size_t)MB_BOZ * N, (const T*)m.kcby, ty, uy,
+                                                         wx, wz, vy, N);
+        if ((rc = ddzk_launch<T>(c, zt, ty, fbx, 0)) || (rc = ddx_launch<T>(c, ty, fbz, c->nz)) ||
+            (rc = ddzk_launch<T>(c, zt, uy, abx, 0)) || (rc = ddx_launch<T>(c, uy, abz, c->nz)) ||
+            (rc = ddzk_launch<T>(c, zt, wx, p1, 0)) || (rc = ddx_launch<T>(c, wz, p2, c->nz)) ||
+            (rc = ddzk_launch<T>(c, zt, vy, q1, 0)) || (rc = ddx_launch<T>(c, vy, q2, c->nz)))
+            return rc;
+        kb_curls_kernel<T><<<nb, 256, 0, c->stream>>>(fbx, fbz, abx, avx, avz, t3y, N);
+        if ((rc = ddzk_launch<T>(c, zt, fbx, r1, 0)) || (rc = ddx_launch<T>(c, fbz, r2, c->nz)) ||
+            (rc = ddzk_launch<T>(c, zt, abx, s1, 0)) || (rc = ddx_launch<T>(c, abz, s2, c->nz)) ||
+            (rc = ddzk_launch<T>(c, zt, t3y, u1, 0)) || (rc = ddx_launch<T>(c, t3y, u2, c->nz)))
+            return rc;
+        kb_accum_kernel<T><<<nb, 256, 0, c->stream>>>(kb, kb + N, fxx, fxz, avx, avz, dA, (const T*)m.kcby, r1, r2,
+                                                      u1, u2, s1, s2, p1, p2, q1, q2, N);
+        c->launches += 3;
+        CKL();
+    }
+    return SPARC_OK;
+}
+
+// kernel_b * scale for x and z, and the vector-potential kernel as the y
+// component of CURL_KERN of (kernel_bx, 0, kernel_bz), in FP64
+__global__ void kb_finish_kernel(double* __restrict__ out, const double* __restrict__ acc, double scale, int nsum,
+                                 long long acc_ss, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double x = 0, z = 0;
+    for (int s = 0; s < nsum; ++s) {
+        x += acc[s * acc_ss + t];
+        z += acc[s * acc_ss + n + t];
+    }
+    out[t] = x * scale;
+    out[n + t] = z * scale;
+}
+
+}  // namespace
+
+int mhd2d_derive(sparc_ctx* c, int s0, int G, bool adjoint, void* out, long long ofs) {
+    if (!c->mhd || c->P.option != 18) return fail(c, SPARC_EINVAL, "kernel snapshots of the MHD forms need option 18");
+    return c->f32 ? mhd2d_derive_t<float>(c, s0, G, adjoint, (float*)out, ofs)
+                  : mhd2d_derive_t<double>(c, s0, G, adjoint, (double*)out, ofs);
+}
+
+int mhd2d_kernel_b_reset(sparc_ctx* c) {
+    MhdState& m = *c->mhd;
+    if (!m.kbacc) {
+        int rc = dalloc(c, (void**)&m.kbacc, (size_t)c->S * 2 * c->N * 8);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(m.kbacc, 0, (size_t)c->S * 2 * c->N * 8, c->stream));
+    return SPARC_OK;
+}
+
+int mhd2d_kernel_b_accumulate(sparc_ctx* c, const void* fst, long long sfs, const void* adj, long long afs, int s0,
+                              int G) {
+    MhdState& m = *c->mhd;
+    if (!m.kbacc) { int rc = mhd2d_kernel_b_reset(c); if (rc) return rc; }
+    return c->f32 ? mhd2d_kernel_b_t<float>(c, (const float*)fst, sfs, (const float*)adj, afs, s0, G)
+                  : mhd2d_kernel_b_t<double>(c, (const double*)fst, sfs, (const double*)adj, afs, s0, G);
+}
+
+int mhd2d_kernels_b(sparc_ctx* c, int src, int sum_slots, double* kbx, double* kbz, double* kpsi) {
+    MhdState& m = *c->mhd;
+    if (!m.kbacc) return fail(c, SPARC_ESTATE, "no B-field kernel accumulation yet");
+    const long long N = c->N;
+    // kernels.f90:498-514 (2-D: dimen = (diml 1e-8 xlength 1e-8 dimb)^-1)
+    const double dimb = std::sqrt(4.0 * c->pi * c->dimc * c->dimc * c->dimrho);
+    const double dimen = 1.0 / (c->diml * (double)1.0e-8f * R4(c->P.xlength) * (double)1.0e-8f * dimb);
+    const double scale = (double)c->steps * R4(c->P.timestep) * dimen;
+    double* out = nullptr;
+    int rc = dalloc(c, (void**)&out, (size_t)4 * N * 8);
+    if (rc) return rc;
+    const double* acc = m.kbacc + (sum_slots ? 0 : (size_t)src * 2 * N);
+    kb_finish_kernel<<<nb256(N), 256, 0, c->stream>>>(out, acc, scale, sum_slots ? c->S : 1, 2 * N, N);
+    c->launches++;
+    // psi kernel: ddzkern(kernel_bx, 0) - d kernel_bz/dx (FP64 multipliers)
+    void* rx0 = m.rx;
+    m.rx = m.rx64;
+    rc = ddz_launch<double>(c, c->zt64, out, out + 2 * N, 0, 1, 0);
+    if (!rc) {
+        zfilter_phys_kernel<double><<<dim3(nb256(c->NP), 1), 256, 0, c->stream>>>(out + 2 * N, c->NP, c->nz, 0);
+        rc = ddx_launch<double>(c, out + N, out + 3 * N, c->nz);
+    }
+    m.rx = rx0;
+    if (!rc) {
+        axpby_kernel<<<nb256(N), 256, 0, c->stream>>>(out + 2 * N, out + 2 * N, 1.0, out + 3 * N, -1.0, N);
+        c->launches += 2;
+        if (kbx) CK(cudaMemcpyAsync(kbx, out, N * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (kbz) CK(cudaMemcpyAsync(kbz, out + N, N * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (kpsi) CK(cudaMemcpyAsync(kpsi, out + 2 * N, N * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    cudaFree(out);
+    c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)out), c->allocs.end());
+    c->dev_bytes -= (long long)4 * N * 8;
+    return rc;
+}
+
+const double* mhd_kernel_c2(const sparc_ctx* c) { return (c->mhd && c->P.option == 18) ? c->mhd->kc2 : nullptr; }
+const double* mhd_kernel_rho0(const sparc_ctx* c) { return (c->mhd && c->P.option == 18) ? c->mhd->krho : nullptr; }

@@ -40,7 +40,7 @@ EXPORTS = [
     "sparc_gpu_kernels", "sparc_gpu_ddx", "sparc_gpu_ddy", "sparc_gpu_ddz", "sparc_gpu_damp",
     "sparc_gpu_stream", "sparc_gpu_launch_count", "sparc_gpu_device_bytes", "sparc_gpu_info",
     "sparc_gpu_sync", "sparc_gpu_spec_to_phys_noalloc", "sparc_gpu_autotune", "sparc_gpu_set_mhd_background",
-    "sparc_gpu_set_mhd2d_background",
+    "sparc_gpu_set_mhd2d_background", "sparc_gpu_kernels_b",
 ]
 
 
@@ -108,6 +108,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_kernel_accumulate": ([P, I, P], I),
         "sparc_gpu_kernel_reset": ([P], I),
         "sparc_gpu_kernels": ([P, I, I, D, D, D], I),
+        "sparc_gpu_kernels_b": ([P, I, I, D, D, D], I),
         "sparc_gpu_ddx": ([P, D, D], I),
         "sparc_gpu_ddy": ([P, D, D], I),
         "sparc_gpu_ddz": ([P, D, D, I], I),

@@ -267,3 +267,9 @@ class Solver:
         kc = np.zeros(self.shape); kr = np.zeros(self.shape); hs = np.zeros(self.shape)
         self._ck(self.L.sparc_gpu_kernels(self.h, slot, int(sum_slots), _dp(kc), _dp(kr), _dp(hs)))
         return kc, kr, hs
+
+    def kernels_b(self, slot: int = 0, sum_slots: bool = False):
+        """Option 18: (kernel_bx, kernel_bz, kernel_vectorpsi) of the adjoint context."""
+        kx = np.zeros(self.shape); kz = np.zeros(self.shape); kp = np.zeros(self.shape)
+        self._ck(self.L.sparc_gpu_kernels_b(self.h, slot, int(sum_slots), _dp(kx), _dp(kz), _dp(kp)))
+        return kx, kz, kp

@@ -360,3 +360,79 @@ def test_mhd_register_fft_derivatives(gpu_lib, oracle_mod, option, nx, ny, nz, n
     for f in range(6):
         if np.abs(po[f]).max() > 0:
             assert rel_l2(pg[f], po[f]) < TOL64, ("pml", f, rel_l2(pg[f], po[f]))
+
+
+# ---- sensitivity kernels of option 18 (kernels.f90:197-453) --------------------
+
+def _kernel_pair(prec):
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case2d(prec)
+    pa = p.replace(compute_forward=False, compute_adjoint=True)
+    fwd, adj = Solver(p, tab), Solver(pa, tab)
+    for s in (fwd, adj):
+        s.set_mhd2d_background(*bg)
+    a1, pml1 = _state2d(p, 51)
+    a2, pml2 = _state2d(p, 52)
+    fwd.set_state(a1 * 1e3, pml1)
+    adj.set_state(a2 * 1e3, pml2)
+    return p, tab, bg, fwd, adj
+
+
+@pytest.mark.parametrize("nsnap", [1, 2])
+def test_mhd2d_kernels_match_oracle(gpu_lib, oracle_mod, nsnap):
+    """K_c, K_rho, hessian on the 2-D MHD background (rho0, c^2 varying in x)
+    and the B-field kernels (kernel_bx, kernel_bz, kernel_vectorpsi) against
+    the oracle on the GPU's own snapshot fields, FP64 <= 1e-10."""
+    p, tab, bg, fwd, adj = _kernel_pair("f64")
+    o = oracle_mod.Oracle(p, tab)
+    o.set_mhd2d(*bg)
+    o.kernel_reset()
+    adj.kernel_reset()
+    graw = tab[:, 4] * o.info()["rsun"] / 1e12
+    for k in range(nsnap):
+        fwd.step(2)
+        adj.step(2)
+        fwd.snapshot(k, nsnap)
+        adj.kernel_accumulate(fwd, k)
+        af, _ = fwd.state()
+        acc = np.stack([fwd.field(9), fwd.field(10), fwd.field(11)])
+        aa, _ = adj.state()
+        o.kernel_accumulate(np.concatenate([af[0:3], acc]), aa[3:6], graw)
+        o.kernel_accumulate_b(af[0:3], aa[3:6])
+    steps = int(fwd.info()["steps"])
+    ref = o.kernel_finish(steps)
+    refb = o.kernel_finish_b(steps)
+    kc, kr, hs = adj.kernels()
+    kbx, kbz, kpsi = adj.kernels_b()
+    assert rel_l2(hs, ref[2]) < 1e-12
+    assert rel_l2(kc, ref[0]) < TOL64, rel_l2(kc, ref[0])
+    assert rel_l2(kr, ref[1]) < TOL64, rel_l2(kr, ref[1])
+    for got, want, name in ((kbx, refb[0], "bx"), (kbz, refb[1], "bz"), (kpsi, refb[2], "psi")):
+        assert np.abs(want).max() > 0, name
+        assert rel_l2(got, want) < TOL64, (name, rel_l2(got, want))
+
+
+def test_mhd2d_kernels_fp32(gpu_lib):
+    """The FP32 path (FP32 fields, FP64 sums) against FP64 on the same inputs."""
+    out = []
+    for prec in ("f64", "f32"):
+        p, tab, bg, fwd, adj = _kernel_pair(prec)
+        adj.kernel_reset()
+        for k in range(2):
+            fwd.step(3)
+            adj.step(3)
+            fwd.snapshot(k, 2)
+            adj.kernel_accumulate(fwd, k)
+        out.append(adj.kernels() + adj.kernels_b())
+    for q, name in enumerate(("kc", "krho", "hessian", "bx", "bz", "psi")):
+        assert rel_l2(out[1][q], out[0][q]) < 1e-3, (name, rel_l2(out[1][q], out[0][q]))
+
+
+def test_mhd3d_kernels_are_refused(gpu_lib):
+    from sparc_gb300.native import SparcError
+    from sparc_gb300.solver import Solver
+    p, tab, bg = _case()
+    s = Solver(p, tab)
+    s.set_mhd_background(*bg)
+    with pytest.raises(SparcError):
+        s.snapshot(0, 1)

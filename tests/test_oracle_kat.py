@@ -417,3 +417,75 @@ def test_mhd8_drives_induction_and_both_pml_layers():
     assert np.abs(st[5:]).max() > 0                       # b from the induction equation
     for i in range(6):
         assert np.abs(pml[i, :4]).max() > 0 and np.abs(pml[i, 4:]).max() > 0, i
+
+
+def _filter_var_z(v):
+    """FILTER_VAR_Z (kernels.f90:845-881) on (nz, ny, nx)."""
+    co = [0.75390625, 0.41015625, -0.234375, 0.087890625, -0.01953125, 0.001953125]
+    nz = v.shape[0]
+    out = v.copy()
+    for k in (1, 2, 3, 4):
+        out[k] = 0.5 * (v[k + 1] + v[k - 1])
+    for k in range(5, nz - 5):
+        out[k] = co[0] * v[k] + sum(0.5 * co[i] * (v[k - i] + v[k + i]) for i in range(1, 6))
+    for k in (nz - 5, nz - 4, nz - 3, nz - 2):
+        out[k] = 0.5 * (v[k + 1] + v[k - 1])
+    return out
+
+
+def test_mhd2d_b_kernels_reduce_to_the_2d_algebra():
+    """The MAGNETIC_KERNELS block (kernels.f90:337-453), restated in the oracle
+    term by term on 3-vectors, against its 2-D reduction (B0 = (Bx, 0, Bz),
+    curl B0 = (0, curlby, 0), d/dy = 0: every cross product has one
+    component and each curl two derivatives), built here from the oracle's
+    d/dx and d/dz with bc 0 and FILTER_VAR_Z (CURL_KERN's ddzkern)."""
+    from oracle import oracle as O
+    p, tab, bg = _mhd2d_case()
+    o = O.Oracle(p, tab)
+    o.set_mhd2d(*bg)
+    rng = np.random.default_rng(21)
+    sh = (p.nz, 1, p.nx)
+    fxx, fxz, avx, avz = (rng.standard_normal(sh) for _ in range(4))
+    z0 = np.zeros(sh)
+    fxi = np.stack([fxx, z0, fxz])
+    av = np.stack([avx, z0, avz])
+    o.kernel_reset()
+    o.kernel_accumulate_b(fxi, av)
+    kb = o.kernel_finish_b(15)
+    Dx = o.ddx
+    Dz0 = lambda v: _filter_var_z(o.ddz(v, 0))
+    m = o.mhd_profiles()
+    info = o.info()
+    dimb = np.sqrt(4.0 * info["pi"] * info["dimc"] ** 2 * info["dimrho"])
+    psi = bg[3]
+    kbox = -Dz0(psi) / dimb
+    kboz = m["boz"]
+    cby = Dz0(kbox) - Dx(kboz)
+    ty = kbox * fxz - fxx * kboz
+    fbx, fbz = -Dz0(ty), Dx(ty)
+    t2y = Dz0(fbx) - Dx(fbz)
+    t3y = avx * fbz - fbx * avz
+    uy = kbox * avz - avx * kboz
+    abx, abz = -Dz0(uy), Dx(uy)
+    t4y = Dz0(abx) - Dx(abz)
+    sy = Dz0(-avz * cby) - Dx(avx * cby)
+    dA = Dx(avx) + _filter_var_z(o.ddz(avz, 1))
+    vy = fxx * dA * kboz - kbox * fxz * dA
+    kx = -avz * t2y - Dz0(t3y) - fxz * t4y + sy * fxz - fxz * cby * dA - Dz0(vy)
+    kz = avx * t2y + Dx(t3y) + fxx * t4y - sy * fxx + fxx * cby * dA + Dx(vy)
+    ts = float(np.float32(p.timestep))
+    dimen = 1.0 / (info["diml"] * float(np.float32(1e-8)) * float(np.float32(p.xlength))
+                   * float(np.float32(1e-8)) * dimb)
+    assert rel_l2(kb[0], kx * 15 * ts * dimen) < 1e-11
+    assert rel_l2(kb[1], kz * 15 * ts * dimen) < 1e-11
+    kpsi = Dz0(kx * 15 * ts * dimen) - Dx(kz * 15 * ts * dimen)
+    assert rel_l2(kb[2], kpsi) < 1e-11
+    # bilinear in (xi, v_adjoint); zero without a field
+    o.kernel_reset()
+    o.kernel_accumulate_b(2.0 * fxi, av)
+    assert rel_l2(o.kernel_finish_b(15), 2.0 * kb) < 1e-14
+    o0 = O.Oracle(p, tab)
+    o0.set_mhd2d(bg[0], bg[1], bg[2], np.zeros_like(bg[3]))
+    o0.kernel_reset()
+    o0.kernel_accumulate_b(fxi, av)
+    assert np.abs(o0.kernel_finish_b(15)).max() == 0.0
