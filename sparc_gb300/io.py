@@ -200,3 +200,16 @@ def write_kernels(directory: str, contrib: str, kc: np.ndarray, krho: np.ndarray
         write_fits(path, arr, {"TIME": int(time)})
         out[name] = path
     return out
+
+
+def write_kernels_b(directory: str, contrib: str, kbx: np.ndarray, kbz: np.ndarray, kpsi: np.ndarray,
+                    time: int = 0) -> dict:
+    """kernel_bx_XX.fits, kernel_bz_XX.fits, kernel_vectorpsi_XX.fits of a 2-D
+    magnetic run (kernels.f90:509-512; no kernel_by in 2-D), arrays (nz, 1, nx)."""
+    os.makedirs(directory, exist_ok=True)
+    out = {}
+    for name, arr in (("kernel_bx", kbx), ("kernel_bz", kbz), ("kernel_vectorpsi", kpsi)):
+        path = os.path.join(directory, f"{name}_{contrib}.fits")
+        write_fits(path, arr, {"TIME": int(time)})
+        out[name] = path
+    return out

@@ -1,5 +1,7 @@
 """The reference's on-disk formats (vz_cc.bin, FITS BITPIX -64, kernel_info,
 timeline): layout checks and round trips, no GPU."""
+import os
+
 import numpy as np
 
 from sparc_gb300 import io
@@ -67,3 +69,15 @@ def test_forward_output_set(tmp_path):
     assert io.read_kernel_info(paths["kernel_info"]) == [0, p.maxtime]
     k = io.write_kernels(str(tmp_path), "01", rec, 2 * rec, 3 * rec, time=p.maxtime)
     assert np.array_equal(io.read_fits(k["kernel_rho"]), 2 * rec)
+
+
+def test_magnetic_kernel_files(tmp_path):
+    """kernel_bx / kernel_bz / kernel_vectorpsi (kernels.f90:509-512): FITS
+    BITPIX -64 with NAXIS2 = 1 for the 2-D box and the TIME keyword."""
+    k = np.random.default_rng(2).standard_normal((3, 12, 1, 16))
+    paths = io.write_kernels_b(str(tmp_path), "03", k[0], k[1], k[2], time=4185)
+    assert sorted(os.path.basename(v) for v in paths.values()) == [
+        "kernel_bx_03.fits", "kernel_bz_03.fits", "kernel_vectorpsi_03.fits"]
+    a, hdr = io.read_fits(paths["kernel_vectorpsi"], with_header=True)
+    assert np.array_equal(a, k[2])
+    assert (hdr["NAXIS1"], hdr["NAXIS2"], hdr["NAXIS3"], hdr["TIME"], hdr["BITPIX"]) == (16, 1, 12, 4185, -64)
