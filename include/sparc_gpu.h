@@ -255,6 +255,39 @@ int sparc_gpu_kernels(sparc_ctx* adj, int src_idx, int sum_slots, double* kc, do
  * the curl of (kernel_bx, 0, kernel_bz)).  Any of the three may be NULL. */
 int sparc_gpu_kernels_b(sparc_ctx* adj, int src_idx, int sum_slots, double* kbx, double* kbz, double* kpsi);
 
+/* ---- adjoint source of a 2-D run (ADJOINT_SOURCE_FILT) -------------------- */
+
+typedef struct {
+    double x00;            /* master pixel x (Mm) of this source (data/master.pixels) */
+    double t1_min;         /* first output time in minutes: the timeline reversed and negated,
+                              divided by 60 (driver.f90:1310-1315) */
+    double dt_min;         /* output cadence in minutes */
+    int have_ridge[3];     /* params.0 (f ridge), params.1 (p1 ridge), params.2 (band-passed set) exist */
+    double ridge[3][3];    /* per set: mindist (Mm), maxdist (Mm), window (min) */
+    int have_band[2];      /* filter.params.0 / .1 exist */
+    double band[2][2];     /* left, right corner (mHz) */
+    int linesearch;        /* 1: windows of sets 0, 1 are read from `windows` (windows.0/.1) */
+} sparc_adjsrc_params;
+
+/* ADJOINT_SOURCE_FILT (driver.f90:1262-1686) of a 2-D context (ny = 1): the
+ * ridge filters (FMODE_FILTER, PMODE_FILTER, FREQ_FILTER), a window and a
+ * COMPUTE_TT travel time per pixel in each set's distance range, and the
+ * time-reversed adjoint source, computed on the GPU from the surface records
+ * of slot src_idx (the synthetic vz_cc, first nt records) and the observed
+ * data (nt, nx) from the host.  windows: int[2][nx][2], (lef, rig) per pixel
+ * of sets 0 and 1, 1-based, 0 for no measurement (written, or read when
+ * linesearch).  adj: (nt, nx), the source.fits of the adjoint run; misfit =
+ * 0.5 sum tau^2 and nmeas as the kernel/misfit file (driver.f90:1668-1674). */
+int sparc_gpu_adjoint_source(sparc_ctx* ctx, int src_idx, const double* data, int nt,
+                             const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit,
+                             int* nmeas);
+
+/* The same from a synthetic (nt, nx) in host memory (a vz_cc.fits read from
+ * disk, as the reference reads it) instead of the context's records. */
+int sparc_gpu_adjoint_source_host(sparc_ctx* ctx, const double* synth, const double* data, int nt,
+                                  const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit,
+                                  int* nmeas);
+
 /* ---- primitives (the reference's derivative routines) ---------------------- */
 
 /* ddx / ddy (derivatives.f90:28-170) and ddz (derivatives.f90:10-24 with

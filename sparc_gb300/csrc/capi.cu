@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "ctx.cuh"
+#include "adjsrc.cuh"
 
 namespace {
 
@@ -1344,6 +1345,70 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)out), c->allocs.end());
     c->dev_bytes -= (long long)3 * c->N * 8;
     return SPARC_OK;
+}
+
+// synth == nullptr: the surface records of slot src on the device
+static int adjoint_source(sparc_ctx* c, int src, const double* synth, const double* data, int nt,
+                          const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit, int* nmeas) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
+    if (c->P.ny != 1) return fail(c, SPARC_EINVAL, "ADJOINT_SOURCE_FILT is written for 2-D runs (ny = 1)");
+    if (src < 0 || src >= c->S || !data || !ap || !windows || !adj || !misfit || !nmeas)
+        return fail(c, SPARC_EINVAL, "bad slot or null argument");
+    if (nt < 1) return fail(c, SPARC_EINVAL, "nt < 1");
+    if (!synth && (!c->rec || slot_nrec(c, src) < nt))
+        return fail(c, SPARC_ESTATE, "fewer surface records than nt (record_surface and steps first)");
+    const long long NP = c->NP;
+    double* acc = nullptr;
+    int rc = dalloc(c, (void**)&acc, (size_t)nt * NP * 8);
+    if (rc) return rc;
+    if (synth) {
+        if (cudaMemcpyAsync(acc, synth, (size_t)nt * NP * 8, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+            rc = fail(c, SPARC_ECUDA, "upload of the synthetic");
+    } else {
+        // the synthetic: records of the slot as FP64 physical planes, on the device
+        const char* base = (const char*)c->rec + (size_t)src * c->rec_max * c->M * csz(c);
+        for (int r0 = 0; r0 < nt && !rc; r0 += c->nz) {
+            const int n = std::min(c->nz, nt - r0);
+            rc = from_spec_dev(c, base + (size_t)r0 * plane_bytes(c), n);
+            if (!rc && cudaMemcpyAsync(acc + (size_t)r0 * NP, c->phys64, (size_t)n * NP * 8, cudaMemcpyDeviceToDevice,
+                                       c->stream) != cudaSuccess)
+                rc = fail(c, SPARC_ECUDA, "copy of the records");
+        }
+    }
+    if (!rc) {
+        AdjSrcArgs a;
+        a.x00 = ap->x00; a.t1 = ap->t1_min; a.dt = ap->dt_min; a.linesearch = ap->linesearch;
+        for (int m = 0; m < 3; ++m) {
+            a.have_ridge[m] = ap->have_ridge[m];
+            for (int q = 0; q < 3; ++q) a.ridge[m][q] = ap->ridge[m][q];
+        }
+        for (int m = 0; m < 2; ++m) {
+            a.have_band[m] = ap->have_band[m];
+            for (int q = 0; q < 2; ++q) a.band[m][q] = ap->band[m][q];
+        }
+        std::string why;
+        const int r = adjsrc_compute(c->stream, acc, data, nt, (int)NP, c->P.xlength, c->P.outputcad, a, windows, adj,
+                                     misfit, nmeas, why);
+        if (r == 1) rc = fail(c, SPARC_EINVAL, why);
+        else if (r == 2) rc = fail(c, SPARC_ECUDA, why);
+    }
+    cudaFree(acc);
+    c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void*)acc), c->allocs.end());
+    c->dev_bytes -= (long long)nt * NP * 8;
+    return rc;
+}
+
+int sparc_gpu_adjoint_source(sparc_ctx* c, int src, const double* data, int nt, const sparc_adjsrc_params* ap,
+                             int* windows, double* adj, double* misfit, int* nmeas) {
+    return adjoint_source(c, src, nullptr, data, nt, ap, windows, adj, misfit, nmeas);
+}
+
+int sparc_gpu_adjoint_source_host(sparc_ctx* c, const double* synth, const double* data, int nt,
+                                  const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit,
+                                  int* nmeas) {
+    if (!synth) return c ? fail(c, SPARC_EINVAL, "null synthetic") : SPARC_EINVAL;
+    return adjoint_source(c, 0, synth, data, nt, ap, windows, adj, misfit, nmeas);
 }
 
 int sparc_gpu_kernels_b(sparc_ctx* c, int src, int sum_slots, double* kbx, double* kbz, double* kpsi) {

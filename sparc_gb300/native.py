@@ -40,7 +40,8 @@ EXPORTS = [
     "sparc_gpu_kernels", "sparc_gpu_ddx", "sparc_gpu_ddy", "sparc_gpu_ddz", "sparc_gpu_damp",
     "sparc_gpu_stream", "sparc_gpu_launch_count", "sparc_gpu_device_bytes", "sparc_gpu_info",
     "sparc_gpu_sync", "sparc_gpu_spec_to_phys_noalloc", "sparc_gpu_autotune", "sparc_gpu_set_mhd_background",
-    "sparc_gpu_set_mhd2d_background", "sparc_gpu_kernels_b",
+    "sparc_gpu_set_mhd2d_background", "sparc_gpu_kernels_b", "sparc_gpu_adjoint_source",
+    "sparc_gpu_adjoint_source_host",
 ]
 
 
@@ -48,6 +49,16 @@ class SparcError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"sparc_gpu status {status}: {msg}")
         self.status = status
+
+
+class CAdjSrcParams(ctypes.Structure):
+    """sparc_adjsrc_params (include/sparc_gpu.h)."""
+    _fields_ = [
+        ("x00", ctypes.c_double), ("t1_min", ctypes.c_double), ("dt_min", ctypes.c_double),
+        ("have_ridge", ctypes.c_int * 3), ("ridge", (ctypes.c_double * 3) * 3),
+        ("have_band", ctypes.c_int * 2), ("band", (ctypes.c_double * 2) * 2),
+        ("linesearch", ctypes.c_int),
+    ]
 
 
 class CParams(ctypes.Structure):
@@ -122,6 +133,10 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_autotune": ([P, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float)], I),
         "sparc_gpu_set_mhd_background": ([P, D, D, D, D, D, D], I),
         "sparc_gpu_set_mhd2d_background": ([P, D, D, D, D], I),
+        "sparc_gpu_adjoint_source": ([P, I, D, I, ctypes.POINTER(CAdjSrcParams), ctypes.POINTER(I), D, D,
+                                      ctypes.POINTER(I)], I),
+        "sparc_gpu_adjoint_source_host": ([P, D, D, I, ctypes.POINTER(CAdjSrcParams), ctypes.POINTER(I), D, D,
+                                           ctypes.POINTER(I)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

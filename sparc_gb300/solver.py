@@ -268,6 +268,53 @@ class Solver:
         self._ck(self.L.sparc_gpu_kernels(self.h, slot, int(sum_slots), _dp(kc), _dp(kr), _dp(hs)))
         return kc, kr, hs
 
+    def adjoint_source(self, data, x00: float, t1_min: float, dt_min: float, ridges: dict, bands: dict,
+                       windows: dict | None = None, slot: int = 0, nt: int | None = None, synth=None):
+        """ADJOINT_SOURCE_FILT (driver.f90:1262-1686) of a 2-D run on the GPU,
+        from this context's surface records of `slot` (the synthetic) and the
+        observed data (nt, nx).  ridges: {0, 1, 2} -> (mindist, maxdist,
+        window) of params.0..2; bands: {0, 1} -> (left, right) mHz of
+        filter.params.0/1; windows: {0, 1} -> {pixel: (lef, rig)} of a line
+        search, else None; synth: a synthetic (nt, nx) from the host instead
+        of the records.  Returns (adj (nt, nx), misfit, nmeas, windows)."""
+        data = _f64(np.asarray(data, dtype=np.float64))
+        nt = data.shape[0] if nt is None else int(nt)
+        nx = self.p.nx
+        if data.shape != (nt, nx):
+            raise ValueError(f"data must be ({nt}, {nx})")
+        ap = native.CAdjSrcParams()
+        ap.x00, ap.t1_min, ap.dt_min = float(x00), float(t1_min), float(dt_min)
+        for m in range(3):
+            ap.have_ridge[m] = int(m in ridges)
+            for q, v in enumerate(ridges.get(m, (0.0, 0.0, 0.0))):
+                ap.ridge[m][q] = float(v)
+        for m in range(2):
+            ap.have_band[m] = int(m in bands)
+            for q, v in enumerate(bands.get(m, (0.0, 0.0))):
+                ap.band[m][q] = float(v)
+        ap.linesearch = int(windows is not None)
+        win = np.zeros((2, nx, 2), dtype=np.int32)
+        if windows is not None:
+            for m in (0, 1):
+                for i, (lef, rig) in windows.get(m, {}).items():
+                    win[m, i] = (lef, rig)
+        adj = np.zeros((nt, nx))
+        mis = ctypes.c_double()
+        nm = ctypes.c_int()
+        wp = win.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        if synth is None:
+            self._ck(self.L.sparc_gpu_adjoint_source(self.h, slot, _dp(data), nt, ctypes.byref(ap), wp, _dp(adj),
+                                                     ctypes.byref(mis), ctypes.byref(nm)))
+        else:
+            synth = _f64(np.asarray(synth, dtype=np.float64))
+            if synth.shape != (nt, nx):
+                raise ValueError(f"synthetic must be ({nt}, {nx})")
+            self._ck(self.L.sparc_gpu_adjoint_source_host(self.h, _dp(synth), _dp(data), nt, ctypes.byref(ap), wp,
+                                                          _dp(adj), ctypes.byref(mis), ctypes.byref(nm)))
+        wout = {m: {i: (int(win[m, i, 0]), int(win[m, i, 1])) for i in range(nx) if win[m, i, 0] > 0}
+                for m in (0, 1)}
+        return adj, mis.value, nm.value, wout
+
     def kernels_b(self, slot: int = 0, sum_slots: bool = False):
         """Option 18: (kernel_bx, kernel_bz, kernel_vectorpsi) of the adjoint context."""
         kx = np.zeros(self.shape); kz = np.zeros(self.shape); kp = np.zeros(self.shape)

@@ -489,3 +489,39 @@ def test_mhd2d_b_kernels_reduce_to_the_2d_algebra():
     o0.kernel_reset()
     o0.kernel_accumulate_b(fxi, av)
     assert np.abs(o0.kernel_finish_b(15)).max() == 0.0
+
+
+# ---- adjoint source (ADJOINT_SOURCE_FILT, driver.f90:1262-1686) -------------------
+
+def test_adjsrc_inverse_and_compute_tt():
+    from oracle import adjoint_source as A
+    m = np.array([[1.0, -0.5, 0.25], [1.0, 0.0, 0.0], [1.0, 0.5, 0.25]])
+    assert np.allclose(A.inverse3(m), np.linalg.inv(m), rtol=1e-14, atol=1e-14)
+    t = np.arange(81) * 0.5
+    w = lambda s: np.cos(2 * np.pi * 0.2 * (t - 20 - s)) * np.exp(-((t - 20 - s) / 4.0) ** 2)
+    for s in (0.0, 0.13, -0.31):
+        assert abs(A.compute_tt(w(0.0), w(s), 0.5) - s) < 0.02, s
+    assert list(A.distmat(6)) == [0.0, 1.0, 2.0, 3.0, -2.0, -1.0]
+
+
+def test_adjsrc_zero_for_equal_data_and_measures_a_shift():
+    from adjsrc_cases import CASE, delayed, ridge_field
+    from oracle import adjoint_source as A
+    c = CASE
+    t = np.arange(c["nt"]) * 0.5
+    acc = ridge_field(c["nx"], c["nt"], c["xlength"], c["outputcad"], seed=3)
+    adj0, mis0, n0, win, taus0 = A.adjoint_source_filt(acc, acc.copy(), c["xlength"], c["outputcad"], c["x00"], t,
+                                                        c["ridges"], c["bands"])
+    assert n0 > 20 and mis0 < 1e-20 and max(abs(v) for v in taus0.values()) < 1e-9
+    assert np.abs(adj0).max() < 1e-9 * np.abs(acc).max()
+    shift = 12.0                                     # s
+    adj, mis, n, win2, taus = A.adjoint_source_filt(acc, delayed(acc, shift, c["outputcad"]), c["xlength"],
+                                                    c["outputcad"], c["x00"], t, c["ridges"], c["bands"])
+    tt = np.array(list(taus.values())) * 60.0       # minutes -> s
+    assert n == n0 and win2 == win
+    assert np.median(np.abs(tt - shift)) < 1.5, np.median(tt)
+    assert mis > 0 and np.abs(adj).max() > 0
+    # a line search reuses the windows (windows.0/1) and measures the same
+    adj3, mis3, n3, _, _ = A.adjoint_source_filt(acc, delayed(acc, shift, c["outputcad"]), c["xlength"],
+                                                 c["outputcad"], c["x00"], t, c["ridges"], c["bands"], windows_in=win)
+    assert np.array_equal(adj3, adj) and mis3 == mis and n3 == n
