@@ -213,3 +213,60 @@ def write_kernels_b(directory: str, contrib: str, kbx: np.ndarray, kbz: np.ndarr
         write_fits(path, arr, {"TIME": int(time)})
         out[name] = path
     return out
+
+
+def write_adjoint_source(directory: str, adj: np.ndarray, t1_min: float, tn_min: float, time: int = 0,
+                         two_d: bool = True) -> dict:
+    """adjoint_srcXX/source.fits (writefits_3D of adj, (nt, 1, nx) or
+    (nt, nx); TIME = the time step at writing) and adjoint_srcXX/information
+    (nt, t(1)*60, t(nt)*60 and '2D' for a 2-D run; driver.f90:1647-1660)."""
+    os.makedirs(directory, exist_ok=True)
+    a = np.asarray(adj, dtype=np.float64)
+    if a.ndim == 2:
+        a = a[:, None, :]
+    paths = {"source.fits": os.path.join(directory, "source.fits"),
+             "information": os.path.join(directory, "information")}
+    write_fits(paths["source.fits"], a, {"TIME": int(time)})
+    with open(paths["information"], "w") as f:
+        f.write(f"{a.shape[0]:12d}\n{t1_min * 60.0:25.16E}\n{tn_min * 60.0:25.16E}\n")
+        if two_d:
+            f.write(" 2D\n")
+    return paths
+
+
+def write_misfit(path: str, index: int, nmeas: int, misfit: float) -> None:
+    """kernel/misfit_XX_YY: source index, number of measurements and
+    0.5 sum tau^2 on one line (driver.f90:1664-1674)."""
+    with open(path, "w") as f:
+        f.write(f"{int(index):12d}{int(nmeas):12d}{float(misfit):25.16E}\n")
+
+
+def write_windows(directory: str, windows: dict) -> list:
+    """windows.0 / windows.1 (driver.f90:1310-1325, 1489-1491): one `lef rig`
+    line per measurement of the f and p1 sets in pixel order; `windows` maps
+    set -> {pixel: (lef, rig)} as Solver.adjoint_source returns it."""
+    os.makedirs(directory, exist_ok=True)
+    out = []
+    for m in (0, 1):
+        path = os.path.join(directory, f"windows.{m}")
+        with open(path, "w") as f:
+            for i in sorted(windows.get(m, {})):
+                lef, rig = windows[m][i]
+                f.write(f"{int(lef):12d}{int(rig):12d}\n")
+        out.append(path)
+    return out
+
+
+def read_windows(directory: str, pixels: dict) -> dict:
+    """windows.0 / windows.1 back into set -> {pixel: (lef, rig)}; the
+    reference reads the lines in the order it measures, so `pixels` gives,
+    per set, the pixels in measurement order."""
+    out = {}
+    for m in (0, 1):
+        path = os.path.join(directory, f"windows.{m}")
+        if not os.path.exists(path):
+            continue
+        with open(path) as f:
+            rows = [tuple(int(v) for v in line.split()[:2]) for line in f if line.strip()]
+        out[m] = dict(zip(pixels.get(m, []), rows))
+    return out

@@ -81,3 +81,18 @@ def test_magnetic_kernel_files(tmp_path):
     a, hdr = io.read_fits(paths["kernel_vectorpsi"], with_header=True)
     assert np.array_equal(a, k[2])
     assert (hdr["NAXIS1"], hdr["NAXIS2"], hdr["NAXIS3"], hdr["TIME"], hdr["BITPIX"]) == (16, 1, 12, 4185, -64)
+
+
+def test_adjoint_source_files(tmp_path):
+    adj = np.random.default_rng(4).standard_normal((30, 16))
+    paths = io.write_adjoint_source(str(tmp_path / "adjoint_src01"), adj, 0.25, 14.75, time=1799)
+    a, hdr = io.read_fits(paths["source.fits"], with_header=True)
+    assert a.shape == (30, 1, 16) and np.array_equal(a[:, 0], adj) and hdr["TIME"] == 1799
+    lines = open(paths["information"]).read().split()
+    assert int(lines[0]) == 30 and float(lines[1]) == 15.0 and float(lines[2]) == 885.0 and lines[3] == "2D"
+    io.write_misfit(str(tmp_path / "misfit_01_00"), 1, 42, 0.125)
+    assert open(tmp_path / "misfit_01_00").read().split() == ["1", "42", "1.2500000000000000E-01"]
+    win = {0: {5: (10, 50), 3: (8, 48)}, 1: {7: (20, 50)}}
+    io.write_windows(str(tmp_path), win)
+    back = io.read_windows(str(tmp_path), {0: [3, 5], 1: [7]})
+    assert back == {0: {3: (8, 48), 5: (10, 50)}, 1: {7: (20, 50)}}
