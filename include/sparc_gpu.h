@@ -288,6 +288,17 @@ int sparc_gpu_adjoint_source_host(sparc_ctx* ctx, const double* synth, const dou
                                   const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit,
                                   int* nmeas);
 
+/* MISFIT_ALL (driver.f90:1702-2076) of a 2-D run, the line search's misfit:
+ * for the bands 2-3.5, 3.5-4.5 and 4.5-6 mHz, the three sets of
+ * sparc_gpu_adjoint_source (ap's ridges; its bands are not used) with
+ * MISFIT_ALL's ridge speeds and arrival polynomial.  synth: the synthetic
+ * (nt, nx) on the host, or NULL for the records of slot src_idx.  windows:
+ * int[3][2][nx][2], the band's sets 0 and 1 (windows.all.N), written or read
+ * (ap->linesearch); misfit: double[3][3] = 0.5 sum tau^2 and nmeas:
+ * int[3][3] per band and set (kernel/misfit_all_XX_YY). */
+int sparc_gpu_misfit_all(sparc_ctx* ctx, int src_idx, const double* synth, const double* data, int nt,
+                         const sparc_adjsrc_params* ap, int* windows, double* misfit, int* nmeas);
+
 /* ---- primitives (the reference's derivative routines) ---------------------- */
 
 /* ddx / ddy (derivatives.f90:28-170) and ddz (derivatives.f90:10-24 with

@@ -262,3 +262,71 @@ def adjoint_source_filt(acc: np.ndarray, dat: np.ndarray, xlength: float, output
             measure(2, i, filt2, lef, rig, a_, d_, c_)
     adj = adj * nt / 60.0
     return adj, 0.5 * misfit, nmeas, windows, taus
+
+
+MISFIT_BANDS = ((2.0, 3.5), (3.5, 4.5), (4.5, 6.0))    # driver.f90:1812-1824 (mHz)
+
+
+def misfit_all(acc: np.ndarray, dat: np.ndarray, xlength: float, outputcad: float, x00: float, t: np.ndarray,
+               ridges: dict, windows_in: dict | None = None):
+    """MISFIT_ALL (driver.f90:1702-2076) of a 2-D run: for each of three
+    frequency bands the f, p1 and band-passed sets of ADJOINT_SOURCE_FILT,
+    with its own ridge speeds (1.01, 1.465 Mm/min) and arrival polynomial,
+    measure tau per pixel; no adjoint source.
+
+    Returns (misfit[band][set] = 0.5 sum tau^2, nmeas[band][set], windows
+    {(band, set): {pixel: (lef, rig)}} of sets 0 and 1); windows_in, keyed
+    the same way, are read in a line search (windows.all.N)."""
+    nt, nx = acc.shape
+    linesearch = windows_in is not None
+    x = np.arange(nx) / nx
+    distances = np.abs((x - 0.5) * xlength * r4(1e-8) - x00)
+    dt = t[1] - t[0]
+    N = nx * nt
+    spec = np.fft.fftn(acc.astype(np.complex128))
+    specd = np.fft.fftn(dat.astype(np.complex128))
+    vel = (1.01, 1.465)
+    pcoef = (r4(22.5000), r4(0.235317), r4(0.00134167), r4(-1.32222e-05), r4(3.00000e-08))
+    mis = np.zeros((3, 3))
+    nmeas = np.zeros((3, 3), dtype=int)
+    windows = {}
+    for b, (lc, rc) in enumerate(MISFIT_BANDS):
+        filt = freq_filter(lc, rc, nt, outputcad)
+        sets = {0: fmode_filter(nx, nt, xlength, outputcad) * filt[:, None],
+                1: pmode_filter(nx, nt, xlength, outputcad) * filt[:, None],
+                2: np.ones((nt, nx)) * filt[:, None]}
+        for pord in (0, 1, 2):
+            if pord not in ridges:
+                continue
+            mindist, maxdist, window = ridges[pord]
+            halftime = int(np.floor(window / (2.0 * dt) + 0.5))
+            a_ = np.fft.ifftn(spec * sets[pord]) * N
+            d_ = np.fft.ifftn(specd * sets[pord]) * N
+            if pord < 2:
+                windows[(b, pord)] = {}
+            for i in range(nx):
+                if not (distances[i] > mindist and distances[i] < maxdist):
+                    continue
+                if pord < 2 and linesearch:
+                    lef, rig = windows_in[(b, pord)][i]
+                elif pord < 2:
+                    timest = int(np.floor(distances[i] / vel[pord] * 1.0 / dt))
+                    timefin = timest + 40
+                    loc = int(np.argmax(np.abs(a_[timest - 1:timefin, i].real))) + timest
+                    lef, rig = loc - halftime, loc + halftime
+                else:
+                    d = distances[i]
+                    if d < 250.0:
+                        v = (pcoef[0] - t[0] + pcoef[1] * d + pcoef[2] * d ** 2.0 + pcoef[3] * d ** 3.0
+                             + pcoef[4] * d ** 4.0) / dt
+                        timesmax = int(np.floor(abs(v) + 0.5)) * (1 if v >= 0 else -1) + 1
+                        loc = int(np.argmax(a_[timesmax - 7:timesmax + 6, i].real)) + timesmax - 6
+                    else:
+                        loc = int(np.argmax(a_[:, i].real)) + 1
+                    lef, rig = loc - halftime, loc + halftime
+                if pord < 2:
+                    windows[(b, pord)][i] = (lef, rig)
+                tau = compute_tt(a_[lef - 1:rig, i].real, d_[lef - 1:rig, i].real, dt)
+                mis[b, pord] = mis[b, pord] + tau ** 2.0
+                nmeas[b, pord] += 1
+    return mis * 0.5, nmeas, windows

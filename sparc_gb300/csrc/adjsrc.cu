@@ -120,6 +120,9 @@ struct RecvArgs {
     double dt, t1, x0, xlength;
     double mindist, maxdist;
     int halftime;
+    double vel[2];         // ridge speeds of sets 0, 1 (Mm/min)
+    double pc[5];          // arrival polynomial of set 2 (min, Mm)
+    int spectrum;          // 1: the windowed spectrum for the adjoint source; 0: tau only
 };
 
 // one CTA per pixel i: window, COMPUTE_TT, ||ccdot||^2 and the windowed
@@ -144,7 +147,7 @@ __global__ void receiver_kernel(RecvArgs a, const double2* __restrict__ A, const
                 lef = win[2 * i];
                 rig = win[2 * i + 1];
             } else if (a.mode < 2) {
-                const double vel = a.mode == 0 ? 0.75 : 1.00;
+                const double vel = a.vel[a.mode];
                 const int timest = (int)floor(d / vel * 1.0 / a.dt), timefin = timest + 40;
                 if (timest < 1 || timefin > nt) { atomicExch(err, 1); s_active = 0; }
                 else {
@@ -155,8 +158,8 @@ __global__ void receiver_kernel(RecvArgs a, const double2* __restrict__ A, const
                     }
                 }
             } else if (d < 250.0) {
-                const double p1 = (double)13.4090f, p2 = (double)0.3421f, p3 = (double)-0.0005f;
-                const double v = (p1 - a.t1 + p2 * d + p3 * pow(d, 2.0) + 0.0 * pow(d, 3.0) + 0.0 * pow(d, 4.0)) / a.dt;
+                const double v = (a.pc[0] - a.t1 + a.pc[1] * d + a.pc[2] * pow(d, 2.0) + a.pc[3] * pow(d, 3.0) +
+                                  a.pc[4] * pow(d, 4.0)) / a.dt;
                 const int tsm = (v >= 0 ? (int)floor(v + 0.5) : -(int)floor(-v + 0.5)) + 1;
                 if (tsm - 6 < 1 || tsm + 6 > nt) { atomicExch(err, 1); s_active = 0; }
                 else {
@@ -182,7 +185,8 @@ __global__ void receiver_kernel(RecvArgs a, const double2* __restrict__ A, const
     }
     __syncthreads();
     if (!s_active) {
-        for (int q = threadIdx.x; q < nt; q += blockDim.x) R[(long long)i * nt + q] = make_double2(0.0, 0.0);
+        if (a.spectrum)                            // R (and C) exist only when the spectrum is formed
+            for (int q = threadIdx.x; q < nt; q += blockDim.x) R[(long long)i * nt + q] = make_double2(0.0, 0.0);
         if (threadIdx.x == 0) { flag[i] = 0; tau_out[i] = 0.0; }
         return;
     }
@@ -247,6 +251,13 @@ __global__ void receiver_kernel(RecvArgs a, const double2* __restrict__ A, const
             const double p2 = inv[2][0] * cc[loc - 1] + inv[2][1] * cc[loc] + inv[2][2] * cc[loc + 1];
             tau = -p1 * 0.5 / p2;
         }
+        s_tau = tau;
+        tau_out[i] = tau;
+        flag[i] = 1;
+    }
+    __syncthreads();
+    if (!a.spectrum) return;
+    if (threadIdx.x == 0) {
         // sum(ccdot(i,1,lef:rig)**2.) of the complex derivative
         double2 nrm = make_double2(0.0, 0.0);
         for (int t = lef; t <= s_rig; ++t) {
@@ -255,10 +266,8 @@ __global__ void receiver_kernel(RecvArgs a, const double2* __restrict__ A, const
         }
         const double2 den = make_double2(nrm.x * a.dt, nrm.y * a.dt);
         const double q2 = den.x * den.x + den.y * den.y;
+        const double tau = s_tau;
         s_con = make_double2(-tau * den.x / q2, tau * den.y / q2);      // -tau / den
-        s_tau = tau;
-        tau_out[i] = tau;
-        flag[i] = 1;
     }
     __syncthreads();
     // the windowed time derivative's spectrum (1-D DFT over t), times con
@@ -391,6 +400,10 @@ int adjsrc_compute(cudaStream_t s, const double* acc_dev, const double* dat_host
         ra.dt = a.dt; ra.t1 = a.t1; ra.x0 = a.x00; ra.xlength = xlength;
         ra.mindist = a.ridge[mode][0]; ra.maxdist = a.ridge[mode][1];
         ra.halftime = (int)std::floor(a.ridge[mode][2] / (2.0 * a.dt) + 0.5);
+        ra.vel[0] = 0.75; ra.vel[1] = 1.00;                        // driver.f90:1461-1462
+        const double pc[5] = {r4(13.4090), r4(0.3421), r4(-0.0005), 0.0, 0.0};   // driver.f90:1557-1559
+        for (int q = 0; q < 5; ++q) ra.pc[q] = pc[q];
+        ra.spectrum = 1;
         if (mode < 2) cudaMemcpyAsync(d_win, windows + (size_t)mode * 2 * nx, 2 * nx * sizeof(int),
                                       cudaMemcpyHostToDevice, s);
         const size_t smc = (size_t)(2 * nt) * 8;
@@ -429,5 +442,97 @@ int adjsrc_compute(cudaStream_t s, const double* acc_dev, const double* dat_host
     }
     *misfit = 0.5 * sum_tau2;
     *nmeas = count;
+    return 0;
+}
+
+int misfit_all_compute(cudaStream_t s, const double* acc_dev, const double* dat_host, int nt, int nx, double xlength,
+                       double outputcad, const AdjSrcArgs& a, int* windows, double* misfit, int* nmeas,
+                       std::string& why) {
+    if (nt < 8 || nx < 4) { why = "need at least 8 outputs and 4 pixels"; return 1; }
+    if (nt > 12000) { why = "more than 12000 outputs"; return 1; }
+    const long long n = (long long)nt * nx;
+    std::vector<double> fm0, pm0;
+    ridge_filter(fm0, nx, nt, xlength, outputcad, true);
+    ridge_filter(pm0, nx, nt, xlength, outputcad, false);
+    std::vector<double> Wt(2 * nt), Wx(2 * nx);
+    for (int q = 0; q < nt; ++q) { Wt[2 * q] = std::cos(2.0 * M_PI * q / nt); Wt[2 * q + 1] = -std::sin(2.0 * M_PI * q / nt); }
+    for (int q = 0; q < nx; ++q) { Wx[2 * q] = std::cos(2.0 * M_PI * q / nx); Wx[2 * q + 1] = -std::sin(2.0 * M_PI * q / nx); }
+    DevBuf B;
+    double2 *d_Wt = B.get<double2>(nt), *d_Wx = B.get<double2>(nx);
+    double *d_dat = B.get<double>(n), *d_filt = B.get<double>(n), *d_tau = B.get<double>(nx);
+    double2 *spec = B.get<double2>(n), *specd = B.get<double2>(n), *tmp = B.get<double2>(n), *tmp2 = B.get<double2>(n);
+    double2 *A = B.get<double2>(n), *D = B.get<double2>(n);
+    int *d_flag = B.get<int>(nx), *d_win = B.get<int>(2 * nx), *d_err = B.get<int>(1);
+    if (B.err != cudaSuccess) { why = std::string("device allocation: ") + cudaGetErrorString(B.err); return 2; }
+    cudaMemcpyAsync(d_Wt, Wt.data(), nt * 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_Wx, Wx.data(), nx * 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_dat, dat_host, n * 8, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d_err, 0, 4, s);
+    auto dft2 = [&](const double2* in, const double* in_re, double2* out, int sign) {
+        dft_axis_kernel<<<nbk(n), 256, 0, s>>>(in, in_re, tmp2, nt, nx, nx, 1, d_Wt, sign);
+        dft_axis_kernel<<<nbk(n), 256, 0, s>>>(tmp2, nullptr, out, nx, nt, 1, nx, d_Wx, sign);
+    };
+    dft2(nullptr, acc_dev, spec, -1);
+    dft2(nullptr, d_dat, specd, -1);
+    static const double bands[3][2] = {{2.0, 3.5}, {3.5, 4.5}, {4.5, 6.0}};     // driver.f90:1812-1824
+    std::vector<double> filt3((size_t)n);
+    for (int b = 0; b < 3; ++b) {
+        const std::vector<double> filt = freq_filter(bands[b][0], bands[b][1], nt, outputcad);
+        for (int mode = 0; mode < 3; ++mode) {
+            misfit[b * 3 + mode] = 0.0;
+            nmeas[b * 3 + mode] = 0;
+            if (!a.have_ridge[mode]) continue;
+            const std::vector<double>& base = mode == 0 ? fm0 : pm0;
+            for (int j = 0; j < nt; ++j)
+                for (int i = 0; i < nx; ++i)
+                    filt3[(size_t)j * nx + i] = (mode == 2 ? 1.0 : base[(size_t)j * nx + i]) * filt[j];
+            cudaMemcpyAsync(d_filt, filt3.data(), n * 8, cudaMemcpyHostToDevice, s);
+            spec_filter_kernel<<<nbk(n), 256, 0, s>>>(tmp, spec, d_filt, nullptr, nx, n);
+            dft2(tmp, nullptr, A, +1);
+            spec_filter_kernel<<<nbk(n), 256, 0, s>>>(tmp, specd, d_filt, nullptr, nx, n);
+            dft2(tmp, nullptr, D, +1);
+            RecvArgs ra;
+            ra.nx = nx; ra.nt = nt; ra.mode = mode; ra.linesearch = (mode < 2 && a.linesearch) ? 1 : 0;
+            ra.dt = a.dt; ra.t1 = a.t1; ra.x0 = a.x00; ra.xlength = xlength;
+            ra.mindist = a.ridge[mode][0]; ra.maxdist = a.ridge[mode][1];
+            ra.halftime = (int)std::floor(a.ridge[mode][2] / (2.0 * a.dt) + 0.5);
+            ra.vel[0] = 1.01; ra.vel[1] = 1.465;                                  // driver.f90:1805-1806
+            const double pc[5] = {r4(22.5000), r4(0.235317), r4(0.00134167), r4(-1.32222e-05), r4(3.00000e-08)};
+            for (int q = 0; q < 5; ++q) ra.pc[q] = pc[q];                         // driver.f90:1909-1913
+            ra.spectrum = 0;
+            int* wb = windows + ((size_t)b * 2 + (mode < 2 ? mode : 0)) * 2 * nx;
+            if (mode < 2) cudaMemcpyAsync(d_win, wb, 2 * nx * sizeof(int), cudaMemcpyHostToDevice, s);
+            const size_t smc = (size_t)(2 * nt) * 8;
+            if (smc > 48 * 1024) cudaFuncSetAttribute((const void*)receiver_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)smc);
+            receiver_kernel<<<nx, 128, smc, s>>>(ra, A, D, nullptr, d_Wt, d_win, nullptr, d_tau, d_flag, d_err);
+            std::vector<double> tau(nx);
+            std::vector<int> flag(nx);
+            cudaMemcpyAsync(tau.data(), d_tau, nx * 8, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(flag.data(), d_flag, nx * 4, cudaMemcpyDeviceToHost, s);
+            if (mode < 2 && !a.linesearch)
+                cudaMemcpyAsync(wb, d_win, 2 * nx * sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess) {
+                why = std::string("CUDA error: ") + cudaGetErrorString(cudaGetLastError());
+                return 2;
+            }
+            double sum = 0.0;
+            for (int i = 0; i < nx; ++i)
+                if (flag[i]) { sum = sum + std::pow(tau[i], 2.0); ++nmeas[b * 3 + mode]; }
+            misfit[b * 3 + mode] = sum * 0.5;
+        }
+    }
+    int herr = 0;
+    cudaMemcpyAsync(&herr, d_err, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        why = std::string("CUDA error: ") + cudaGetErrorString(cudaGetLastError());
+        return 2;
+    }
+    if (herr) {
+        why = herr == 1 ? "a measurement window starts or ends outside the record"
+                        : (herr == 2 ? "a window [lef, rig] lies outside the record"
+                                     : "a cross-correlation peak sits at the end of the lag range");
+        return 1;
+    }
     return 0;
 }

@@ -21,3 +21,11 @@ struct AdjSrcArgs {
 int adjsrc_compute(cudaStream_t s, const double* acc_dev, const double* dat_host, int nt, int nx, double xlength,
                    double outputcad, const AdjSrcArgs& a, int* windows, double* adj_host, double* misfit,
                    int* nmeas, std::string& why);
+
+// MISFIT_ALL (driver.f90:1702-2076): for the bands 2-3.5, 3.5-4.5, 4.5-6 mHz
+// the three sets of ADJOINT_SOURCE_FILT with MISFIT_ALL's ridge speeds and
+// arrival polynomial; misfit[band][set] = 0.5 sum tau^2, nmeas[band][set];
+// windows: [3][2][nx][2] (the band's sets 0 and 1; windows.all.N).
+int misfit_all_compute(cudaStream_t s, const double* acc_dev, const double* dat_host, int nt, int nx, double xlength,
+                       double outputcad, const AdjSrcArgs& a, int* windows, double* misfit, int* nmeas,
+                       std::string& why);

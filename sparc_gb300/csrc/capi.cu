@@ -1347,13 +1347,15 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     return SPARC_OK;
 }
 
-// synth == nullptr: the surface records of slot src on the device
+// synth == nullptr: the surface records of slot src on the device.
+// adj != nullptr: ADJOINT_SOURCE_FILT (misfit, nmeas: one value);
+// adj == nullptr: MISFIT_ALL (misfit, nmeas: [3 bands][3 sets]).
 static int adjoint_source(sparc_ctx* c, int src, const double* synth, const double* data, int nt,
                           const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit, int* nmeas) {
     if (!c) return SPARC_EINVAL;
     if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first");
-    if (c->P.ny != 1) return fail(c, SPARC_EINVAL, "ADJOINT_SOURCE_FILT is written for 2-D runs (ny = 1)");
-    if (src < 0 || src >= c->S || !data || !ap || !windows || !adj || !misfit || !nmeas)
+    if (c->P.ny != 1) return fail(c, SPARC_EINVAL, "the adjoint source and misfit are written for 2-D runs (ny = 1)");
+    if (src < 0 || src >= c->S || !data || !ap || !windows || !misfit || !nmeas)
         return fail(c, SPARC_EINVAL, "bad slot or null argument");
     if (nt < 1) return fail(c, SPARC_EINVAL, "nt < 1");
     if (!synth && (!c->rec || slot_nrec(c, src) < nt))
@@ -1388,8 +1390,10 @@ static int adjoint_source(sparc_ctx* c, int src, const double* synth, const doub
             for (int q = 0; q < 2; ++q) a.band[m][q] = ap->band[m][q];
         }
         std::string why;
-        const int r = adjsrc_compute(c->stream, acc, data, nt, (int)NP, c->P.xlength, c->P.outputcad, a, windows, adj,
-                                     misfit, nmeas, why);
+        const int r = adj ? adjsrc_compute(c->stream, acc, data, nt, (int)NP, c->P.xlength, c->P.outputcad, a, windows,
+                                           adj, misfit, nmeas, why)
+                          : misfit_all_compute(c->stream, acc, data, nt, (int)NP, c->P.xlength, c->P.outputcad, a,
+                                               windows, misfit, nmeas, why);
         if (r == 1) rc = fail(c, SPARC_EINVAL, why);
         else if (r == 2) rc = fail(c, SPARC_ECUDA, why);
     }
@@ -1401,13 +1405,19 @@ static int adjoint_source(sparc_ctx* c, int src, const double* synth, const doub
 
 int sparc_gpu_adjoint_source(sparc_ctx* c, int src, const double* data, int nt, const sparc_adjsrc_params* ap,
                              int* windows, double* adj, double* misfit, int* nmeas) {
+    if (!adj) return c ? fail(c, SPARC_EINVAL, "null adjoint source") : SPARC_EINVAL;
     return adjoint_source(c, src, nullptr, data, nt, ap, windows, adj, misfit, nmeas);
+}
+
+int sparc_gpu_misfit_all(sparc_ctx* c, int src, const double* synth, const double* data, int nt,
+                         const sparc_adjsrc_params* ap, int* windows, double* misfit, int* nmeas) {
+    return adjoint_source(c, src, synth, data, nt, ap, windows, nullptr, misfit, nmeas);
 }
 
 int sparc_gpu_adjoint_source_host(sparc_ctx* c, const double* synth, const double* data, int nt,
                                   const sparc_adjsrc_params* ap, int* windows, double* adj, double* misfit,
                                   int* nmeas) {
-    if (!synth) return c ? fail(c, SPARC_EINVAL, "null synthetic") : SPARC_EINVAL;
+    if (!synth || !adj) return c ? fail(c, SPARC_EINVAL, "null synthetic or adjoint source") : SPARC_EINVAL;
     return adjoint_source(c, 0, synth, data, nt, ap, windows, adj, misfit, nmeas);
 }
 

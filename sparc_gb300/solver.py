@@ -315,6 +315,39 @@ class Solver:
                 for m in (0, 1)}
         return adj, mis.value, nm.value, wout
 
+    def misfit_all(self, data, x00: float, t1_min: float, dt_min: float, ridges: dict,
+                   windows: dict | None = None, slot: int = 0, nt: int | None = None, synth=None):
+        """MISFIT_ALL (driver.f90:1702-2076) of a 2-D run on the GPU.  Returns
+        (misfit (3 bands, 3 sets) = 0.5 sum tau^2, nmeas (3, 3), windows
+        {(band, set): {pixel: (lef, rig)}}); windows given -> line search."""
+        data = _f64(np.asarray(data, dtype=np.float64))
+        nt = data.shape[0] if nt is None else int(nt)
+        nx = self.p.nx
+        ap = native.CAdjSrcParams()
+        ap.x00, ap.t1_min, ap.dt_min = float(x00), float(t1_min), float(dt_min)
+        for m in range(3):
+            ap.have_ridge[m] = int(m in ridges)
+            for q, v in enumerate(ridges.get(m, (0.0, 0.0, 0.0))):
+                ap.ridge[m][q] = float(v)
+        ap.linesearch = int(windows is not None)
+        win = np.zeros((3, 2, nx, 2), dtype=np.int32)
+        if windows is not None:
+            for (b, m), d in windows.items():
+                for i, (lef, rig) in d.items():
+                    win[b, m, i] = (lef, rig)
+        mis = np.zeros((3, 3))
+        nm = np.zeros((3, 3), dtype=np.int32)
+        sp = None
+        if synth is not None:
+            synth = _f64(np.asarray(synth, dtype=np.float64))
+            sp = _dp(synth)
+        self._ck(self.L.sparc_gpu_misfit_all(self.h, slot, sp, _dp(data), nt, ctypes.byref(ap),
+                                             win.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(mis),
+                                             nm.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        wout = {(b, m): {i: (int(win[b, m, i, 0]), int(win[b, m, i, 1])) for i in range(nx) if win[b, m, i, 0] > 0}
+                for b in range(3) for m in (0, 1) if m in ridges}
+        return mis, nm.astype(int), wout
+
     def kernels_b(self, slot: int = 0, sum_slots: bool = False):
         """Option 18: (kernel_bx, kernel_bz, kernel_vectorpsi) of the adjoint context."""
         kx = np.zeros(self.shape); kz = np.zeros(self.shape); kp = np.zeros(self.shape)

@@ -69,3 +69,21 @@ def test_adjoint_source_refuses_3d(gpu_lib):
     s = Solver(p, table_for(p))
     with pytest.raises(SparcError):
         s.adjoint_source(np.zeros((20, p.nx)), 0.0, 0.0, 0.5, {0: (1, 2, 3)}, {}, synth=np.zeros((20, p.nx)))
+
+
+def test_misfit_all_matches_oracle(gpu_lib):
+    from oracle import adjoint_source as A
+    c = CASE
+    p, s = _ctx()
+    t = np.arange(c["nt"]) * 0.5
+    acc = ridge_field(c["nx"], c["nt"], c["xlength"], c["outputcad"], seed=7)
+    dat = delayed(acc, -9.0, c["outputcad"])
+    mg, ng, wg = s.misfit_all(dat, c["x00"], t[0], 0.5, c["ridges"], synth=acc)
+    mo, no, wo = A.misfit_all(acc, dat, c["xlength"], c["outputcad"], c["x00"], t, c["ridges"])
+    assert np.array_equal(ng, no) and wg == wo
+    assert np.all(np.abs(mg - mo) <= 1e-10 * mo)
+    # line search on the stored windows (windows.all.N)
+    dat2 = delayed(acc, 15.0, c["outputcad"])
+    mg2, ng2, _ = s.misfit_all(dat2, c["x00"], t[0], 0.5, c["ridges"], windows=wg, synth=acc)
+    mo2, no2, _ = A.misfit_all(acc, dat2, c["xlength"], c["outputcad"], c["x00"], t, c["ridges"], windows_in=wo)
+    assert np.array_equal(ng2, no2) and np.all(np.abs(mg2 - mo2) <= 1e-10 * mo2)

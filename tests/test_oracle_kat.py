@@ -525,3 +525,18 @@ def test_adjsrc_zero_for_equal_data_and_measures_a_shift():
     adj3, mis3, n3, _, _ = A.adjoint_source_filt(acc, delayed(acc, shift, c["outputcad"]), c["xlength"],
                                                  c["outputcad"], c["x00"], t, c["ridges"], c["bands"], windows_in=win)
     assert np.array_equal(adj3, adj) and mis3 == mis and n3 == n
+
+
+def test_misfit_all_zero_for_equal_data():
+    """MISFIT_ALL (driver.f90:1702-2076): three bands x three sets, zero misfit
+    when the data equal the synthetic, measurements in every band and set."""
+    from adjsrc_cases import CASE, delayed, ridge_field
+    from oracle import adjoint_source as A
+    c = CASE
+    t = np.arange(c["nt"]) * 0.5
+    acc = ridge_field(c["nx"], c["nt"], c["xlength"], c["outputcad"], seed=6)
+    m0, n0, w0 = A.misfit_all(acc, acc.copy(), c["xlength"], c["outputcad"], c["x00"], t, c["ridges"])
+    assert m0.shape == (3, 3) and np.all(n0 > 10) and np.abs(m0).max() < 1e-18
+    m1, n1, w1 = A.misfit_all(acc, delayed(acc, 12.0, c["outputcad"]), c["xlength"], c["outputcad"], c["x00"], t,
+                              c["ridges"])
+    assert np.array_equal(n1, n0) and w1 == w0 and np.all(m1 > 0)
