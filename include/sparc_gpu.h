@@ -299,6 +299,34 @@ int sparc_gpu_adjoint_source_host(sparc_ctx* ctx, const double* synth, const dou
 int sparc_gpu_misfit_all(sparc_ctx* ctx, int src_idx, const double* synth, const double* data, int nt,
                          const sparc_adjsrc_params* ap, int* windows, double* misfit, int* nmeas);
 
+/* ---- model update of an inversion iteration (grad.py) --------------------- */
+
+/* Replaces grad.py:152-186 (the kernel sums are the caller's, as grad.py
+ * reads them from kernel/*.fits).  Host arrays (nz,ny,nx) of the context's
+ * grid, FP64: kc_sum = sum of kernel_c, kpsi_sum = sum of kernel_vectorpsi,
+ * hess_sum = sum of |hessian| over the sources; rho_z[nz] the density
+ * column of the background (the third column of the polytrope file).
+ * hess = max(hess_sum rho_z / max, 5e-3); grad_c = filterz 'smooth' of
+ * filterx(kc_sum / hess); grad_psi = gaussian_filter1d along z (sigma 2,
+ * reflect) of antisymmetrize(filterx(kpsi_sum / hess)).  Either output may
+ * be NULL (its kernel sum may then be NULL).  Needs set_background. */
+int sparc_gpu_gradient(sparc_ctx* ctx, const double* kc_sum, const double* kpsi_sum, const double* hess_sum,
+                       const double* rho_z, double* grad_c, double* grad_psi);
+
+/* Replaces grad.py:188-301 (steepest descent and conjugate gradient; the
+ * LBFGS branch there is switched off and names an undefined variable).
+ * last_grad_psi NULL: steepest descent, update = gradient, *con = 0.  Else
+ * conjugate gradient: con = max(0, sum g (g - g_last) / sum g_last^2) of the
+ * vectorpsi gradients, update = gradient + con * last update (last_update_psi
+ * and, when update_c is asked for, last_update_c required).  With nmodels >
+ * 0 writes test_psi[nmodels][nz*ny*nx], model i+1 = model_psi + eps (i+1)
+ * rms(model_psi) update_psi / max|update_psi| (grad.py uses eps 1e-7 and 5
+ * models).  update_c, update_psi and con may be NULL. */
+int sparc_gpu_update_models(sparc_ctx* ctx, const double* grad_c, const double* grad_psi,
+                            const double* last_grad_psi, const double* last_update_c,
+                            const double* last_update_psi, const double* model_psi, double eps, int nmodels,
+                            double* update_c, double* update_psi, double* test_psi, double* con);
+
 /* ---- primitives (the reference's derivative routines) ---------------------- */
 
 /* ddx / ddy (derivatives.f90:28-170) and ddz (derivatives.f90:10-24 with

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsparc_gpu.so")
-SOURCES = ["capi.cu", "modal.cu", "fft.cu", "noalloc.cu", "fused.cu", "mhd.cu", "adjsrc.cu"]
+SOURCES = ["capi.cu", "modal.cu", "fft.cu", "noalloc.cu", "fused.cu", "mhd.cu", "adjsrc.cu", "update.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

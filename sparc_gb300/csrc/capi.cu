@@ -12,6 +12,7 @@
 
 #include "ctx.cuh"
 #include "adjsrc.cuh"
+#include "update.cuh"
 
 namespace {
 
@@ -1426,6 +1427,156 @@ int sparc_gpu_kernels_b(sparc_ctx* c, int src, int sum_slots, double* kbx, doubl
     if (!c->mhd || c->P.option != 18) return fail(c, SPARC_EINVAL, "B-field kernels belong to option 18");
     if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
     return mhd2d_kernels_b(c, src, sum_slots, kbx, kbz, kpsi);
+}
+
+// ---------------------------------------------------------------------------
+// model update of an inversion iteration (grad.py:158-301)
+// ---------------------------------------------------------------------------
+static int ensure_update(sparc_ctx* c) {
+    if (c->upd) return SPARC_OK;
+    int rc = ensure_spec64(c);
+    if (rc) return rc;
+    return dalloc(c, (void**)&c->upd, ((size_t)3 * c->N + c->M + c->nz + kReduceScratch + 8) * 8);
+}
+
+// scratch: fields f0, f1, f2 (N each), the filterx multiplier (M), rho_z
+// (nz) and the reduction slots
+struct UpdBufs { double *f0, *f1, *f2, *mul, *rho, *res, *red; };
+static UpdBufs upd_bufs(sparc_ctx* c) {
+    UpdBufs b;
+    b.f0 = c->upd;
+    b.f1 = b.f0 + c->N;
+    b.f2 = b.f1 + c->N;
+    b.mul = b.f2 + c->N;
+    b.rho = b.mul + c->M;
+    b.res = b.rho + c->nz;
+    b.red = b.res + 8;
+    return b;
+}
+
+// filterx (grad.py:47-61) of src into dst: the half spectrum along x times
+// rfft(exp(-x^2 / 32)), x = fftfreq(nx) nx.  The Gaussian is real and even,
+// so its rfft is the real cosine sum; the same factor multiplies every ky.
+static int filterx_dev(sparc_ctx* c, const UpdBufs& b, const double* src, double* dst) {
+    const int nx = c->P.nx, ny = c->P.ny, H = nx / 2 + 1;
+    std::vector<double> g(nx), mul((size_t)c->M);
+    for (int i = 0; i < nx; ++i) {
+        const double x = (double)(i <= (nx - 1) / 2 ? i : i - nx);
+        g[i] = std::exp(-(x * x) / (2.0 * 16.0));
+    }
+    const double two_pi = 2.0 * std::acos(-1.0);      // numpy's rfft: full FP64 pi, not the context's REAL*4 one
+    for (int k = 0; k < H; ++k) {
+        double acc = 0.0;
+        for (int i = 0; i < nx; ++i) acc += g[i] * std::cos(two_pi * (double)((long long)k * i % nx) / nx);
+        for (int y = 0; y < ny; ++y) mul[(size_t)y * H + k] = acc;
+    }
+    int rc = upload(c, b.mul, mul.data(), mul.size() * 8);
+    if (rc) return rc;
+    fft_phys_to_spec<double>(src, c->spec64, c->tmp64, nx, ny, c->nz, c->tw_x, c->tw_y, c->stream, b.mul);
+    fft_spec_to_phys<double>(c->spec64, dst, c->tmp64, nx, ny, c->nz, c->tw_x, c->tw_y, c->stream);
+    CKL();
+    // mul is a host vector: the upload must land before it goes out of scope
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+int sparc_gpu_gradient(sparc_ctx* c, const double* kc_sum, const double* kpsi_sum, const double* hess_sum,
+                       const double* rho_z, double* grad_c, double* grad_psi) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->have_bg) return fail(c, SPARC_ESTATE, "set_background first (the transform tables)");
+    if (!hess_sum || !rho_z) return fail(c, SPARC_EINVAL, "null hessian or rho_z");
+    if ((grad_c && !kc_sum) || (grad_psi && !kpsi_sum)) return fail(c, SPARC_EINVAL, "null kernel for a requested gradient");
+    int rc = ensure_update(c);
+    if (rc) return rc;
+    const UpdBufs b = upd_bufs(c);
+    const long long N = c->N, NP = c->NP;
+    if ((rc = upload(c, b.f0, hess_sum, N * 8))) return rc;
+    if ((rc = upload(c, b.rho, rho_z, (size_t)c->nz * 8))) return rc;
+    launch_precondition(b.f0, b.rho, NP, c->nz, b.res, c->stream);
+    CKL();
+    if (grad_c) {
+        if ((rc = upload(c, b.f1, kc_sum, N * 8))) return rc;
+        launch_divide(b.f1, b.f1, b.f0, N, c->stream);
+        if ((rc = filterx_dev(c, b, b.f1, b.f2))) return rc;
+        launch_filterz_smooth(b.f1, b.f2, NP, c->nz, c->stream);
+        CKL();
+        CK(cudaMemcpyAsync(grad_c, b.f1, N * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (grad_psi) {
+        if ((rc = upload(c, b.f1, kpsi_sum, N * 8))) return rc;
+        launch_divide(b.f1, b.f1, b.f0, N, c->stream);
+        if ((rc = filterx_dev(c, b, b.f1, b.f2))) return rc;
+        launch_antisymmetrize(b.f1, b.f2, (long long)c->nz * c->P.ny, c->P.nx, c->stream);
+        if (!launch_gaussian_z(b.f2, b.f1, NP, c->nz, 2.0, c->stream)) return fail(c, SPARC_EINVAL, "gaussian taps");
+        CKL();
+        CK(cudaMemcpyAsync(grad_psi, b.f2, N * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
+}
+
+int sparc_gpu_update_models(sparc_ctx* c, const double* grad_c, const double* grad_psi, const double* last_grad_psi,
+                            const double* last_update_c, const double* last_update_psi, const double* model_psi,
+                            double eps, int nmodels, double* update_c, double* update_psi, double* test_psi,
+                            double* con) {
+    if (!c) return SPARC_EINVAL;
+    if (!grad_psi) return fail(c, SPARC_EINVAL, "null gradient_vectorpsi");
+    const bool cg = last_grad_psi != nullptr;
+    if (cg && (!last_update_psi || (update_c && !last_update_c)))
+        return fail(c, SPARC_EINVAL, "conjugate gradient needs the last gradient_vectorpsi, update_c and update_vectorpsi");
+    if (update_c && !grad_c) return fail(c, SPARC_EINVAL, "update_c requested without gradient_c");
+    if (nmodels < 0 || (nmodels > 0 && (!model_psi || !test_psi))) return fail(c, SPARC_EINVAL, "bad test-model request");
+    int rc = ensure_update(c);
+    if (rc) return rc;
+    const UpdBufs b = upd_bufs(c);
+    const long long N = c->N;
+    double h[3] = {0.0, 0.0, 0.0};
+    double cn = 0.0;
+    if ((rc = upload(c, b.f0, grad_psi, N * 8))) return rc;
+    if (cg) {
+        // con = sum g (g - g_last) / sum g_last^2, floored at 0 (grad.py:218-223)
+        if ((rc = upload(c, b.f1, last_grad_psi, N * 8))) return rc;
+        launch_reduce(b.res, b.f1, nullptr, N, b.red, c->stream);
+        launch_sub(b.f1, b.f0, b.f1, N, c->stream);
+        launch_reduce(b.res + 4, b.f0, b.f1, N, b.red, c->stream);
+        CKL();
+        double hr[8];
+        CK(cudaMemcpyAsync(hr, b.res, sizeof(hr), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        cn = hr[4] / hr[0];
+        if (cn < 0) cn = 0.0;
+        if ((rc = upload(c, b.f1, last_update_psi, N * 8))) return rc;
+        launch_axpy_c(b.f0, b.f0, b.f1, cn, N, c->stream);
+        CKL();
+    }
+    if (con) *con = cn;
+    if (update_psi) CK(cudaMemcpyAsync(update_psi, b.f0, N * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (update_c) {
+        if ((rc = upload(c, b.f1, grad_c, N * 8))) return rc;
+        if (cg) {
+            if ((rc = upload(c, b.f2, last_update_c, N * 8))) return rc;
+            launch_axpy_c(b.f1, b.f1, b.f2, cn, N, c->stream);
+            CKL();
+        }
+        CK(cudaMemcpyAsync(update_c, b.f1, N * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (nmodels > 0) {
+        // test_vectorpsi_i = model + eps i rms(model) u / max|u| (grad.py:282-301)
+        if ((rc = upload(c, b.f1, model_psi, N * 8))) return rc;
+        launch_reduce(b.res, b.f0, nullptr, N, b.red, c->stream);        // res[1] = max |u|
+        launch_reduce(b.res + 4, b.f1, nullptr, N, b.red, c->stream);    // res[4] = sum model^2
+        CKL();
+        CK(cudaMemcpyAsync(h, b.res + 4, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        const double scale = std::sqrt(h[0] / (double)N);
+        for (int i = 1; i <= nmodels; ++i) {
+            launch_test_model(b.f2, b.f1, b.f0, b.res, eps * i * scale, N, c->stream);
+            CKL();
+            CK(cudaMemcpyAsync(test_psi + (size_t)(i - 1) * N, b.f2, N * 8, cudaMemcpyDeviceToHost, c->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return SPARC_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -90,6 +90,9 @@ struct sparc_ctx {
     // option 10: the state is physical ([src][field] slots of fs complex
     // elements each hold one dense (nz, ny, nx) real field)
     MhdState* mhd = nullptr;
+    // model update (grad.py): three N-point FP64 fields, the filterx
+    // multiplier (M) and reduction scratch, allocated on first use
+    double* upd = nullptr;
 };
 
 

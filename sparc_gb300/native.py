@@ -41,7 +41,7 @@ EXPORTS = [
     "sparc_gpu_stream", "sparc_gpu_launch_count", "sparc_gpu_device_bytes", "sparc_gpu_info",
     "sparc_gpu_sync", "sparc_gpu_spec_to_phys_noalloc", "sparc_gpu_autotune", "sparc_gpu_set_mhd_background",
     "sparc_gpu_set_mhd2d_background", "sparc_gpu_kernels_b", "sparc_gpu_adjoint_source",
-    "sparc_gpu_adjoint_source_host", "sparc_gpu_misfit_all",
+    "sparc_gpu_adjoint_source_host", "sparc_gpu_misfit_all", "sparc_gpu_gradient", "sparc_gpu_update_models",
 ]
 
 
@@ -139,6 +139,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                            ctypes.POINTER(I)], I),
         "sparc_gpu_misfit_all": ([P, I, D, D, I, ctypes.POINTER(CAdjSrcParams), ctypes.POINTER(I), D,
                                   ctypes.POINTER(I)], I),
+        "sparc_gpu_gradient": ([P, D, D, D, D, D, D], I),
+        "sparc_gpu_update_models": ([P, D, D, D, D, D, D, ctypes.c_double, I, D, D, D, D], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -24,6 +24,10 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_D)
 
 
+def _dpn(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
 def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -347,6 +351,51 @@ class Solver:
         wout = {(b, m): {i: (int(win[b, m, i, 0]), int(win[b, m, i, 1])) for i in range(nx) if win[b, m, i, 0] > 0}
                 for b in range(3) for m in (0, 1) if m in ridges}
         return mis, nm.astype(int), wout
+
+    def gradient(self, kc_sum, kpsi_sum, hess_sum, rho_z):
+        """grad.py:152-186 on the GPU: (gradient_c, gradient_vectorpsi) from the
+        kernels summed over sources, the summed |hessian| and the density
+        column rho_z of the background.  A kernel sum given as None skips its
+        gradient (returned as None)."""
+        hs = _f64(hess_sum)
+        rz = _f64(rho_z)
+        if hs.shape != self.shape or rz.shape != (self.p.nz,):
+            raise ValueError(f"hess_sum must be {self.shape} and rho_z ({self.p.nz},)")
+        kc = None if kc_sum is None else _f64(kc_sum)
+        kp = None if kpsi_sum is None else _f64(kpsi_sum)
+        for a in (kc, kp):
+            if a is not None and a.shape != self.shape:
+                raise ValueError(f"kernel sums must be {self.shape}")
+        gc = None if kc is None else np.zeros(self.shape)
+        gp = None if kp is None else np.zeros(self.shape)
+        self._ck(self.L.sparc_gpu_gradient(self.h, _dpn(kc), _dpn(kp), _dp(hs), _dp(rz), _dpn(gc), _dpn(gp)))
+        return gc, gp
+
+    def update_models(self, grad_c, grad_psi, model_psi, last=None, eps: float = 1e-7, nmodels: int = 5):
+        """grad.py:188-301 on the GPU: the update direction (steepest descent,
+        or conjugate gradient with last = (last gradient_vectorpsi, last
+        update_c, last update_vectorpsi)) and the line-search test models.
+        Returns (update_c or None, update_psi, test_psi (nmodels, ...), con)."""
+        gp = _f64(grad_psi)
+        gc = None if grad_c is None else _f64(grad_c)
+        mp = _f64(model_psi)
+        arrs = [gp, mp] + ([] if gc is None else [gc])
+        lg = lc = lp = None
+        if last is not None:
+            lg, lc, lp = (None if a is None else _f64(a) for a in last)
+            arrs += [a for a in (lg, lc, lp) if a is not None]
+        for a in arrs:
+            if a.shape != self.shape:
+                raise ValueError(f"fields must be {self.shape}")
+        uc = None if gc is None else np.zeros(self.shape)
+        up = np.zeros(self.shape)
+        tp = np.zeros((int(nmodels),) + self.shape)
+        con = ctypes.c_double(0.0)
+        self._ck(self.L.sparc_gpu_update_models(self.h, _dpn(gc), _dp(gp), _dpn(lg), _dpn(lc), _dpn(lp), _dp(mp),
+                                                float(eps), int(nmodels), _dpn(uc), _dp(up),
+                                                _dp(tp) if nmodels > 0 else None,
+                                                ctypes.cast(ctypes.pointer(con), _D)))
+        return uc, up, tp, con.value
 
     def kernels_b(self, slot: int = 0, sum_slots: bool = False):
         """Option 18: (kernel_bx, kernel_bz, kernel_vectorpsi) of the adjoint context."""

@@ -1,0 +1,55 @@
+"""Host logic of the model-update file flow (grad.py:150-301): file names,
+the kernel sums, the choice of direction and the test_c copies, with the
+device calls stood in by the oracle so that it runs without a GPU."""
+import os
+
+import numpy as np
+
+from cases import small_params_2d
+
+
+class OracleSolver:
+    """Solver.gradient / Solver.update_models restated by the oracle."""
+
+    def __init__(self, p):
+        self.shape = (p.nz, p.ny, p.nx)
+
+    def gradient(self, kc, kpsi, hess, rho_z):
+        from oracle import model_update as U
+        return U.gradient(kc, kpsi, hess, rho_z)
+
+    def update_models(self, g_c, g_psi, model, last=None, eps=1e-7, nmodels=5):
+        from oracle import model_update as U
+        u_c, u_psi, con = U.update_direction(g_c, g_psi, last)
+        return u_c, u_psi, U.test_models(model, u_psi, eps=eps, n=nmodels), con
+
+
+def test_model_update_file_flow(tmp_path):
+    from sparc_gb300 import inversion, io
+    p = small_params_2d(nx=32, nz=24)
+    rng = np.random.default_rng(4)
+    (tmp_path / "kernel").mkdir()
+    for src in (1, 2, 3):
+        for name in ("kernel_c", "kernel_vectorpsi", "hessian"):
+            io.write_fits(str(tmp_path / "kernel" / f"{name}_{src:02d}.fits"), rng.standard_normal((p.nz, p.nx)))
+    kc, kpsi, hess = inversion.sum_kernels(str(tmp_path), 3)
+    assert kc.shape == (p.nz, 1, p.nx) and (hess >= 0).all()
+    direct = sum(np.abs(io.read_fits(str(tmp_path / "kernel" / f"hessian_{s:02d}.fits"))) for s in (1, 2, 3))
+    assert np.allclose(hess[:, 0, :], direct, rtol=0, atol=1e-15)
+    (tmp_path / "update").mkdir()
+    io.write_fits(str(tmp_path / "update" / "model_vectorpsi_00.fits"), rng.standard_normal((p.nz, 1, p.nx)))
+    s = OracleSolver(p)
+    rho = np.linspace(1.0, 0.1, p.nz)
+    r = inversion.model_update(s, str(tmp_path), 1, 3, rho, conjugate_gradient=True)     # iteration 1: steepest
+    assert r.con == 0.0
+    got = sorted(os.listdir(tmp_path / "update"))
+    want = sorted(["model_vectorpsi_00.fits", "gradient_c_00.fits", "gradient_vectorpsi_00.fits", "update_c_00.fits",
+                   "update_vectorpsi_00.fits"] + [f"test_vectorpsi_{i}.fits" for i in range(1, 6)])
+    assert got == want
+    io.write_fits(str(tmp_path / "update" / "model_vectorpsi_01.fits"), rng.standard_normal((p.nz, 1, p.nx)))
+    io.write_fits(str(tmp_path / "update" / "model_c_01.fits"), np.ones((p.nz, 1, p.nx)))
+    r2 = inversion.model_update(s, str(tmp_path), 2, 3, rho, conjugate_gradient=True, nmodels=2)
+    names = set(os.listdir(tmp_path / "update"))
+    assert {"update_psi_01.fits", "update_c_01.fits", "test_c_1.fits", "test_c_2.fits"} <= names
+    assert "update_vectorpsi_01.fits" not in names                 # the CG branch's own name (grad.py:230)
+    assert r2.test_psi.shape == (2, p.nz, 1, p.nx)

@@ -540,3 +540,42 @@ def test_misfit_all_zero_for_equal_data():
     m1, n1, w1 = A.misfit_all(acc, delayed(acc, 12.0, c["outputcad"]), c["xlength"], c["outputcad"], c["x00"], t,
                               c["ridges"])
     assert np.array_equal(n1, n0) and w1 == w0 and np.all(m1 > 0)
+
+
+# ---- model update (grad.py:158-301) --------------------------------------------------
+
+def test_model_update_filters_pin():
+    """gaussian_z against scipy.ndimage.gaussian_filter1d (mode 'reflect', as
+    grad.py calls it); filterz 'smooth' zeroes plane 4 and the top plane (its
+    temp array starts at zero); filterx is a circular convolution with the
+    unnormalised Gaussian."""
+    from oracle import model_update as U
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal((40, 1, 24))
+    gf = pytest.importorskip("scipy.ndimage").gaussian_filter1d
+    assert rel_l2(U.gaussian_z(a, 2.0), gf(a, sigma=2.0, axis=0)) < 1e-14
+    s = U.filterz_smooth(a)
+    assert np.all(s[4] == 0) and np.all(s[-1] == 0) and np.array_equal(s[0], a[0])
+    assert np.allclose(s[2], 0.5 * (a[1] + a[3]))
+    x = np.fft.fftfreq(24) * 24
+    g = np.exp(-x ** 2 / 32.0)
+    conv = np.stack([[np.array([np.sum(a[k, 0] * np.roll(g[::-1], i + 1)) for i in range(24)])] for k in range(40)])
+    assert rel_l2(U.filterx(a), conv) < 1e-12
+    anti = U.antisymmetrize(a)
+    assert np.allclose(anti, -anti[..., ::-1])
+
+
+def test_model_update_directions_and_models():
+    from oracle import model_update as U
+    rng = np.random.default_rng(9)
+    g_c, g_psi = rng.standard_normal((2, 30, 1, 16))
+    u_c, u_psi, con = U.update_direction(g_c, g_psi)
+    assert con == 0.0 and u_psi is g_psi
+    lg, lu_c, lu_psi = rng.standard_normal((3, 30, 1, 16))
+    u_c, u_psi, con = U.update_direction(g_c, g_psi, (lg, lu_c, lu_psi))
+    want = max(np.sum(g_psi * (g_psi - lg)) / np.sum(lg ** 2), 0.0)
+    assert con == pytest.approx(want) and np.allclose(u_psi, g_psi + want * lu_psi)
+    m = rng.standard_normal((30, 1, 16))
+    tm = U.test_models(m, u_psi)
+    assert tm.shape == (5, 30, 1, 16)
+    assert np.allclose(tm[2] - m, 3e-7 * np.sqrt(np.mean(m ** 2)) * u_psi / np.abs(u_psi).max())
