@@ -173,3 +173,131 @@ def flux_sheet_background(p, table: np.ndarray, b_surf: float = 300.0, w_mm: flo
     rho = rho_q[:, None, None] * pres / pq
     c = np.broadcast_to(c_q[:, None, None], (nz, 1, nx)).copy()
     return rho, c, pres, psi
+
+
+# ---- magnetohydrostatic sheet from a vector potential (code_python/tubex.py) ----
+
+TUBEX_RSUN_MM = 695.9894      # tubex.py:9 (its own value of R_sun in Mm)
+TUBEX_GRAV = 2.775e4          # tubex.py:44
+TUBEX_CONVERT = 1e8           # tubex.py:45 (Mm -> cm)
+
+
+def _x_derivative(a: np.ndarray, period: float) -> np.ndarray:
+    """d/dx along the last axis by the FFT (period `period`); the Nyquist
+    term of an even length drops out, as it does in a real inverse FFT."""
+    n = a.shape[-1]
+    k = 2.0 * np.pi * np.fft.rfftfreq(n, d=period / n)
+    return np.fft.irfft(np.fft.rfft(a, axis=-1) * (1j * k), n=n, axis=-1)
+
+
+def _x_integral(a: np.ndarray, period: float) -> np.ndarray:
+    """The periodic antiderivative along the last axis by the FFT: the mean
+    (k = 0) term has no periodic integral and is dropped, as is Nyquist."""
+    n = a.shape[-1]
+    k = 2.0 * np.pi * np.fft.rfftfreq(n, d=period / n)
+    f = np.fft.rfft(a, axis=-1)
+    inv = np.zeros_like(k)
+    inv[1:] = 1.0 / k[1:]
+    return np.fft.irfft(f * (-1j * inv), n=n, axis=-1)
+
+
+def vector_potential_background(solver, table: np.ndarray, lx_mm: float = 400.0, a0: float = 5000.0,
+                                decay_x: float = 10.0, decay_z: float = 10.0, decay_z_start: float = 12.0,
+                                zero_b: bool = True) -> dict:
+    """The 2-D magnetohydrostatic backgrounds of code_python/tubex.py:27-141
+    (true and starting models of an inversion for the vector potential).
+
+    A(x, z) = a0 f(x) exp(z / decay), f = -(x/dx) / (1 + (x/dx)^4), with
+    x = -lx/2 .. lx/2 (nx points, no endpoint) and z = (r/R_sun - 1) R_sun in
+    Mm from the background table.  True field: the analytic B_x = -dA/dz,
+    B_z = dA/dx (tubex.py:53-54); starting field from the numerical
+    derivatives of A_start (decay_z_start).  With the true field's Lorentz
+    force F = dB_x/dz - dB_z/dx, the pressure is the periodic x-integral of
+    B_z F, pinned to the table's p at x index 0, and the density balances
+    dp/dz + B_x F against gravity, pinned the same way (tubex.py:69-90);
+    c^2 = c_q^2 rho_q / p_q * p / rho.  zero_b (tubex.py:10, on in the
+    reference) zeroes both fields and potentials, leaving the quiet column.
+
+    The z derivatives are the compact scheme with ibc = 1 divided by the
+    same derivative of z (tubex.py:14-17,33-36), here from the library's FP64
+    ddz on the GPU (solver: a context of shape (nz, 1, nx) on this table); x
+    derivatives and the x integral are FFT ones (the fftcalculus module the
+    script imports is not in the reference).  Returns (nz, 1, nx) arrays:
+    bx, bz, psi (A sqrt(4 pi) / R_sun, the model_vectorpsi unit) for 'true'
+    and 'start', and p, rho, c shared by both models.
+    """
+    nz = table.shape[0]
+    nz_s, ny_s, nx = solver.shape
+    if nz_s != nz or ny_s != 1:
+        raise ValueError(f"solver must be (nz={nz}, 1, nx), got {solver.shape}")
+    x = np.linspace(-lx_mm / 2.0, lx_mm / 2.0, num=nx, endpoint=False)
+    z = (table[:, 0] - 1.0) * TUBEX_RSUN_MM
+    p_q, rho_q, c2_q = table[:, 3], table[:, 2], table[:, 1] ** 2
+
+    def grid(col_z, row_x):                     # (nz, 1, nx) outer product
+        return (np.asarray(col_z)[:, None] * np.asarray(row_x)[None, :])[:, None, :]
+
+    dz_idx = solver.ddz(np.broadcast_to(z[:, None, None], (nz, 1, nx)), 1)
+
+    def derivz(a):
+        return solver.ddz(a, 1) / dz_idx
+
+    fx = -(x / decay_x) / (1.0 + (x / decay_x) ** 4)
+    dfx = -decay_x ** 3 * (decay_x ** 4 - 3.0 * x ** 4) / (decay_x ** 4 + x ** 4) ** 2
+    gz = np.exp(z / decay_z)
+    bx = -a0 * grid(gz / decay_z, fx)
+    bz = a0 * grid(gz, dfx)
+    a_true = a0 * grid(gz, fx)
+    a_start = a0 * grid(np.exp(z / decay_z_start), fx)
+    bx_start = -derivz(a_start)
+    bz_start = _x_derivative(a_start, lx_mm)
+    if zero_b:
+        bx = np.zeros_like(bx); bz = np.zeros_like(bz)
+        bx_start = np.zeros_like(bx); bz_start = np.zeros_like(bx)
+        a_start = np.zeros_like(a_start); a_true = np.zeros_like(a_true)
+    force = derivz(bx) - _x_derivative(bz, lx_mm)
+    hz = bx * force
+    hx = bz * force
+    pres = _x_integral(hx, lx_mm)
+    pres = pres - (pres[:, :, :1] - p_q[:, None, None])
+    dzp = derivz(pres)
+    if (pres / p_q[:, None, None] - 1.0).min() < -1.0:
+        raise ValueError("negative pressure")
+    rho = -(hz + dzp) / (TUBEX_GRAV * TUBEX_CONVERT)
+    rho = rho - (rho[:, :, :1] - rho_q[:, None, None])
+    if (rho / rho_q[:, None, None] - 1.0).min() < -1.0:
+        raise ValueError("negative density")
+    c = np.sqrt((c2_q * rho_q / p_q)[:, None, None] * pres / rho)
+    s4 = np.sqrt(4.0 * np.pi)
+    return {"true": {"bx": bx, "bz": bz, "psi": a_true * s4 / TUBEX_RSUN_MM},
+            "start": {"bx": bx_start, "bz": bz_start, "psi": a_start * s4 / TUBEX_RSUN_MM},
+            "p": pres, "rho": rho, "c": c, "x_mm": x, "z_mm": z}
+
+
+def write_vector_potential_models(modeldir: str, models: dict) -> list:
+    """The FITS files tubex.py:143-160 writes, (nz, nx) arrays under
+    modeldir/true and modeldir/start: B_z2D, B_x2D (times sqrt(4 pi)),
+    true_vectorpsi, model_vectorpsi_ls00, pressure2D, density2D,
+    soundspeed2D and model_c_ls00."""
+    import os
+    from . import io
+    s4 = np.sqrt(4.0 * np.pi)
+    t, st = os.path.join(modeldir, "true"), os.path.join(modeldir, "start")
+    os.makedirs(t, exist_ok=True)
+    os.makedirs(st, exist_ok=True)
+    out = []
+
+    def put(path, a):
+        io.write_fits(path, np.asarray(a)[:, 0, :])
+        out.append(path)
+
+    put(os.path.join(t, "B_z2D.fits"), models["true"]["bz"] * s4)
+    put(os.path.join(t, "B_x2D.fits"), models["true"]["bx"] * s4)
+    put(os.path.join(t, "true_vectorpsi.fits"), models["true"]["psi"])
+    put(os.path.join(st, "model_vectorpsi_ls00.fits"), models["start"]["psi"])
+    for d in (t, st):
+        put(os.path.join(d, "pressure2D.fits"), models["p"])
+        put(os.path.join(d, "density2D.fits"), models["rho"])
+        put(os.path.join(d, "soundspeed2D.fits"), models["c"])
+    put(os.path.join(st, "model_c_ls00.fits"), models["c"])
+    return out

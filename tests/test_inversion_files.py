@@ -53,3 +53,24 @@ def test_model_update_file_flow(tmp_path):
     assert {"update_psi_01.fits", "update_c_01.fits", "test_c_1.fits", "test_c_2.fits"} <= names
     assert "update_vectorpsi_01.fits" not in names                 # the CG branch's own name (grad.py:230)
     assert r2.test_psi.shape == (2, p.nz, 1, p.nx)
+
+
+def test_vector_potential_background_host_logic():
+    """The library's tubex.py generator with the oracle standing in for the
+    GPU z derivative, against the oracle's own restatement (the host logic:
+    layout, pinning rows, the FFT calculus, units)."""
+    from oracle import backgrounds as B
+    from oracle.oracle import Oracle
+    from sparc_gb300.background import polytrope_table, vector_potential_background
+    nz, nx = 96, 64
+    tab = polytrope_table(nz, z_bot_mm=-25.0, z_top_mm=1.2)
+    o = Oracle(small_params_2d(nx=nx, nz=nz, xlength=400e8, ylength=400e8), tab)
+    o.shape = (nz, 1, nx)
+    got = vector_potential_background(o, tab, a0=30.0, zero_b=False)
+    ref = B.tubex(tab, o, nx=nx, a0=30.0, zero_b=False)
+    for key in ("p", "rho", "c"):
+        assert np.allclose(got[key], ref[key], rtol=1e-10, atol=0), key
+    for m in ("true", "start"):
+        for f in ("bx", "bz", "psi"):
+            d = np.abs(got[m][f] - ref[m][f]).max()
+            assert d <= 1e-10 * np.abs(ref[m][f]).max(), (m, f, d)

@@ -579,3 +579,39 @@ def test_model_update_directions_and_models():
     tm = U.test_models(m, u_psi)
     assert tm.shape == (5, 30, 1, 16)
     assert np.allclose(tm[2] - m, 3e-7 * np.sqrt(np.mean(m ** 2)) * u_psi / np.abs(u_psi).max())
+
+
+def test_tubex_restatement_pins():
+    """The restatement of code_python/tubex.py: the shipped zeroB run gives
+    back the quiet column; the compact z derivative of A reproduces the
+    analytic B_x = -dA/dz; the FFT calculus differentiates and integrates
+    band-limited fields exactly."""
+    from cases import small_params_2d
+    from oracle import backgrounds as B
+    from oracle.oracle import Oracle
+    from sparc_gb300.background import polytrope_table
+    nz, nx = 120, 128
+    tab = polytrope_table(nz, z_bot_mm=-25.0, z_top_mm=1.2)
+    o = Oracle(small_params_2d(nx=nx, nz=nz, xlength=400e8, ylength=400e8), tab)
+    r = B.tubex(tab, o, nx=nx)
+    assert np.array_equal(r["p"][:, 0, :], np.broadcast_to(tab[:, 3, None], (nz, nx)))
+    assert np.array_equal(r["rho"][:, 0, :], np.broadcast_to(tab[:, 2, None], (nz, nx)))
+    assert np.abs(r["c"][:, 0, :] / tab[:, 1, None] - 1).max() < 1e-14
+    assert not any(np.any(r[m][f]) for m in ("true", "start") for f in ("bx", "bz", "psi"))
+    # the starting field's B_x is the numerical -dA/dz; against the analytic one
+    a0, dx, dz = 20.0, 10.0, 12.0
+    r = B.tubex(tab, o, nx=nx, a0=a0, zero_b=False)
+    assert not r["negative"]
+    x = np.linspace(-200.0, 200.0, nx, endpoint=False)
+    z = (tab[:, 0] - 1.0) * B.RSUN
+    fx = -(x / dx) / (1 + (x / dx) ** 4)
+    bx_exact = -a0 * (np.exp(z / dz) / dz)[:, None] * fx[None, :]
+    # (the table's grid spacing jumps near z = 0: the compact scheme is good to ~1e-4 there)
+    assert np.abs(r["start"]["bx"][:, 0, :] - bx_exact).max() < 5e-4 * np.abs(bx_exact).max()
+    # the FFT calculus on a band-limited periodic field
+    L = 400.0
+    f = np.sin(2 * np.pi * 3 * (x[:, None] + 200) / L) + 0.5 + np.cos(2 * np.pi * 5 * x[:, None] / L) * z[None, :]
+    df = (2 * np.pi * 3 / L) * np.cos(2 * np.pi * 3 * (x[:, None] + 200) / L) \
+        - (2 * np.pi * 5 / L) * np.sin(2 * np.pi * 5 * x[:, None] / L) * z[None, :]
+    assert np.abs(B.fft_differentiate(f, L) - df).max() < 1e-12
+    assert np.abs(B.fft_integrate(df, L) - (f - f.mean(axis=0))).max() < 1e-12
