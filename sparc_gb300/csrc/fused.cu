@@ -41,6 +41,18 @@ constexpr int CH = FUSED_CH;   // z-levels per thread
 constexpr int GZ = 5;          // ghost rows of the tile on each side (reach of the z filter)
 constexpr int GX = 2;          // ghost entries of an exchange line on each side (compact stencil)
 
+// Paired FP32 arithmetic (FFMA2 / FADD2 / FMUL2, sm_100 and later): one
+// instruction for both components of a complex value.  Used where the
+// multiplier is the same for both components and hoisted out of the loops
+// (beta, dt, the compact-scheme and filter coefficients), so the pairs cost
+// no extra moves; each keeps the association of the scalar expression it
+// replaces.
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(make_float2(-1.f, -1.f), b, a); }
+
 struct Aff {             // u -> B + M u   (B complex, M real)
     float2 B;
     float M;
@@ -125,6 +137,7 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     const float* gg = tb + 3 * NZP;
     const float* GG = tb + 4 * NZP;
     float2 u[CH];
+    const float2 C1p = bc2(c.C1), C2p = bc2(c.C2);
     // interior right-hand side on every level (dbyd2.f90:88-92); the
     // thread's own levels come from registers (own[q] == xp[j0+q]), the two
     // levels on each side from the neighbours' entries of the line
@@ -135,7 +148,7 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
         const float2 bm1 = q >= 1 ? own[q - 1] : xp[j - 1];
         const float2 bp1 = q + 1 < CH ? own[q + 1] : xp[j + 1];
         const float2 bp2 = q + 2 < CH ? own[q + 2] : xp[j + 2];
-        u[q] = c.C1 * (bp1 - bm1) + c.C2 * (bp2 - bm2);
+        u[q] = pfma(C2p, psub(bp2, bm2), pmul(C1p, psub(bp1, bm1)));
     }
     if (lo) {   // rows 0 and 1 (dbyd2.f90:104-173)
         const float2 b0 = xp[0], b1 = xp[1], b2 = xp[2], b3 = xp[3], b4 = xp[4];
@@ -355,12 +368,13 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     // rather than a (stage 1), fixed at compile time
     auto stage = [&](auto hs_c, const float beta) {
         constexpr bool hs = decltype(hs_c)::value;
+        const float2 BT = bc2(beta);
         // ---- temp xi_z into the first exchange line ----
         float2 own[CH];
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             float2 v = TA(2, j0 + q);
-            if (hs) v = v + beta * sc[2][q];
+            if (hs) v = pfma(BT, sc[2][q], v);
             own[q] = v;
             xa[j0 + q] = v;
         }
@@ -397,12 +411,12 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
             float2 xx = TA(0, j), xz = TA(2, j), vx = TA(3, j);
-            if (hs) { xx = xx + beta * sc[0][q]; xz = xz + beta * sc[2][q]; vx = vx + beta * sc[3][q]; }
+            if (hs) { xx = pfma(BT, sc[0][q], xx); xz = pfma(BT, sc[2][q], xz); vx = pfma(BT, sc[3][q], vx); }
             float2 div = imul(kx, xx) + d[q];
             float2 xy, vy;
             if (D3) {
                 xy = TA(1, j); vy = TA(4, j);
-                if (hs) { xy = xy + beta * sc[1][q]; vy = vy + beta * sc[4][q]; }
+                if (hs) { xy = pfma(BT, sc[1][q], xy); vy = pfma(BT, sc[4][q], vy); }
                 div = div + imul(ky, xy);
             }
             const float2 p = -ZC2R[j] * div - ZGP[j] * xz;
@@ -432,7 +446,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
             float2 vz = TA(5, j);
-            if (hs) vz = vz + beta * sc[5][q];
+            if (hs) vz = pfma(BT, sc[5][q], vz);
             sc[5][q] = qt[q] - ZRIST[j] * d[q] - gd * vz;
             sc[2][q] = vz;
         }
@@ -470,12 +484,13 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
 
     // ---- update a += dt*scr, pml += dt*scrpml (step.f90:114-116) ----
     const float dt = A.dt;
+    const float2 DT = bc2(dt);
     #pragma unroll
     for (int f = 0; f < 6; ++f)
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             float2* a = tp + f * P * LZ + j0 + q;
-            *a = *a + dt * sc[f][q];
+            *a = pfma(DT, sc[f][q], *a);
         }
     if (pml_t) {
         #pragma unroll
@@ -504,8 +519,12 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             #pragma unroll
             for (int q = 0; q < CH; ++q) {
                 const int j = j0 + q;
-                out[q] = c0 * V[j] + h1 * (V[j - 1] + V[j + 1]) + h2 * (V[j - 2] + V[j + 2]) +
-                         h3 * (V[j - 3] + V[j + 3]) + h4 * (V[j - 4] + V[j + 4]) + h5 * (V[j - 5] + V[j + 5]);
+                float2 acc = pmul(bc2(c0), V[j]);
+                acc = pfma(bc2(h1), padd(V[j - 1], V[j + 1]), acc);
+                acc = pfma(bc2(h2), padd(V[j - 2], V[j + 2]), acc);
+                acc = pfma(bc2(h3), padd(V[j - 3], V[j + 3]), acc);
+                acc = pfma(bc2(h4), padd(V[j - 4], V[j + 4]), acc);
+                out[q] = pfma(bc2(h5), padd(V[j - 5], V[j + 5]), acc);
             }
             if (flo || fhi) {   // FILTER_VARS_3D / _2D boundary rows
                 #pragma unroll
