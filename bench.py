@@ -332,6 +332,45 @@ def cpu_baseline(p, tab, steps=1):
                       f"(one source), {dt:.1f} s"}
 
 
+def _production_worker(bar, q, steps):
+    """One single-threaded FP64 oracle solve of the 128x128x150 grid (run in a
+    spawned process; the reference's production model is one solve per core)."""
+    from oracle import oracle
+    from sparc_gb300 import sources
+    p, tab = workload(True)
+    oracle.set_threads(1)
+    o = oracle.Oracle(p.replace(precision="f64", nsrc=1), tab)
+    o.set_source(1, sources.gaussian_plane(p)[None].copy(), sources.ricker_series(p, 100))
+    o.step(1)                       # warm-up
+    bar.wait(timeout=600)
+    t0 = time.monotonic()
+    o.step(steps)
+    t1 = time.monotonic()
+    o.close()
+    q.put((t0, t1, p.points))
+
+
+def cpu_production(n: int | None = None, steps: int = 1):
+    """The reference's production model on the host: n concurrent
+    single-threaded solves (one source each, one per core), started together;
+    aggregate point-steps over the span from the first start to the last end."""
+    import multiprocessing as mp
+    n = n or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    bar, q = ctx.Barrier(n), ctx.Queue()
+    procs = [ctx.Process(target=_production_worker, args=(bar, q, steps)) for _ in range(n)]
+    for pr in procs:
+        pr.start()
+    res = [q.get(timeout=900) for _ in range(n)]
+    for pr in procs:
+        pr.join(timeout=60)
+    span = max(r[1] for r in res) - min(r[0] for r in res)
+    pts = sum(r[2] for r in res) * steps
+    return {"value": pts / span / 1e6, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": f"{n} concurrent single-threaded FP64 oracle solves of 128x128x150 (one source each), "
+                      f"{steps} timed step(s) each after one warm-up, {span:.1f} s span"}
+
+
 def arm_config(p0, cad, S, nplanes):
     """The workload both arms name (the reference arm times a bounded sample of it)."""
     return {"workload": f"quiet-Sun {p0.nx}x{p0.ny}x{p0.nz} forward+adjoint time step with "
@@ -375,6 +414,11 @@ def run_reference(args):
                                    "the sample"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    o.close()
+    try:
+        line["cpu_baseline"]["production"] = cpu_production()
+    except Exception as e:
+        line["cpu_baseline"]["production"] = {"value": None, "sample": f"failed: {e}"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -564,6 +608,10 @@ def main():
         except Exception as e:  # the oracle is only the reported baseline
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                     "sample": f"failed: {e}"}
+        try:
+            line["cpu_baseline"]["production"] = cpu_production()
+        except Exception as e:
+            line["cpu_baseline"]["production"] = {"value": None, "sample": f"failed: {e}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
