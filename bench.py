@@ -250,6 +250,38 @@ def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, 
     return st
 
 
+def config1_full():
+    """The 1-h configuration at full length: plain FP64 forward of the
+    128x128x150 quiet-Sun box, one source, time = 0..maxtime (1801 steps of
+    2 s), the surface vz of every output (30 s) recorded on the device and
+    read back at the end; device time with CUDA events."""
+    import torch
+    from sparc_gb300 import sources
+    from sparc_gb300.background import polytrope_table
+    from sparc_gb300.params import config_quiet_128
+    from sparc_gb300.solver import Solver
+    p = config_quiet_128().replace(precision="f64", nsrc=1)
+    s = Solver(p, polytrope_table(p.nz))
+    s.set_source_series(sources.gaussian_plane(p), sources.ricker_series(p, p.maxtime + 8))
+    nrec = p.maxtime // p.steps + 1
+    s.record_surface(nrec)
+    st = torch.cuda.ExternalStream(s.stream_ptr)
+    s.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(st)
+    s.step(p.maxtime + 1)
+    e1.record(st)
+    rec = s.records()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    s.close()
+    n = p.maxtime + 1
+    return {"grid": [p.nx, p.ny, p.nz], "steps": n, "dtype": "f64", "records": int(rec.shape[0]),
+            "device_s": ms * 1e-3, "wall_s": wall, "value": p.points * n / (ms * 1e-3) / 1e6, "unit": UNIT,
+            "finite": bool(np.isfinite(rec).all())}
+
+
 def small_step_latency(n=60):
     """Per-step device time of a 128x128x150 single-source FP32 forward solve
     (the 1-h configuration's grid), steps replayed from captured graphs vs
@@ -581,6 +613,12 @@ def main():
     if ws == 1:
         log("small-grid step latency")
         line["small_grid_step"] = small_step_latency()
+        if not args.skip_fp64:
+            log("1-h configuration, full length")
+            try:
+                line["config1_full"] = config1_full()
+            except Exception as e:   # reported, not fatal
+                line["config1_full"] = {"error": str(e)}
     if ws == 1 and not args.skip_mhd:
         log("MHD flux tube")
         try:

@@ -190,6 +190,17 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if ((rc = dalloc(c, &c->rbuf, (size_t)S * c->fs * cs))) return bail(rc);
     if ((rc = dalloc(c, &c->zt, (size_t)ZT_COUNT * c->nz * es))) return bail(rc);
     if ((rc = dalloc(c, &c->pt, (size_t)PT_COUNT * c->M * es))) return bail(rc);
+    {
+        // per-stage kernels run one thread per (mode, source): the default CTA
+        // is the largest of 128, 64, 32 threads whose grid still gives every
+        // SM two CTAs (small grids, e.g. 128x128 with 8320 modes, need 32)
+        int dev = 0, nsm = 152;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaGetLastError();
+        const long long cols = (long long)c->M * S;
+        c->stage_block = 128;
+        while (c->stage_block > 32 && (cols + c->stage_block - 1) / c->stage_block < 2LL * nsm) c->stage_block /= 2;
+    }
     if (c->f32) {
         // the fused step covers the quiet displacement forms (options 4, 17)
         c->use_fused = fused_supported(c->nz) && (p->option == 4 || p->option == 17) &&
@@ -773,6 +784,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     U.fs = c->fs; U.ps = c->ps; U.M = c->M; U.nz = c->nz; U.nzpml = c->nzpml; U.option = P.option;
     U.dt = (T)c->deltat;
     U.clk = A.clk;
+    U.block = c->stage_block;
 }
 
 // Enqueue nsteps time steps on the context's stream: per step the fused FP32
@@ -844,6 +856,19 @@ template <typename T>
 static int do_steps(sparc_ctx* c, int nsteps) {
     if (nsteps == 0) return SPARC_OK;
     if (c->mhd) return mhd_steps(c, nsteps);
+    // A long call replays one graph of kGraphChunk steps (every kernel reads
+    // the clock on the device, so a captured chunk is valid at any time) and
+    // a graph of the remainder: capture and instantiation stay bounded.  Each
+    // chunk's last step also writes scr; the call's last step is still the
+    // last to write it.
+    constexpr int kGraphChunk = 64;
+    if (c->use_graphs && nsteps > kGraphChunk) {
+        for (int i = 0; i < nsteps / kGraphChunk; ++i) {
+            const int rc = do_steps<T>(c, kGraphChunk);
+            if (rc) return rc;
+        }
+        return do_steps<T>(c, nsteps % kGraphChunk);
+    }
     if (c->use_graphs) {
         sparc_ctx::GraphEntry* ge = nullptr;
         for (auto& g : c->graphs)
@@ -925,13 +950,15 @@ int sparc_gpu_autotune(sparc_ctx* c, int steps, int* choice, float* ms_per_step)
     if (c->mhd) return fail(c, SPARC_EINVAL, "option 10 has no launch variants to tune");
     if (steps < 1) return fail(c, SPARC_EINVAL, "steps < 1");
     const bool fused = c->use_fused && c->f32;
-    const int cand[2] = {fused ? 4 : 128, fused ? 2 : 64};
+    const int cand[3] = {fused ? 4 : 128, fused ? 2 : 64, 32};
+    const int ncand = fused ? 2 : 3;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     float best = 0.f;
     int pick = cand[0];
-    for (int v : cand) {
+    for (int ic = 0; ic < ncand; ++ic) {
+        const int v = cand[ic];
         if (fused) c->fused_pencils = v; else c->stage_block = v;
         c->epoch++;
         int rc = c->f32 ? do_steps<float>(c, steps) : do_steps<double>(c, steps);   // capture and warm

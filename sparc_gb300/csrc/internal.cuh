@@ -223,6 +223,18 @@ __device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, 
     return w;
 }
 
+// butterfly sum and difference; in FP32 one paired instruction each (FADD2,
+// and FFMA2 with -1, which rounds exactly as the subtraction)
+__device__ __forceinline__ double2 bsum(double2 a, double2 c) { return a + c; }
+__device__ __forceinline__ double2 bdif(double2 a, double2 c) { return make_double2(a.x - c.x, a.y - c.y); }
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float2 bsum(float2 a, float2 c) { return __fadd2_rn(a, c); }
+__device__ __forceinline__ float2 bdif(float2 a, float2 c) { return __ffma2_rn(make_float2(-1.f, -1.f), c, a); }
+#else
+__device__ __forceinline__ float2 bsum(float2 a, float2 c) { return a + c; }
+__device__ __forceinline__ float2 bdif(float2 a, float2 c) { return make_float2(a.x - c.x, a.y - c.y); }
+#endif
+
 // in-register DFT of length R (decimation in frequency): on return v[brev(k)]
 // holds X[k]; w[j] = W_R^j for j < R/2
 template <typename CT, int R>
@@ -235,8 +247,8 @@ __device__ __forceinline__ void reg_dft(CT (&v)[R], const CT (&w)[R / 2]) {
             #pragma unroll
             for (int k = 0; k < half; ++k) {
                 const CT a = v[b + k], c = v[b + k + half];
-                v[b + k] = a + c;
-                const CT d = a - c;
+                v[b + k] = bsum(a, c);
+                const CT d = bdif(a, c);
                 v[b + k + half] = (k == 0) ? d : cmul(d, w[k * step]);
             }
         }
@@ -311,6 +323,7 @@ template <typename T> struct UpdateArgs {
     int M, nz, nzpml, option;
     T dt;
     SlotClock clk;      // the horizontal filter follows each slot's clock
+    int block;          // threads per CTA (32, 64 or 128), as the stage kernels
 };
 
 // fused FP32 step (fused.cu)

@@ -412,14 +412,15 @@ void launch_set_time(int* time, int value, cudaStream_t s) { set_time_kernel<<<1
 void launch_tick(int* time, cudaStream_t s) { tick_kernel<<<1, 1, 0, s>>>(time); }
 
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s) {
-    const int b = A.block == 64 ? 64 : 128;
+    const int b = A.block == 32 ? 32 : A.block == 64 ? 64 : 128;
     dim3 grid((A.M + b - 1) / b, nsrc);
     if (A.option == 2) stage_velocity_kernel<T><<<grid, b, 0, s>>>(A);
     else stage_kernel<T><<<grid, b, 0, s>>>(A);
 }
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s) {
-    dim3 grid((A.M + 127) / 128, nsrc);
-    update_kernel<T><<<grid, 128, 0, s>>>(A);
+    const int b = A.block == 32 ? 32 : A.block == 64 ? 64 : 128;
+    dim3 grid((A.M + b - 1) / b, nsrc);
+    update_kernel<T><<<grid, b, 0, s>>>(A);
 }
 template <typename T>
 void launch_zderiv(const T* zt, const Compact<T>& cc, const typename CplxOf<T>::type* in,

@@ -56,9 +56,11 @@ def test_autotune_keeps_results(gpu_lib, prec):
     s1, s2 = Solver(p, tab), Solver(p, tab)
     for s in (s1, s2):
         s.set_state(a0, pml0)
-    pick = s1.autotune(2)                      # 8 ordinary steps
-    assert list(pick.values())[0] in (2, 4, 64, 128) and pick["ms_per_step"] > 0
+    pick = s1.autotune(2)                      # 2 warm + 2 timed ordinary steps per candidate
+    assert list(pick.values())[0] in (2, 4, 32, 64, 128) and pick["ms_per_step"] > 0
+    n_auto = s1.time
+    assert n_auto == (8 if prec == "f32" else 12)
     s1.step(3)
-    s2.step(11)
-    assert s1.time == s2.time == 11
+    s2.step(n_auto + 3)
+    assert s1.time == s2.time == n_auto + 3
     assert np.array_equal(s1.state()[0], s2.state()[0])
