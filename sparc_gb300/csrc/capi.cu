@@ -205,6 +205,12 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
         // the fused step covers the quiet displacement forms (options 4, 17)
         c->use_fused = fused_supported(c->nz) && (p->option == 4 || p->option == 17) &&
                        getenv("SPARC_FP32_PER_STAGE") == nullptr;
+        // modes per CTA of the fused step before any autotuning (a switch the
+        // tests use to compare the variants)
+        if (const char* e = getenv("SPARC_FUSED_MODES")) {
+            const int v = atoi(e);
+            if (v == 2 || v == 4 || (v == 8 && fused_fits(8, c->nz, c->nzpml))) c->fused_pencils = v;
+        }
         if (c->use_fused &&
             (rc = dalloc(c, (void**)&c->ftab, (size_t)FZ_COUNT * fused_nzp(c->nz) * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
@@ -950,8 +956,8 @@ int sparc_gpu_autotune(sparc_ctx* c, int steps, int* choice, float* ms_per_step)
     if (c->mhd) return fail(c, SPARC_EINVAL, "option 10 has no launch variants to tune");
     if (steps < 1) return fail(c, SPARC_EINVAL, "steps < 1");
     const bool fused = c->use_fused && c->f32;
-    const int cand[3] = {fused ? 4 : 128, fused ? 2 : 64, 32};
-    const int ncand = fused ? 2 : 3;
+    const int cand[3] = {fused ? 4 : 128, fused ? 2 : 64, fused ? 8 : 32};
+    const int ncand = (fused && !fused_fits(8, c->nz, c->nzpml)) ? 2 : 3;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));

@@ -237,8 +237,10 @@ __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
 
 }  // namespace
 
-// P modes per CTA (2 or 4): every pencil's arithmetic is the same for either,
-// so the results are too; the launch bounds keep 128 registers per thread.
+// P modes per CTA (2, 4 or 8): every pencil's arithmetic is the same for
+// each, so the results are too; the launch bounds keep 128 registers per
+// thread (P = 8 at W = 2: one 512-thread CTA per SM, the z tables loaded once
+// per eight modes).
 template <bool D3, int W, int P>
 __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -600,6 +602,11 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
 int fused_w(int nz) { return (nz + 32 * CH - 1) / (32 * CH); }
 int fused_nzp(int nz) { return 32 * CH * fused_w(nz); }
 
+// whether P modes per CTA fit the 227 KB of shared memory a CTA may use
+bool fused_fits(int P, int nz, int nzpml) {
+    return fused_layout(P, fused_w(nz), nzpml).total <= 227 * 1024;
+}
+
 size_t fused_smem_bytes(int nz, int nzpml, int W) {
     (void)nz;
     return (size_t)fused_layout(4, W, nzpml).total;
@@ -620,11 +627,11 @@ static void fused_attr(int nzpml) {
 void fused_prepare(int nz, int nzpml) {
     const int W = fused_w(nz);
     if (W == 1) {
-        fused_attr<true, 1, 2>(nzpml); fused_attr<true, 1, 4>(nzpml);
-        fused_attr<false, 1, 2>(nzpml); fused_attr<false, 1, 4>(nzpml);
+        fused_attr<true, 1, 2>(nzpml); fused_attr<true, 1, 4>(nzpml); fused_attr<true, 1, 8>(nzpml);
+        fused_attr<false, 1, 2>(nzpml); fused_attr<false, 1, 4>(nzpml); fused_attr<false, 1, 8>(nzpml);
     } else {
-        fused_attr<true, 2, 2>(nzpml); fused_attr<true, 2, 4>(nzpml);
-        fused_attr<false, 2, 2>(nzpml); fused_attr<false, 2, 4>(nzpml);
+        fused_attr<true, 2, 2>(nzpml); fused_attr<true, 2, 4>(nzpml); fused_attr<true, 2, 8>(nzpml);
+        fused_attr<false, 2, 2>(nzpml); fused_attr<false, 2, 4>(nzpml); fused_attr<false, 2, 8>(nzpml);
     }
 }
 
@@ -638,6 +645,7 @@ static void launch_fused_t(const FusedArgs& A, int nsrc, cudaStream_t s) {
 template <bool D3, int W>
 static void launch_fused_p(const FusedArgs& A, int nsrc, cudaStream_t s) {
     if (A.pencils == 2) launch_fused_t<D3, W, 2>(A, nsrc, s);
+    else if (A.pencils == 8) launch_fused_t<D3, W, 8>(A, nsrc, s);
     else launch_fused_t<D3, W, 4>(A, nsrc, s);
 }
 

@@ -352,6 +352,7 @@ struct FusedArgs {
 constexpr int FUSED_CH = 5;
 void fused_prepare(int nz, int nzpml);
 size_t fused_smem_bytes(int nz, int nzpml, int W);
+bool fused_fits(int P, int nz, int nzpml);
 int fused_supported(int nz);
 int fused_w(int nz);
 int fused_nzp(int nz);

@@ -57,10 +57,32 @@ def test_autotune_keeps_results(gpu_lib, prec):
     for s in (s1, s2):
         s.set_state(a0, pml0)
     pick = s1.autotune(2)                      # 2 warm + 2 timed ordinary steps per candidate
-    assert list(pick.values())[0] in (2, 4, 32, 64, 128) and pick["ms_per_step"] > 0
+    assert list(pick.values())[0] in (2, 4, 8, 32, 64, 128) and pick["ms_per_step"] > 0
     n_auto = s1.time
-    assert n_auto == (8 if prec == "f32" else 12)
+    assert n_auto == 12                        # three candidates
     s1.step(3)
     s2.step(n_auto + 3)
     assert s1.time == s2.time == n_auto + 3
     assert np.array_equal(s1.state()[0], s2.state()[0])
+
+
+@pytest.mark.parametrize("nz", [48, 200])
+def test_fused_cta_shapes_agree(gpu_lib, nz, monkeypatch):
+    """The fused FP32 step with 2, 4 and 8 modes per CTA (one and two warps
+    per pencil) gives bitwise the same state."""
+    from sparc_gb300 import sources
+    from sparc_gb300.solver import Solver
+    p = small_params(precision="f32", nz=nz, nsrc=2)
+    tab = table_for(p)
+    out = {}
+    for P in ("2", "4", "8"):
+        monkeypatch.setenv("SPARC_FUSED_MODES", P)
+        with Solver(p, tab) as s:
+            s.set_source_series(sources.gaussian_plane(p, 2.0), sources.ricker_series(p, 80, delay=20.0), slot=0)
+            s.set_source_series(sources.gaussian_plane(p, 2.0, 5.0), sources.ricker_series(p, 80, delay=30.0), slot=1)
+            s.step(37)
+            out[P] = [s.state(k) for k in range(2)]
+    for P in ("2", "8"):
+        for k in range(2):
+            assert np.array_equal(out[P][k][0], out["4"][k][0]) and np.array_equal(out[P][k][1], out["4"][k][1])
+    assert np.abs(out["4"][0][0]).max() > 0
