@@ -205,8 +205,17 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
         // the fused step covers the quiet displacement forms (options 4, 17)
         c->use_fused = fused_supported(c->nz) && (p->option == 4 || p->option == 17) &&
                        getenv("SPARC_FP32_PER_STAGE") == nullptr;
-        // modes per CTA of the fused step before any autotuning (a switch the
-        // tests use to compare the variants)
+        // modes per CTA of the fused step before any autotuning: 8 (one
+        // 512-thread CTA per SM) when it fits and the grid still gives every SM
+        // two CTAs, else 4; SPARC_FUSED_MODES forces a shape (a switch the tests
+        // use to compare the variants)
+        {
+            int dev = 0, nsm = 152;
+            if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaGetLastError();
+            const long long ctas8 = (long long)((c->M + 7) / 8) * S;
+            c->fused_pencils = (fused_fits(8, c->nz, c->nzpml) && ctas8 >= 2LL * nsm) ? 8 : 4;
+        }
         if (const char* e = getenv("SPARC_FUSED_MODES")) {
             const int v = atoi(e);
             if (v == 2 || v == 4 || (v == 8 && fused_fits(8, c->nz, c->nzpml))) c->fused_pencils = v;
