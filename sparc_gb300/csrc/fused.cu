@@ -53,6 +53,15 @@ __device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(make_float2(-1.f, -1.f), b, a); }
 
+// Entry idx of the z tables (scalars in shared memory) as a pair (t, t), the
+// multiplier of a paired product with a complex value.  Tables stored as
+// pairs would save the broadcast but cost 24 KB of shared memory (and of L1)
+// per CTA; measured slower.
+__device__ __forceinline__ float2 zt2(const float* zs, int idx) {
+    const float t = zs[idx];
+    return make_float2(t, t);
+}
+
 struct Aff {             // u -> B + M u   (B complex, M real)
     float2 B;
     float M;
@@ -124,18 +133,16 @@ __device__ __forceinline__ Aff pencil_scan(Aff mine, int t, Aff* wb, int pi) {
 // 0..NZP-1, ghosts at -2, -1, NZP, NZP+1; own[q] = xp[j0+q]) for the owned
 // levels j0..j0+CH-1,
 // boundary code BC (dbyd2.f90:94-173 for the right-hand side; top is the
-// caller-set value of bc 3).  tb: the five scan rows (ibd, m, H, g, G) of BC.
+// caller-set value of bc 3).  zs, r0: the z tables and the first of the five
+// scan rows (ibd, m, H, g, G) of BC.
 template <int BC, int W>
 __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const float2 (&own)[CH],
-                                       const float* __restrict__ tb, int nz, float2 top, int j0, bool lo, bool hi,
-                                       int t, Aff* wbF, Aff* wbB, int pi, const Compact<float> c,
+                                       const float* __restrict__ zs, int r0, int nz, float2 top, int j0, bool lo,
+                                       bool hi, int t, Aff* wbF, Aff* wbB, int pi, const Compact<float> c,
                                        float2 (&out)[CH]) {
     constexpr int NZP = 160 * W;
-    const float* ibd = tb;
-    const float* mm = tb + NZP;
-    const float* HH = tb + 2 * NZP;
-    const float* gg = tb + 3 * NZP;
-    const float* GG = tb + 4 * NZP;
+    const int ibd = r0 * NZP, mm = (r0 + 1) * NZP, HH = (r0 + 2) * NZP, gg = (r0 + 3) * NZP, GG = (r0 + 4) * NZP;
+    auto Z = [&](int row, int j) { return zt2(zs, row + j); };
     float2 u[CH];
     const float2 C1p = bc2(c.C1), C2p = bc2(c.C2);
     // interior right-hand side on every level (dbyd2.f90:88-92); the
@@ -184,28 +191,28 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     #pragma unroll
     for (int q = 0; q < CH; ++q) {
         const int j = j0 + q;
-        run = ibd[j] * u[q] + mm[j] * run;
+        run = pfma(Z(mm, j), run, pmul(Z(ibd, j), u[q]));
         u[q] = run;
     }
     Aff mine;
     mine.B = run;
-    mine.M = HH[j0 + CH - 1];
+    mine.M = Z(HH, j0 + CH - 1).x;
     const float2 uin = pencil_scan<W, true>(mine, t, wbF, pi).B;    // ud(j0-1)
     #pragma unroll
-    for (int q = 0; q < CH; ++q) u[q] = u[q] + HH[j0 + q] * uin;
+    for (int q = 0; q < CH; ++q) u[q] = pfma(Z(HH, j0 + q), uin, u[q]);
     // back substitution x(j) = u(j) + g(j) x(j+1)
     float2 xr = make_float2(0.f, 0.f);
     #pragma unroll
     for (int q = CH - 1; q >= 0; --q) {
-        xr = u[q] + gg[j0 + q] * xr;
+        xr = pfma(Z(gg, j0 + q), xr, u[q]);
         out[q] = xr;
     }
     Aff bm;
     bm.B = xr;
-    bm.M = GG[j0];
+    bm.M = Z(GG, j0).x;
     const float2 xin = pencil_scan<W, false>(bm, t, wbB, pi).B;     // x(j0+CH)
     #pragma unroll
-    for (int q = 0; q < CH; ++q) out[q] = out[q] + GG[j0 + q] * xin;
+    for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
 }
 
 __device__ __forceinline__ int pmlidx(int j, int nz, int nb, int nt) {
@@ -327,6 +334,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
     const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;
     const float gd = (mvalid && A.damp) ? A.pt[PT_DAMP * M + m] : 0.f;
+    const float2 NGD = bc2(-gd);
     // threads that own rows with special rules
     const bool lo = (j0 == 0);                                       // rows 0, 1
     const bool hi = (j0 <= nz - 1) && (j0 + CH > nz - 2);            // rows nz-2, nz-1
@@ -355,15 +363,8 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
 
     float2* tp = tile + pi * LZ + GZ;                    // field f, level j: tp[f*P*LZ + j]
     auto TA = [&](int f, int j) -> float2 { return tp[f * P * LZ + j]; };
-    const float* ZST = zs + FZ_ST * NZP;
-    const float* ZC2R = zs + FZ_C2R * NZP;
-    const float* ZGP = zs + FZ_GP * NZP;
-    const float* ZRI = zs + FZ_RI * NZP;
-    const float* ZE1 = zs + FZ_E1 * NZP;
-    const float* ZE2 = zs + FZ_E2 * NZP;
-    const float* ZRIST = zs + FZ_RIST * NZP;
-    const float* ZAZ = zs + FZ_AZ * NZP;
-    const float* ZBZ = zs + FZ_BZ * NZP;
+    // z table entry of row r at level j, as a pair
+    auto Z2 = [&](int r, int j) { return zt2(zs, r * NZP + j); };
     Aff* wb = wbuf + pi * W;                              // scan slot k at wb + k*P*W
 
     // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
@@ -392,9 +393,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         float2 d[CH];
-        zsolve<BCX, W>(xa, own, zs + FZ_SX * NZP, nz, top, j0, lo, hi, t, wb, wb + P * W, pi, A.cc, d);
+        zsolve<BCX, W>(xa, own, zs, FZ_SX, nz, top, j0, lo, hi, t, wb, wb + P * W, pi, A.cc, d);
         #pragma unroll
-        for (int q = 0; q < CH; ++q) d[q] = d[q] * ZST[j0 + q];
+        for (int q = 0; q < CH; ++q) d[q] = pmul(Z2(FZ_ST, j0 + q), d[q]);
         if (pml_t) {   // psi_vz (displacement.f90 PML rows)
             #pragma unroll
             for (int q = 0; q < CH; ++q) {
@@ -402,7 +403,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
                 if (j < nz && ip >= 0) {
                     float2 psi = ptile[ip * P + pi];
                     if (hs) psi = psi + beta * spt[ip * P + pi];
-                    spt[ip * P + pi] = ZAZ[j] * d[q] + ZBZ[j] * psi;
+                    spt[ip * P + pi] = Z2(FZ_AZ, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
                     d[q] = d[q] + psi;
                 }
             }
@@ -421,15 +422,15 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
                 if (hs) { xy = pfma(BT, sc[1][q], xy); vy = pfma(BT, sc[4][q], vy); }
                 div = div + imul(ky, xy);
             }
-            const float2 p = -ZC2R[j] * div - ZGP[j] * xz;
-            qt[q] = ZE1[j] * div + ZE2[j] * xz;            // -g rho'/rho0
+            const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
+            qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
             xb[j] = p;
             own[q] = p;
-            const float ri = ZRI[j];
-            sc[3][q] = -ri * imul(kx, p) - gd * vx;
+            const float ri = Z2(FZ_RI, j).x;
+            sc[3][q] = pfma(NGD, vx, -ri * imul(kx, p));
             sc[0][q] = vx;
             if (D3) {
-                sc[4][q] = -ri * imul(ky, p) - gd * vy;
+                sc[4][q] = pfma(NGD, vy, -ri * imul(ky, p));
                 sc[1][q] = vy;
             }
         }
@@ -442,14 +443,14 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         // ---- dp'/dz, RHS v_z and xi_z ----
-        zsolve<BCP, W>(xb, own, zs + FZ_SP * NZP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, wb + 2 * P * W,
+        zsolve<BCP, W>(xb, own, zs, FZ_SP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, wb + 2 * P * W,
                        wb + 3 * P * W, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
             float2 vz = TA(5, j);
             if (hs) vz = pfma(BT, sc[5][q], vz);
-            sc[5][q] = qt[q] - ZRIST[j] * d[q] - gd * vz;
+            sc[5][q] = pfma(NGD, vz, psub(qt[q], pmul(Z2(FZ_RIST, j), d[q])));
             sc[2][q] = vz;
         }
         if (pml_t) {   // psi_p
@@ -457,11 +458,11 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             for (int q = 0; q < CH; ++q) {
                 const int j = j0 + q, ip = pmlidx(j, nz, nb, nt);
                 if (j < nz && ip >= 0) {
-                    const float2 dd = d[q] * ZST[j];
+                    const float2 dd = Z2(FZ_ST, j).x * d[q];
                     float2 psi = ptile[(nzpml + ip) * P + pi];
                     if (hs) psi = psi + beta * spt[(nzpml + ip) * P + pi];
-                    spt[(nzpml + ip) * P + pi] = ZAZ[j] * dd + ZBZ[j] * psi;
-                    sc[5][q] = sc[5][q] - ZRI[j] * psi;
+                    spt[(nzpml + ip) * P + pi] = Z2(FZ_AZ, j).x * dd + Z2(FZ_BZ, j).x * psi;
+                    sc[5][q] = sc[5][q] - Z2(FZ_RI, j).x * psi;
                 }
             }
         }
