@@ -41,18 +41,6 @@ constexpr int CH = FUSED_CH;   // z-levels per thread
 constexpr int GZ = 5;          // ghost rows of the tile on each side (reach of the z filter)
 constexpr int GX = 2;          // ghost entries of an exchange line on each side (compact stencil)
 
-// Paired FP32 arithmetic (FFMA2 / FADD2 / FMUL2, sm_100 and later): one
-// instruction for both components of a complex value.  Used where the
-// multiplier is the same for both components and hoisted out of the loops
-// (beta, dt, the compact-scheme and filter coefficients), so the pairs cost
-// no extra moves; each keeps the association of the scalar expression it
-// replaces.
-__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(make_float2(-1.f, -1.f), b, a); }
-
 // Entry idx of the z tables (scalars in shared memory) as a pair (t, t), the
 // multiplier of a paired product with a complex value.  Tables stored as
 // pairs would save the broadcast but cost 24 KB of shared memory (and of L1)

@@ -223,6 +223,17 @@ __device__ __forceinline__ CT tw_n(const double* __restrict__ tw, int q, int n, 
     return w;
 }
 
+// Paired FP32 arithmetic (FFMA2 / FADD2 / FMUL2, sm_100 and later): one
+// instruction for both components of a float2 (the two parts of a complex
+// value, or two neighbouring pencils).  bc2 broadcasts a multiplier shared by
+// both components; psub is an FFMA2 with -1, which rounds exactly as the
+// subtraction.
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(make_float2(-1.f, -1.f), b, a); }
+
 // butterfly sum and difference; in FP32 one paired instruction each (FADD2,
 // and FFMA2 with -1, which rounds exactly as the subtraction)
 __device__ __forceinline__ double2 bsum(double2 a, double2 c) { return a + c; }

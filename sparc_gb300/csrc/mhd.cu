@@ -300,6 +300,10 @@ __device__ __forceinline__ T compact_rhs_row(int j, int nz, int bc, Ld B, T bot,
     return (c.alpha2 * Rn1 - c.beta1 * Rn2) * c.cnst;
 }
 
+// bytes of the five coefficient tables of the paired chunk kernel, rounded up
+// so the float2 buffers after them are 8-byte aligned
+__host__ __device__ inline size_t zchunk2_tables_bytes(int nz) { return (((size_t)5 * nz + 1) * 4 + 15) & ~(size_t)15; }
+
 // d/dz of dense fields (DBYD2 * stretch) by chunks: 32 pencils per CTA (one
 // per lane), NCH warps, warp w owning planes [w*cs, w*cs + cs).  Forward
 // elimination y_j = (R_j - low_j y_{j-1}) ibd_j is affine in y_{j-1}: each
@@ -431,6 +435,133 @@ __global__ void __launch_bounds__(32 * NCH) zderiv_chunk_kernel(const T* __restr
         for (int j = e, i = e - s + 2; j >= s; --j, --i) {
             pj = pj * (-tga[j + 1]);
             o[(long long)j * npix] = (Y[i * 32] + pj * xin) * tst[j];
+        }
+    }
+}
+
+// zderiv_chunk_kernel<float> with two neighbouring pencils per lane (64 per
+// CTA, npix even): the planes move as float2, and the compact right-hand
+// side, the two recurrences and the scaling are paired FP32 instructions on
+// both pencils.  The coefficient tables and the products of the multipliers
+// are shared by the pair.  Same elimination, chunking and carry composition
+// as the scalar kernel.
+template <int NCH>
+__global__ void __launch_bounds__(32 * NCH) zderiv_chunk2_kernel(const float* __restrict__ zt, Compact<float> cc,
+                                                                 const float* __restrict__ in,
+                                                                 float* __restrict__ out, long long npix, int nz,
+                                                                 int bc, long long fstride,
+                                                                 const float* __restrict__ topsrc, float topscale) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int cs = (nz + NCH - 1) / NCH, rows = cs + 4;
+    float* tmf = (float*)smraw;              // [nz] -low_j ibd_j
+    float* tib = tmf + nz;                   // [nz] ibd_j
+    float* tlo = tib + nz;                   // [nz] low_j
+    float* tga = tlo + nz;                   // [nz+1] gam_j (gam_nz = 0)
+    float* tst = tga + nz + 1;               // [nz] stretch_j
+    float2* Cy = (float2*)(smraw + zchunk2_tables_bytes(nz));   // [NCH][32] chunk-end values
+    float* Cp = (float*)(Cy + NCH * 32);     // [NCH][32] chunk multiplier products
+    float2* Yall = (float2*)(Cp + NCH * 32); // [NCH][rows][32]
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    {
+        const float* low = zt + (ZT_TH + 3 * bc) * nz;
+        const float* ibd = zt + (ZT_TH + 3 * bc + 1) * nz;
+        const float* gam = zt + (ZT_TH + 3 * bc + 2) * nz;
+        for (int j = threadIdx.x; j <= nz; j += blockDim.x) {
+            if (j < nz) {
+                const float l = j > 0 ? low[j] : 0.f, ib = ibd[j];
+                tlo[j] = l;
+                tib[j] = ib;
+                tmf[j] = -l * ib;
+                tst[j] = zt[ZT_STRETCH * nz + j];
+            }
+            tga[j] = (j > 0 && j < nz) ? gam[j] : 0.f;
+        }
+    }
+    float2* Y = Yall + (long long)w * rows * 32 + lane;   // Y[i * 32] = plane s - 2 + i
+    const long long m = (long long)blockIdx.x * 64 + 2 * lane;
+    const bool on = m < npix;                             // npix even: both pencils or neither
+    const float* b = in + blockIdx.y * fstride + (on ? m : 0);
+    float* o = out + blockIdx.y * fstride + m;
+    const int s = w * cs, e = min(nz, s + cs) - 1;
+    auto B = [&](int j) -> float2 { return *(const float2*)(b + (long long)j * npix); };
+    float2 top = make_float2(0.f, 0.f);
+    if (topsrc && on) {
+        const float2 tv = *(const float2*)(topsrc + blockIdx.y * fstride + (long long)(nz - 1) * npix + m);
+        top = pmul(bc2(topscale), tv);
+    }
+    if (s <= e) {
+        for (int i = 0; i < e - s + 5; ++i) {
+            const int j = s - 2 + i;
+            if (j >= 0 && j < nz) {
+                const unsigned dst = (unsigned)__cvta_generic_to_shared(Y + i * 32);
+                const float* src = b + (long long)j * npix;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+            } else {
+                Y[i * 32] = make_float2(0.f, 0.f);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto Bs = [&](int j) -> float2 { return (j >= s - 2 && j <= e + 2) ? Y[(j - s + 2) * 32] : B(j); };
+    auto rhs_row = [&](int j) -> float2 {
+        return make_float2(compact_rhs_row<float>(j, nz, bc, [&](int k) { return Bs(k).x; }, 0.f, top.x, cc),
+                           compact_rhs_row<float>(j, nz, bc, [&](int k) { return Bs(k).y; }, 0.f, top.y, cc));
+    };
+    const float2 Z2 = make_float2(0.f, 0.f);
+    float2 Rlo0 = Z2, Rlo1 = Z2, Rhi2 = Z2, Rhi1 = Z2;
+    if (s <= e && s <= 1) { Rlo0 = rhs_row(0); Rlo1 = rhs_row(1); }
+    if (s <= e && e >= nz - 2) { Rhi2 = rhs_row(nz - 2); Rhi1 = rhs_row(nz - 1); }
+    const float2 C1p = bc2(cc.C1), C2p = bc2(cc.C2);
+    float2 y = Z2;
+    float pr = 1.f;
+    if (s <= e) {
+        float2 wm2 = Y[0], wm1 = Y[32], w0 = Y[64], w1 = Y[96], w2 = Y[128];
+        for (int j = s, i = 2; j <= e; ++j, ++i) {
+            float2 R;
+            if (j >= 2 && j <= nz - 3) R = pfma(C2p, psub(w2, wm2), pmul(C1p, psub(w1, wm1)));
+            else R = j == 0 ? Rlo0 : (j == 1 ? Rlo1 : (j == nz - 2 ? Rhi2 : Rhi1));
+            y = pmul(bc2(tib[j]), pfma(bc2(-tlo[j]), y, R));
+            pr = pr * tmf[j];
+            wm2 = wm1; wm1 = w0; w0 = w1; w1 = w2;
+            if (j < e) w2 = Y[(i + 3) * 32];
+            Y[i * 32] = y;
+        }
+    }
+    Cy[w * 32 + lane] = y;
+    Cp[w * 32 + lane] = pr;
+    __syncthreads();
+    float2 cin = Z2;
+    for (int q = 0; q < w; ++q) cin = pfma(bc2(Cp[q * 32 + lane]), cin, Cy[q * 32 + lane]);
+    float2 x = Z2;
+    pr = 1.f;
+    if (s <= e) {
+        if (w > 0) {
+            float pj = 1.f;
+            for (int j = s, i = 2; j <= e; ++j, ++i) {
+                pj = pj * tmf[j];
+                Y[i * 32] = pfma(bc2(pj), cin, Y[i * 32]);
+            }
+        }
+        for (int j = e, i = e - s + 2; j >= s; --j, --i) {
+            const float g = tga[j + 1];
+            x = pfma(bc2(-g), x, Y[i * 32]);
+            pr = pr * (-g);
+            Y[i * 32] = x;
+        }
+    }
+    __syncthreads();
+    Cy[w * 32 + lane] = x;
+    Cp[w * 32 + lane] = pr;
+    __syncthreads();
+    float2 xin = Z2;
+    for (int q = NCH - 1; q > w; --q) xin = pfma(bc2(Cp[q * 32 + lane]), xin, Cy[q * 32 + lane]);
+    if (s <= e && on) {
+        float pj = 1.f;
+        for (int j = e, i = e - s + 2; j >= s; --j, --i) {
+            pj = pj * (-tga[j + 1]);
+            *(float2*)(o + (long long)j * npix) = pmul(bc2(tst[j]), pfma(bc2(pj), xin, Y[i * 32]));
         }
     }
 }
@@ -861,6 +992,20 @@ int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfiel
     constexpr int NCH = 8;
     const int cs = (c->nz + NCH - 1) / NCH;
     const size_t sm = ((size_t)5 * c->nz + 1 + 2 * NCH * 32 + (size_t)NCH * (cs + 4) * 32) * sizeof(T);
+    if constexpr (sizeof(T) == 4) {
+        // two pencils per lane when the pencil count is even
+        const size_t sm2 = zchunk2_tables_bytes(c->nz) + (size_t)NCH * 32 * (8 + 4) + (size_t)NCH * (cs + 4) * 32 * 8;
+        if ((c->NP & 1) == 0 && sm2 <= 200 * 1024 && getenv("SPARC_ZCHUNK_SCALAR") == nullptr) {
+            cudaFuncSetAttribute((const void*)zderiv_chunk2_kernel<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm2);
+            dim3 g((unsigned)((c->NP + 63) / 64), nfield);
+            zderiv_chunk2_kernel<NCH><<<g, 32 * NCH, sm2, c->stream>>>(zt, cc_of<T>(c), in, out, c->NP, c->nz, bc,
+                                                                      fstride, topsrc, topscale);
+            c->launches++;
+            CKL();
+            return SPARC_OK;
+        }
+    }
     if (sizeof(T) == 4 && sm <= 200 * 1024) {
         cudaFuncSetAttribute((const void*)zderiv_chunk_kernel<T, NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);

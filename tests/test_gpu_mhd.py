@@ -436,3 +436,34 @@ def test_mhd3d_kernels_are_refused(gpu_lib):
     s.set_mhd_background(*bg)
     with pytest.raises(SparcError):
         s.snapshot(0, 1)
+
+
+@pytest.mark.parametrize("option", [10, 18])
+def test_mhd_fp32_paired_z_solve(gpu_lib, oracle_mod, option, monkeypatch):
+    """The FP32 chunked z solve with two pencils per lane (paired FP32
+    instructions) against the one-pencil kernel, through 16 steps of the MHD
+    forms: the same elimination, so the states agree to FP32 rounding."""
+    from sparc_gb300.solver import Solver
+    out = []
+    for scalar in (False, True):
+        if scalar:
+            monkeypatch.setenv("SPARC_ZCHUNK_SCALAR", "1")
+        else:
+            monkeypatch.delenv("SPARC_ZCHUNK_SCALAR", raising=False)
+        if option == 10:
+            p, tab, bg = _case("f32")
+            s = Solver(p, tab)
+            s.set_mhd_background(*bg)
+            a0, pml0 = _state(p, 32)
+            s.set_state(a0, pml0)
+        else:
+            p, tab, bg = _case2d("f32")
+            s = Solver(p, tab)
+            s.set_mhd2d_background(*bg)
+        s.set_source_series(gaussian_plane(p), oracle_mod.forward_source(p, 200) * 1e3)
+        s.step(16)
+        out.append(s.state()[0])
+        s.close()
+    assert np.abs(out[1]).max() > 0
+    for f in range(out[0].shape[0]):
+        assert rel_l2(out[0][f], out[1][f]) < 1e-5, (f, rel_l2(out[0][f], out[1][f]))
