@@ -69,6 +69,15 @@ struct MhdState {
     double* krho = nullptr;    // [N] rho0 (non-dimensional)
     double* rx64 = nullptr;    // [nx] FP64 d/dx multipliers (kernel scaling in FP64)
     double* kbacc = nullptr;   // [S][2][N] B-field kernel sums (x, z)
+    // a second stream for derivative launches of a stage that are independent
+    // of the ones on the context's stream (fork / join through two events)
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t evf = nullptr, evj = nullptr;
+    ~MhdState() {
+        if (evf) cudaEventDestroy(evf);
+        if (evj) cudaEventDestroy(evj);
+        if (s2) cudaStreamDestroy(s2);
+    }
 };
 
 namespace {
@@ -1031,6 +1040,9 @@ int mhd_create(sparc_ctx* c) {
     MhdState& m = *c->mhd;
     const size_t es = esz(c);
     int rc;
+    CK(cudaStreamCreateWithFlags(&m.s2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&m.evf, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&m.evj, cudaEventDisableTiming));
     if ((rc = dalloc(c, &m.bg, (size_t)MB_COUNT * c->N * es))) return rc;
     CK(cudaMemsetAsync(m.bg, 0, (size_t)MB_COUNT * c->N * es, c->stream));   // 2-D leaves the y rows at 0
     if ((rc = dalloc(c, &m.pab, (size_t)2 * std::max(c->nzpml, 1) * c->NP * es))) return rc;
@@ -1853,12 +1865,41 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
     const dim3 g(nb256(N), S);
     auto Wp = [&](int s, int f) { return work + ((size_t)s * MW_COUNT + f) * N; };
     int rc;
+    // independent derivatives of a group run on the second stream (side)
+    // while the rest run on the context's stream; join before their consumer
+    auto fork = [&]() -> int {
+        CK(cudaEventRecord(m.evf, c->stream));
+        CK(cudaStreamWaitEvent(m.s2, m.evf, 0));
+        return SPARC_OK;
+    };
+    auto join = [&]() -> int {
+        CK(cudaEventRecord(m.evj, m.s2));
+        CK(cudaStreamWaitEvent(c->stream, m.evj, 0));
+        return SPARC_OK;
+    };
+    auto side = [&](auto&& f) -> int {
+        cudaStream_t s0 = c->stream;
+        c->stream = m.s2;
+        const int r = f();
+        c->stream = s0;
+        return r;
+    };
+    const long long wst = (long long)MW_COUNT * N;
     mhd_temp_kernel<T><<<g, 256, 0, c->stream>>>(A, a, scr, beta, hs, bg, work);
     c->launches++;
     CKL();
     // DAMP_VELOCITY (damping.f90:125-159) through the normalised 2-D transforms;
     // it needs only the temporaries, so its terms are ready for the RHS kernel
     const bool damp = c->P.damp_waves != 0;
+    // div: ddxyz(xi_x, xi_y, xi_z, bc 1); d/dy and d/dz beside the damping
+    // transforms and d/dx
+    if ((rc = fork())) return rc;
+    if ((rc = side([&]() -> int {
+             for (int s = 0; s < S; ++s)
+                 if (int r = ddy_launch<T>(c, Wp(s, MW_T1), Wp(s, MW_DY), nz)) return r;
+             return ddz_launch<T>(c, zt, Wp(0, MW_T2), Wp(0, MW_DZ), 1, S, wst);
+         })))
+        return rc;
     if (damp) {
         typedef typename CplxOf<T>::type CT;
         for (int s = 0; s < S; ++s)
@@ -1871,42 +1912,57 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
             }
         CKL();
     }
-    // div: ddxyz(xi_x, xi_y, xi_z, bc 1)
-    for (int s = 0; s < S; ++s) {
-        if ((rc = ddx_launch<T>(c, Wp(s, MW_T0), Wp(s, MW_DX), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_T1), Wp(s, MW_DY), nz)))
-            return rc;
-    }
-    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_T2), Wp(0, MW_DZ), 1, S, (long long)MW_COUNT * N))) return rc;
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_T0), Wp(s, MW_DX), nz))) return rc;
+    if ((rc = join())) return rc;
     mhd_div_kernel<T><<<g, 256, 0, c->stream>>>(A, bg, work, pab, pml, spml, beta, hs);
     c->launches++;
     CKL();
     // grad p: ddxyz(p, bc 0) and psi_p
-    for (int s = 0; s < S; ++s) {
-        if ((rc = ddx_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPX), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPY), nz)))
-            return rc;
-    }
-    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 0, S, (long long)MW_COUNT * N))) return rc;
-    // induction: ddxyz(flux3, by, flux3, bx, flux2, dzflux2); ddxyz(flux2, bz, flux1, flux3, flux1, dzflux1)
-    for (int s = 0; s < S; ++s) {
-        if ((rc = ddx_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BY), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BX), nz)) ||
-            (rc = ddx_launch<T>(c, Wp(s, MW_F2), Wp(s, MW_BZ), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_F1), Wp(s, MW_F3), nz)))
-            return rc;
-    }
-    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_F2), Wp(0, MW_DZF2), 1, S, (long long)MW_COUNT * N)) ||
-        (rc = ddz_launch<T>(c, zt, Wp(0, MW_F1), Wp(0, MW_DZF1), 1, S, (long long)MW_COUNT * N)))
+    if ((rc = fork())) return rc;
+    if ((rc = side([&]() -> int {
+             for (int s = 0; s < S; ++s)
+                 if (int r = ddy_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPY), nz)) return r;
+             return ddz_launch<T>(c, zt, Wp(0, MW_P), Wp(0, MW_GPZ), 0, S, wst);
+         })))
         return rc;
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_P), Wp(s, MW_GPX), nz))) return rc;
+    if ((rc = join())) return rc;
+    // induction: ddxyz(flux3, by, flux3, bx, flux2, dzflux2); ddxyz(flux2, bz, flux1, flux3, flux1, dzflux1).
+    // d/dy(flux1) overwrites flux3, so it follows the join, after both reads of flux3
+    if ((rc = fork())) return rc;
+    if ((rc = side([&]() -> int {
+             for (int s = 0; s < S; ++s)
+                 if (int r = ddy_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BX), nz)) return r;
+             if (int r = ddz_launch<T>(c, zt, Wp(0, MW_F2), Wp(0, MW_DZF2), 1, S, wst)) return r;
+             return ddz_launch<T>(c, zt, Wp(0, MW_F1), Wp(0, MW_DZF1), 1, S, wst);
+         })))
+        return rc;
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_F3), Wp(s, MW_BY), nz)) || (rc = ddx_launch<T>(c, Wp(s, MW_F2), Wp(s, MW_BZ), nz)))
+            return rc;
+    if ((rc = join())) return rc;
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddy_launch<T>(c, Wp(s, MW_F1), Wp(s, MW_F3), nz))) return rc;
     mhd_b_kernel<T><<<g, 256, 0, c->stream>>>(A, work, pab, pml, spml, beta, hs);
     c->launches++;
     CKL();
     // curl b: ddxyz(by, curlbz, bz, curlbx, bx, dzbx); ddxyz(bz, curlby, bx, flux1, by, dzby)
-    for (int s = 0; s < S; ++s) {
-        if ((rc = ddx_launch<T>(c, Wp(s, MW_BY), Wp(s, MW_CBZ), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBX), nz)) ||
-            (rc = ddx_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBY), nz)) || (rc = ddy_launch<T>(c, Wp(s, MW_BX), Wp(s, MW_F1), nz)))
-            return rc;
-    }
-    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_BX), Wp(0, MW_DZBX), 1, S, (long long)MW_COUNT * N)) ||
-        (rc = ddz_launch<T>(c, zt, Wp(0, MW_BY), Wp(0, MW_DZBY), 1, S, (long long)MW_COUNT * N)))
+    if ((rc = fork())) return rc;
+    if ((rc = side([&]() -> int {
+             for (int s = 0; s < S; ++s)
+                 if (int r = ddy_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBX), nz)) return r;
+             for (int s = 0; s < S; ++s)
+                 if (int r = ddy_launch<T>(c, Wp(s, MW_BX), Wp(s, MW_F1), nz)) return r;
+             return ddz_launch<T>(c, zt, Wp(0, MW_BY), Wp(0, MW_DZBY), 1, S, wst);
+         })))
         return rc;
+    for (int s = 0; s < S; ++s)
+        if ((rc = ddx_launch<T>(c, Wp(s, MW_BY), Wp(s, MW_CBZ), nz)) || (rc = ddx_launch<T>(c, Wp(s, MW_BZ), Wp(s, MW_CBY), nz)))
+            return rc;
+    if ((rc = ddz_launch<T>(c, zt, Wp(0, MW_BX), Wp(0, MW_DZBX), 1, S, wst))) return rc;
+    if ((rc = join())) return rc;
     SlotClock clk;
     memset(&clk, 0, sizeof(clk));
     clk.t0 = c->d_t0; clk.time = c->d_time; clk.freq = c->freq_filtering; clk.two_d = 0;
