@@ -318,12 +318,20 @@ def small_step_latency(n=60):
     return out
 
 
+def _hbm_peak() -> float:
+    """Measured HBM copy bandwidth (GB/s) of MEASURED_PEAKS.json, else the fallback."""
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        return float(json.load(open(pk)).get("hbm_gbs", 6800.0))
+    return 6800.0
+
+
 def mhd_section(p0, tab, steps=5, warmup=2, precs=("f64", "f32")):
     """The flux-tube configuration: linearised MHD (option 10) at the bench
     grid on a 2 kG, 3 Mm self-similar tube, one source, forward steps in FP64
     and FP32 (device time per step, CUDA events on the context's stream)."""
     import torch
-    from sparc_gb300 import sources
+    from sparc_gb300 import bytes_model, sources
     from sparc_gb300.background import flux_tube_background
     from sparc_gb300.solver import Solver
     pm = p0.replace(option=10, npmltop=0, nsrc=1)
@@ -342,7 +350,11 @@ def mhd_section(p0, tab, steps=5, warmup=2, precs=("f64", "f32")):
         e1.record(st)
         e1.synchronize()
         ms = e0.elapsed_time(e1) / steps
-        out[prec] = {"ms_per_step": ms, "value": pm.points / (ms * 1e-3) / 1e6, "unit": UNIT}
+        bps = bytes_model.mhd_schedule_bytes_per_point_step(prec)
+        gbs = bps * pm.points / (ms * 1e-3) / 1e9
+        out[prec] = {"ms_per_step": ms, "value": pm.points / (ms * 1e-3) / 1e6, "unit": UNIT,
+                     "alg_bytes_per_point_step": bps, "hbm_achieved_gbs": gbs,
+                     "hbm_frac": gbs / _hbm_peak()}
         s.close()
     return out
 

@@ -102,6 +102,23 @@ def reference_schedule_bytes_per_point_step(precision: str) -> float:
     return REFERENCE_SCHEDULE_ACCESSES * (4 if precision == "f32" else 8)
 
 
+#: Linearised MHD, displacement form (option 10, the flux tube): the
+#: compulsory field accesses per grid-point-step of the minimal schedule.
+#: Per stage: the quiet form's 29, the three induction intermediates b
+#: (written, then read by the curl pass), their three derivative passes and
+#: the Lorentz terms, and 14 three-dimensional background fields (B0, curl
+#: B0, the horizontal gradients of p0 and rho0, and the ones the quiet form
+#: holds as z columns); about 81 accesses.  Five stages and the update with
+#: the z filter of six fields (18) make 423 per point-step: 1.69 kB in FP32,
+#: 3.38 kB in FP64.  This is the per-unit figure of the flux-tube roofline.
+MHD_SCHEDULE_ACCESSES = 5 * 81 + 18
+
+
+def mhd_schedule_bytes_per_point_step(precision: str) -> float:
+    """1692 B (FP32) / 3384 B (FP64) per grid-point-step of option 10."""
+    return MHD_SCHEDULE_ACCESSES * (4 if precision == "f32" else 8)
+
+
 FUSED_STEP = 12
 
 
