@@ -73,6 +73,7 @@ struct MhdState {
     // of the ones on the context's stream (fork / join through two events)
     cudaStream_t s2 = nullptr;
     cudaEvent_t evf = nullptr, evj = nullptr;
+    bool zchunk_scalar = false;   // FP32 z solve with one pencil per lane (SPARC_ZCHUNK_SCALAR, for the tests)
     ~MhdState() {
         if (evf) cudaEventDestroy(evf);
         if (evj) cudaEventDestroy(evj);
@@ -1004,7 +1005,7 @@ int ddz_launch(sparc_ctx* c, const T* zt, const T* in, T* out, int bc, int nfiel
     if constexpr (sizeof(T) == 4) {
         // two pencils per lane when the pencil count is even
         const size_t sm2 = zchunk2_tables_bytes(c->nz) + (size_t)NCH * 32 * (8 + 4) + (size_t)NCH * (cs + 4) * 32 * 8;
-        if ((c->NP & 1) == 0 && sm2 <= 200 * 1024 && getenv("SPARC_ZCHUNK_SCALAR") == nullptr) {
+        if ((c->NP & 1) == 0 && sm2 <= 200 * 1024 && !(c->mhd && c->mhd->zchunk_scalar)) {
             cudaFuncSetAttribute((const void*)zderiv_chunk2_kernel<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sm2);
             dim3 g((unsigned)((c->NP + 63) / 64), nfield);
@@ -1040,6 +1041,7 @@ int mhd_create(sparc_ctx* c) {
     MhdState& m = *c->mhd;
     const size_t es = esz(c);
     int rc;
+    m.zchunk_scalar = getenv("SPARC_ZCHUNK_SCALAR") != nullptr;
     CK(cudaStreamCreateWithFlags(&m.s2, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&m.evf, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&m.evj, cudaEventDisableTiming));
