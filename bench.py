@@ -318,6 +318,50 @@ def small_step_latency(n=60):
     return out
 
 
+def accuracy_section(solartime_h: float = 0.1, nsrc: int = 2):
+    """Errors of the FP32 path against FP64 on the same inputs, as the bench
+    states them for its results: the forward x adjoint kernel workflow on
+    the 128x128x150 quiet-Sun box (sources 10 Mm apart, 8 receivers on a
+    5 Mm ring, zero observations), FP32 fields with FP64 accumulation
+    against the FP64 path (itself within 1e-10 of the CPU oracle).  Reports
+    the relative L2 of the surface seismograms and of each kernel, and the
+    largest travel-time shift (COMPUTE_TT) over the receivers the wave has
+    reached (rms at least 1 % of the strongest)."""
+    from sparc_gb300 import sources
+    from sparc_gb300.background import polytrope_table
+    from sparc_gb300.params import config_quiet_128
+    from sparc_gb300.pipeline import KernelPipeline, compute_tt
+    p = config_quiet_128().replace(solartime=solartime_h, nsrc=nsrc)
+    tab = polytrope_table(p.nz)
+    planes = [sources.gaussian_plane(p, 1.0, x0, 0.0) for x0 in (-5.0, 5.0)][:nsrc]
+    series = sources.ricker_series(p, p.maxtime + 10)
+    pix = sources.receiver_pixels(p, n=8, radius_mm=5.0)
+    res = {}
+    t0 = time.perf_counter()
+    for prec in ("f64", "f32"):
+        pl = KernelPipeline(p.replace(precision=prec), tab, segment=8)
+        res[prec] = pl.run(planes, series, np.zeros((nsrc, pl.nt, p.ny, p.nx)), pix)
+    a, b = res["f64"], res["f32"]
+
+    def rel(x, y):
+        return float(np.linalg.norm((x - y).ravel()) / max(np.linalg.norm(y.ravel()), 1e-300))
+
+    dt = p.timestep * p.steps
+    shifts = []
+    for s in range(nsrc):
+        rms = np.sqrt(np.mean(a.seismograms[s] ** 2, axis=0))
+        for r in range(len(pix)):
+            if rms[r] >= 1e-2 * rms.max():
+                shifts.append(abs(compute_tt(a.seismograms[s, :, r], b.seismograms[s, :, r], dt)))
+    return {"workload": f"kernel workflow, {p.nx}x{p.ny}x{p.nz}, {nsrc} sources, {p.maxtime + 1} steps "
+                        f"({solartime_h} h), FP32 against FP64",
+            "seismogram_rel_l2": rel(b.seismograms, a.seismograms),
+            "kernel_rel_l2": {q: rel(getattr(b, q), getattr(a, q)) for q in ("kc", "krho", "hessian")},
+            "max_tt_shift_s": float(max(shifts)) if shifts else None, "receivers_timed": len(shifts),
+            "tolerances": {"seismogram_rel_l2": 1e-4, "tt_shift_s": 0.05},
+            "wall_s": time.perf_counter() - t0}
+
+
 def _hbm_peak() -> float:
     """Measured HBM copy bandwidth (GB/s) of MEASURED_PEAKS.json, else the fallback."""
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -632,6 +676,12 @@ def main():
                 line["config1_full"] = config1_full()
             except Exception as e:   # reported, not fatal
                 line["config1_full"] = {"error": str(e)}
+    if ws == 1 and not args.skip_fp64:
+        log("FP32 against FP64")
+        try:
+            line["accuracy"] = accuracy_section()
+        except Exception as e:   # reported, not fatal
+            line["accuracy"] = {"error": str(e)}
     if ws == 1 and not args.skip_mhd:
         log("MHD flux tube")
         try:
