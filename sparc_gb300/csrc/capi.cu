@@ -833,6 +833,7 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
         Fz.src_mode = A.src_mode; Fz.series = A.series; Fz.nseries = A.nseries;
         Fz.clk = A.clk;
         Fz.pencils = c->fused_pencils;
+        Fz.err = c->d_flag + 1;
     }
     for (int it = 0; it < nsteps; ++it) {
         if (fused) {
@@ -1038,6 +1039,15 @@ int sparc_gpu_set_time(sparc_ctx* c, int t) {
 int sparc_gpu_sync(sparc_ctx* c, int check_finite) {
     if (!c) return SPARC_EINVAL;
     CK(cudaStreamSynchronize(c->stream));
+    if (c->use_fused && c->f32) {
+        // a bounded device wait of the fused step that gave up (the z-table bulk copy)
+        int tflag = 0;
+        CK(cudaMemcpy(&tflag, c->d_flag + 1, 4, cudaMemcpyDeviceToHost));
+        if (tflag) {
+            CK(cudaMemset(c->d_flag + 1, 0, 4));
+            return fail(c, SPARC_ETIMEDOUT, "fused step: the bounded wait for the z-table bulk copy gave up");
+        }
+    }
     if (check_finite && c->have_bg) {
         CK(cudaMemsetAsync(c->d_flag, 0, 4, c->stream));
         long long n = (long long)c->S * c->nf * c->fs * 2;

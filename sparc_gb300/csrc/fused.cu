@@ -209,7 +209,7 @@ __device__ __forceinline__ int pmlidx(int j, int nz, int nb, int nt) {
 
 // shared-memory layout (byte offsets), identical on host and device
 struct FusedLayout {
-    int tile, xa, xb, ptile, spt, wbuf, zs, lagw, lagi, total;
+    int tile, xa, xb, ptile, spt, wbuf, zs, lagw, lagi, mbar, total;
 };
 __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
     const int NZP = 160 * W, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX;
@@ -226,6 +226,8 @@ __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
     o = (o + 15) & ~15;
     L.lagw = o;  o += 8 * 8;
     L.lagi = o;  o += 8 * 4;
+    o = (o + 7) & ~7;
+    L.mbar = o;  o += 8;                  // mbarrier of the z-table bulk copy
     L.total = (o + 15) & ~15;
     return L;
 }
@@ -252,6 +254,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     Aff* wbuf = (Aff*)(smraw + Ly.wbuf);                  // [4 scans][P][W]
     float* zs = (float*)(smraw + Ly.zs);                  // [FZ_COUNT][NZP]
     double* lagw = (double*)(smraw + Ly.lagw);            // [8] Lagrange weights of this slot
+    const unsigned mbar = (unsigned)__cvta_generic_to_shared(smraw + Ly.mbar);
     int* lagi = (int*)(smraw + Ly.lagi);                  // [8]: sample index of each weight
     const int nthr = blockDim.x;
     const int pi = threadIdx.x / TP;                      // pencil within the CTA
@@ -269,6 +272,20 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     // 16 B vector copies need every row start z*M + m0 to be even (M even)
     const bool vec = ((M & 1) == 0) && (m0 + P <= M);
 
+    // ---- the z tables: one bulk copy (TMA engine) into shared memory, issued
+    // by thread 0 and awaited, with a bounded wait, after the cooperative
+    // loads below; 16-byte aligned at both ends, a multiple of 16 bytes ----
+    if (threadIdx.x == 0) {
+        const unsigned bytes = FZ_COUNT * NZP * 4;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(zs);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                     ::"r"(dst), "l"(A.ftab), "r"(bytes), "r"(mbar)
+                     : "memory");
+    }
     // ---- zero the ghost and padding rows of the tile and the exchange lines ----
     {
         const int nl = LZ - nz;                       // GZ below + (NZP - nz + GZ) above, per row
@@ -315,9 +332,16 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         lagw[threadIdx.x] = w;
         lagi[threadIdx.x] = id < 0 ? 0 : id;
     }
-    for (int r = threadIdx.x; r < FZ_COUNT * NZP / 4; r += nthr)
-        ((float4*)zs)[r] = __ldg((const float4*)A.ftab + r);
-    __syncthreads();
+    __syncthreads();                                      // the mbarrier is initialised
+    {
+        unsigned done = 0;
+        for (int it = 0; it < (1 << 22) && !done; ++it)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done)
+                         : "r"(mbar)
+                         : "memory");
+        if (!done && threadIdx.x == 0) atomicExch(A.err, 1);
+    }
 
     const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
     const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;

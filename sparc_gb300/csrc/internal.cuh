@@ -358,7 +358,8 @@ struct FusedArgs {
     const float2* planes; long long plane_ss; int L;
     const double* series; int nseries;
     SlotClock clk;
-    int pencils;        // modes per CTA: 2 or 4 (same results; a tuning choice)
+    int pencils;        // modes per CTA: 2, 4 or 8 (same results; a tuning choice)
+    int* err;           // set to 1 if the bounded wait for the z-table bulk copy gave up
 };
 constexpr int FUSED_CH = 5;
 void fused_prepare(int nz, int nzpml);
