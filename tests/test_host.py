@@ -127,3 +127,14 @@ def test_compute_tt_recovers_a_shift():
         tau = compute_tt(u0, w(t - shift), dt)
         assert abs(tau - shift) < 2.0, (shift, tau)
     assert abs(compute_tt(u0, u0, dt)) < 1e-6
+
+
+def test_roofline_credits():
+    """The per-unit figures of the roofline lines: the quiet form's minimal
+    per-stage schedule (163.3 field accesses per point-step) and the flux
+    tube's (423), in bytes per grid-point-step."""
+    assert abs(bytes_model.reference_schedule_bytes_per_point_step("f32") - 653.333) < 1e-3
+    assert abs(bytes_model.reference_schedule_bytes_per_point_step("f64") - 1306.667) < 1e-3
+    assert bytes_model.MHD_SCHEDULE_ACCESSES == 423
+    assert bytes_model.mhd_schedule_bytes_per_point_step("f32") == 1692
+    assert bytes_model.mhd_schedule_bytes_per_point_step("f64") == 3384
