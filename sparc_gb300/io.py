@@ -202,6 +202,36 @@ def write_kernels(directory: str, contrib: str, kc: np.ndarray, krho: np.ndarray
     return out
 
 
+def timestamp(time: int, width: int = 6) -> str:
+    """The zero-padded decimal time of the reference's file names
+    (convert_to_string, initialize.f90:1092-1120, timestamp_size 6)."""
+    return str(int(time)).zfill(width)
+
+
+def write_partial_state(directory: str, solver, time: int, forward: bool, slot: int = 0) -> list:
+    """WRITE_OUT_PARTIAL_STATE (all_modules.f90:750-785, called at
+    driver.f90:481,484 on the output cadence): xi (forward runs only), v and
+    the last stage's acc = scr(:,:,:,4:6) of one source slot as
+    <name>_<time>_partial.fits (TIME keyword, planes 1..nz), the y
+    components only in 3-D.  `solver` is a Solver after a step call (field
+    0..5 = a, 9..11 = scr(4..6))."""
+    os.makedirs(directory, exist_ok=True)
+    three_d = solver.p.ny > 1
+    names = []
+    if forward:
+        names += [("xix", 0), ("xiz", 2)] + ([("xiy", 1)] if three_d else [])
+    names += [("acc_x", 9), ("acc_z", 11), ("vx", 3), ("vz", 5)]
+    if three_d:
+        names += [("acc_y", 10), ("vy", 4)]
+    out = []
+    ts = timestamp(time)
+    for name, f in names:
+        path = os.path.join(directory, f"{name}_{ts}_partial.fits")
+        write_fits(path, solver.field(f, slot), {"TIME": int(time)})
+        out.append(path)
+    return out
+
+
 def write_kernels_b(directory: str, contrib: str, kbx: np.ndarray, kbz: np.ndarray, kpsi: np.ndarray,
                     time: int = 0) -> dict:
     """kernel_bx_XX.fits, kernel_bz_XX.fits, kernel_vectorpsi_XX.fits of a 2-D

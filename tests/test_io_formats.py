@@ -96,3 +96,30 @@ def test_adjoint_source_files(tmp_path):
     io.write_windows(str(tmp_path), win)
     back = io.read_windows(str(tmp_path), {0: [3, 5], 1: [7]})
     assert back == {0: {3: (8, 48), 5: (10, 50)}, 1: {7: (20, 50)}}
+
+
+def test_partial_state_files(tmp_path):
+    """WRITE_OUT_PARTIAL_STATE's names, fields and TIME keyword, from any
+    object with the Solver's field accessor."""
+    import numpy as np
+    from sparc_gb300 import io
+    from sparc_gb300.params import SparcParams
+
+    class FakeSolver:
+        def __init__(self, p):
+            self.p = p
+
+        def field(self, f, slot=0):
+            return np.full((self.p.nz, self.p.ny, self.p.nx), float(f * 10 + slot))
+
+    p3 = SparcParams(nx=8, ny=8, nz=16)
+    files = io.write_partial_state(str(tmp_path / "fwd"), FakeSolver(p3), 1234, forward=True, slot=1)
+    names = sorted(f.split("/")[-1] for f in files)
+    assert names == sorted(f"{n}_001234_partial.fits" for n in
+                           ("xix", "xiz", "xiy", "acc_x", "acc_z", "vx", "vz", "acc_y", "vy"))
+    a, hdr = io.read_fits(str(tmp_path / "fwd" / "acc_z_001234_partial.fits"), with_header=True)
+    assert a.shape == (16, 8, 8) and np.all(a == 111.0) and int(hdr["TIME"]) == 1234
+    p2 = SparcParams(nx=8, ny=1, nz=16, option=17)
+    files = io.write_partial_state(str(tmp_path / "adj"), FakeSolver(p2), 45, forward=False)
+    assert sorted(f.split("/")[-1] for f in files) == sorted(
+        f"{n}_000045_partial.fits" for n in ("acc_x", "acc_z", "vx", "vz"))
