@@ -232,6 +232,75 @@ def write_partial_state(directory: str, solver, time: int, forward: bool, slot: 
     return out
 
 
+def _state_units():
+    """diml, dimc, dimrho, dimb as the reference forms them from its REAL*4
+    literals (initialize.f90:38,751-757)."""
+    def r4(x):
+        return float(np.float32(x))
+    pi, dimc, dimrho, diml = r4(3.14159265358979), r4(1.0e6), r4(1.0e-3), r4(69598946770.0)
+    dimb = (4.0 * pi * dimc ** 2.0 * dimrho) ** 0.5
+    return diml, dimc, dimrho, dimb
+
+
+def _full_state_layout(p):
+    """(file name, state field, unit) of WRITE_OUT_FULL_STATE for the form of
+    p, and the PML auxiliaries' names (all_modules.f90:623-694)."""
+    diml, dimc, dimrho, dimb = _state_units()
+    magnetic = p.option in (8, 10, 18)
+    if p.option in (2, 8):                    # velocity forms: rho, vx, vy, vz, p (, bx, by, bz)
+        fields = [("p", 4, dimrho * dimc ** 2.0), ("vy", 2, dimc), ("rho", 0, dimrho), ("vx", 1, dimc),
+                  ("vz", 3, dimc)]
+        if p.option == 8:
+            fields += [("bx", 5, dimb), ("by", 6, dimb), ("bz", 7, dimb)]
+    else:                                     # displacement forms: xi, v
+        fields = [("xix", 0, diml), ("xiz", 2, diml), ("vx", 3, dimc), ("vz", 5, dimc)]
+        if p.ny > 1:
+            fields += [("xiy", 1, diml), ("vy", 4, dimc)]
+    pml = ["psivz", "psip"] + (["psidzbx", "psidzby", "psiinductionbx", "psiinductionby"] if magnetic else [])
+    return fields, pml
+
+
+def write_full_state(directory: str, solver, time: int, slot: int = 0, remove_previous: bool = False) -> list:
+    """WRITE_OUT_FULL_STATE (all_modules.f90:623-694): the state of one slot
+    in the reference's units as <name>_<time>_full.fits, and the PML
+    auxiliaries (nzpml planes) as they are.  The reference first deletes the
+    directory's earlier *full* files; remove_previous=True does the same."""
+    os.makedirs(directory, exist_ok=True)
+    if remove_previous:
+        for f in os.listdir(directory):
+            if "full" in f:
+                os.remove(os.path.join(directory, f))
+    a, pml = solver.state(slot)
+    fields, pnames = _full_state_layout(solver.p)
+    ts = timestamp(time)
+    out = []
+    for name, f, unit in fields:
+        path = os.path.join(directory, f"{name}_{ts}_full.fits")
+        write_fits(path, a[f] * unit, {"TIME": int(time)})
+        out.append(path)
+    for i, name in enumerate(pnames):
+        path = os.path.join(directory, f"{name}_{ts}_full.fits")
+        write_fits(path, pml[i], {"TIME": int(time)})
+        out.append(path)
+    return out
+
+
+def read_full_state(directory: str, solver, time: int, slot: int = 0) -> None:
+    """READ_IN_INITIAL_CONDITION (all_modules.f90:530-621): the files of
+    write_full_state back into the slot's state, divided by the units.  The
+    reference reads xi_y and v_y even in 2-D, where it never writes them;
+    here the y components are read where they exist and are zero otherwise."""
+    fields, pnames = _full_state_layout(solver.p)
+    ts = timestamp(time)
+    a = np.zeros((solver.nf,) + solver.shape)
+    for name, f, unit in fields:
+        a[f] = read_fits(os.path.join(directory, f"{name}_{ts}_full.fits")).reshape(solver.shape) / unit
+    pml = np.zeros((solver.npv, solver.p.nzpml, solver.p.ny, solver.p.nx))
+    for i, name in enumerate(pnames):
+        pml[i] = read_fits(os.path.join(directory, f"{name}_{ts}_full.fits")).reshape(pml.shape[1:])
+    solver.set_state(a, pml, slot=slot)
+
+
 def write_kernels_b(directory: str, contrib: str, kbx: np.ndarray, kbz: np.ndarray, kpsi: np.ndarray,
                     time: int = 0) -> dict:
     """kernel_bx_XX.fits, kernel_bz_XX.fits, kernel_vectorpsi_XX.fits of a 2-D

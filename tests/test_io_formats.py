@@ -123,3 +123,47 @@ def test_partial_state_files(tmp_path):
     files = io.write_partial_state(str(tmp_path / "adj"), FakeSolver(p2), 45, forward=False)
     assert sorted(f.split("/")[-1] for f in files) == sorted(
         f"{n}_000045_partial.fits" for n in ("acc_x", "acc_z", "vx", "vz"))
+
+
+def test_full_state_round_trip(tmp_path):
+    """WRITE_OUT_FULL_STATE / READ_IN_INITIAL_CONDITION: names, units and a
+    round trip through the files, for the displacement, velocity and MHD
+    forms, with a stand-in of the Solver's state accessors."""
+    import numpy as np
+    from sparc_gb300 import io
+    from sparc_gb300.params import SparcParams
+
+    class FakeSolver:
+        def __init__(self, p, nf, npv, seed):
+            self.p, self.nf, self.npv = p, nf, npv
+            self.shape = (p.nz, p.ny, p.nx)
+            rng = np.random.default_rng(seed)
+            self.a = rng.standard_normal((nf,) + self.shape)
+            self.pml = rng.standard_normal((npv, p.nzpml, p.ny, p.nx))
+            self.got = None
+
+        def state(self, slot=0):
+            return self.a, self.pml
+
+        def set_state(self, a, pml, slot=0):
+            self.got = (a, pml)
+
+    diml, dimc, dimrho, dimb = io._state_units()
+    for opt, ny, nf, npv, names in ((4, 8, 6, 2, ("xix", "xiy", "xiz", "vx", "vy", "vz", "psivz", "psip")),
+                                    (17, 1, 6, 2, ("xix", "xiz", "vx", "vz", "psivz", "psip")),
+                                    (8, 8, 8, 6, ("rho", "vx", "vy", "vz", "p", "bx", "by", "bz", "psivz",
+                                                  "psip", "psidzbx", "psidzby", "psiinductionbx",
+                                                  "psiinductionby"))):
+        p = SparcParams(nx=8, ny=ny, nz=16, option=opt, npmlbot=3, npmltop=3)
+        src = FakeSolver(p, nf, npv, opt)
+        d = tmp_path / f"opt{opt}"
+        files = io.write_full_state(str(d), src, 30, slot=0)
+        assert sorted(f.split("/")[-1] for f in files) == sorted(f"{n}_000030_full.fits" for n in names)
+        dst = FakeSolver(p, nf, npv, 99)
+        io.read_full_state(str(d), dst, 30)
+        a, pml = dst.got
+        used = [f for _, f, _ in io._full_state_layout(p)[0]]
+        assert np.allclose(a[used], src.a[used], rtol=1e-15, atol=0) and np.array_equal(pml, src.pml)
+    first = io.read_fits(str(tmp_path / "opt4" / "xix_000030_full.fits"))
+    assert np.allclose(first, FakeSolver(SparcParams(nx=8, ny=8, nz=16, option=4, npmlbot=3, npmltop=3), 6, 2, 4).a[0] * diml,
+                       rtol=1e-15, atol=0)
