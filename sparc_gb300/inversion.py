@@ -99,3 +99,36 @@ def model_update(solver: Solver, datadir: str, iterno: int, num_src: int, rho_z:
             put(f"test_c_{i}.fits", model_c)          # c is not updated (grad.py:285-293)
         put(f"test_vectorpsi_{i}.fits", test_psi[i - 1])
     return UpdateResult(g_c, g_psi, u_c, u_psi, test_psi, con, files)
+
+
+def _count_master_pixels(datadir: str) -> int:
+    with open(os.path.join(datadir, "master.pixels")) as f:
+        return sum(1 for _ in f)
+
+
+def total_misfit(datadir: str, iterno: int | None = None) -> float:
+    """misfit.py: the sum of the third column of update/misfit_II over the
+    first nmasterpixels rows (one row per source).  iterno None takes the
+    last iteration, as the script does from the count of misfit files."""
+    upd = os.path.join(datadir, "update")
+    if iterno is None:
+        n = len([f for f in os.listdir(upd) if f.startswith("misfit_") and "all" not in f])
+        if n == 0:
+            raise FileNotFoundError("no misfit files in " + upd)
+        iterno = n - 1
+    col = np.loadtxt(os.path.join(upd, f"misfit_{_two(iterno)}"), usecols=[2], ndmin=1)
+    return float(np.sum(col[:_count_master_pixels(datadir)]))
+
+
+def linesearch_misfits(datadir: str, iterno: int | None = None, n_linesearches: int = 5) -> list:
+    """lsmisfit.py: per test model, the sum of the third column of
+    update/linesearch_II over that model's block of nmasterpixels rows."""
+    upd = os.path.join(datadir, "update")
+    if iterno is None:
+        n = len([f for f in os.listdir(upd) if f.startswith("linesearch_") and "all" not in f])
+        if n == 0:
+            raise FileNotFoundError("no linesearch files in " + upd)
+        iterno = n - 1
+    col = np.loadtxt(os.path.join(upd, f"linesearch_{_two(iterno)}"), usecols=[2], ndmin=1)
+    npix = _count_master_pixels(datadir)
+    return [float(np.sum(col[i * npix:(i + 1) * npix])) for i in range(n_linesearches)]

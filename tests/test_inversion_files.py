@@ -74,3 +74,27 @@ def test_vector_potential_background_host_logic():
         for f in ("bx", "bz", "psi"):
             d = np.abs(got[m][f] - ref[m][f]).max()
             assert d <= 1e-10 * np.abs(ref[m][f]).max(), (m, f, d)
+
+
+def test_misfit_sums(tmp_path):
+    """misfit.py / lsmisfit.py over the files the pipeline writes
+    (io.write_misfit lines concatenated per source and per test model)."""
+    from sparc_gb300 import inversion, io
+    (tmp_path / "update").mkdir()
+    (tmp_path / "master.pixels").write_text("-5.0\n3.0\n")
+    vals = [1.5, 2.25]
+    with open(tmp_path / "update" / "misfit_00", "w") as f:
+        for k, v in enumerate(vals):
+            tmpf = tmp_path / "m"
+            io.write_misfit(str(tmpf), k + 1, 10, v)
+            f.write(tmpf.read_text())
+    (tmp_path / "update" / "misfit_all_00").write_text("ignored\n")
+    assert abs(inversion.total_misfit(str(tmp_path)) - 3.75) < 1e-15
+    with open(tmp_path / "update" / "linesearch_00", "w") as f:
+        for ls in range(5):
+            for k in range(2):
+                tmpf = tmp_path / "m"
+                io.write_misfit(str(tmpf), k + 1, 10, 0.5 * (ls + 1) + k)
+                f.write(tmpf.read_text())
+    got = inversion.linesearch_misfits(str(tmp_path))
+    assert np.allclose(got, [2 * 0.5 * (ls + 1) + 1 for ls in range(5)])
