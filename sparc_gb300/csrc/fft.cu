@@ -171,6 +171,71 @@ __global__ void __launch_bounds__(256) cols_fft_sq_kernel(const typename CplxOf<
     }
 }
 
+// cols_fft_sq_kernel forward, the real multiplier mul[ky][kx], and
+// cols_fft_sq_kernel inverse in one pass, in place on [plane][y][kx] columns:
+// after the forward passes thread r holds the indices r + R k2, which are the
+// ones the inverse's first pass loads, so both halves are the standalone
+// kernels' arithmetic and the result equals the two-kernel path bit for bit
+template <typename T, int R>
+__global__ void __launch_bounds__(256) cols_filter_sq_kernel(typename CplxOf<T>::type* __restrict__ data, int H,
+                                                             const double* __restrict__ tw,
+                                                             const T* __restrict__ mul) {
+    typedef typename CplxOf<T>::type CT;
+    constexpr int n = R * R, NC = 256 / R;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    CT* Z = (CT*)smraw;                                  // [k1][n2][c]
+    const int ntile = (H + NC - 1) / NC;
+    const long long plane = blockIdx.x / ntile;
+    const int kx0 = (blockIdx.x % ntile) * NC;
+    const int c = threadIdx.x % NC, r = threadIdx.x / NC;
+    const bool cv = kx0 + c < H;
+    const long long base = plane * (long long)n * H + kx0 + c;
+    CT wf[R / 2], wi[R / 2];
+    #pragma unroll
+    for (int j = 0; j < R / 2; ++j) {
+        wf[j] = tw_n<T, CT>(tw, j * R, n, (T)-1);
+        wi[j] = tw_n<T, CT>(tw, j * R, n, (T)1);
+    }
+    CT v[R];
+    #pragma unroll
+    for (int n1 = 0; n1 < R; ++n1) v[n1] = cv ? data[base + (long long)(R * n1 + r) * H] : czero<CT>();
+    // forward, pass 1 (thread n2 = r) and pass 2 (thread k1 = r)
+    reg_dft<CT, R>(v, wf);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = v[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, n, (T)-1));
+        Z[(k1 * R + r) * NC + c] = y;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) v[n2] = Z[(r * R + n2) * NC + c];
+    reg_dft<CT, R>(v, wf);
+    CT u[R];
+    #pragma unroll
+    for (int k2 = 0; k2 < R; ++k2) {
+        const CT X = v[brev<R>(k2)];
+        u[k2] = cv ? __ldg(&mul[(long long)(r + R * k2) * H + kx0 + c]) * X : czero<CT>();
+    }
+    __syncthreads();                                     // every thread has read its forward tile
+    // inverse, pass 1 (thread n2 = r holds indices R n1 + r) and pass 2
+    reg_dft<CT, R>(u, wi);
+    #pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+        CT y = u[brev<R>(k1)];
+        if (k1 > 0 && r > 0) y = cmul(y, tw_n<T, CT>(tw, r * k1, n, (T)1));
+        Z[(k1 * R + r) * NC + c] = y;
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int n2 = 0; n2 < R; ++n2) u[n2] = Z[(r * R + n2) * NC + c];
+    reg_dft<CT, R>(u, wi);
+    if (cv) {
+        #pragma unroll
+        for (int k2 = 0; k2 < R; ++k2) data[base + (long long)(r + R * k2) * H] = u[brev<R>(k2)];
+    }
+}
+
 // inverse real transform along x (length nx = R*R), two rows per complex
 // FFT as rows_c2r_kernel, NP = 256/R row pairs per CTA
 template <typename T, int R>
@@ -299,15 +364,11 @@ __global__ void spec_mul_kernel(typename CplxOf<T>::type* spec, const T* __restr
 // phys -> normalised half-spectrum; with mul, each spectral plane is also
 // multiplied by the real pencil multiplier mul[m] (in the column pass when
 // there is one)
+// rows of nx reals -> rows of H complex (the forward row pass of fft_phys_to_spec)
 template <typename T>
-void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
-                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s,
-                      const T* mul) {
+static void rows_forward(const T* phys, typename CplxOf<T>::type* dst, int nx, long long nrows, T scale,
+                         const double* tw_x, cudaStream_t s) {
     typedef typename CplxOf<T>::type CT;
-    const int H = nx / 2 + 1;
-    const long long nrows = (long long)ny * nplanes;
-    CT* dst = (ny == 1) ? spec : tmp;
-    const T scale = (T)(1.0 / ((double)nx * ny));
     const int Rx = sq_radix(nx);
     if (Rx) {
         const long long rows_per_cta = 2LL * (256 / Rx);
@@ -326,6 +387,18 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
         set_smem<T>((const void*)rows_r2c_kernel<T>, sm);
         rows_r2c_kernel<T><<<(unsigned)((nrows + 1) / 2), thr, sm, s>>>(phys, dst, nx, nrows, scale, tw_x);
     }
+}
+
+template <typename T>
+void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp,
+                      int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s,
+                      const T* mul) {
+    typedef typename CplxOf<T>::type CT;
+    const int H = nx / 2 + 1;
+    const long long nrows = (long long)ny * nplanes;
+    CT* dst = (ny == 1) ? spec : tmp;
+    const T scale = (T)(1.0 / ((double)nx * ny));
+    rows_forward<T>(phys, dst, nx, nrows, scale, tw_x, s);
     const int Ry = sq_radix(ny);
     if (ny > 1 && Ry) {
         const int NC = 256 / Ry, ntile = (H + NC - 1) / NC;
@@ -351,6 +424,31 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
         const long long n = (long long)nplanes * ny * H;
         spec_mul_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(spec, mul, ny * H, n);
     }
+}
+
+// rows of H complex -> rows of nx reals (the inverse row pass of fft_spec_to_phys_g)
+template <typename T>
+static void rows_inverse(const typename CplxOf<T>::type* src, T* phys, int nx, int ny, long long nrows,
+                         int rppg, long long rgs, const double* tw_x, cudaStream_t s) {
+    typedef typename CplxOf<T>::type CT;
+    const int Rx = sq_radix(nx);
+    const long long npairs = (nrows + 1) / 2;
+    if (Rx == 16) {
+        const size_t sm = (size_t)16 * 16 * 17 * sizeof(CT);
+        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 16>, sm);
+        rows_c2r_sq_kernel<T, 16><<<(unsigned)((npairs + 15) / 16), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
+        return;
+    }
+    if (Rx == 8) {
+        const size_t sm = (size_t)32 * 8 * 9 * sizeof(CT);
+        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 8>, sm);
+        rows_c2r_sq_kernel<T, 8><<<(unsigned)((npairs + 31) / 32), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
+        return;
+    }
+    size_t sm = 2 * (size_t)nx * sizeof(CT);
+    int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
+    set_smem<T>((const void*)rows_c2r_kernel<T>, sm);
+    rows_c2r_kernel<T><<<(unsigned)npairs, thr, sm, s>>>(src, phys, nx, nrows, tw_x, ny, rppg, rgs);
 }
 
 template <typename T>
@@ -387,24 +485,38 @@ void fft_spec_to_phys_g(const typename CplxOf<T>::type* spec, int ppg, long long
         rppg = nplanes;      // tmp is contiguous
         rgs = 0;
     }
-    const int Rx = sq_radix(nx);
-    const long long npairs = (nrows + 1) / 2;
-    if (Rx == 16) {
-        const size_t sm = (size_t)16 * 16 * 17 * sizeof(CT);
-        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 16>, sm);
-        rows_c2r_sq_kernel<T, 16><<<(unsigned)((npairs + 15) / 16), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
-        return;
+    rows_inverse<T>(src, phys, nx, ny, nrows, rppg, rgs, tw_x, s);
+}
+
+// phys -> out through the half spectrum times the real pencil multiplier
+// mul[ky][kx] (damping, horizontal filter).  For ny = 64 or 256 the column
+// passes run as one kernel in place on tmp (3 launches); otherwise as
+// fft_phys_to_spec + fft_spec_to_phys through spec (4 or 5).  Returns the
+// number of launches.
+template <typename T>
+int fft_filter_phys(const T* phys, T* out, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp, int nx,
+                    int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s, const T* mul) {
+    typedef typename CplxOf<T>::type CT;
+    const int Ry = sq_radix(ny);
+    if (!(ny > 1 && Ry)) {
+        fft_phys_to_spec<T>(phys, spec, tmp, nx, ny, nplanes, tw_x, tw_y, s, mul);
+        fft_spec_to_phys<T>(spec, out, tmp, nx, ny, nplanes, tw_x, tw_y, s);
+        return ny > 1 ? 5 : 3;
     }
-    if (Rx == 8) {
-        const size_t sm = (size_t)32 * 8 * 9 * sizeof(CT);
-        set_smem<T>((const void*)rows_c2r_sq_kernel<T, 8>, sm);
-        rows_c2r_sq_kernel<T, 8><<<(unsigned)((npairs + 31) / 32), 256, sm, s>>>(src, phys, nrows, tw_x, ny, rppg, rgs);
-        return;
+    const int H = nx / 2 + 1;
+    const long long nrows = (long long)ny * nplanes;
+    rows_forward<T>(phys, tmp, nx, nrows, (T)(1.0 / ((double)nx * ny)), tw_x, s);
+    const int NC = 256 / Ry, ntile = (H + NC - 1) / NC;
+    const size_t smc = (size_t)ny * NC * sizeof(CT);
+    if (Ry == 16) {
+        set_smem<T>((const void*)cols_filter_sq_kernel<T, 16>, smc);
+        cols_filter_sq_kernel<T, 16><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, H, tw_y, mul);
+    } else {
+        set_smem<T>((const void*)cols_filter_sq_kernel<T, 8>, smc);
+        cols_filter_sq_kernel<T, 8><<<(unsigned)(ntile * (long long)nplanes), 256, smc, s>>>(tmp, H, tw_y, mul);
     }
-    size_t sm = 2 * (size_t)nx * sizeof(CT);
-    int thr = nx / 2 < 256 ? (nx / 2 < 32 ? 32 : nx / 2) : 256;
-    set_smem<T>((const void*)rows_c2r_kernel<T>, sm);
-    rows_c2r_kernel<T><<<(unsigned)npairs, thr, sm, s>>>(src, phys, nx, nrows, tw_x, ny, rppg, rgs);
+    rows_inverse<T>(tmp, out, nx, ny, nrows, nplanes, 0LL, tw_x, s);
+    return 3;
 }
 
 template <typename T>
@@ -588,6 +700,8 @@ int launch_check_finite_f32(const float* p, long long n, int* flag, cudaStream_t
 }
 
 #define INST(T)                                                                                                   \
+    template int fft_filter_phys<T>(const T*, T*, CplxOf<T>::type*, CplxOf<T>::type*, int, int, int, const double*, \
+                                    const double*, cudaStream_t, const T*);                                       \
     template void fft_phys_to_spec<T>(const T*, CplxOf<T>::type*, CplxOf<T>::type*, int, int, int, const double*, \
                                       const double*, cudaStream_t, const T*);                                     \
     template void fft_spec_to_phys<T>(const CplxOf<T>::type*, T*, CplxOf<T>::type*, int, int, int, const double*, \

@@ -409,6 +409,11 @@ void fft_phys_to_spec(const T* phys, typename CplxOf<T>::type* spec, typename Cp
 template <typename T>
 void fft_spec_to_phys(const typename CplxOf<T>::type* spec, T* phys, typename CplxOf<T>::type* tmp,
                       int nx, int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s);
+// phys -> out through the spectrum times the real multiplier mul[ky][kx];
+// returns the number of launches
+template <typename T>
+int fft_filter_phys(const T* phys, T* out, typename CplxOf<T>::type* spec, typename CplxOf<T>::type* tmp, int nx,
+                    int ny, int nplanes, const double* tw_x, const double* tw_y, cudaStream_t s, const T* mul);
 // the same with grouped input planes: plane p of the input starts at
 // spec + (p / ppg) * gstride + (p % ppg) * ny * (nx/2+1) (complex elements);
 // phys and tmp are contiguous

@@ -917,12 +917,6 @@ __global__ void mhd_record_kernel(const T* __restrict__ a, T* __restrict__ rec, 
 
 unsigned nb256(long long n) { return (unsigned)((n + 255) / 256); }
 
-// launches of one filtered transform pair (phys -> spec x multiplier -> phys):
-// rows, columns (which apply the multiplier on the register path) and back
-int filter_pair_launches(const sparc_ctx* c) {
-    const bool sq_y = c->P.ny == 64 || c->P.ny == 256;
-    return c->P.ny > 1 ? (sq_y ? 4 : 5) : 3;
-}
 
 template <typename T>
 int ddx_launch(sparc_ctx* c, const T* in, T* out, long long nplanes) {
@@ -1645,10 +1639,8 @@ int mhd2d_stage(sparc_ctx* c, T beta, int hs) {
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 2; ++q) {
                 const int src = q == 0 ? MW_T3 : MW_T5, dst = q == 0 ? MW_DX : MW_DZ;
-                fft_phys_to_spec<T>(Wp(s, src), (CT*)m.spec, (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream,
-                                    (const T*)c->pt + (size_t)PT_DAMP * c->M);
-                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, dst), (CT*)c->tmp, c->P.nx, 1, nz, c->tw_x, c->tw_y, c->stream);
-                c->launches += filter_pair_launches(c);
+                c->launches += fft_filter_phys<T>(Wp(s, src), Wp(s, dst), (CT*)m.spec, (CT*)c->tmp, c->P.nx, 1, nz,
+                                                  c->tw_x, c->tw_y, c->stream, (const T*)c->pt + (size_t)PT_DAMP * c->M);
             }
         CKL();
     }
@@ -1817,11 +1809,9 @@ int mhd8_stage(sparc_ctx* c, T beta, int hs) {
         typedef typename CplxOf<T>::type CT;
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 3; ++q) {
-                fft_phys_to_spec<T>(Wp(s, V8_T1 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
-                                    c->tw_y, c->stream, (const T*)c->pt + (size_t)PT_DAMP * c->M);
-                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, V8_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
-                                    c->tw_y, c->stream);
-                c->launches += filter_pair_launches(c);
+                c->launches += fft_filter_phys<T>(Wp(s, V8_T1 + q), Wp(s, V8_DMX + q), (CT*)m.spec, (CT*)c->tmp,
+                                                  c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y, c->stream,
+                                                  (const T*)c->pt + (size_t)PT_DAMP * c->M);
             }
         CKL();
     }
@@ -1906,11 +1896,9 @@ int mhd_stage(sparc_ctx* c, T beta, int hs) {
         typedef typename CplxOf<T>::type CT;
         for (int s = 0; s < S; ++s)
             for (int q = 0; q < 3; ++q) {
-                fft_phys_to_spec<T>(Wp(s, MW_T3 + q), (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y,
-                                    c->stream, (const T*)c->pt + (size_t)PT_DAMP * c->M);
-                fft_spec_to_phys<T>((CT*)m.spec, Wp(s, MW_DMX + q), (CT*)c->tmp, c->P.nx, c->P.ny, nz, c->tw_x,
-                                    c->tw_y, c->stream);
-                c->launches += filter_pair_launches(c);
+                c->launches += fft_filter_phys<T>(Wp(s, MW_T3 + q), Wp(s, MW_DMX + q), (CT*)m.spec, (CT*)c->tmp,
+                                                  c->P.nx, c->P.ny, nz, c->tw_x, c->tw_y, c->stream,
+                                                  (const T*)c->pt + (size_t)PT_DAMP * c->M);
             }
         CKL();
     }
@@ -2015,10 +2003,8 @@ int mhd_steps_t(sparc_ctx* c, int nsteps) {
             if (tl < 0 || (two_d ? (tl + 1) : tl) % c->freq_filtering != 0) continue;
             for (int f = 0; f < (two_d ? 6 : 5); ++f) {
                 T* fp = (T*)c->a + ((size_t)s * c->nf + f) * 2 * c->fs;
-                fft_phys_to_spec<T>(fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream,
-                                    (const T*)c->pt + (size_t)PT_HF * c->M);
-                fft_spec_to_phys<T>((CT*)m.spec, fp, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x, c->tw_y, c->stream);
-                c->launches += filter_pair_launches(c);
+                c->launches += fft_filter_phys<T>(fp, fp, (CT*)m.spec, (CT*)c->tmp, c->P.nx, c->P.ny, c->nz, c->tw_x,
+                                                  c->tw_y, c->stream, (const T*)c->pt + (size_t)PT_HF * c->M);
             }
             CKL();
         }
