@@ -63,3 +63,25 @@ def test_table_row_counts_match_header():
     rows = dict(re.findall(r"#define (SPARC_[ZP]TAB_ROWS) (\d+)", hdr))
     assert int(rows["SPARC_ZTAB_ROWS"]) == native.ZTAB_ROWS
     assert int(rows["SPARC_PTAB_ROWS"]) == native.PTAB_ROWS
+
+
+def test_binding_argument_counts_match_header():
+    """Every prototype of include/sparc_gpu.h has as many parameters as the
+    ctypes binding declares for it (argtypes), so a changed signature cannot
+    be called with a stale one."""
+    from sparc_gb300 import native
+    txt = open(os.path.join(ROOT, "include", "sparc_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    protos = dict((m.group(1), m.group(2)) for m in
+                  re.finditer(r"\b(sparc_gpu_\w+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S))
+    L = native.load()
+    checked = 0
+    for name, params in protos.items():
+        f = getattr(L, name)
+        if f.argtypes is None:
+            continue
+        p = params.strip()
+        n = 0 if p in ("", "void") else len(p.split(","))
+        assert n == len(f.argtypes), (name, n, len(f.argtypes))
+        checked += 1
+    assert checked >= 30
