@@ -130,12 +130,25 @@ def fused_step_alg_bytes(p, write_scr: bool = False) -> int:
     return (FUSED_STEP + (6 if write_scr else 0)) * f + 4 * pf + plane
 
 
-#: DRAM traffic (read + write) of one fused-step launch per source, measured
-#: with ncu at 256x256x300 FP32 (profiles/fused_step_f32_256x256x300.md);
-#: traffic grows in proportion to the number of sources.
+#: DRAM traffic (read + write) of one fused-step launch per source:
+#: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a
+#: single-source forward step (no scr written) at 256x256x300 FP32.  Traffic
+#: grows in proportion to the number of sources, so a batched launch is
+#: credited with this figure times nsrc; it is a scaled constant, not a
+#: measurement of the run that reports it.
 MEASURED_FUSED_TRAFFIC_PER_SOURCE = {(256, 256, 300, "f32"): 921.7e6}
+
+#: Warp instructions executed by one fused-step launch per source
+#: (smsp__inst_executed.sum of the same ncu capture), for the issue-side
+#: roofline: a launch of nsrc sources issues this many times nsrc.
+MEASURED_FUSED_WARP_INST_PER_SOURCE = {(256, 256, 300, "f32"): 517.5e6}
 
 
 def fused_traffic_per_launch(p):
     v = MEASURED_FUSED_TRAFFIC_PER_SOURCE.get((p.nx, p.ny, p.nz, p.precision))
+    return None if v is None else v * p.nsrc
+
+
+def fused_warp_inst_per_launch(p):
+    v = MEASURED_FUSED_WARP_INST_PER_SOURCE.get((p.nx, p.ny, p.nz, p.precision))
     return None if v is None else v * p.nsrc

@@ -220,6 +220,10 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
             const int v = atoi(e);
             if (v == 2 || v == 4 || (v == 8 && fused_fits(8, c->nz, c->nzpml))) c->fused_pencils = v;
         }
+        // SPARC_TEST_FUSED_NO_TABLE_COPY: the fused step issues no z-table
+        // copy, so its bounded wait runs out with nothing in flight (a switch
+        // the tests use to exercise the timeout path)
+        c->fused_test_nocopy = getenv("SPARC_TEST_FUSED_NO_TABLE_COPY") != nullptr;
         if (c->use_fused &&
             (rc = dalloc(c, (void**)&c->ftab, (size_t)FZ_COUNT * fused_nzp(c->nz) * 4))) return bail(rc);
         if ((rc = dalloc(c, (void**)&c->zt64, (size_t)ZT_COUNT * c->nz * 8))) return bail(rc);
@@ -834,6 +838,8 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
         Fz.clk = A.clk;
         Fz.pencils = c->fused_pencils;
         Fz.err = c->d_flag + 1;
+        Fz.no_copy = c->fused_test_nocopy;
+        Fz.wait_limit = c->fused_test_nocopy ? 64 : (1 << 22);
     }
     for (int it = 0; it < nsteps; ++it) {
         if (fused) {

@@ -41,6 +41,7 @@ struct sparc_ctx {
     float* ftab = nullptr;                        // fused FP32 step: z table [FZ_COUNT][fused_nzp(nz)]
     int use_fused = 0;
     int fused_pencils = 4;                        // modes per CTA of the fused step (autotuned)
+    int fused_test_nocopy = 0;                    // test switch: the fused step's table copy is not issued
     int stage_block = 128;                        // threads per CTA of the per-stage kernels (autotuned)
     double* zt64 = nullptr; double* pt64 = nullptr;
     double* tw_x = nullptr; double* tw_y = nullptr;

@@ -203,6 +203,17 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
 }
 
+// Poll phase 0 of an mbarrier at most `limit` times; true once it completed.
+__device__ __forceinline__ bool mbar_wait(unsigned mbar, int limit) {
+    unsigned done = 0;
+    for (int it = 0; it < limit && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(mbar)
+                     : "memory");
+    return done != 0;
+}
+
 __device__ __forceinline__ int pmlidx(int j, int nz, int nb, int nt) {
     return j < nb ? j : (j >= nz - nt ? nb + (j - (nz - nt)) : -1);
 }
@@ -281,10 +292,14 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
-                     ::"r"(dst), "l"(A.ftab), "r"(bytes), "r"(mbar)
-                     : "memory");
+        if (!A.no_copy) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                "l"(A.ftab), "r"(bytes), "r"(mbar)
+                : "memory");
+        }
     }
     // ---- zero the ghost and padding rows of the tile and the exchange lines ----
     {
@@ -333,14 +348,16 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         lagi[threadIdx.x] = id < 0 ? 0 : id;
     }
     __syncthreads();                                      // the mbarrier is initialised
-    {
-        unsigned done = 0;
-        for (int it = 0; it < (1 << 22) && !done; ++it)
-            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}\n"
-                         : "=r"(done)
-                         : "r"(mbar)
-                         : "memory");
-        if (!done && threadIdx.x == 0) atomicExch(A.err, 1);
+    // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
+    // reports it and leaves without computing or storing (its modes keep the
+    // state of the previous step), thread 0 first waiting out a copy still in
+    // flight so that nothing lands in shared memory after the CTA has gone
+    if (__syncthreads_or(!mbar_wait(mbar, A.wait_limit))) {
+        if (threadIdx.x == 0) {
+            atomicExch(A.err, 1);
+            if (!A.no_copy) mbar_wait(mbar, 1 << 22);
+        }
+        return;
     }
 
     const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;

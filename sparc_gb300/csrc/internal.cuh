@@ -360,6 +360,8 @@ struct FusedArgs {
     SlotClock clk;
     int pencils;        // modes per CTA: 2, 4 or 8 (same results; a tuning choice)
     int* err;           // set to 1 if the bounded wait for the z-table bulk copy gave up
+    int wait_limit;     // polls of that wait before it gives up
+    int no_copy;        // test switch: issue no bulk copy, so the wait runs out with nothing in flight
 };
 constexpr int FUSED_CH = 5;
 void fused_prepare(int nz, int nzpml);

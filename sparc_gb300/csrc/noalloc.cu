@@ -39,10 +39,15 @@ bool g_ready[kMaxDevices];
 int scratch_address(void** out, std::string& why) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (e != cudaSuccess) {
         why = std::string("cudaGetDevice failed: ") + cudaGetErrorString(e);
         cudaGetLastError();
         return SPARC_ECUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        why = "device index " + std::to_string(dev) + " is outside the no-allocation address table (devices 0.." +
+              std::to_string(kMaxDevices - 1) + ")";
+        return SPARC_EINVAL;
     }
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_ready[dev]) {

@@ -22,3 +22,8 @@ def test_reference_arm_line():
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert cb["production"]["value"] > 0 and cb["production"]["cores"] >= 1
+    # the line's labels agree with each other: value = point-steps of one
+    # bench step of the named workload / ms_per_step
+    pts = line["config"]["point_steps_per_step"]
+    assert abs(pts / (line["ms_per_step"] * 1e-3) / 1e6 - line["value"]) <= 1e-9 * line["value"]
+    assert line["sample"]["kernel_accumulation_ms"] > 0 and line["sample"]["forward_step_ms"] > 0

@@ -1,0 +1,164 @@
+"""Direct parity with the FP64 oracle at the benchmark configurations, not
+through the small cases: the CUDA path (C ABI) and the oracle advance the same
+seeded state with the same forward source.
+
+* 128x128x150 quiet Sun (the 1-h configuration), 31 steps: crosses the
+  30-step horizontal filter and records three surface planes;
+* 256x256x300 quiet Sun (the bench grid), 3 steps;
+* 256x256x300 flux tube (option 10), 2 steps.
+
+Tolerances: FP64 <= 1e-10 relative L2 per field, PML auxiliary and record.
+FP32 (the fused step at the quiet-Sun grids, the physical-space path for the
+flux tube) against the same FP64 oracle: state <= 2e-5 relative L2 per field
+(1e-4 for the flux tube), surface seismograms <= 1e-4."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import rel_l2, smooth_state
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+
+
+@pytest.fixture(scope="module")
+def oracle_mod():
+    from oracle import oracle
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    return oracle
+
+
+def _quiet(p):
+    from sparc_gb300.background import polytrope_table
+    return polytrope_table(p.nz)
+
+
+def _oracle_run(oracle_mod, p, tab, a0, pml0, plane, series, nsteps, bg=None):
+    """The oracle's state after nsteps, and its surface v_z after every step
+    on the output cadence (time 0, 15, 30, ...)."""
+    o = oracle_mod.Oracle(p, tab)
+    if bg is not None:
+        o.set_mhd(*bg)
+    o.set_state(a0, pml0)
+    o.set_source(1, plane[None].copy(), series)
+    orad = int(o.info()["o_rad"])
+    recs = []
+    for i in range(nsteps):
+        o.step(1)
+        if i % p.steps == 0:
+            a, _, _ = o.state()
+            recs.append(a[5, orad - 1].copy())
+    a, _, pml = o.state()
+    o.close()
+    return a, pml, np.array(recs)
+
+
+def _gpu_run(p, tab, a0, pml0, plane, series, nsteps, bg=None):
+    from sparc_gb300.solver import Solver
+    g = Solver(p, tab)
+    if bg is not None:
+        g.set_mhd_background(*bg)
+    g.set_state(a0, pml0)
+    g.set_source_series(plane, series)
+    g.record_surface(nsteps // p.steps + 2)
+    g.step(nsteps)
+    g.sync(check_finite=True)
+    a, pml = g.state()
+    recs = g.records()
+    g.close()
+    return a, pml, recs
+
+
+def _check(p, got, ref, tol_state, tol_rec, what):
+    (ag, pg, rg), (ao, po, ro) = got, ref
+    for f in range(6):
+        e = rel_l2(ag[f], ao[f])
+        assert e < tol_state, (what, "field", f, e)
+    for f in range(pg.shape[0]):
+        if np.abs(po[f]).max() > 0:
+            e = rel_l2(pg[f], po[f])
+            assert e < tol_state, (what, "pml", f, e)
+    n = min(len(rg), len(ro))
+    assert n == len(ro) >= 1, (what, len(rg), len(ro))
+    e = rel_l2(rg[:n, 0] if rg.ndim == 4 else rg[:n], ro[:n])
+    assert e < tol_rec, (what, "records", e)
+
+
+@pytest.fixture(scope="module")
+def config1(oracle_mod):
+    from sparc_gb300 import sources
+    from sparc_gb300.params import config_quiet_128
+    p = config_quiet_128()
+    tab = _quiet(p)
+    a0, pml0 = smooth_state(p, seed=101)
+    plane = sources.gaussian_plane(p, 1.0, 3.0, -2.0)
+    series = oracle_mod.forward_source(p, 200) * 1e3
+    ref = _oracle_run(oracle_mod, p, tab, a0, pml0, plane, series, 31)
+    return p, tab, a0, pml0, plane, series, ref
+
+
+def test_config1_fp64_31_steps(gpu_lib, config1):
+    p, tab, a0, pml0, plane, series, ref = config1
+    got = _gpu_run(p, tab, a0, pml0, plane, series, 31)
+    _check(p, got, ref, TOL64, TOL64, "128x128x150 FP64")
+
+
+def test_config1_fp32_fused_31_steps(gpu_lib, config1):
+    p, tab, a0, pml0, plane, series, ref = config1
+    got = _gpu_run(p.replace(precision="f32"), tab, a0, pml0, plane, series, 31)
+    _check(p, got, ref, 2e-5, 1e-4, "128x128x150 FP32 fused")
+
+
+@pytest.fixture(scope="module")
+def bench_grid(oracle_mod):
+    from sparc_gb300 import sources
+    from sparc_gb300.params import config_quiet_256
+    p = config_quiet_256()
+    tab = _quiet(p)
+    a0, pml0 = smooth_state(p, seed=202)
+    plane = sources.gaussian_plane(p, 1.0, -7.0, 11.0)
+    series = oracle_mod.forward_source(p, 200) * 1e3
+    ref = _oracle_run(oracle_mod, p, tab, a0, pml0, plane, series, 3)
+    return p, tab, a0, pml0, plane, series, ref
+
+
+def test_bench_grid_fp64_3_steps(gpu_lib, bench_grid):
+    p, tab, a0, pml0, plane, series, ref = bench_grid
+    got = _gpu_run(p, tab, a0, pml0, plane, series, 3)
+    _check(p, got, ref, TOL64, TOL64, "256x256x300 FP64")
+
+
+def test_bench_grid_fp32_fused_3_steps(gpu_lib, bench_grid):
+    p, tab, a0, pml0, plane, series, ref = bench_grid
+    got = _gpu_run(p.replace(precision="f32"), tab, a0, pml0, plane, series, 3)
+    _check(p, got, ref, 2e-5, 1e-4, "256x256x300 FP32 fused")
+
+
+@pytest.fixture(scope="module")
+def flux_tube(oracle_mod):
+    from sparc_gb300 import sources
+    from sparc_gb300.background import flux_tube_background
+    from sparc_gb300.params import config_quiet_256
+    p = config_quiet_256().replace(option=10, npmltop=0)
+    tab = _quiet(p)
+    bg = flux_tube_background(p, tab)
+    a0, pml0 = smooth_state(p, seed=303, scale=1e-6, npv=6)
+    plane = sources.gaussian_plane(p, 1.0, 20.0, 0.0)
+    series = oracle_mod.forward_source(p, 200) * 1e3
+    ref = _oracle_run(oracle_mod, p, tab, a0, pml0, plane, series, 2, bg=bg)
+    return p, tab, bg, a0, pml0, plane, series, ref
+
+
+def test_flux_tube_fp64_2_steps(gpu_lib, flux_tube):
+    p, tab, bg, a0, pml0, plane, series, ref = flux_tube
+    got = _gpu_run(p, tab, a0, pml0, plane, series, 2, bg=bg)
+    _check(p, got, ref, TOL64, TOL64, "flux tube FP64")
+
+
+def test_flux_tube_fp32_2_steps(gpu_lib, flux_tube):
+    p, tab, bg, a0, pml0, plane, series, ref = flux_tube
+    got = _gpu_run(p.replace(precision="f32"), tab, a0, pml0, plane, series, 2, bg=bg)
+    _check(p, got, ref, 1e-4, 1e-4, "flux tube FP32")

@@ -1,0 +1,140 @@
+"""The reference's one shipped configuration, on its own inputs.
+
+params.i with the Spectral / Adjoint Instruction files gives a 256x1x300
+box, 400 Mm wide, 2 s steps, PML 10 at the bottom; magnetic, so '2D' selects
+option 18, and option 17 without the field.  The background is the shipped
+`polytrope` table; the source sits at the master.pixels x; the adjoint source
+and MISFIT_ALL use the shipped ridge settings (data/params.0, params.1) and
+band corners (data/filter.params.0, .1).  These inputs reach the GPU machine as
+tests/golden/shipped_inputs.npz (written by tests/golden/make_shipped.py).
+
+* options 17 and 18, 31 steps from a seeded state with the shipped forward
+  source: CUDA path against the FP64 oracle, <= 1e-10 relative L2 per field
+  (FP64); the fused FP32 step of option 17 <= 2e-5;
+* a 2-hour forward run (4186 steps, 280 surface records) on the shipped
+  polytrope, "observed" data from the same run with the sound speed raised
+  by 0.3 %: the adjoint source (ADJOINT_SOURCE_FILT) and MISFIT_ALL of the
+  GPU against the numpy restatement in the oracle, <= 1e-10, identical
+  windows and measurement counts."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from cases import rel_l2, smooth_state
+
+pytestmark = pytest.mark.gpu
+TOL64 = 1e-10
+
+
+@pytest.fixture(scope="module")
+def shipped():
+    sys.path.insert(0, os.path.dirname(__file__))
+    from golden.make_shipped import load
+    return load()
+
+
+@pytest.fixture(scope="module")
+def oracle_mod():
+    from oracle import oracle
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    return oracle
+
+
+def _source(p, x00, oracle_mod):
+    from sparc_gb300 import sources
+    plane = sources.master_pixel_plane(p, x00)
+    series = sources.gabor_series(p, p.maxtime + 10) * 1e3
+    return plane, series
+
+
+@pytest.mark.parametrize("option,prec", [(17, "f64"), (17, "f32"), (18, "f64")])
+def test_shipped_31_steps_match_oracle(gpu_lib, oracle_mod, shipped, option, prec):
+    from sparc_gb300.background import flux_sheet_background
+    from sparc_gb300.solver import Solver
+    p = shipped["params"].replace(option=option)
+    tab = shipped["polytrope"]
+    npv = 6 if option == 18 else 2
+    a0, pml0 = smooth_state(p, seed=404 + option, scale=1e-6 if option == 18 else 1e-3, npv=npv)
+    plane, series = _source(p, shipped["x00"], oracle_mod)
+    bg = flux_sheet_background(p, tab) if option == 18 else None
+    o = oracle_mod.Oracle(p, tab)
+    g = Solver(p.replace(precision=prec), tab)
+    if bg is not None:
+        o.set_mhd2d(*bg)
+        g.set_mhd2d_background(*bg)
+    for s in (o, g):
+        s.set_state(a0, pml0)
+    o.set_source(1, plane[None].copy(), series)
+    g.set_source_series(plane, series)
+    o.step(31)
+    g.step(31)
+    g.sync(check_finite=True)
+    ao, _, po = o.state()
+    ag, pg = g.state()
+    tol = TOL64 if prec == "f64" else 2e-5
+    for f in (0, 2, 3, 5):
+        e = rel_l2(ag[f], ao[f])
+        assert e < tol, (option, prec, f, e)
+    for f in range(po.shape[0]):
+        if np.abs(po[f]).max() > 0:
+            assert rel_l2(pg[f], po[f]) < tol, (option, prec, "pml", f)
+    o.close()
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def two_hour_records(gpu_lib, oracle_mod, shipped):
+    """Surface v_z of a 2-hour option-17 forward run on the shipped polytrope
+    (the synthetic), and of the same run with c raised by 0.3 % (the
+    "observations"), both FP64 on the GPU."""
+    from sparc_gb300.solver import Solver
+    p = shipped["params"].replace(option=17)
+    plane, series = _source(p, shipped["x00"], oracle_mod)
+    out = []
+    for cscale in (1.0, 1.003):
+        tab = shipped["polytrope"].copy()
+        tab[:, 1] *= cscale
+        g = Solver(p, tab)
+        g.set_source_series(plane, series)
+        nrec = p.maxtime // p.steps + 1
+        g.record_surface(nrec)
+        g.step(p.maxtime + 1)
+        out.append(g.records()[:, 0, :])
+        g.close()
+    return p, out[0], out[1]
+
+
+def test_shipped_adjoint_source_matches_oracle(gpu_lib, shipped, two_hour_records):
+    from oracle import adjoint_source as A
+    from sparc_gb300.solver import Solver
+    p, syn, dat = two_hour_records
+    assert syn.shape == (p.maxtime // p.steps + 1, p.nx) and np.abs(syn).max() > 0
+    nt = syn.shape[0]
+    t = np.arange(nt) * (p.outputcad / 60.0)
+    x00, ridges, bands = shipped["x00"], shipped["ridges"], shipped["bands"]
+    s = Solver(p, shipped["polytrope"])
+    adj_g, mis_g, n_g, win_g = s.adjoint_source(dat, x00, t[0], t[1] - t[0], ridges, bands, synth=syn)
+    adj_o, mis_o, n_o, win_o, _ = A.adjoint_source_filt(syn, dat, p.xlength, p.outputcad, x00, t, ridges, bands)
+    assert n_g == n_o and n_g > 50
+    assert win_g == win_o
+    assert mis_o > 0 and abs(mis_g - mis_o) <= 1e-10 * mis_o
+    assert rel_l2(adj_g, adj_o) < TOL64, rel_l2(adj_g, adj_o)
+    s.close()
+
+
+def test_shipped_misfit_all_matches_oracle(gpu_lib, shipped, two_hour_records):
+    from oracle import adjoint_source as A
+    from sparc_gb300.solver import Solver
+    p, syn, dat = two_hour_records
+    nt = syn.shape[0]
+    t = np.arange(nt) * (p.outputcad / 60.0)
+    x00, ridges = shipped["x00"], shipped["ridges"]
+    s = Solver(p, shipped["polytrope"])
+    mg, ng, wg = s.misfit_all(dat, x00, t[0], t[1] - t[0], ridges, synth=syn)
+    mo, no, wo = A.misfit_all(syn, dat, p.xlength, p.outputcad, x00, t, ridges)
+    assert np.array_equal(ng, no) and ng.sum() > 50 and wg == wo
+    assert np.all(np.abs(mg - mo) <= 1e-10 * np.maximum(mo, 1e-300))
+    s.close()
