@@ -148,21 +148,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_pair(p, tab, nplanes, seed=0):
-    """Forward and adjoint solvers with seeded sources on every slot."""
+def source_inputs(p, nplanes, gi, seed=0):
+    """Seeded inputs of global source gi: forward source plane (a Gaussian at
+    a random surface position) and adjoint residuals at the receivers."""
+    from sparc_gb300 import sources
+    rng = np.random.default_rng([seed, gi])
+    x0, y0 = rng.uniform(-60, 60, size=2)
+    pix = sources.receiver_pixels(p)
+    res = rng.standard_normal((len(pix), nplanes)) * 1e-6
+    return sources.gaussian_plane(p, 1.0, x0, y0), sources.adjoint_planes(p, res, pix)
+
+
+def make_pair(p, tab, nplanes, src_ids, seed=0):
+    """Forward and adjoint solvers with the seeded sources src_ids (global
+    indices, one per slot)."""
     from sparc_gb300 import sources
     from sparc_gb300.solver import Solver
-    pf = p
     pa = p.replace(compute_forward=False, compute_adjoint=True)
-    fwd, adj = Solver(pf, tab), Solver(pa, tab)
-    rng = np.random.default_rng(seed)
+    fwd, adj = Solver(p, tab), Solver(pa, tab)
     series = sources.ricker_series(p, 20000)
-    pix = sources.receiver_pixels(p)
-    for s in range(p.nsrc):
-        x0, y0 = rng.uniform(-60, 60, size=2)
-        fwd.set_source_series(sources.gaussian_plane(p, 1.0, x0, y0), series, slot=s)
-        res = rng.standard_normal((len(pix), nplanes)) * 1e-6
-        adj.set_source_lagrange(sources.adjoint_planes(p, res, pix), slot=s)
+    for s, gi in enumerate(src_ids):
+        plane, adjp = source_inputs(p, nplanes, gi, seed)
+        fwd.set_source_series(plane, series, slot=s)
+        adj.set_source_lagrange(adjp, slot=s)
     return fwd, adj
 
 
@@ -387,21 +395,39 @@ def _hbm_peak() -> float:
     return 6800.0
 
 
-def mhd_section(p0, tab, steps=5, warmup=2, precs=("f64", "f32")):
-    """The flux-tube configuration: linearised MHD (option 10) at the bench
-    grid on a 2 kG, 3 Mm self-similar tube, one source, forward steps in FP64
-    and FP32 (device time per step, CUDA events on the context's stream)."""
+def mhd_section(steps=5, warmup=2, precs=("f64", "f32"), grid=None, acc_steps=150):
+    """The flux-tube configuration: linearised MHD (option 10) at 256x256x300
+    on the magnetohydrostatic flux tube (2 kG and 3 Mm at its narrowest,
+    box top at the surface), one source 20 Mm from the axis.  Per precision:
+    device time per forward step (CUDA events on the context's stream, after
+    `warmup` steps), then the run continued to acc_steps steps with surface
+    records every output; FP32 is stated against FP64 on those records (the
+    seismograms) and on the final state."""
     import torch
     from sparc_gb300 import bytes_model, sources
-    from sparc_gb300.background import flux_tube_background
+    from sparc_gb300.background import config3_background, polytrope_table
+    from sparc_gb300.params import config_flux_tube_256
     from sparc_gb300.solver import Solver
-    pm = p0.replace(option=10, npmltop=0, nsrc=1)
-    bg = flux_tube_background(pm, tab)
-    out = {"grid": [pm.nx, pm.ny, pm.nz], "background": "self-similar flux tube, 2 kG, 3 Mm at z = 0"}
+    pm, tab = config_flux_tube_256()
+    if grid:
+        pm = pm.replace(nx=grid[0], ny=grid[1], nz=grid[2])
+        tab = polytrope_table(grid[2], z_bot_mm=-25.0, z_top_mm=0.0)
+    pm = pm.replace(nsrc=1)
+    out = {"grid": [pm.nx, pm.ny, pm.nz]}
+    bg = None
+    res = {}
     for prec in precs:
         s = Solver(pm.replace(precision=prec), tab)
+        if bg is None:
+            t0 = time.perf_counter()
+            bg, info = config3_background(pm, tab, s.ddz)     # FP64 set-up, the context's FP64 d/dz
+            info["setup_s"] = time.perf_counter() - t0
+            out["background"] = {"what": "magnetohydrostatic flux tube from an azimuthal vector potential, "
+                                         "2 kG and 3 Mm at z = -8 Mm, widening over 8 Mm; box -25..0 Mm",
+                                 **info}
         s.set_mhd_background(*bg)
         s.set_source_series(sources.gaussian_plane(pm, 1.0, 20.0, 0.0), sources.ricker_series(pm, 4000))
+        s.record_surface(acc_steps // pm.steps + 2)
         s.step(warmup)
         s.sync()
         st = torch.cuda.ExternalStream(s.stream_ptr)
@@ -416,7 +442,22 @@ def mhd_section(p0, tab, steps=5, warmup=2, precs=("f64", "f32")):
         out[prec] = {"ms_per_step": ms, "value": pm.points / (ms * 1e-3) / 1e6, "unit": UNIT,
                      "alg_bytes_per_point_step": bps, "hbm_achieved_gbs": gbs,
                      "hbm_frac": gbs / _hbm_peak()}
+        if acc_steps > warmup + steps:
+            s.step(acc_steps - warmup - steps)
+            s.sync(check_finite=True)
+            res[prec] = (s.records(), s.state()[0])
         s.close()
+    if "f64" in res and "f32" in res:
+        (r64, a64), (r32, a32) = res["f64"], res["f32"]
+
+        def rel(x, y):
+            return float(np.linalg.norm((x - y).ravel()) / max(np.linalg.norm(y.ravel()), 1e-300))
+
+        out["accuracy"] = {"steps": acc_steps, "records": int(r64.shape[0]),
+                           "seismogram_rel_l2": rel(r32, r64),
+                           "state_rel_l2": [rel(a32[f], a64[f]) for f in range(6)],
+                           "what": "FP32 against FP64 on the same inputs: surface v_z records every output "
+                                   "and the six fields after acc_steps steps"}
     return out
 
 
@@ -476,11 +517,13 @@ def cpu_production(n: int | None = None, steps: int = 1):
                       f"{steps} timed step(s) each after one warm-up, {span:.1f} s span"}
 
 
-def arm_config(p0, cad, S, nplanes):
+def arm_config(p0, cad, S, nplanes, ws=1):
     """The workload both arms name (the reference arm times a bounded sample of it)."""
     return {"workload": f"quiet-Sun {p0.nx}x{p0.ny}x{p0.nz} forward+adjoint time step with "
-                        f"sensitivity-kernel accumulation every {cad} steps, {S} sources batched",
+                        f"sensitivity-kernel accumulation every {cad} steps, {S} sources batched per GPU",
             "grid": [p0.nx, p0.ny, p0.nz], "nsrc": S, "point_steps_per_step": 2 * p0.points * S,
+            "sources_global": S * ws, "sharding": "sources round-robin over the ranks; kernels summed by one "
+                                                  "FP64 all-reduce in device memory",
             "l2": "inputs larger than L2 (state of each context > 30 GB)",
             "adjoint_source_samples": nplanes}
 
@@ -563,15 +606,13 @@ def main():
     from sparc_gb300 import build as b
     b.build()
     from sparc_gb300 import bytes_model
+    from sparc_gb300 import dist as sd
     p0, tab = workload(args.small)
     if args.mhd_only:
-        if args.mhd_grid:
-            from sparc_gb300.background import polytrope_table
-            nx, ny, nz = (int(v) for v in args.mhd_grid.lower().split("x"))
-            p0 = p0.replace(nx=nx, ny=ny, nz=nz)
-            tab = polytrope_table(nz, z_bot_mm=-25.0, z_top_mm=1.2)
-        print(json.dumps({"mhd": mhd_section(p0, tab, steps=max(1, args.steps), warmup=max(1, args.warmup),
-                                             precs=tuple(args.mhd_prec.split(",")))}), flush=True)
+        grid = tuple(int(v) for v in args.mhd_grid.lower().split("x")) if args.mhd_grid else None
+        print(json.dumps({"mhd": mhd_section(steps=max(1, args.steps), warmup=max(1, args.warmup),
+                                             precs=tuple(args.mhd_prec.split(",")), grid=grid, acc_steps=0)}),
+              flush=True)
         return 0
     K, W = max(1, args.steps), max(3, args.warmup)
     peaks = {}
@@ -588,7 +629,7 @@ def main():
     log("plain FP64")
     if not args.skip_fp64:
         p64 = p0.replace(precision="f64", nsrc=1)
-        fwd, adj = make_pair(p64, tab, args.nplanes, seed=rank)
+        fwd, adj = make_pair(p64, tab, args.nplanes, sd.shard_sources(ws, rank, ws), seed=1)
         cad = fwd.info()["steps"]
         tuning64 = {"forward": fwd.autotune(1), "adjoint": adj.autotune(1)}
         run_steps(fwd, adj, W, cad)
@@ -605,9 +646,11 @@ def main():
 
     # ---- batched FP32 ----
     log("batched FP32")
+    # the global source list (nsrc per rank) split round-robin over the ranks
     S = args.nsrc
+    mine = sd.shard_sources(S * ws, rank, ws)
     p32 = p0.replace(precision="f32", nsrc=S)
-    fwd, adj = make_pair(p32, tab, args.nplanes, seed=1000 + rank)
+    fwd, adj = make_pair(p32, tab, args.nplanes, mine, seed=2)
     cad = fwd.info()["steps"]
     # launch variants with identical results, picked by timing real steps
     # (part of the warm-up: 4 steps per context)
@@ -649,8 +692,6 @@ def main():
         from sparc_gb300 import sources
         from sparc_gb300.solver import Solver
         pa = p32.replace(compute_forward=False, compute_adjoint=True)
-        rng = np.random.default_rng(7)
-        pix = sources.receiver_pixels(p32)
         series = sources.ricker_series(p32, 20000)
 
         def pinned(shape):
@@ -658,11 +699,11 @@ def main():
 
         plane_h = [pinned((p32.ny, p32.nx)) for _ in range(S)]
         adj_h = [pinned((args.nplanes, p32.ny, p32.nx)) for _ in range(S)]
-        for s in range(S):
-            x0, y0 = rng.uniform(-60, 60, size=2)
-            plane_h[s][...] = sources.gaussian_plane(p32, 1.0, x0, y0)
-            adj_h[s][...] = sources.adjoint_planes(p32, rng.standard_normal((len(pix), args.nplanes)) * 1e-6, pix)
+        for s, gi in enumerate(mine):
+            plane_h[s][...], adj_h[s][...] = source_inputs(p32, args.nplanes, gi, seed=3)
         fwd, adj = Solver(p32, tab), Solver(pa, tab)
+        ksum = torch.empty((3, p32.nz, p32.ny, p32.nx), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
         Ke = max(K, cad)                      # at least one kernel accumulation (every cad steps)
         nrec = Ke // cad + 2
         rec_h = pinned((nrec, p32.ny, p32.nx))
@@ -679,9 +720,16 @@ def main():
             r = fwd.records(slot=s)
             rec_h[: r.shape[0]] = r
             d2h += r.nbytes
-        kc, kr, hs = adj.kernels(sum_slots=True)
-        k_h[0][...] = kc; k_h[1][...] = kr; k_h[2][...] = hs
-        d2h += 3 * kc.nbytes
+        # kernels summed over this rank's sources into device memory, then
+        # over all ranks by one FP64 all-reduce (grad.py:158-165), then one
+        # device-to-host copy
+        adj.kernels_into(ksum.data_ptr(), sum_slots=True)
+        adj.sync()
+        sd.reduce_kernels(ksum)
+        kd = ksum.cpu().numpy()
+        for i in range(3):
+            k_h[i][...] = kd[i]
+        d2h += kd.nbytes
         dt = time.perf_counter() - t0
         h2d = S * (plane_h[0].nbytes + series.nbytes + adj_h[0].nbytes)
         e2e = {"value": 2 * N * S * Ke * ws / dt / 1e6, "unit": UNIT,
@@ -693,7 +741,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (f64 set-up and kernel accumulation)", "data": "synthetic",
-        "config": arm_config(p0, cad, S, args.nplanes),
+        "config": arm_config(p0, cad, S, args.nplanes, ws),
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -740,7 +788,7 @@ def main():
     if ws == 1 and not args.skip_mhd:
         log("MHD flux tube")
         try:
-            line["mhd"] = mhd_section(p0, tab)
+            line["mhd"] = mhd_section(grid=(p0.nx, p0.ny, p0.nz) if args.small else None)
         except Exception as e:   # reported, not fatal
             line["mhd"] = {"error": str(e)}
     if args.serve_requests > 0 and ws == 1:

@@ -247,6 +247,15 @@ int sparc_gpu_kernel_reset(sparc_ctx* adj);
 int sparc_gpu_kernels(sparc_ctx* adj, int src_idx, int sum_slots, double* kc, double* krho,
                       double* hessian);
 
+/* The same final scaling into a caller-owned DEVICE buffer of 3*nx*ny*nz
+ * doubles: K_c, K_rho, hessian, each (nz,ny,nx).  The work is enqueued on
+ * the context's stream (sparc_gpu_stream) and the call returns without
+ * waiting: a caller that reads `dev_out` from another stream orders it after
+ * that stream first.  This is the form a multi-GPU driver sums across ranks
+ * with one FP64 all-reduce in device memory (grad.py:158-165 sums the
+ * per-source kernel files on the host). */
+int sparc_gpu_kernels_device(sparc_ctx* adj, int src_idx, int sum_slots, double* dev_out);
+
 /* Option 18 (2-D MHD): the B-field kernels of the MAGNETIC_KERNELS block
  * (kernels.f90:337-453) accumulated beside K_c, K_rho and the hessian, with
  * B0 and curl B0 formed as kernel mode forms them from the vector potential
@@ -302,7 +311,7 @@ int sparc_gpu_misfit_all(sparc_ctx* ctx, int src_idx, const double* synth, const
 /* ---- model update of an inversion iteration (grad.py) --------------------- */
 
 /* Replaces grad.py:152-186 (the kernel sums are the caller's, as grad.py
- * reads them from kernel/*.fits).  Host arrays (nz,ny,nx) of the context's
+ * reads them from the kernel_*.fits files).  Host arrays (nz,ny,nx) of the context's
  * grid, FP64: kc_sum = sum of kernel_c, kpsi_sum = sum of kernel_vectorpsi,
  * hess_sum = sum of |hessian| over the sources; rho_z[nz] the density
  * column of the background (the third column of the polytrope file).

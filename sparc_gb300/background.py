@@ -131,6 +131,131 @@ def flux_tube_background(p, table: np.ndarray, b_surf: float = 2000.0, r_surf_mm
     return rho, c, pres, bx, by, bz
 
 
+def _dxdy(nx: int, ny: int, lx: float, ly: float):
+    """Spectral d/dx and d/dy (cm) of real (nz, ny, nx) fields; the Nyquist
+    multipliers are 0, as the reference's c2r gives them."""
+    kx = 2.0 * np.pi * np.fft.rfftfreq(nx, d=lx / nx)
+    if nx % 2 == 0:
+        kx[-1] = 0.0
+    ky = 2.0 * np.pi * np.fft.fftfreq(ny, d=ly / ny)
+    if ny % 2 == 0:
+        ky[ny // 2] = 0.0
+
+    def dx(f):
+        return np.fft.irfft(np.fft.rfft(f, axis=2) * (1j * kx)[None, None, :], n=nx, axis=2)
+
+    def dy(f):
+        return np.fft.ifft(np.fft.fft(f, axis=1) * (1j * ky)[None, :, None], axis=1).real
+
+    return dx, dy
+
+
+def mhs_flux_tube_background(p, table: np.ndarray, ddz, b0: float = 2000.0, r0_mm: float = 3.0,
+                             z_min_mm: float = -8.0, d_mm: float = 8.0, x0_mm: float = 0.0, y0_mm: float = 0.0):
+    """Axisymmetric magnetic flux tube in magnetohydrostatic balance on the
+    quiet column (the 3-D form of code_python/tubex.py:46-90), as the cgs
+    arrays a magnetic run reads (rho, c, p, B_x, B_y, B_z; READ_IN_FIELD,
+    all_modules.f90:486-513), each (nz, ny, nx), FP64.
+
+    Field: B = curl(A_phi e_phi) with
+        A_phi(r, z) = (Phi / 2 pi r) (1 - exp(-r^2 / R(z)^2)),  Phi = pi b0 R0^2,
+    i.e. B_z = (Phi / pi R^2) exp(-r^2/R^2), B_r = r B_z R'(z) / R, taken
+    analytically: divergence-free, flux Phi at every height.  The radius
+    R(z) = R0 sqrt(1 + ((z - z_min) / D)^2) is narrowest (R0, axis field b0)
+    at z_min and widens smoothly above and below (R R'' <= R0^2 / D^2), so
+    the tube's curvature forces stay a fraction of its pressure deficit.
+    Balance: with the Lorentz force F = (curl B) x B / 4 pi formed by the
+    solver's own operators (spectral d/dx, d/dy; d/dz the compact scheme
+    with ibc 1, ddz(f, 1) / ddz(z, 1) as tubex.py:14-17 forms it),
+      * p solves the horizontal balance grad_h p = F_h in the least-squares
+        sense on each plane (div_h grad_h p = div_h F_h, FFT), pinned to the
+        table's p at the box corner, far from the tube (tubex.py:71-73);
+      * rho = (F_z - dp/dz) / g balances the vertical force, pinned the same
+        way to the table's rho (tubex.py:84-86): far from the tube the column
+        is the table's, whose own hydrostatic residual is kept as it is;
+      * c^2 = c_q^2 rho_q / p_q * p / rho (tubex.py:98).
+    ddz(f, bc): the FP64 compact z derivative of an (nz, ny, nx) array of
+    this grid (Solver.ddz of any context on this table).
+
+    Returns ((rho, c, p, bx, by, bz), info).  info holds the force-balance
+    residual R = grad p - F - rho g (g pointing down) relative to the largest
+    Lorentz force, with the table's own hydrostatic residual Q(z) taken out
+    of R_z, and the smallest p / p_q and rho / rho_q.  A tube the column
+    cannot hold (p or rho <= 0 anywhere) raises ValueError.
+    """
+    nx, ny, nz = p.nx, p.ny, p.nz
+    z = (table[:, 0] - 1.0) * RSUN_CM
+    c_q, rho_q, p_q, g_q = table[:, 1], table[:, 2], table[:, 3], table[:, 4]
+    dz_idx = ddz(np.ascontiguousarray(np.broadcast_to(z[:, None, None], (nz, ny, nx))), 1)[:, :1, :1]
+
+    def dz(f):
+        return ddz(np.ascontiguousarray(f), 1) / dz_idx
+
+    dx, dy = _dxdy(nx, ny, p.xlength, p.ylength)
+    r0, zm, dd = r0_mm * 1e8, z_min_mm * 1e8, d_mm * 1e8
+    u = (z - zm) / dd
+    R = r0 * np.sqrt(1.0 + u * u)
+    dR = r0 * u / (dd * np.sqrt(1.0 + u * u))
+    phi = np.pi * b0 * r0 * r0
+    x = (np.arange(nx) / nx - 0.5) * p.xlength - x0_mm * 1e8
+    y = (np.arange(ny) / ny - 0.5) * p.ylength - y0_mm * 1e8
+    X, Y = np.meshgrid(x, y)
+    E = np.exp(-(X * X + Y * Y)[None] / (R * R)[:, None, None])
+    bz = (phi / (np.pi * R * R))[:, None, None] * E
+    br_r = (phi * dR / (np.pi * R ** 3))[:, None, None] * E         # B_r / r
+    bx = br_r * X[None]
+    by = br_r * Y[None]
+    del E, br_r
+    jx = dy(bz) - dz(by)
+    jy = dz(bx) - dx(bz)
+    jz = dx(by) - dy(bx)
+    f4 = 4.0 * np.pi
+    fx = (jy * bz - jz * by) / f4
+    fy = (jz * bx - jx * bz) / f4
+    fz = (jx * by - jy * bx) / f4
+    del jx, jy, jz
+    # horizontal balance: div_h grad_h p = div_h F_h per plane (FFT over y, x)
+    kx = 2.0 * np.pi * np.fft.fftfreq(nx, d=p.xlength / nx)
+    ky = 2.0 * np.pi * np.fft.fftfreq(ny, d=p.ylength / ny)
+    k2 = kx[None, :] ** 2 + ky[:, None] ** 2
+    k2[0, 0] = 1.0
+    div = np.fft.fft2(fx) * (1j * kx)[None, None, :] + np.fft.fft2(fy) * (1j * ky)[None, :, None]
+    ptil = np.fft.ifft2(-div / k2[None]).real
+    del div
+    pres = p_q[:, None, None] + (ptil - ptil[:, :1, :1])
+    del ptil
+    dzp = dz(pres)
+    rho = (fz - dzp) / g_q[:, None, None]
+    rho = rho - (rho[:, :1, :1] - rho_q[:, None, None])
+    if pres.min() <= 0.0 or rho.min() <= 0.0:
+        raise ValueError(f"the column cannot hold this tube: min p/p_q = {(pres / p_q[:, None, None]).min():.3g}, "
+                         f"min rho/rho_q = {(rho / rho_q[:, None, None]).min():.3g}")
+    c = np.sqrt((c_q ** 2 * rho_q / p_q)[:, None, None] * pres / rho)
+    # residual of grad p = F + rho g, the table's own hydrostatic residual
+    # (the same in the quiet column) taken out of the z component
+    q = dz(np.broadcast_to(p_q[:, None, None], (nz, ny, nx)))[:, :1, :1] + (rho_q * g_q)[:, None, None]
+    rx = dx(pres) - fx
+    ry = dy(pres) - fy
+    rz = dzp - fz + rho * g_q[:, None, None] - q
+    fmag = np.sqrt(fx * fx + fy * fy + fz * fz)
+    fmax = float(fmag.max())
+    info = {
+        "lorentz_max_dyn_cm3": fmax,
+        "residual_h_max_rel": float(max(np.abs(rx).max(), np.abs(ry).max()) / fmax) if fmax > 0 else 0.0,
+        "residual_z_max_rel": float(np.abs(rz).max() / fmax) if fmax > 0 else 0.0,
+        "residual_l2_rel": float(np.sqrt(np.sum(rx * rx + ry * ry + rz * rz)) / np.sqrt(np.sum(fmag * fmag)))
+        if fmax > 0 else 0.0,
+        "table_hydrostatic_residual_rel": float(np.abs(q).max() / np.abs(rho_q * g_q).max()),
+        "min_p_ratio": float((pres / p_q[:, None, None]).min()),
+        "min_rho_ratio": float((rho / rho_q[:, None, None]).min()),
+        "b_axis_max_G": float(np.abs(bz).max()),
+        "b_axis_top_G": float(bz[-1].max()),
+        "beta_axis_top": float(8.0 * np.pi * pres[-1].min() / max(bz[-1].max() ** 2, 1e-300)),
+        "radius_top_mm": float(R[-1] / 1e8),
+    }
+    return (rho, c, pres, bx, by, bz), info
+
+
 def flux_sheet_background(p, table: np.ndarray, b_surf: float = 300.0, w_mm: float = 10.0,
                           z_fade_mm: float = 0.0, fade_mm: float = 0.2, x0_mm: float = 0.0,
                           p_floor: float = 0.2):
@@ -301,3 +426,11 @@ def write_vector_potential_models(modeldir: str, models: dict) -> list:
         put(os.path.join(d, "soundspeed2D.fits"), models["c"])
     put(os.path.join(st, "model_c_ls00.fits"), models["c"])
     return out
+
+
+def config3_background(p, table: np.ndarray, ddz):
+    """The flux-tube configuration's background: the magnetohydrostatic
+    tube of mhs_flux_tube_background with its defaults (2 kG and 3 Mm at
+    z = -8 Mm, widening over D = 8 Mm; about 1 kG and 4.2 Mm at the
+    surface), on the box centre.  Returns ((rho, c, p, bx, by, bz), info)."""
+    return mhs_flux_tube_background(p, table, ddz)

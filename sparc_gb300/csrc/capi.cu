@@ -69,6 +69,75 @@ Tri tri_for(int nz, int ibc) {
     return t;
 }
 
+// Elimination rows of the fused step for boundary code ibc (FP64): 1/betad,
+// the forward multipliers m, their products H from each chunk's first level,
+// the backward multipliers g and their products G from each chunk's last
+// level (chunks of FUSED_CH levels; padding levels up to nzp are zero).
+struct FusedRows {
+    std::vector<double> ibd, mm, HH, gg, GG;
+};
+FusedRows fused_rows(int nz, int nzp, const Tri& t) {
+    FusedRows r;
+    r.ibd.assign(nzp, 0.0); r.mm.assign(nzp, 0.0); r.gg.assign(nzp, 0.0); r.HH.assign(nzp, 0.0);
+    r.GG.assign(nzp, 0.0);
+    for (int j = 0; j < nz; ++j) {
+        r.ibd[j] = 1.0 / t.betad[j];
+        r.mm[j] = (j == 0) ? 0.0 : -t.low[j] / t.betad[j];
+        r.gg[j] = (j == nz - 1) ? 0.0 : -t.gam[j + 1];
+    }
+    for (int j0 = 0; j0 < nzp; j0 += FUSED_CH) {
+        const int j1 = j0 + FUSED_CH;
+        double pr = 1.0;
+        for (int j = j0; j < j1; ++j) { pr *= r.mm[j]; r.HH[j] = pr; }
+        pr = 1.0;
+        for (int j = j1 - 1; j >= j0; --j) { pr *= r.gg[j]; r.GG[j] = pr; }
+    }
+    return r;
+}
+
+// Look-back products of the fused step's carries: fwd[4t + i-2] is the
+// product of the chunk multipliers Mc(t-1)..Mc(t-i+1) (i = 2..5), the factor
+// of chunk t-i's value in the carry into chunk t; bwd[4t + i-2] likewise with
+// the backward chunk multipliers Gc(t+1)..Gc(t+i-1) for chunk t+i.  Returns
+// the largest product over FUSED_KB chunks, the factor of the first chunk the
+// carries leave out, over the chunks that hold real levels (the carries into
+// padding chunks reach no real row: their H and G rows are zero).
+double fused_lookback(const FusedRows& r, int tp, int nz, std::vector<double>& fwd, std::vector<double>& bwd) {
+    std::vector<double> Mc(tp), Gc(tp);
+    for (int t = 0; t < tp; ++t) {
+        Mc[t] = r.HH[t * FUSED_CH + FUSED_CH - 1];
+        Gc[t] = r.GG[t * FUSED_CH];
+    }
+    fwd.assign((size_t)4 * tp, 0.0);
+    bwd.assign((size_t)4 * tp, 0.0);
+    double worst = 0.0;
+    for (int t = 0; t < tp; ++t) {
+        double pf = 1.0, pb = 1.0;
+        for (int i = 2; i <= FUSED_KB + 1; ++i) {
+            pf = (t - i + 1 >= 0) ? pf * Mc[t - i + 1] : 0.0;
+            pb = (t + i - 1 < tp) ? pb * Gc[t + i - 1] : 0.0;
+            if (i <= FUSED_KB) {
+                fwd[(size_t)4 * t + i - 2] = pf;
+                bwd[(size_t)4 * t + i - 2] = pb;
+            } else if (t * FUSED_CH < nz) {
+                worst = std::max(worst, std::max(std::fabs(pf), std::fabs(pb)));
+            }
+        }
+    }
+    return worst;
+}
+
+// Whether the look-back carries of the fused step are exact to the stated
+// bound for the two boundary codes of a form (xi_z and p')
+bool fused_lookback_ok(int nz, int bcx, int bcp) {
+    const int nzp = fused_nzp(nz), tp = nzp / FUSED_CH;
+    for (int b : {bcx, bcp}) {
+        std::vector<double> f, g;
+        if (fused_lookback(fused_rows(nz, nzp, tri_for(nz, b)), tp, nz, f, g) > FUSED_LOOKBACK_BOUND) return false;
+    }
+    return true;
+}
+
 // ddz of one z-profile (dbyd2 + stretch), divisions as in mtridag.f90:100-107
 void host_dbyd2(const std::vector<double>& b, std::vector<double>& a, int ibc, const Compact<double>& cc,
                 const Tri& t) {
@@ -204,7 +273,8 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     if (c->f32) {
         // the fused step covers the quiet displacement forms (options 4, 17)
         c->use_fused = fused_supported(c->nz) && (p->option == 4 || p->option == 17) &&
-                       getenv("SPARC_FP32_PER_STAGE") == nullptr;
+                       getenv("SPARC_FP32_PER_STAGE") == nullptr &&
+                       fused_lookback_ok(c->nz, p->option == 4 ? 1 : 3, p->option == 4 ? 0 : 2);
         // modes per CTA of the fused step before any autotuning: 8 (one
         // 512-thread CTA per SM) when it fits and the grid still gives every SM
         // two CTAs, else 4; SPARC_FUSED_MODES forces a shape (a switch the tests
@@ -490,24 +560,19 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
             }
             const int bcs[2] = {d3 ? 1 : 3, d3 ? 0 : 2};
             const int base[2] = {FZ_SX, FZ_SP};
+            const int lbase[2] = {FZ_LX, FZ_LP};
+            const int tp = NZP / FUSED_CH;
             for (int k = 0; k < 2; ++k) {
-                const int b = bcs[k];
-                std::vector<double> ibd(NZP, 0.0), mm(NZP, 0.0), gg(NZP, 0.0), HH(NZP, 0.0), GG(NZP, 0.0);
-                for (int j = 0; j < nz; ++j) {
-                    ibd[j] = 1.0 / tri[b].betad[j];
-                    mm[j] = (j == 0) ? 0.0 : -tri[b].low[j] / tri[b].betad[j];
-                    gg[j] = (j == nz - 1) ? 0.0 : -tri[b].gam[j + 1];
-                }
-                for (int j0 = 0; j0 < NZP; j0 += FUSED_CH) {
-                    const int j1 = j0 + FUSED_CH;
-                    double pr = 1.0;
-                    for (int j = j0; j < j1; ++j) { pr *= mm[j]; HH[j] = pr; }
-                    pr = 1.0;
-                    for (int j = j1 - 1; j >= j0; --j) { pr *= gg[j]; GG[j] = pr; }
-                }
-                const std::vector<double>* rows[5] = {&ibd, &mm, &HH, &gg, &GG};
+                const FusedRows fr = fused_rows(nz, NZP, tri[bcs[k]]);
+                const std::vector<double>* rows[5] = {&fr.ibd, &fr.mm, &fr.HH, &fr.gg, &fr.GG};
                 for (int r = 0; r < 5; ++r)
                     for (int j = 0; j < NZP; ++j) put(base[k] + r, j, (*rows[r])[j]);
+                std::vector<double> lf, lb;
+                fused_lookback(fr, tp, nz, lf, lb);
+                for (int i = 0; i < 4 * tp; ++i) {
+                    put(lbase[k], i, lf[i]);
+                    put(lbase[k] + 1, i, lb[i]);
+                }
             }
             if ((rc = upload(c, c->ftab, ft.data(), ft.size() * 4))) return rc;
         }
@@ -1378,8 +1443,9 @@ int sparc_gpu_kernel_accumulate(sparc_ctx* fwd, int snap, sparc_ctx* c) {
     return SPARC_OK;
 }
 
-int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* krho, double* hess) {
-    if (!c) return SPARC_EINVAL;
+// Final scaling of the kernels (kernels.f90:523-539) into the device buffer
+// out (3 N doubles), enqueued on the context's stream.
+static int kernels_finish(sparc_ctx* c, int src, int sum_slots, double* out) {
     if (!c->kacc) return fail(c, SPARC_ESTATE, "no kernel accumulation yet");
     if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
     int stepskern = c->steps;                         // kernels.f90:190
@@ -1387,14 +1453,28 @@ int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* 
     double dimen = std::pow(c->diml * (double)1.0e-8f, -3.0);            // kernels.f90:523
     if (c->P.ny <= 4) dimen = 1.0 / (c->diml * (double)1.0e-8f * R4(c->P.xlength) * (double)1.0e-8f);
     double sc = stepskern * ts * dimen * 2.0, sr = stepskern * ts * dimen;
-    double* out = nullptr;
-    int rc = dalloc(c, (void**)&out, (size_t)3 * c->N * 8);
-    if (rc) return rc;
     const double* acc = c->kacc + (sum_slots ? 0 : (size_t)src * 3 * c->N);
     launch_kernel_finish(out, acc, c->zt64, c->NP, c->nz, sc, sr, sum_slots ? c->S : 1, 3 * c->N, c->stream,
                          mhd_kernel_rho0(c), mhd_kernel_c2(c));
     c->launches++;
     CKL();
+    return SPARC_OK;
+}
+
+int sparc_gpu_kernels_device(sparc_ctx* c, int src, int sum_slots, double* dev_out) {
+    if (!c) return SPARC_EINVAL;
+    if (!dev_out) return fail(c, SPARC_EINVAL, "null output buffer");
+    return kernels_finish(c, src, sum_slots, dev_out);
+}
+
+int sparc_gpu_kernels(sparc_ctx* c, int src, int sum_slots, double* kc, double* krho, double* hess) {
+    if (!c) return SPARC_EINVAL;
+    if (!c->kacc) return fail(c, SPARC_ESTATE, "no kernel accumulation yet");
+    if (src < 0 || src >= c->S) return fail(c, SPARC_EINVAL, "bad slot");
+    double* out = nullptr;
+    int rc = dalloc(c, (void**)&out, (size_t)3 * c->N * 8);
+    if (rc) return rc;
+    if ((rc = kernels_finish(c, src, sum_slots, out))) return rc;
     if (kc) CK(cudaMemcpyAsync(kc, out, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
     if (krho) CK(cudaMemcpyAsync(krho, out + c->N, c->N * 8, cudaMemcpyDeviceToHost, c->stream));
     if (hess) CK(cudaMemcpyAsync(hess, out + 2 * c->N, c->N * 8, cudaMemcpyDeviceToHost, c->stream));

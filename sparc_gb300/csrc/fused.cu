@@ -22,13 +22,20 @@
 //     the same instruction stream for every thread of a warp;
 //   * the tridiagonal solves of DBYD2/MTRIDAG (dbyd2.f90:198-201,
 //     mtridag.f90:94-111) are first-order linear recurrences.  Each thread
-//     runs its chunk with a zero carry-in, the chunk maps u -> B + Mc*u are
-//     composed by a scan across the pencil's threads (warp shuffles, then
-//     warps through shared memory), and each thread adds H(j)*carry-in, where
-//     H(j) and Mc are products of the constant elimination multipliers,
-//     precomputed on the host in FP64.  This is the same LU elimination and
-//     back substitution as the sequential form, re-associated.  Padding rows
-//     carry zero multipliers, so they never reach a real row.
+//     runs its chunk with a zero carry-in; the chunk maps u -> B + Mc*u then
+//     give the carry into chunk t as the sum over the preceding chunks of
+//     B(t-i) times the product of the multipliers Mc between them (and the
+//     same from above for the back substitution).  Those products depend on
+//     z only (the matrix is the same for every mode), shrink by about 0.008
+//     per chunk (|multiplier| ~ 0.38 per level), and are precomputed on the
+//     host in FP64: the sum is taken over the KB = 5 nearest chunks, read
+//     from a per-pencil line in shared memory after one barrier.  The terms
+//     left out are below 2^-32 of a chunk value (checked on the host for
+//     every boundary code, else the context runs the per-stage kernels).
+//     Each thread then adds H(j)*carry-in to its levels, H(j) the product of
+//     the multipliers from its chunk start to j.  This is the LU elimination
+//     and back substitution of the sequential form, re-associated.  Padding
+//     rows carry zero multipliers, so they never reach a real row.
 // HBM traffic per step: read a, write a (+ the PML planes and source planes),
 // and scr only on steps whose right-hand side is requested (outputs).
 #include <type_traits>
@@ -40,6 +47,7 @@ namespace {
 constexpr int CH = FUSED_CH;   // z-levels per thread
 constexpr int GZ = 5;          // ghost rows of the tile on each side (reach of the z filter)
 constexpr int GX = 2;          // ghost entries of an exchange line on each side (compact stencil)
+constexpr int KB = FUSED_KB;   // chunks summed by a look-back carry
 
 // Entry idx of the z tables (scalars in shared memory) as a pair (t, t), the
 // multiplier of a paired product with a complex value.  Tables stored as
@@ -50,71 +58,21 @@ __device__ __forceinline__ float2 zt2(const float* zs, int idx) {
     return make_float2(t, t);
 }
 
-struct Aff {             // u -> B + M u   (B complex, M real)
-    float2 B;
-    float M;
-};
-
-// compose: first f, then g  -> g(f(u)) = gB + gM (fB + fM u)
-__device__ __forceinline__ Aff compose(Aff f, Aff g) {
-    Aff r;
-    r.B.x = g.B.x + g.M * f.B.x;
-    r.B.y = g.B.y + g.M * f.B.y;
-    r.M = g.M * f.M;
-    return r;
-}
-
-__device__ __forceinline__ Aff shfl_up(Aff a, int d) {
-    Aff r;
-    r.B.x = __shfl_up_sync(0xffffffffu, a.B.x, d);
-    r.B.y = __shfl_up_sync(0xffffffffu, a.B.y, d);
-    r.M = __shfl_up_sync(0xffffffffu, a.M, d);
-    return r;
-}
-__device__ __forceinline__ Aff shfl_down(Aff a, int d) {
-    Aff r;
-    r.B.x = __shfl_down_sync(0xffffffffu, a.B.x, d);
-    r.B.y = __shfl_down_sync(0xffffffffu, a.B.y, d);
-    r.M = __shfl_down_sync(0xffffffffu, a.M, d);
-    return r;
-}
-
 // Barrier over the TP threads of one pencil (named barrier pi+1; barrier 0
 // stays the CTA-wide __syncthreads).
 __device__ __forceinline__ void pencil_sync(int pi, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(pi + 1), "r"(nthreads) : "memory");
 }
 
-// Exclusive scan of chunk maps over the TP = 32*W threads of one pencil.
-// FWD: carry flows from lower to higher t; otherwise reversed.  wb holds W
-// maps and is used by this scan only (no barrier is needed to reuse it later:
-// the next use of the same slot is separated by the stage's other barriers).
-template <int W, bool FWD>
-__device__ __forceinline__ Aff pencil_scan(Aff mine, int t, Aff* wb, int pi) {
-    const int lane = t & 31;
-    Aff inc = mine;
-    #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        Aff o = FWD ? shfl_up(inc, d) : shfl_down(inc, d);
-        if (FWD ? (lane >= d) : (lane + d < 32)) inc = compose(o, inc);
-    }
-    Aff ex = FWD ? shfl_up(inc, 1) : shfl_down(inc, 1);
-    if (FWD ? (lane == 0) : (lane == 31)) { ex.B = make_float2(0.f, 0.f); ex.M = 1.f; }
-    if (W == 1) return ex;
-    const int warp = t >> 5;
-    if (FWD ? (lane == 31) : (lane == 0)) wb[warp] = inc;
-    pencil_sync(pi, 32 * W);
-    Aff carry;
-    carry.B = make_float2(0.f, 0.f);
-    carry.M = 1.f;
-    // forward: the totals of warps below, in increasing order; backward: of
-    // warps above, in decreasing order
-    #pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const int ww = FWD ? w : (W - 1 - w);
-        if (FWD ? (ww < warp) : (ww > warp)) carry = compose(carry, wb[ww]);
-    }
-    return compose(carry, ex);
+// Carry of a chunk from the KB = 5 nearest chunk values of a look-back line:
+// sum over i = 1..5 of prod(i) * v(i), prod(1) = 1, prod(2..5) = pr.x..pr.w;
+// the far terms first.
+__device__ __forceinline__ float2 lookback(float4 pr, float2 v1, float2 v2, float2 v3, float2 v4, float2 v5) {
+    float2 c = pmul(bc2(pr.w), v5);
+    c = pfma(bc2(pr.z), v4, c);
+    c = pfma(bc2(pr.y), v3, c);
+    c = pfma(bc2(pr.x), v2, c);
+    return padd(v1, c);
 }
 
 // d/dz (without stretch) of the values of one exchange line (xp[j], j in
@@ -122,12 +80,15 @@ __device__ __forceinline__ Aff pencil_scan(Aff mine, int t, Aff* wb, int pi) {
 // levels j0..j0+CH-1,
 // boundary code BC (dbyd2.f90:94-173 for the right-hand side; top is the
 // caller-set value of bc 3).  zs, r0: the z tables and the first of the five
-// scan rows (ibd, m, H, g, G) of BC.
+// elimination rows (1/betad, m, H, g, G) of BC; lb, lb+1: its forward and
+// backward look-back product tables ([t][4] floats each); lf, lk:
+// this pencil's forward and backward look-back lines (chunk t at index t,
+// zero entries at -KB..-1 and TP..TP+KB-1).
 template <int BC, int W>
 __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const float2 (&own)[CH],
-                                       const float* __restrict__ zs, int r0, int nz, float2 top, int j0, bool lo,
-                                       bool hi, int t, Aff* wbF, Aff* wbB, int pi, const Compact<float> c,
-                                       float2 (&out)[CH]) {
+                                       const float* __restrict__ zs, int r0, int lb, int nz, float2 top, int j0,
+                                       bool lo, bool hi, int t, float2* lf, float2* lk, int pi,
+                                       const Compact<float> c, float2 (&out)[CH]) {
     constexpr int NZP = 160 * W;
     const int ibd = r0 * NZP, mm = (r0 + 1) * NZP, HH = (r0 + 2) * NZP, gg = (r0 + 3) * NZP, GG = (r0 + 4) * NZP;
     auto Z = [&](int row, int j) { return zt2(zs, row + j); };
@@ -182,10 +143,12 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
         run = pfma(Z(mm, j), run, pmul(Z(ibd, j), u[q]));
         u[q] = run;
     }
-    Aff mine;
-    mine.B = run;
-    mine.M = Z(HH, j0 + CH - 1).x;
-    const float2 uin = pencil_scan<W, true>(mine, t, wbF, pi).B;    // ud(j0-1)
+    // carry into the chunk: ud(j0-1) from the chunk values below
+    constexpr int TP = 32 * W;
+    lf[t] = run;
+    pencil_sync(pi, TP);
+    const float2 uin = lookback(*(const float4*)(zs + lb * NZP + 4 * t), lf[t - 1], lf[t - 2], lf[t - 3],
+                                lf[t - 4], lf[t - 5]);
     #pragma unroll
     for (int q = 0; q < CH; ++q) u[q] = pfma(Z(HH, j0 + q), uin, u[q]);
     // back substitution x(j) = u(j) + g(j) x(j+1)
@@ -195,10 +158,11 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
         xr = pfma(Z(gg, j0 + q), xr, u[q]);
         out[q] = xr;
     }
-    Aff bm;
-    bm.B = xr;
-    bm.M = Z(GG, j0).x;
-    const float2 xin = pencil_scan<W, false>(bm, t, wbB, pi).B;     // x(j0+CH)
+    // carry from above: x(j0+CH) from the chunk values above
+    lk[t] = xr;
+    pencil_sync(pi, TP);
+    const float2 xin = lookback(*(const float4*)(zs + (lb + 1) * NZP + 4 * t), lk[t + 1], lk[t + 2],
+                                lk[t + 3], lk[t + 4], lk[t + 5]);
     #pragma unroll
     for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
 }
@@ -220,18 +184,17 @@ __device__ __forceinline__ int pmlidx(int j, int nz, int nb, int nt) {
 
 // shared-memory layout (byte offsets), identical on host and device
 struct FusedLayout {
-    int tile, xa, xb, ptile, spt, wbuf, zs, lagw, lagi, mbar, total;
+    int tile, xl, ptile, spt, lines, zs, lagw, lagi, mbar, total;
 };
 __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
-    const int NZP = 160 * W, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX;
+    const int NZP = 160 * W, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX, LL = 32 * W + 2 * KB;
     FusedLayout L;
     int o = 0;
     L.tile = o;  o += 6 * P * LZ * 8;
-    L.xa = o;    o += P * LX * 8;
-    L.xb = o;    o += P * LX * 8;
+    L.xl = o;    o += P * LX * 8;             // one exchange line per pencil (xi_z, then p')
     L.ptile = o; o += 2 * nzpml * P * 8;
     L.spt = o;   o += 2 * nzpml * P * 8;
-    L.wbuf = o;  o += 4 * P * W * (int)sizeof(Aff);
+    L.lines = o; o += 2 * P * LL * 8;         // forward and backward look-back lines per pencil
     o = (o + 15) & ~15;
     L.zs = o;    o += FZ_COUNT * NZP * 4;
     o = (o + 15) & ~15;
@@ -252,17 +215,16 @@ __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
 template <bool D3, int W, int P>
 __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedArgs A) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    constexpr int TP = 32 * W, NZP = TP * CH, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX;
+    constexpr int TP = 32 * W, NZP = TP * CH, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX, LL = TP + 2 * KB;
     constexpr int BCX = D3 ? 1 : 3, BCP = D3 ? 0 : 2;
     const int nz = A.nz, M = A.M, nzpml = A.nzpml, nb = A.npmlbot, nt = A.npmltop;
     const long long fs = A.fs;
     const FusedLayout Ly = fused_layout(P, W, nzpml);
     float2* tile = (float2*)(smraw + Ly.tile);            // [6][P][LZ], level j at GZ + j
-    float2* xab = (float2*)(smraw + Ly.xa);               // [P][LX], level j at GX + j
-    float2* xbb = (float2*)(smraw + Ly.xb);
+    float2* xlb = (float2*)(smraw + Ly.xl);               // [P][LX], level j at GX + j
     float2* ptile = (float2*)(smraw + Ly.ptile);          // [2][nzpml][P]
     float2* spt = (float2*)(smraw + Ly.spt);              // [2][nzpml][P] PML right-hand sides
-    Aff* wbuf = (Aff*)(smraw + Ly.wbuf);                  // [4 scans][P][W]
+    float2* lines = (float2*)(smraw + Ly.lines);          // [P][2][LL], chunk t at KB + t
     float* zs = (float*)(smraw + Ly.zs);                  // [FZ_COUNT][NZP]
     double* lagw = (double*)(smraw + Ly.lagw);            // [8] Lagrange weights of this slot
     const unsigned mbar = (unsigned)__cvta_generic_to_shared(smraw + Ly.mbar);
@@ -275,8 +237,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     const bool mvalid = m < M;
     const int s = blockIdx.y;
     const int j0 = t * CH;
-    float2* xa = xab + pi * LX + GX;
-    float2* xb = xbb + pi * LX + GX;
+    float2* xl = xlb + pi * LX + GX;
+    float2* lf = lines + (2 * pi) * LL + KB;
+    float2* lk = lines + (2 * pi + 1) * LL + KB;
     float2* gA = A.a + (long long)s * 6 * fs;
     float2* gS = A.scr + (long long)s * 6 * fs;
     float2* gP = A.pml + (long long)s * 2 * A.ps;
@@ -301,7 +264,8 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
                 : "memory");
         }
     }
-    // ---- zero the ghost and padding rows of the tile and the exchange lines ----
+    // ---- zero the ghost and padding rows of the tile, the exchange lines'
+    // ghosts and the look-back lines' end entries ----
     {
         const int nl = LZ - nz;                       // GZ below + (NZP - nz + GZ) above, per row
         for (int r = threadIdx.x; r < 6 * P * nl; r += nthr) {
@@ -312,30 +276,48 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         for (int r = threadIdx.x; r < P * 2 * GX; r += nthr) {
             const int line = r / (2 * GX), k = r - line * (2 * GX);
             const int z = k < GX ? k : NZP + k;       // ghost entries below 0 and at NZP, NZP+1
-            xab[line * LX + z] = make_float2(0.f, 0.f);
-            xbb[line * LX + z] = make_float2(0.f, 0.f);
+            xlb[line * LX + z] = make_float2(0.f, 0.f);
+        }
+        for (int r = threadIdx.x; r < 2 * P * 2 * KB; r += nthr) {
+            const int line = r / (2 * KB), k = r - line * (2 * KB);
+            lines[line * LL + (k < KB ? k : TP + k)] = make_float2(0.f, 0.f);
         }
     }
-    // ---- load the a tile and the PML tile (cooperative, 32 B rows) ----
-    for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
-        const int f = r / nz, z = r - f * nz;
-        const float2* src = gA + f * fs + (long long)z * M + m0;
-        float2* dst = tile + f * P * LZ + GZ + z;
-        if (vec) {
-            // P complex values per row: P/2 float4, exactly the CTA's modes
-            #pragma unroll
-            for (int v = 0; v < P / 2; ++v) {
-                const float4 x = *(const float4*)(src + 2 * v);
-                dst[(2 * v) * LZ] = make_float2(x.x, x.y);
-                dst[(2 * v + 1) * LZ] = make_float2(x.z, x.w);
+    // ---- load the a tile and the PML tile: every complex value by its own
+    // asynchronous 8-byte copy into its transposed place, all in flight at
+    // once ([z][m] in HBM, [mode][z] on chip), awaited with the z tables ----
+    {
+        constexpr int RPI = TP;                       // rows advanced per pass: blockDim.x / P
+        const int q = threadIdx.x % P;
+        const bool qv = m0 + q < M;
+        int z = threadIdx.x / P, f = 0;
+        while (z >= nz) { z -= nz; ++f; }
+        for (; f < 6;) {
+            float2* dst = tile + f * P * LZ + q * LZ + GZ + z;
+            if (qv) {
+                const float2* src = gA + f * fs + (long long)z * M + m0 + q;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                                 (unsigned)__cvta_generic_to_shared(dst)),
+                             "l"(__cvta_generic_to_global(src))
+                             : "memory");
+            } else {
+                *dst = make_float2(0.f, 0.f);
             }
-        } else {
-            for (int q = 0; q < P; ++q) dst[q * LZ] = (m0 + q < M) ? src[q] : make_float2(0.f, 0.f);
+            z += RPI;
+            while (z >= nz) { z -= nz; ++f; }
         }
-    }
-    for (int r = threadIdx.x; r < 2 * nzpml; r += nthr) {
-        const float2* src = gP + (long long)r * M + m0;
-        for (int q = 0; q < P; ++q) ptile[r * P + q] = (m0 + q < M) ? src[q] : make_float2(0.f, 0.f);
+        for (int r = threadIdx.x / P; r < 2 * nzpml; r += RPI) {
+            float2* dst = ptile + r * P + q;
+            if (qv) {
+                const float2* src = gP + (long long)r * M + m0 + q;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                                 (unsigned)__cvta_generic_to_shared(dst)),
+                             "l"(__cvta_generic_to_global(src))
+                             : "memory");
+            } else {
+                *dst = make_float2(0.f, 0.f);
+            }
+        }
     }
     const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
     const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
@@ -347,7 +329,8 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         lagw[threadIdx.x] = w;
         lagi[threadIdx.x] = id < 0 ? 0 : id;
     }
-    __syncthreads();                                      // the mbarrier is initialised
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();                                      // the tiles are in, the mbarrier is initialised
     // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
     // reports it and leaves without computing or storing (its modes keep the
     // state of the previous step), thread 0 first waiting out a copy still in
@@ -394,7 +377,6 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     auto TA = [&](int f, int j) -> float2 { return tp[f * P * LZ + j]; };
     // z table entry of row r at level j, as a pair
     auto Z2 = [&](int r, int j) { return zt2(zs, r * NZP + j); };
-    Aff* wb = wbuf + pi * W;                              // scan slot k at wb + k*P*W
 
     // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
     // rather than a (stage 1), fixed at compile time
@@ -408,7 +390,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             float2 v = TA(2, j0 + q);
             if (hs) v = pfma(BT, sc[2][q], v);
             own[q] = v;
-            xa[j0 + q] = v;
+            xl[j0 + q] = v;
         }
         float2 top = make_float2(0.f, 0.f);
         if (!D3 && hi) {   // caller-set top value of bc 3 (physics2d.f90:960)
@@ -422,7 +404,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         float2 d[CH];
-        zsolve<BCX, W>(xa, own, zs, FZ_SX, nz, top, j0, lo, hi, t, wb, wb + P * W, pi, A.cc, d);
+        zsolve<BCX, W>(xl, own, zs, FZ_SX, FZ_LX, nz, top, j0, lo, hi, t, lf, lk, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) d[q] = pmul(Z2(FZ_ST, j0 + q), d[q]);
         if (pml_t) {   // psi_vz (displacement.f90 PML rows)
@@ -453,7 +435,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             }
             const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
             qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
-            xb[j] = p;
+            xl[j] = p;
             own[q] = p;
             const float ri = Z2(FZ_RI, j).x;
             sc[3][q] = pfma(NGD, vx, -ri * imul(kx, p));
@@ -472,8 +454,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         // ---- dp'/dz, RHS v_z and xi_z ----
-        zsolve<BCP, W>(xb, own, zs, FZ_SP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, wb + 2 * P * W,
-                       wb + 3 * P * W, pi, A.cc, d);
+        zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;

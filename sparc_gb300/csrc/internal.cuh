@@ -339,10 +339,20 @@ template <typename T> struct UpdateArgs {
 
 // fused FP32 step (fused.cu)
 // z table of the fused FP32 step, [FZ_COUNT][NZP] (NZP = fused_nzp(nz), padded
-// rows zero): profile rows, then the five scan rows (1/betad, elimination
-// multiplier m, chunk products H of m, back-substitution multiplier g, chunk
-// products G of g) of the xi_z boundary code and of the p' boundary code
-enum { FZ_ST = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_RIST, FZ_AZ, FZ_BZ, FZ_SX = 9, FZ_SP = 14, FZ_COUNT = 19 };
+// rows zero): profile rows, then the five elimination rows (1/betad,
+// elimination multiplier m, chunk products H of m, back-substitution
+// multiplier g, chunk products G of g) of the xi_z boundary code and of the p'
+// boundary code, then the look-back products of each code: a forward row and
+// a backward row, [chunk t][4] floats each (the products of the multipliers
+// of the 1..4 chunks between chunk t and the chunk 2..5 below / above it)
+enum {
+    FZ_ST = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_RIST, FZ_AZ, FZ_BZ, FZ_SX = 9, FZ_SP = 14,
+    FZ_LX = 19, FZ_LP = 21, FZ_COUNT = 23
+};
+constexpr int FUSED_KB = 5;    // chunks summed by a look-back carry of the fused step
+// largest product of chunk multipliers over FUSED_KB chunks (the first term a
+// look-back carry leaves out) for which the fused step is used
+constexpr double FUSED_LOOKBACK_BOUND = 2.3283064365386963e-10;   // 2^-32
 struct FusedArgs {
     float2* a; float2* scr; float2* pml;
     const float* ftab; const float* pt;

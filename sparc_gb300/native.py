@@ -42,6 +42,7 @@ EXPORTS = [
     "sparc_gpu_sync", "sparc_gpu_spec_to_phys_noalloc", "sparc_gpu_autotune", "sparc_gpu_set_mhd_background",
     "sparc_gpu_set_mhd2d_background", "sparc_gpu_kernels_b", "sparc_gpu_adjoint_source",
     "sparc_gpu_adjoint_source_host", "sparc_gpu_misfit_all", "sparc_gpu_gradient", "sparc_gpu_update_models",
+    "sparc_gpu_kernels_device",
 ]
 
 
@@ -119,6 +120,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_kernel_accumulate": ([P, I, P], I),
         "sparc_gpu_kernel_reset": ([P], I),
         "sparc_gpu_kernels": ([P, I, I, D, D, D], I),
+        "sparc_gpu_kernels_device": ([P, I, I, P], I),
         "sparc_gpu_kernels_b": ([P, I, I, D, D, D], I),
         "sparc_gpu_ddx": ([P, D, D], I),
         "sparc_gpu_ddy": ([P, D, D], I),

@@ -211,3 +211,14 @@ def config_quiet_256() -> SparcParams:
     return SparcParams(nx=256, ny=256, nz=300, xlength=200.0e8, ylength=200.0e8,
                        npmlbot=10, npmltop=10, excitdep=-15000000.0, obsheight=20000000.0,
                        solartime=4.0)
+
+
+def config_flux_tube_256():
+    """The flux-tube configuration: option 10 on 256x256x300, 200 Mm
+    periodic, PML 10 at the bottom; the box ends at the surface (z = 0),
+    where a 2 kG tube can still be in magnetohydrostatic balance with the gas
+    pressure (above it the pressure falls by e every ~100 km).  Returns
+    (params, polytrope table)."""
+    from .background import polytrope_table
+    p = config_quiet_256().replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0)
+    return p, polytrope_table(p.nz, z_bot_mm=-25.0, z_top_mm=0.0)

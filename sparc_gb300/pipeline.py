@@ -103,6 +103,32 @@ class KernelPipeline:
         adj = Solver(self.pa, self.table)
         for s in range(self.p.nsrc):
             adj.set_source_lagrange(adj_planes[s], slot=s)
+        self._accumulate(fwd, adj)
+        if sum_slots:
+            res = adj.kernels(sum_slots=True)
+        else:
+            parts = [adj.kernels(slot=s) for s in range(self.p.nsrc)]
+            res = tuple(np.stack([q[i] for q in parts]) for i in range(3))
+        adj.close()
+        return res
+
+    def kernels_device(self, fwd: Solver, adj_planes: np.ndarray, out_ptr: int, stream_sync: bool = True):
+        """As kernels(..., sum_slots=True), the sum written into the device
+        buffer at out_ptr (3 * N doubles) instead of host arrays."""
+        adj = Solver(self.pa, self.table)
+        try:
+            for s in range(self.p.nsrc):
+                adj.set_source_lagrange(adj_planes[s], slot=s)
+            self._accumulate(fwd, adj)
+            adj.kernels_into(out_ptr, sum_slots=True)
+            if stream_sync:
+                adj.sync()
+        finally:
+            adj.close()
+
+    def _accumulate(self, fwd: Solver, adj: Solver):
+        """Adjoint run with the kernel accumulation: forward segments
+        recomputed from the device checkpoints, latest first."""
         adj.kernel_reset()
         fwd.record_surface(1, enable=False)          # recomputed segments add no records
         G = (self.nt + self.L - 1) // self.L
@@ -116,13 +142,6 @@ class KernelPipeline:
                 ia = self.maxtime - k * self.cad
                 adj.step(ia + 1 - adj.time)               # adjoint snapshot at time adj_end - k*cad
                 adj.kernel_accumulate(fwd, k - k0)
-        if sum_slots:
-            res = adj.kernels(sum_slots=True)
-        else:
-            parts = [adj.kernels(slot=s) for s in range(self.p.nsrc)]
-            res = tuple(np.stack([q[i] for q in parts]) for i in range(3))
-        adj.close()
-        return res
 
     def run(self, planes, series, obs_records, pixels, window=None, sum_slots=False) -> KernelResult:
         fwd, recs = self.forward(planes, series)
@@ -131,3 +150,42 @@ class KernelPipeline:
         fwd.close()
         seis = np.stack([[recs[s, :, iy, ix] for (iy, ix) in pixels] for s in range(self.p.nsrc)])
         return KernelResult(kc, kr, hs, np.swapaxes(seis, 1, 2), recs)
+
+
+@dataclasses.dataclass
+class ShardedResult:
+    kernels: object          # torch float64 tensor (3, nz, ny, nx): K_c, K_rho, hessian summed over ALL sources
+    sources: list            # global indices of the sources this rank ran
+    records: np.ndarray      # (len(sources), nrec, ny, nx) this rank's surface records
+
+
+def run_sharded(p: SparcParams, table: np.ndarray, planes, series, obs_records, pixels, window=None,
+                segment: int = 8, group=None, device=None) -> ShardedResult:
+    """The kernel workflow over a global source list on several GPUs (one
+    process per GPU): rank r of W runs the sources shard_sources(n, r, W) as
+    one batch, writes its kernel sum into a device tensor and the ranks sum
+    those with one FP64 all-reduce (grad.py:158-165).  planes, obs_records:
+    global lists / arrays indexed by source; series: one series or one per
+    source.  Every rank returns the same summed kernels."""
+    import torch
+    from . import dist as sd
+    rank, world = sd.rank_world(group)
+    n = len(planes)
+    mine = sd.shard_sources(n, rank, world)
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    ksum = (torch.empty if mine else torch.zeros)((3, p.nz, p.ny, p.nx), dtype=torch.float64, device=dev)
+    recs = np.zeros((0, 0, p.ny, p.nx))
+    if mine:
+        # the library writes ksum on its own stream: nothing of torch's may
+        # still be in flight on that memory
+        torch.cuda.current_stream(dev).synchronize()
+        pl = KernelPipeline(p.replace(nsrc=len(mine)), table, segment)
+        ser = [series[i] for i in mine] if np.ndim(series) == 2 else series
+        fwd, recs = pl.forward([planes[i] for i in mine], ser)
+        try:
+            adjp = pl.adjoint_planes(recs, np.asarray(obs_records)[mine], pixels, window)
+            pl.kernels_device(fwd, adjp, ksum.data_ptr())
+        finally:
+            fwd.close()
+    sd.reduce_kernels(ksum, group)
+    return ShardedResult(ksum, mine, recs)

@@ -2,9 +2,11 @@
 
 A request is one forward solve, or a forward solve followed by its adjoint
 solve (adjoint source = the time-reversed surface residual at receivers on a
-ring around the source), on one of several grid sizes.  The engine keeps, per
-(grid size, role), pools of batched contexts -- fields resident in HBM, one
-CUDA stream each -- and runs an event loop:
+ring around the source), on one of several grid sizes, on the quiet Sun or on
+the magnetohydrostatic flux tube (linearised MHD, option 10, the tube on the
+box centre, the source anywhere).  The engine keeps, per (grid size, role,
+background), pools of batched contexts -- fields resident in HBM, one CUDA
+stream each -- and runs an event loop:
 
   * arrivals join a queue; a queued request is admitted into a free slot of a
     pool of its grid size, or into a new pool if the HBM budget allows one
@@ -28,9 +30,11 @@ import time
 import numpy as np
 
 from . import sources
-from .background import polytrope_table
-from .params import SparcParams
+from .background import mhs_flux_tube_background, polytrope_table
+from .params import OPT_MHD_PML_3D_DISPL, SparcParams
 from .solver import Solver
+
+QUIET, TUBE = "quiet", "tube"
 
 
 @dataclasses.dataclass
@@ -47,27 +51,48 @@ class Request:
     records: np.ndarray | None = None        # forward surface vz records (nrec, ny, nx)
     adj_records: np.ndarray | None = None    # adjoint surface vz records
     phase: int = 0
+    background: str = QUIET                  # QUIET or TUBE
 
     @property
     def latency(self) -> float:
         return self.finished - self.arrival
 
 
-def grid_params(grid, precision: str, base: SparcParams | None = None) -> SparcParams:
+def grid_params(grid, precision: str, base: SparcParams | None = None, background: str = QUIET) -> SparcParams:
+    """200 Mm periodic box for every grid size; the flux tube runs option 10
+    with the PML at the bottom only (its box ends at the surface)."""
     nx, ny, nz = grid
     b = base or SparcParams()
-    length = 200.0e8                          # 200 Mm periodic box for every grid size
-    return b.replace(nx=nx, ny=ny, nz=nz, xlength=length, ylength=length, npmlbot=10, npmltop=10,
-                     excitdep=-15000000.0, obsheight=20000000.0, precision=precision)
+    length = 200.0e8
+    p = b.replace(nx=nx, ny=ny, nz=nz, xlength=length, ylength=length, npmlbot=10, npmltop=10,
+                  excitdep=-15000000.0, obsheight=20000000.0, precision=precision)
+    if background == TUBE:
+        p = p.replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0)
+    return p
+
+
+def grid_table(nz: int, background: str = QUIET) -> np.ndarray:
+    """The quiet column: -25 .. +1.2 Mm; under the flux tube -25 .. 0 Mm."""
+    return polytrope_table(nz) if background == QUIET else polytrope_table(nz, z_bot_mm=-25.0, z_top_mm=0.0)
 
 
 class Pool:
     """One batched context (one grid size, one role) with `slots` slots."""
 
-    def __init__(self, p: SparcParams, table, role: str, slots: int, max_records: int):
+    def __init__(self, p: SparcParams, table, role: str, slots: int, max_records: int, background: str = QUIET,
+                 tube_cache: dict | None = None):
         self.role = role
+        self.background = background
         self.p = p.replace(nsrc=slots, compute_forward=(role == "fwd"), compute_adjoint=(role == "adj"))
         self.solver = Solver(self.p, table)
+        if background == TUBE:
+            # the magnetohydrostatic tube of this grid, built once (FP64, with
+            # this context's FP64 z derivative) and shared by its pools
+            key = (self.p.nx, self.p.ny, self.p.nz)
+            cache = tube_cache if tube_cache is not None else {}
+            if key not in cache:
+                cache[key] = mhs_flux_tube_background(self.p, table, self.solver.ddz)[0]
+            self.solver.set_mhd_background(*cache[key])
         self.solver.record_surface(max_records)
         self.requests: list = [None] * slots
         self.series = sources.ricker_series(self.p, 8 * max_records * self.p.steps)
@@ -128,26 +153,31 @@ class Engine:
         self.pools: list[Pool] = []
         self.max_pools_per_key = 2
         self.tables: dict = {}
+        self.tubes: dict = {}
         self.cad = (base or SparcParams()).steps
 
-    def _table(self, nz):
-        if nz not in self.tables:
-            self.tables[nz] = polytrope_table(nz)
-        return self.tables[nz]
+    def _table(self, nz, background=QUIET):
+        if (nz, background) not in self.tables:
+            self.tables[(nz, background)] = grid_table(nz, background)
+        return self.tables[(nz, background)]
 
-    def _pool_for(self, grid, role) -> Pool | None:
+    def _pool_for(self, grid, role, background=QUIET) -> Pool | None:
+        def mine(pl):
+            return pl.role == role and pl.background == background and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid)
         for pl in self.pools:
-            if pl.role == role and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid) and pl.free:
+            if mine(pl) and pl.free:
                 return pl
-        same = [pl for pl in self.pools if pl.role == role and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid)]
+        same = [pl for pl in self.pools if mine(pl)]
         if len(same) >= self.max_pools_per_key:
             return None
         # admission by footprint: a new pool only if it fits the HBM budget,
         # after releasing idle pools (least recently created first)
-        p = grid_params(grid, self.precision, self.base)
+        p = grid_params(grid, self.precision, self.base, background)
         slots = self.slots.get(tuple(grid), 4)
         field = (p.nx // 2 + 1) * p.ny * p.nz * (8 if self.precision == "f32" else 16)
         est = slots * field * (15 + (self.max_steps // self.cad + 1) / p.nz) + p.points * 12 + 64e6
+        if background == TUBE:
+            est *= 3.0      # physical state, the MHD work fields and the 3-D background
         if est > self.budget:
             raise RuntimeError(f"a {grid} pool needs {est / 1e9:.1f} GB, above the HBM budget")
         while sum(pl.bytes for pl in self.pools) + est > self.budget:
@@ -156,7 +186,8 @@ class Engine:
                 return None
             idle[0].close()
             self.pools.remove(idle[0])
-        pl = Pool(p, self._table(p.nz), role, slots, self.max_steps // self.cad + 1)
+        pl = Pool(p, self._table(p.nz, background), role, slots, self.max_steps // self.cad + 1, background,
+                  self.tubes)
         self.pools.append(pl)
         return pl
 
@@ -181,7 +212,7 @@ class Engine:
             for q, role in ((adj_queue, "adj"), (queue, "fwd")):
                 keep = []
                 for req in q:
-                    pl = self._pool_for(req.grid, role)
+                    pl = self._pool_for(req.grid, role, req.background)
                     if pl is None:
                         keep.append(req)
                         continue
@@ -223,11 +254,12 @@ class Engine:
 
 
 def poisson_stream(n: int, rate: float = 4.0, seed: int = 0, mix=None, hours=(1.0, 4.0), dt: float = 2.0,
-                   cad: int = 15, compress: float = 1.0, p_adj: float = 0.5) -> list[Request]:
+                   cad: int = 15, compress: float = 1.0, p_adj: float = 0.5, p_tube: float = 0.2) -> list[Request]:
     """Seeded request stream: Poisson arrivals, grid mix (60 % 128^2x150,
     30 % 256^2x300, 10 % 512^2x300 by default), random source position,
-    forward-only or forward+adjoint, 1-4 h of solar time divided by
-    `compress` (time steps rounded up to the output cadence)."""
+    forward-only or forward+adjoint, quiet Sun or (a fraction p_tube) the
+    flux tube, 1-4 h of solar time divided by `compress` (time steps rounded
+    up to the output cadence)."""
     rng = np.random.default_rng(seed)
     mix = mix or [((128, 128, 150), 0.6), ((256, 256, 300), 0.3), ((512, 512, 300), 0.1)]
     grids = [g for g, _ in mix]
@@ -243,7 +275,8 @@ def poisson_stream(n: int, rate: float = 4.0, seed: int = 0, mix=None, hours=(1.
         half = 0.4 * 200.0
         x0, y0 = rng.uniform(-half, half, size=2)
         kind = "fwd+adj" if rng.random() < p_adj else "fwd"
-        out.append(Request(i, g, kind, steps, float(x0), float(y0), t))
+        bgr = TUBE if rng.random() < p_tube else QUIET
+        out.append(Request(i, g, kind, steps, float(x0), float(y0), t, background=bgr))
     return out
 
 

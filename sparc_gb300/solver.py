@@ -397,6 +397,12 @@ class Solver:
                                                 ctypes.cast(ctypes.pointer(con), _D)))
         return uc, up, tp, con.value
 
+    def kernels_into(self, dev_ptr: int, slot: int = 0, sum_slots: bool = False):
+        """Final kernels (K_c, K_rho, hessian; 3 x (nz, ny, nx) doubles) into
+        the device buffer at dev_ptr, enqueued on this context's stream (the
+        caller orders its own reads after that stream)."""
+        self._ck(self.L.sparc_gpu_kernels_device(self.h, slot, int(sum_slots), ctypes.c_void_p(int(dev_ptr))))
+
     def kernels_b(self, slot: int = 0, sum_slots: bool = False):
         """Option 18: (kernel_bx, kernel_bz, kernel_vectorpsi) of the adjoint context."""
         kx = np.zeros(self.shape); kz = np.zeros(self.shape); kp = np.zeros(self.shape)

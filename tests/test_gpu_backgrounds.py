@@ -56,3 +56,20 @@ def test_vector_potential_models_files(gpu_lib, tmp_path):
     p18 = small_params_2d(nx=nx, nz=nz, xlength=400e8, ylength=400e8, option=18)
     with Solver(p18, tab) as s18:
         s18.set_mhd2d_background(m["rho"], m["c"], m["p"], io.read_fits(str(tmp_path / "true" / "true_vectorpsi.fits")))
+
+
+def test_mhs_flux_tube_with_gpu_derivatives_matches_oracle(gpu_lib):
+    """The magnetohydrostatic tube built with the library's FP64 z derivative
+    equals the same construction with the oracle's, <= 1e-10."""
+    from oracle.oracle import Oracle
+    from cases import small_params
+    from sparc_gb300.background import mhs_flux_tube_background, polytrope_table
+    from sparc_gb300.solver import Solver
+    p = small_params(nx=64, ny=64, nz=96, xlength=100e8, ylength=100e8, npmlbot=8, npmltop=0, option=10)
+    tab = polytrope_table(p.nz, z_bot_mm=-25.0, z_top_mm=0.0)
+    with Solver(p, tab) as s:
+        got, gi = mhs_flux_tube_background(p, tab, s.ddz)
+    ref, ri = mhs_flux_tube_background(p, tab, Oracle(p.replace(option=4), tab).ddz)
+    for g, r in zip(got, ref):
+        assert rel_l2(g, r) < 1e-10, rel_l2(g, r)
+    assert gi["min_p_ratio"] > 0.5 and gi["residual_l2_rel"] < 2e-2

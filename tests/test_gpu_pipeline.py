@@ -96,3 +96,27 @@ def test_kernel_pipeline_fp32_against_fp64(gpu_lib):
             if rms[r] >= 1e-2 * rms.max():
                 shifts.append(abs(compute_tt(a.seismograms[s, :, r], b.seismograms[s, :, r], dt)))
     assert len(shifts) >= 8 and max(shifts) < 0.05, shifts
+
+
+def test_run_sharded_on_one_rank_equals_the_batched_sum(gpu_lib):
+    """run_sharded (device kernel sum, all-reduce over the ranks; one rank
+    here) gives the summed kernels of KernelPipeline.run bit for bit, and its
+    kernels_device output equals the host read-out of sparc_gpu_kernels."""
+    import torch
+    from oracle import oracle as O
+    from sparc_gb300 import sources
+    from sparc_gb300.pipeline import KernelPipeline, run_sharded
+    p = pipeline_params(nsrc=3)
+    tab = table_for(p)
+    planes = [sources.gaussian_plane(p, 2.0, x0, 1.0) for x0 in (-6.0, 0.0, 5.0)]
+    series = O.forward_source(p, p.maxtime + 10) * 1e3
+    pix = sources.receiver_pixels(p, n=8, radius_mm=10.0)
+    pl = KernelPipeline(p, tab, segment=4)
+    obs = np.zeros((3, pl.nt, p.ny, p.nx))
+    ref = pl.run(planes, series, obs, pix, sum_slots=True)
+    out = run_sharded(p, tab, planes, series, obs, pix, segment=4)
+    assert out.sources == [0, 1, 2]
+    k = out.kernels.cpu().numpy()
+    assert np.abs(ref.kc).max() > 0
+    assert np.array_equal(k[0], ref.kc) and np.array_equal(k[1], ref.krho) and np.array_equal(k[2], ref.hessian)
+    assert out.kernels.dtype == torch.float64 and out.kernels.is_cuda

@@ -1,6 +1,7 @@
 """Serving: continuous batching with per-slot clocks.  A request's result is
-the same alone and in a mix of concurrent requests of several grid sizes that
-join running batches at different times."""
+the same alone and in a mix of concurrent requests of several grid sizes and
+both backgrounds (quiet Sun, magnetohydrostatic flux tube) that join running
+batches at different times."""
 import copy
 
 import numpy as np
@@ -17,7 +18,7 @@ def engine(precision):
 
 
 def mix():
-    from sparc_gb300.serving import Request
+    from sparc_gb300.serving import TUBE, Request
     return [
         Request(0, (32, 32, 48), "fwd+adj", 60, 3.0, -5.0, 0.00),
         Request(1, (64, 64, 64), "fwd", 90, -20.0, 10.0, 0.00),
@@ -25,6 +26,8 @@ def mix():
         Request(3, (32, 32, 48), "fwd+adj", 75, 12.0, 4.0, 0.02),
         Request(4, (64, 64, 64), "fwd+adj", 60, 5.0, 5.0, 0.05),
         Request(5, (32, 32, 48), "fwd", 30, 0.0, 0.0, 0.10),
+        Request(6, (64, 64, 64), "fwd+adj", 45, 30.0, -10.0, 0.02, background=TUBE),
+        Request(7, (64, 64, 64), "fwd", 60, -15.0, 25.0, 0.04, background=TUBE),
     ]
 
 
@@ -33,8 +36,8 @@ def test_result_same_alone_and_in_mix(gpu_lib, precision):
     eng = engine(precision)
     done = {r.rid: r for r in eng.run(mix())}
     eng.close()
-    assert sorted(done) == list(range(6))
-    for rid in (0, 3, 4):
+    assert sorted(done) == list(range(8))
+    for rid in (0, 3, 4, 6):
         alone = copy.deepcopy([r for r in mix() if r.rid == rid][0])
         alone.arrival = 0.0
         e2 = engine(precision)
@@ -45,6 +48,7 @@ def test_result_same_alone_and_in_mix(gpu_lib, precision):
         assert np.abs(a.records).max() > 0
         np.testing.assert_array_equal(m.records, a.records)
         np.testing.assert_array_equal(m.adj_records, a.adj_records)
+        assert np.isfinite(m.records).all() and np.isfinite(m.adj_records).all()
 
 
 def test_latency_stats_and_stream(gpu_lib):

@@ -78,9 +78,24 @@ def test_shipped_31_steps_match_oracle(gpu_lib, oracle_mod, shipped, option, pre
     for f in (0, 2, 3, 5):
         e = rel_l2(ag[f], ao[f])
         assert e < tol, (option, prec, f, e)
+    pml_bound = [tol] * po.shape[0]
+    if prec == "f32":
+        # the PML auxiliaries within 2e-5 or twice the per-stage FP32
+        # kernels' own error on the same case
+        os.environ["SPARC_FP32_PER_STAGE"] = "1"
+        try:
+            gp = Solver(p.replace(precision=prec), tab)
+        finally:
+            os.environ.pop("SPARC_FP32_PER_STAGE", None)
+        gp.set_state(a0, pml0)
+        gp.set_source_series(plane, series)
+        gp.step(31)
+        pp = gp.state()[1]
+        gp.close()
+        pml_bound = [max(tol, 2 * rel_l2(pp[f], po[f])) for f in range(po.shape[0])]
     for f in range(po.shape[0]):
         if np.abs(po[f]).max() > 0:
-            assert rel_l2(pg[f], po[f]) < tol, (option, prec, "pml", f)
+            assert rel_l2(pg[f], po[f]) < pml_bound[f], (option, prec, "pml", f, rel_l2(pg[f], po[f]))
     o.close()
     g.close()
 

@@ -9,9 +9,10 @@ from sparc_gb300 import serving
 class FakePool:
     created = 0
 
-    def __init__(self, p, table, role, slots, max_records):
+    def __init__(self, p, table, role, slots, max_records, background="quiet", tube_cache=None):
         FakePool.created += 1
         self.role = role
+        self.background = background
         self.p = p.replace(nsrc=slots)
         self.requests = [None] * slots
         self.clock = [0] * slots
@@ -49,7 +50,7 @@ def fake(monkeypatch):
     FakePool.created = 0
     monkeypatch.setattr(serving, "Pool", FakePool)
     monkeypatch.setattr(serving.Engine, "_adjoint_planes", lambda self, pl, req: None)
-    monkeypatch.setattr(serving, "polytrope_table", lambda nz: None)
+    monkeypatch.setattr(serving, "polytrope_table", lambda nz, **kw: None)
     return FakePool
 
 
@@ -79,3 +80,23 @@ def test_a_pool_above_the_budget_is_an_error(fake):
     eng = serving.Engine("f64", hbm_budget=1e9, slots={(512, 512, 300): 2}, max_steps=30)
     with pytest.raises(RuntimeError, match="above the HBM budget"):
         eng.run(reqs, max_wall=30.0)
+
+
+def test_flux_tube_requests_get_their_own_pools(fake):
+    """Requests on the flux tube and on the quiet Sun of the same grid never
+    share a pool: the background belongs to the pool."""
+    reqs = [serving.Request(i, (128, 128, 150), "fwd", 30, 0.0, 0.0, 0.0,
+                            background=(serving.TUBE if i % 2 else serving.QUIET)) for i in range(8)]
+    eng = serving.Engine("f32", hbm_budget=1e12, slots={(128, 128, 150): 8}, max_steps=30)
+    done = eng.run(reqs, max_wall=30.0)
+    assert len(done) == 8
+    kinds = sorted(pl.background for pl in eng.pools)
+    assert kinds == [serving.QUIET, serving.TUBE]
+    for pl in eng.pools:
+        assert pl.p.option == (10 if pl.background == serving.TUBE else 4)
+
+
+def test_stream_mixes_backgrounds():
+    reqs = serving.poisson_stream(200, seed=3, p_tube=0.25)
+    n_tube = sum(r.background == serving.TUBE for r in reqs)
+    assert 30 < n_tube < 70
