@@ -266,7 +266,29 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
         int dev = 0, nsm = 152;
         if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaGetLastError();
-        const long long cols = (long long)c->M * S;
+        // FP64 quiet displacement forms: lanes per pencil (stage_chunk_kernel),
+        // the smallest of 1, 2, 4, 8 that gives one source 64 Ki lanes, with
+        // chunks of at least 12 levels; it depends on the grid only, so a
+        // source's arithmetic does not depend on the batch around it.
+        // SPARC_STAGE_LANES forces 1, 2, 4 or 8 (a switch the tests use to
+        // compare the chunkings)
+        if (!c->f32 && (p->option == 4 || p->option == 17)) {
+            int q = 1;
+            for (int cand = 2; cand <= 8 && (long long)c->M * q < 65536; cand *= 2) {
+                const int ch = (c->nz + cand - 1) / cand;
+                if (ch < 12 || (cand - 1) * ch >= c->nz) break;
+                q = cand;
+            }
+            if (const char* e = getenv("SPARC_STAGE_LANES")) {
+                const int v = atoi(e);
+                const int ch = v > 0 ? (c->nz + v - 1) / v : 0;
+                if ((v == 1 || v == 2 || v == 4 || v == 8) && (v == 1 || (ch >= 2 && (v - 1) * ch < c->nz))) q = v;
+            }
+            c->stage_q = q;
+            c->stage_chunk = (c->nz + q - 1) / q;
+        }
+        if ((rc = dalloc(c, &c->zc, (size_t)4 * c->nz * es))) return bail(rc);
+        const long long cols = (long long)c->M * S * c->stage_q;
         c->stage_block = 128;
         while (c->stage_block > 32 && (cols + c->stage_block - 1) / c->stage_block < 2LL * nsm) c->stage_block /= 2;
     }
@@ -585,6 +607,29 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     } else {
         if ((rc = upload(c, c->zt, c->zt_host.data(), c->zt_host.size() * 8))) return rc;
         if ((rc = upload(c, c->pt, c->pt_host.data(), c->pt_host.size() * 8))) return rc;
+        if (c->stage_q > 1) {
+            // products of the elimination multipliers over each chunk of
+            // stage_chunk levels (stage_chunk_kernel): H(j) from the chunk's
+            // first level up to j of m = -low/betad, G(j) from j to the chunk's
+            // last level of g = -gam(j+1); xi_z code, then p' code
+            const bool d3 = (P.option == 4);
+            const int bcs[2] = {d3 ? 1 : 3, d3 ? 0 : 2};
+            const int C = c->stage_chunk;
+            std::vector<double> zc((size_t)4 * nz, 0.0);
+            for (int k = 0; k < 2; ++k) {
+                const Tri& t = tri[bcs[k]];
+                double* H = zc.data() + (size_t)(2 * k) * nz;
+                double* G = zc.data() + (size_t)(2 * k + 1) * nz;
+                for (int j0 = 0; j0 < nz; j0 += C) {
+                    const int j1 = std::min(j0 + C, nz);
+                    double pr = 1.0;
+                    for (int j = j0; j < j1; ++j) { pr *= -t.low[j] / t.betad[j]; H[j] = pr; }
+                    pr = 1.0;
+                    for (int j = j1 - 1; j >= j0; --j) { pr *= (j == nz - 1) ? 0.0 : -t.gam[j + 1]; G[j] = pr; }
+                }
+            }
+            if ((rc = upload(c, c->zc, zc.data(), zc.size() * 8))) return rc;
+        }
     }
     size_t cs = csz(c);
     CK(cudaMemsetAsync(c->a, 0, (size_t)c->S * c->nf * c->fs * cs, c->stream));
@@ -846,6 +891,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     A.fs = c->fs; A.ps = c->ps; A.M = c->M; A.nz = c->nz;
     A.npmlbot = P.npmlbot; A.npmltop = P.npmltop; A.option = P.option; A.damp = P.damp_waves && P.option != 17;
     A.block = c->stage_block;
+    A.q = c->stage_q; A.chunk = c->stage_chunk; A.zc = (const T*)c->zc;
     A.cc.C1 = (T)c->cc64.C1; A.cc.C2 = (T)c->cc64.C2;
     for (int i = 0; i < 5; ++i) A.cc.Cb[i] = (T)c->cc64.Cb[i];
     for (int i = 0; i < 4; ++i) A.cc.Cf[i] = (T)c->cc64.Cf[i];

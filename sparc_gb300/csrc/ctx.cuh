@@ -43,6 +43,8 @@ struct sparc_ctx {
     int fused_pencils = 4;                        // modes per CTA of the fused step (autotuned)
     int fused_test_nocopy = 0;                    // test switch: the fused step's table copy is not issued
     int stage_block = 128;                        // threads per CTA of the per-stage kernels (autotuned)
+    int stage_q = 1, stage_chunk = 0;             // FP64 stage: lanes per pencil and levels per lane
+    void* zc = nullptr;                           // their chunk products of the multipliers (4 rows of nz)
     double* zt64 = nullptr; double* pt64 = nullptr;
     double* tw_x = nullptr; double* tw_y = nullptr;
     void* tmp = nullptr;          // FFT intermediate, nz*M complex T

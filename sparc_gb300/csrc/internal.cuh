@@ -316,6 +316,8 @@ template <typename T> struct StageArgs {
     int M, nz, npmlbot, npmltop, option, damp;
     int has_scr;
     int block;          // threads per CTA (64 or 128; same results, a tuning choice)
+    int q, chunk;       // lanes per pencil (1, 2, 4, 8) and levels per lane (stage_chunk_kernel)
+    const T* zc;        // its products of the elimination multipliers: H, G of the xi_z code, H, G of the p' code
     T beta;
     Compact<T> cc;
     // source injection at plane ksrc (0-based)

@@ -292,6 +292,261 @@ __global__ void __launch_bounds__(128) stage_velocity_kernel(const StageArgs<T> 
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same RK stage with each z-pencil cut into Q chunks of C levels, one
+// chunk per lane (the Q lanes of a mode are consecutive lanes of one warp).
+// A pencil's two tridiagonal solves are first-order recurrences: each lane
+// eliminates its chunk with a zero carry, the chunk maps u -> B + M u are
+// composed by a scan over the Q lanes (warp shuffles, exact FP64 products),
+// and each level adds H(j) times the carry, H(j) the product of the
+// multipliers from the chunk start to j (host FP64, table zc); the back
+// substitution likewise from above with G(j).  This is the elimination and
+// back substitution of the one-lane form (mtridag.f90:94-111), re-associated.
+// Per solve three passes over the chunk: up (right-hand side, zero-carry
+// elimination -> y), down (fix with H, zero-carry back substitution -> y),
+// and the fix with G feeding the point-wise work of the one-lane form's S2 /
+// S4.  The p' neighbours of the second solve come from the other lanes'
+// chunks in global memory, after a warp barrier.  Q > 1 puts Q times more
+// warps on small grids (8320 modes at 128x128), which the FP64 pipe needs.
+// ---------------------------------------------------------------------------
+template <typename T> struct AffZ {
+    typename CplxOf<T>::type B;
+    T M;
+};
+
+template <typename T, int Q, bool FWD>
+__device__ __forceinline__ typename CplxOf<T>::type chunk_scan(typename CplxOf<T>::type B, T M, int c) {
+    typedef typename CplxOf<T>::type CT;
+    // inclusive scan over the Q lanes of a mode (FWD: from chunk 0 up; else
+    // from chunk Q-1 down), then the exclusive carry into this chunk
+    CT b = B;
+    T mm = M;
+    #pragma unroll
+    for (int d = 1; d < Q; d <<= 1) {
+        CT ob;
+        T om;
+        if (FWD) {
+            ob.x = __shfl_up_sync(0xffffffffu, b.x, d, Q); ob.y = __shfl_up_sync(0xffffffffu, b.y, d, Q);
+            om = __shfl_up_sync(0xffffffffu, mm, d, Q);
+        } else {
+            ob.x = __shfl_down_sync(0xffffffffu, b.x, d, Q); ob.y = __shfl_down_sync(0xffffffffu, b.y, d, Q);
+            om = __shfl_down_sync(0xffffffffu, mm, d, Q);
+        }
+        if (FWD ? (c >= d) : (c + d < Q)) {      // this chunk's map after the other's
+            b = b + mm * ob;
+            mm = mm * om;
+        }
+    }
+    CT ex;
+    if (FWD) {
+        ex.x = __shfl_up_sync(0xffffffffu, b.x, 1, Q); ex.y = __shfl_up_sync(0xffffffffu, b.y, 1, Q);
+        if (c == 0) ex = czero<CT>();
+    } else {
+        ex.x = __shfl_down_sync(0xffffffffu, b.x, 1, Q); ex.y = __shfl_down_sync(0xffffffffu, b.y, 1, Q);
+        if (c == Q - 1) ex = czero<CT>();
+    }
+    return ex;
+}
+
+// Right-hand side of the compact first derivative at level j (dbyd2.f90:
+// 88-173) of the values ld(j'), boundary code bc; bot / top: the caller-set
+// values of bc 2 / 3.
+template <typename CT, typename T, typename Load>
+__device__ __forceinline__ CT compact_rhs(int j, int nz, int bc, Load ld, CT bot, CT top, const Compact<T>& c) {
+    if (j >= 2 && j <= nz - 3) return c.C1 * (ld(j + 1) - ld(j - 1)) + c.C2 * (ld(j + 2) - ld(j - 2));
+    if (j <= 1) {
+        const CT b0 = ld(0), b1 = ld(1), b2 = ld(2), b3 = ld(3), b4 = ld(4);
+        const CT r1 = c.Cb[0] * b0 + c.Cb[1] * b1 + c.Cb[2] * b2 + c.Cb[3] * b3 + c.Cb[4] * b4;
+        if (j == 1) return r1;
+        if (bc == 0) return czero<CT>();
+        if (bc == 2) return bot;
+        const CT r0 = c.Cf[0] * b0 + c.Cf[1] * b1 + c.Cf[2] * b2 + c.Cf[3] * b3;
+        return (c.alpha2 * r0 - c.beta1 * r1) * c.cnst;
+    }
+    const CT b0 = ld(nz - 1), b1 = ld(nz - 2), b2 = ld(nz - 3), b3 = ld(nz - 4), b4 = ld(nz - 5);
+    const CT rn2 = -(c.Cb[0] * b0 + c.Cb[1] * b1 + c.Cb[2] * b2 + c.Cb[3] * b3 + c.Cb[4] * b4);
+    if (j == nz - 2) return rn2;
+    if (bc == 0) return czero<CT>();
+    if (bc == 3) return top;
+    const CT rn1 = -(c.Cf[0] * b0 + c.Cf[1] * b1 + c.Cf[2] * b2 + c.Cf[3] * b3);
+    return (c.alpha2 * rn1 - c.beta1 * rn2) * c.cnst;
+}
+
+// One chunked solve: d/dz (without stretch) of ld over the lane's chunk
+// [j0, j1) of boundary code bc; y: the pencil's scratch column (this lane's
+// levels only; written only when store, i.e. by lanes of real modes).
+// emit(j, dz) is called for every level of the chunk, top down.  zh, zg: the
+// H and G rows of bc for this chunking.
+template <typename T, int Q, typename Load, typename Emit>
+__device__ __forceinline__ void chunk_solve(int j0, int j1, int c, int nz, int bc, Load ld,
+                                            typename CplxOf<T>::type top, const T* __restrict__ low,
+                                            const T* __restrict__ ibd, const T* __restrict__ gam,
+                                            const T* __restrict__ zh, const T* __restrict__ zg, const Compact<T>& cc,
+                                            typename CplxOf<T>::type* __restrict__ y, long long M, bool store,
+                                            Emit emit) {
+    typedef typename CplxOf<T>::type CT;
+    // up: zero-carry elimination UD(J) = (R(J) - A(J) UD(J-1)) / BETAD(J)
+    CT run = czero<CT>();
+    for (int j = j0; j < j1; ++j) {
+        const CT R = compact_rhs<CT, T>(j, nz, bc, ld, czero<CT>(), top, cc);
+        run = (R - __ldg(&low[j]) * run) * __ldg(&ibd[j]);
+        if (store) y[(long long)j * M] = run;
+    }
+    const CT uin = chunk_scan<T, Q, true>(run, j1 > j0 ? __ldg(&zh[j1 - 1]) : (T)1, c);
+    // down: UD(J) = y(J) + H(J) uin, then zero-carry back substitution
+    CT x = czero<CT>();
+    for (int j = j1 - 1; j >= j0; --j) {
+        const CT ud = y[(long long)j * M] + __ldg(&zh[j]) * uin;
+        x = (j == j1 - 1) ? ud : ud - __ldg(&gam[j + 1]) * x;
+        if (store) y[(long long)j * M] = x;
+    }
+    const CT xin = chunk_scan<T, Q, false>(x, j1 > j0 ? __ldg(&zg[j0]) : (T)1, c);
+    for (int j = j1 - 1; j >= j0; --j) emit(j, y[(long long)j * M] + __ldg(&zg[j]) * xin);
+}
+
+template <typename T, int Q>
+__global__ void __launch_bounds__(128) stage_chunk_kernel(const StageArgs<T> A) {
+    typedef typename CplxOf<T>::type CT;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = gt % Q;
+    const int m0 = gt / Q;
+    const bool valid = m0 < A.M;
+    const int m = valid ? m0 : A.M - 1;      // lanes past the last mode repeat it and store nothing
+    const int s = blockIdx.y;
+    const int nz = A.nz, C = A.chunk;
+    const int j0 = c * C, j1 = min(j0 + C, nz);
+    const long long M = A.M, fs = A.fs;
+    CT* __restrict__ a = A.a + (long long)s * 6 * fs + m;
+    CT* __restrict__ scr = A.scr + (long long)s * 6 * fs + m;
+    CT* __restrict__ pml = A.pml + (long long)s * 2 * A.ps + m;
+    CT* __restrict__ spml = A.scrpml + (long long)s * 2 * A.ps + m;
+    CT* __restrict__ y = A.ybuf + (long long)s * fs + m;
+    CT* __restrict__ pb = A.pbuf + (long long)s * fs + m;
+    CT* __restrict__ rb = A.rbuf + (long long)s * fs + m;
+    const T* __restrict__ zt = A.zt;
+    const T* __restrict__ zc = A.zc;
+    const T kx = __ldg(&A.pt[PT_KX * M + m]);
+    const T ky = __ldg(&A.pt[PT_KY * M + m]);
+    const T gd = A.damp ? __ldg(&A.pt[PT_DAMP * M + m]) : (T)0;
+    const T beta = A.beta;
+    const bool hs = A.has_scr != 0;
+    const bool opt3d = (A.option == 4);
+    const int nb = A.npmlbot, nt = A.npmltop;
+    const int bcx = opt3d ? 1 : 3, bcp = opt3d ? 0 : 2;
+
+    auto temp = [&](int f, int j) -> CT {
+        long long o = f * fs + (long long)j * M;
+        CT v = a[o];
+        if (hs) v = v + beta * scr[o];
+        return v;
+    };
+    auto pmlidx = [&](int j) -> int { return j < nb ? j : (j >= nz - nt ? nb + (j - (nz - nt)) : -1); };
+
+    // ---- solve 1: d(xi_z)/dz; then div, p', rho' and the horizontal RHS (S2) ----
+    CT top = czero<CT>();
+    if (!opt3d && j1 == nz) {   // physics2d.f90:960: dxizdz(nz) = -dxixdx(nz) * unstretch(nz)
+        CT xx = temp(0, nz - 1);
+        top = -(imul(kx, xx) * __ldg(&zt[ZT_UNSTRETCH * nz + nz - 1]));
+    }
+    chunk_solve<T, Q>(j0, j1, c, nz, bcx, [&](int j) { return temp(2, j); }, top, zt + (ZT_TH + 3 * bcx) * nz,
+                      zt + (ZT_TH + 3 * bcx + 1) * nz, zt + (ZT_TH + 3 * bcx + 2) * nz, zc, zc + nz, A.cc, y, M,
+                      valid, [&](int j, CT ud) {
+        if (!valid) return;
+        CT dz = ud * __ldg(&zt[ZT_STRETCH * nz + j]);
+        int ip = pmlidx(j);
+        if (ip >= 0) {
+            long long o = (long long)ip * M;
+            CT psi = pml[o];
+            if (hs) psi = psi + beta * spml[o];
+            spml[o] = __ldg(&zt[ZT_AZ * nz + j]) * dz + __ldg(&zt[ZT_BZ * nz + j]) * psi;
+            dz = dz + psi;
+        }
+        CT xx = temp(0, j), xz = temp(2, j);
+        CT div;
+        if (opt3d) div = imul(kx, xx) + imul(ky, temp(1, j)) + dz;
+        else div = imul(kx, xx) + dz;
+        CT p = -__ldg(&zt[ZT_C2RHO0 * nz + j]) * div - __ldg(&zt[ZT_GRADP0 * nz + j]) * xz;
+        CT r = -__ldg(&zt[ZT_RHO0 * nz + j]) * div - __ldg(&zt[ZT_GRADRHO0 * nz + j]) * xz;
+        long long o = (long long)j * M;
+        pb[o] = p;
+        rb[o] = r;
+        CT vx = temp(3, j);
+        const T ri = __ldg(&zt[ZT_RHOINV * nz + j]);
+        bool zero_row = opt3d ? (j == 0 || j == nz - 1) : (j == 0);
+        if (opt3d) {
+            CT vy = temp(4, j);
+            CT rvx = -ri * imul(kx, p);
+            CT rvy = -ri * imul(ky, p);
+            if (A.damp) { rvx = rvx - gd * vx; rvy = rvy - gd * vy; }
+            if (zero_row) { rvx = czero<CT>(); rvy = czero<CT>(); vx = czero<CT>(); vy = czero<CT>(); }
+            scr[3 * fs + o] = rvx;
+            scr[4 * fs + o] = rvy;
+            scr[0 * fs + o] = vx;
+            scr[1 * fs + o] = vy;
+        } else {
+            CT rvx = -ri * imul(kx, p);
+            if (zero_row) { rvx = czero<CT>(); vx = czero<CT>(); }
+            scr[3 * fs + o] = rvx;
+            scr[0 * fs + o] = vx;
+            scr[4 * fs + o] = czero<CT>();
+            scr[1 * fs + o] = czero<CT>();
+        }
+    });
+    // the second solve reads p' two levels into the neighbouring chunks
+    __syncwarp();
+
+    // ---- solve 2: dp'/dz; RHS v_z (+ source, damping) and xi_z (S4) ----
+    CT F = czero<CT>();
+    const int tl = *A.clk.time - A.clk.t0[s];
+    const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl) && A.ksrc >= j0 && A.ksrc < j1;
+    if (src_on) {
+        const CT* pl = A.planes + (long long)s * A.plane_ss + m;
+        if (A.src_mode == 1) {
+            T w = (tl < A.nseries) ? (T)A.series[(long long)s * A.nseries + tl] : (T)0;
+            F = w * pl[0];
+        } else {
+            int idx[7];
+            double w[7];
+            const int nw = lagrange_dev(A.clk, tl, A.L, idx, w);
+            #pragma unroll
+            for (int l = 0; l < 7; ++l)
+                if (l < nw) F = F + (T)w[l] * pl[(long long)idx[l] * M];
+        }
+    }
+    chunk_solve<T, Q>(j0, j1, c, nz, bcp, [&](int j) { return pb[(long long)j * M]; }, czero<CT>(),
+                      zt + (ZT_TH + 3 * bcp) * nz, zt + (ZT_TH + 3 * bcp + 1) * nz, zt + (ZT_TH + 3 * bcp + 2) * nz,
+                      zc + 2 * nz, zc + 3 * nz, A.cc, y, M, valid, [&](int j, CT ud) {
+        if (!valid) return;
+        CT dp = ud * __ldg(&zt[ZT_STRETCH * nz + j]);
+        int ip = pmlidx(j);
+        if (ip >= 0) {
+            long long o = (long long)ip * M + A.ps;
+            CT psi = pml[o];
+            if (hs) psi = psi + beta * spml[o];
+            spml[o] = __ldg(&zt[ZT_AZ * nz + j]) * dp + __ldg(&zt[ZT_BZ * nz + j]) * psi;
+            dp = dp + psi;
+        }
+        long long o = (long long)j * M;
+        CT vz = temp(5, j);
+        const T ri = __ldg(&zt[ZT_RHOINV * nz + j]);
+        const T gz = __ldg(&zt[ZT_G * nz + j]);
+        CT r = rb[o];
+        CT rv;
+        if (opt3d) {
+            rv = -ri * dp;
+            rv = rv - (gz * ri) * r;
+        } else {
+            rv = -ri * (dp + gz * r);
+        }
+        if (src_on && j == A.ksrc) rv = rv + A.src_scale * F;
+        if (A.damp) rv = rv - gd * vz;
+        bool zero_row = opt3d ? (j == 0 || j == nz - 1) : (j == 0);
+        if (zero_row) { rv = czero<CT>(); vz = czero<CT>(); }
+        scr[5 * fs + o] = rv;
+        scr[2 * fs + o] = vz;
+    });
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     typedef typename CplxOf<T>::type CT;
@@ -413,6 +668,13 @@ void launch_tick(int* time, cudaStream_t s) { tick_kernel<<<1, 1, 0, s>>>(time);
 
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s) {
     const int b = A.block == 32 ? 32 : A.block == 64 ? 64 : 128;
+    if (A.option != 2 && A.q > 1) {
+        dim3 grid((unsigned)(((long long)A.M * A.q + b - 1) / b), nsrc);
+        if (A.q == 2) stage_chunk_kernel<T, 2><<<grid, b, 0, s>>>(A);
+        else if (A.q == 4) stage_chunk_kernel<T, 4><<<grid, b, 0, s>>>(A);
+        else stage_chunk_kernel<T, 8><<<grid, b, 0, s>>>(A);
+        return;
+    }
     dim3 grid((A.M + b - 1) / b, nsrc);
     if (A.option == 2) stage_velocity_kernel<T><<<grid, b, 0, s>>>(A);
     else stage_kernel<T><<<grid, b, 0, s>>>(A);

@@ -217,8 +217,17 @@ def config_flux_tube_256():
     """The flux-tube configuration: option 10 on 256x256x300, 200 Mm
     periodic, PML 10 at the bottom; the box ends at the surface (z = 0),
     where a 2 kG tube can still be in magnetohydrostatic balance with the gas
-    pressure (above it the pressure falls by e every ~100 km).  Returns
-    (params, polytrope table)."""
+    pressure (above it the pressure falls by e every ~100 km); receivers
+    200 km and the source 400 km below it.  Returns (params, polytrope
+    table)."""
     from .background import polytrope_table
-    p = config_quiet_256().replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0)
+    p = config_quiet_256().replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0, obsheight=TUBE_OBSHEIGHT,
+                                   excitdep=TUBE_EXCITDEP)
     return p, polytrope_table(p.nz, z_bot_mm=-25.0, z_top_mm=0.0)
+
+
+#: observation height and source depth of the flux-tube box (cm): its top is
+#: z = 0, so the receivers (an adjoint source) and the forward source sit 200
+#: and 400 km below it, strictly inside on every grid of 32 levels or more
+TUBE_OBSHEIGHT = -2.0e7
+TUBE_EXCITDEP = -4.0e7

@@ -31,7 +31,7 @@ import numpy as np
 
 from . import sources
 from .background import mhs_flux_tube_background, polytrope_table
-from .params import OPT_MHD_PML_3D_DISPL, SparcParams
+from .params import OPT_MHD_PML_3D_DISPL, TUBE_EXCITDEP, TUBE_OBSHEIGHT, SparcParams
 from .solver import Solver
 
 QUIET, TUBE = "quiet", "tube"
@@ -60,14 +60,15 @@ class Request:
 
 def grid_params(grid, precision: str, base: SparcParams | None = None, background: str = QUIET) -> SparcParams:
     """200 Mm periodic box for every grid size; the flux tube runs option 10
-    with the PML at the bottom only (its box ends at the surface)."""
+    with the PML at the bottom only, receivers and source 200 and 400 km
+    below the top (its box ends at the surface)."""
     nx, ny, nz = grid
     b = base or SparcParams()
     length = 200.0e8
     p = b.replace(nx=nx, ny=ny, nz=nz, xlength=length, ylength=length, npmlbot=10, npmltop=10,
                   excitdep=-15000000.0, obsheight=20000000.0, precision=precision)
     if background == TUBE:
-        p = p.replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0)
+        p = p.replace(option=OPT_MHD_PML_3D_DISPL, npmltop=0, obsheight=TUBE_OBSHEIGHT, excitdep=TUBE_EXCITDEP)
     return p
 
 
