@@ -1451,11 +1451,11 @@ int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const
     if (c->f32) {
         to_t_kernel<float><<<nb256(npz), 256, 0, c->stream>>>((float*)m.pab, W(W_AZ), npz);
         to_t_kernel<float><<<nb256(npz), 256, 0, c->stream>>>((float*)m.pab + npz, W(W_BZP), npz);
-        to_t_kernel<float><<<1, 256, 0, c->stream>>>((float*)m.g, d_g, nz);
+        to_t_kernel<float><<<nb256(nz), 256, 0, c->stream>>>((float*)m.g, d_g, nz);
     } else {
         to_t_kernel<double><<<nb256(npz), 256, 0, c->stream>>>((double*)m.pab, W(W_AZ), npz);
         to_t_kernel<double><<<nb256(npz), 256, 0, c->stream>>>((double*)m.pab + npz, W(W_BZP), npz);
-        to_t_kernel<double><<<1, 256, 0, c->stream>>>((double*)m.g, d_g, nz);
+        to_t_kernel<double><<<nb256(nz), 256, 0, c->stream>>>((double*)m.g, d_g, nz);
     }
     CKL();
     // source planes: erad_2d = e_rad, orad_2d = o_rad (physics2d.f90:334-341)
