@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--mhd-grid", default="", help="NXxNYxNZ of the flux-tube line (default: the bench grid)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the serving stream (0: skip)")
     ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
+    ap.add_argument("--full-length", default="", choices=["", "config4", "config3", "serving"],
+                    help="one full-length workload instead of the bench line (see full_length_*)")
     return ap.parse_args()
 
 
@@ -253,25 +255,29 @@ def issue_roofline(winst, launch_ms, clocks, sm_count):
                       "times nsrc"}
 
 
-def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, seed: int = 0):
+def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, seed: int = 0,
+                    max_wall: float = 240.0):
     """Config-5 stream: Poisson arrivals (rate/s) of 1-4 h forward or
     forward+adjoint requests on 128^2x150 / 256^2x300 / 512^2x300 (60/30/10 %),
     request lengths divided by `compress`.  Latency = finish - arrival (wall)."""
     from sparc_gb300.serving import Engine, latency_stats, poisson_stream
+    import torch
     reqs = poisson_stream(n, rate=rate, seed=seed, compress=compress)
-    eng = Engine(precision=precision, hbm_budget=120e9,
+    budget = 0.85 * torch.cuda.mem_get_info()[0]          # HBM free at the start, with a margin
+    eng = Engine(precision=precision, hbm_budget=budget,
                  slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
                  max_steps=max(r.nsteps for r in reqs))
     t0 = time.perf_counter()
     try:
-        done = eng.run(reqs, max_wall=240.0)
+        done = eng.run(reqs, max_wall=max_wall)
     finally:
         eng.close()
     wall = time.perf_counter() - t0
     pts = sum(r.grid[0] * r.grid[1] * r.grid[2] * r.nsteps * (2 if r.kind == "fwd+adj" else 1) for r in done)
     st = latency_stats(done)
     st.update({"precision": precision, "Mpoint_steps_per_s": pts / wall / 1e6, "wall_s": wall,
-               "compress": compress, "rate_per_s": rate})
+               "compress": compress, "rate_per_s": rate, "hbm_budget_gb": budget / 1e9,
+               "flux_tube_requests": sum(r.background == "tube" for r in done)})
     return st
 
 
@@ -462,6 +468,128 @@ def mhd_section(steps=5, warmup=2, precs=("f64", "f32"), grid=None, acc_steps=15
     return out
 
 
+def _rel(x, y) -> float:
+    return float(np.linalg.norm((np.asarray(x) - np.asarray(y)).ravel()) / max(np.linalg.norm(np.asarray(y).ravel()),
+                                                                                1e-300))
+
+
+def _tt_shifts(a, b, dt):
+    """Travel-time shifts (COMPUTE_TT) of seismograms b against a, (nrec,
+    nreceivers), on the receivers the wave has reached (rms >= 1 % of the
+    strongest)."""
+    from sparc_gb300.pipeline import compute_tt
+    rms = np.sqrt(np.mean(a ** 2, axis=0))
+    return [abs(compute_tt(a[:, r], b[:, r], dt)) for r in range(a.shape[1]) if rms[r] >= 1e-2 * rms.max()]
+
+
+def full_length_config4(batch=8, segment=24, compare=2):
+    """The 32-source forward x adjoint kernel workflow at full length: 256^2 x
+    300 quiet Sun, 4 h of solar time (the pipeline's forward run, adjoint run
+    and forward recomputation from device checkpoints), FP32 fields with FP64
+    accumulation, in batches of `batch` sources (the checkpoints and snapshot
+    store of 32 sources at once would exceed HBM).  The first `compare`
+    sources are run again through the FP64 pipeline one by one: their kernels
+    and seismograms are stated against FP64."""
+    from sparc_gb300 import sources
+    from sparc_gb300.pipeline import KernelPipeline
+    p0, tab = workload(False)
+    S = 32
+    series = sources.ricker_series(p0, p0.maxtime + 10)
+    pix = sources.receiver_pixels(p0)
+    planes = [source_inputs(p0, 64, gi, seed=4)[0] for gi in range(S)]
+    ksum = None
+    keep = {}
+    t0 = time.perf_counter()
+    batches = []
+    for b0 in range(0, S, batch):
+        tb = time.perf_counter()
+        pl = KernelPipeline(p0.replace(precision="f32", nsrc=batch), tab, segment=segment)
+        res = pl.run(planes[b0:b0 + batch], series, np.zeros((batch, pl.nt, p0.ny, p0.nx)), pix)
+        k = np.stack([res.kc.sum(0), res.krho.sum(0), res.hessian.sum(0)])
+        ksum = k if ksum is None else ksum + k
+        for i in range(b0, min(b0 + batch, compare)):
+            keep[i] = (res.kc[i - b0], res.krho[i - b0], res.hessian[i - b0], res.seismograms[i - b0])
+        batches.append(time.perf_counter() - tb)
+        log(f"config4: sources {b0}..{b0 + batch - 1} in {batches[-1]:.1f} s")
+        del res, pl
+    wall32 = time.perf_counter() - t0
+    steps = p0.maxtime + 1
+    out = {"workload": f"forward x adjoint kernel workflow, {p0.nx}x{p0.ny}x{p0.nz}, {S} sources, "
+                       f"{p0.solartime} h ({steps} steps per run; forward, adjoint and recomputed forward)",
+           "precision": "f32 fields, f64 set-up and accumulation", "batch": batch, "segment": segment,
+           "wall_s": wall32, "batch_wall_s": batches,
+           "point_steps": 3 * steps * p0.points * S,
+           "Mpoint_steps_per_s": 3 * steps * p0.points * S / wall32 / 1e6,
+           "kernel_sum_finite": bool(np.isfinite(ksum).all()), "kernel_sum_max_abs": float(np.abs(ksum).max())}
+    cmp = []
+    dt = p0.timestep * p0.steps
+    for i in range(compare):
+        tb = time.perf_counter()
+        pl = KernelPipeline(p0.replace(precision="f64", nsrc=1), tab, segment=segment)
+        r64 = pl.run([planes[i]], series, np.zeros((1, pl.nt, p0.ny, p0.nx)), pix)
+        kc, kr, hs, seis = keep[i]
+        sh = _tt_shifts(r64.seismograms[0], seis, dt)
+        cmp.append({"source": i, "fp64_wall_s": time.perf_counter() - tb,
+                    "seismogram_rel_l2": _rel(seis, r64.seismograms[0]),
+                    "kernel_rel_l2": {"kc": _rel(kc, r64.kc[0]), "krho": _rel(kr, r64.krho[0]),
+                                      "hessian": _rel(hs, r64.hessian[0])},
+                    "max_tt_shift_s": float(max(sh)) if sh else None, "receivers_timed": len(sh)})
+        del pl, r64
+    out["fp32_against_fp64"] = cmp
+    return out
+
+
+def full_length_config3(hours_fp64=1.0):
+    """The flux-tube configuration at full length: option 10 on the
+    magnetohydrostatic tube, 256^2 x 300, one source 20 Mm from the axis,
+    4 h of solar time forward in FP32, and the first `hours_fp64` hours in FP64
+    (130 ms per FP64 step makes the whole 4 h a 17-minute run); the FP32
+    seismograms (8 receivers on a 10 Mm ring around the source) are stated
+    against FP64 over that window."""
+    import torch
+    from sparc_gb300 import sources
+    from sparc_gb300.background import config3_background
+    from sparc_gb300.params import config_flux_tube_256
+    from sparc_gb300.solver import Solver
+    pm, tab = config_flux_tube_256()
+    pm = pm.replace(nsrc=1, solartime=4.0)
+    pix = sources.receiver_pixels(pm, n=8, radius_mm=10.0, x0_mm=20.0)
+    plane = sources.gaussian_plane(pm, 1.0, 20.0, 0.0)
+    series = sources.ricker_series(pm, pm.maxtime + 10)
+    out = {"grid": [pm.nx, pm.ny, pm.nz], "background": "magnetohydrostatic flux tube (config3_background)"}
+    bg = None
+    seis = {}
+    for prec, hours in (("f32", pm.solartime), ("f64", hours_fp64)):
+        p = pm.replace(precision=prec, solartime=hours)
+        s = Solver(p, tab)
+        if bg is None:
+            bg, info = config3_background(p, tab, s.ddz)
+            out["background_residual_l2_rel"] = info["residual_l2_rel"]
+        s.set_mhd_background(*bg)
+        s.set_source_series(plane, series)
+        n = p.maxtime + 1
+        s.record_surface(n // p.steps + 2)
+        st = torch.cuda.ExternalStream(s.stream_ptr)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(st)
+        s.step(n)
+        e1.record(st)
+        rec = s.records()
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+        s.sync(check_finite=True)
+        seis[prec] = np.stack([rec[:, iy, ix] for (iy, ix) in pix], axis=1)
+        out[prec] = {"hours": hours, "steps": n, "device_s": ms * 1e-3, "wall_s": wall,
+                     "Mpoint_steps_per_s": p.points * n / (ms * 1e-3) / 1e6, "records": int(rec.shape[0])}
+        s.close()
+    k = seis["f64"].shape[0]
+    sh = _tt_shifts(seis["f64"], seis["f32"][:k], pm.timestep * pm.steps)
+    out["fp32_against_fp64"] = {"window_records": k, "seismogram_rel_l2": _rel(seis["f32"][:k], seis["f64"]),
+                                "max_tt_shift_s": float(max(sh)) if sh else None, "receivers_timed": len(sh)}
+    return out
+
+
 def cpu_baseline(p, tab, steps=1):
     from oracle import oracle
     threads = os.cpu_count() or 1
@@ -609,6 +737,12 @@ def main():
     from sparc_gb300 import bytes_model
     from sparc_gb300 import dist as sd
     p0, tab = workload(args.small)
+    if args.full_length:
+        fn = {"config4": full_length_config4, "config3": full_length_config3,
+              "serving": lambda: serving_section("f32", args.serve_requests, min(args.serve_compress, 4.0),
+                                                 max_wall=1800.0)}[args.full_length]
+        print(json.dumps({"full_length": args.full_length, "result": fn()}), flush=True)
+        return 0
     if args.mhd_only:
         grid = tuple(int(v) for v in args.mhd_grid.lower().split("x")) if args.mhd_grid else None
         print(json.dumps({"mhd": mhd_section(steps=max(1, args.steps), warmup=max(1, args.warmup),

@@ -266,15 +266,19 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
         int dev = 0, nsm = 152;
         if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaGetLastError();
-        // FP64 quiet displacement forms: lanes per pencil (stage_chunk_kernel),
-        // the smallest of 1, 2, 4, 8 that gives one source 64 Ki lanes, with
-        // chunks of at least 12 levels; it depends on the grid only, so a
-        // source's arithmetic does not depend on the batch around it.
+        // FP64 quiet displacement forms: lanes per pencil (stage_chunk_kernel
+        // and update_chunk_kernel).  One lane per pencil when a source has at
+        // least 32 Ki pencils (the chunked form's carries and shuffles then
+        // cost more than the extra lanes give: 256x256 forward and adjoint
+        // run side by side 14 % faster on one lane than on two); else the
+        // smallest of 2, 4, 8 that gives one source 64 Ki lanes, with chunks
+        // of at least 12 levels.  It depends on the grid only, so a source's
+        // arithmetic does not depend on the batch around it.
         // SPARC_STAGE_LANES forces 1, 2, 4 or 8 (a switch the tests use to
         // compare the chunkings)
         if (!c->f32 && (p->option == 4 || p->option == 17)) {
             int q = 1;
-            for (int cand = 2; cand <= 8 && (long long)c->M * q < 65536; cand *= 2) {
+            for (int cand = 2; cand <= 8 && c->M < 32768 && (long long)c->M * q < 65536; cand *= 2) {
                 const int ch = (c->nz + cand - 1) / cand;
                 if (ch < 12 || (cand - 1) * ch >= c->nz) break;
                 q = cand;
@@ -558,28 +562,27 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
     int rc;
     if (c->f32) {
         if (c->use_fused) {
-            // z table of the fused FP32 step, built in FP64 and rounded once
-            // (layout beside FZ_COUNT): profile entries (with the buoyancy
-            // products g rho0/rho0 and g drho0/dz / rho0 folded), and the LU
+            // z table of the fused FP32 step, built in FP64 and rounded once:
+            // profile rows (with the buoyancy products g rho0/rho0 and
+            // g drho0/dz / rho0 folded), and the LU
             // elimination multipliers of the xi_z and p' boundary codes with
-            // their chunk products (chunks of FUSED_CH levels; padding levels
+            // their chunk products (chunks of FUSED_CH levels; padding rows
             // up to NZP carry zero multipliers)
             const int NZP = fused_nzp(nz);
             const bool d3 = (P.option == 4);
             std::vector<float> ft((size_t)FZ_COUNT * NZP, 0.f);
-            // entry e of level j in the block group at `block` holding `w` entries per level
-            auto put = [&](int block, int w, int j, int e, double v) { ft[(size_t)block * NZP + (size_t)j * w + e] = (float)v; };
+            auto put = [&](int row, int j, double v) { ft[(size_t)row * NZP + j] = (float)v; };
             for (int j = 0; j < nz; ++j) {
                 const double st = ZR(ZT_STRETCH)[j], ri = ZR(ZT_RHOINV)[j], g = ZR(ZT_G)[j];
-                put(FZ_PA, 4, j, 0, st);
-                put(FZ_PA, 4, j, 1, ZR(ZT_C2RHO0)[j]);
-                put(FZ_PA, 4, j, 2, ZR(ZT_GRADP0)[j]);
-                put(FZ_PA, 4, j, 3, g * ri * ZR(ZT_RHO0)[j]);
-                put(FZ_PB, 4, j, 0, g * ri * ZR(ZT_GRADRHO0)[j]);
-                put(FZ_PB, 4, j, 1, ri);
-                put(FZ_PB, 4, j, 2, ri * st);
-                put(FZ_PB, 4, j, 3, ZR(ZT_AZ)[j]);
-                put(FZ_PC, 1, j, 0, ZR(ZT_BZ)[j]);
+                put(FZ_ST, j, st);
+                put(FZ_C2R, j, ZR(ZT_C2RHO0)[j]);
+                put(FZ_GP, j, ZR(ZT_GRADP0)[j]);
+                put(FZ_RI, j, ri);
+                put(FZ_E1, j, g * ri * ZR(ZT_RHO0)[j]);
+                put(FZ_E2, j, g * ri * ZR(ZT_GRADRHO0)[j]);
+                put(FZ_RIST, j, ri * st);
+                put(FZ_AZ, j, ZR(ZT_AZ)[j]);
+                put(FZ_BZ, j, ZR(ZT_BZ)[j]);
             }
             const int bcs[2] = {d3 ? 1 : 3, d3 ? 0 : 2};
             const int base[2] = {FZ_SX, FZ_SP};
@@ -587,18 +590,14 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
             const int tp = NZP / FUSED_CH;
             for (int k = 0; k < 2; ++k) {
                 const FusedRows fr = fused_rows(nz, NZP, tri[bcs[k]]);
-                for (int j = 0; j < NZP; ++j) {
-                    put(base[k], 2, j, 0, fr.ibd[j]);
-                    put(base[k], 2, j, 1, fr.mm[j]);
-                    put(base[k] + 2, 2, j, 0, fr.HH[j]);
-                    put(base[k] + 2, 2, j, 1, fr.gg[j]);
-                    put(base[k] + 4, 1, j, 0, fr.GG[j]);
-                }
+                const std::vector<double>* rows[5] = {&fr.ibd, &fr.mm, &fr.HH, &fr.gg, &fr.GG};
+                for (int r = 0; r < 5; ++r)
+                    for (int j = 0; j < NZP; ++j) put(base[k] + r, j, (*rows[r])[j]);
                 std::vector<double> lf, lb;
                 fused_lookback(fr, tp, nz, lf, lb);
                 for (int i = 0; i < 4 * tp; ++i) {
-                    ft[(size_t)lbase[k] * NZP + i] = (float)lf[i];
-                    ft[(size_t)(lbase[k] + 1) * NZP + i] = (float)lb[i];
+                    put(lbase[k], i, lf[i]);
+                    put(lbase[k] + 1, i, lb[i]);
                 }
             }
             if ((rc = upload(c, c->ftab, ft.data(), ft.size() * 4))) return rc;
@@ -920,6 +919,7 @@ static void make_args(sparc_ctx* c, StageArgs<T>& A, UpdateArgs<T>& U) {
     U.dt = (T)c->deltat;
     U.clk = A.clk;
     U.block = c->stage_block;
+    U.q = c->stage_q; U.chunk = c->stage_chunk; U.ybuf = CP<T>(c->ybuf);
 }
 
 // Enqueue nsteps time steps on the context's stream: per step the fused FP32

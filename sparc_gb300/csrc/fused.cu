@@ -49,6 +49,15 @@ constexpr int GZ = 5;          // ghost rows of the tile on each side (reach of 
 constexpr int GX = 2;          // ghost entries of an exchange line on each side (compact stencil)
 constexpr int KB = FUSED_KB;   // chunks summed by a look-back carry
 
+// Entry idx of the z tables (scalars in shared memory) as a pair (t, t), the
+// multiplier of a paired product with a complex value.  Tables stored as
+// pairs would save the broadcast but cost 24 KB of shared memory (and of L1)
+// per CTA; measured slower.
+__device__ __forceinline__ float2 zt2(const float* zs, int idx) {
+    const float t = zs[idx];
+    return make_float2(t, t);
+}
+
 // Barrier over the TP threads of one pencil (named barrier pi+1; barrier 0
 // stays the CTA-wide __syncthreads).
 __device__ __forceinline__ void pencil_sync(int pi, int nthreads) {
@@ -70,9 +79,9 @@ __device__ __forceinline__ float2 lookback(float4 pr, float2 v1, float2 v2, floa
 // 0..NZP-1, ghosts at -2, -1, NZP, NZP+1; own[q] = xp[j0+q]) for the owned
 // levels j0..j0+CH-1,
 // boundary code BC (dbyd2.f90:94-173 for the right-hand side; top is the
-// caller-set value of bc 3).  zs, r0: the z tables and the first block of
-// BC's elimination entries ((1/betad, m), (H, g), G per level); lb, lb+1: its
-// forward and backward look-back product tables ([t][4] floats each); lf, lk:
+// caller-set value of bc 3).  zs, r0: the z tables and the first of the five
+// elimination rows (1/betad, m, H, g, G) of BC; lb, lb+1: its forward and
+// backward look-back product tables ([t][4] floats each); lf, lk:
 // this pencil's forward and backward look-back lines (chunk t at index t,
 // zero entries at -KB..-1 and TP..TP+KB-1).
 template <int BC, int W>
@@ -81,9 +90,8 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
                                        bool lo, bool hi, int t, float2* lf, float2* lk, int pi,
                                        const Compact<float> c, float2 (&out)[CH]) {
     constexpr int NZP = 160 * W;
-    const float2* EA = (const float2*)(zs + r0 * NZP);          // (1/betad, m) per level
-    const float2* EB = (const float2*)(zs + (r0 + 2) * NZP);    // (H, g) per level
-    const float* EC = zs + (r0 + 4) * NZP;                      // G per level
+    const int ibd = r0 * NZP, mm = (r0 + 1) * NZP, HH = (r0 + 2) * NZP, gg = (r0 + 3) * NZP, GG = (r0 + 4) * NZP;
+    auto Z = [&](int row, int j) { return zt2(zs, row + j); };
     float2 u[CH];
     const float2 C1p = bc2(c.C1), C2p = bc2(c.C2);
     // interior right-hand side on every level (dbyd2.f90:88-92); the
@@ -131,8 +139,8 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     float2 run = make_float2(0.f, 0.f);
     #pragma unroll
     for (int q = 0; q < CH; ++q) {
-        const float2 e = EA[j0 + q];
-        run = pfma(bc2(e.y), run, pmul(bc2(e.x), u[q]));
+        const int j = j0 + q;
+        run = pfma(Z(mm, j), run, pmul(Z(ibd, j), u[q]));
         u[q] = run;
     }
     // carry into the chunk: ud(j0-1) from the chunk values below
@@ -141,14 +149,13 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     pencil_sync(pi, TP);
     const float2 uin = lookback(*(const float4*)(zs + lb * NZP + 4 * t), lf[t - 1], lf[t - 2], lf[t - 3],
                                 lf[t - 4], lf[t - 5]);
-    // each level: u(j) += H(j) * carry, then the back substitution
-    // x(j) = u(j) + g(j) x(j+1) with a zero carry from above
+    #pragma unroll
+    for (int q = 0; q < CH; ++q) u[q] = pfma(Z(HH, j0 + q), uin, u[q]);
+    // back substitution x(j) = u(j) + g(j) x(j+1)
     float2 xr = make_float2(0.f, 0.f);
     #pragma unroll
     for (int q = CH - 1; q >= 0; --q) {
-        const float2 e = EB[j0 + q];
-        const float2 uq = pfma(bc2(e.x), uin, u[q]);
-        xr = pfma(bc2(e.y), xr, uq);
+        xr = pfma(Z(gg, j0 + q), xr, u[q]);
         out[q] = xr;
     }
     // carry from above: x(j0+CH) from the chunk values above
@@ -157,7 +164,7 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     const float2 xin = lookback(*(const float4*)(zs + (lb + 1) * NZP + 4 * t), lk[t + 1], lk[t + 2],
                                 lk[t + 3], lk[t + 4], lk[t + 5]);
     #pragma unroll
-    for (int q = 0; q < CH; ++q) out[q] = pfma(bc2(EC[j0 + q]), xin, out[q]);
+    for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
 }
 
 // Poll phase 0 of an mbarrier at most `limit` times; true once it completed.
@@ -170,7 +177,6 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, int limit) {
                      : "memory");
     return done != 0;
 }
-
 
 // shared-memory layout (byte offsets), identical on host and device
 struct FusedLayout {
@@ -379,10 +385,8 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
 
     float2* tp = tile + pi * LZ + GZ;                    // field f, level j: tp[f*P*LZ + j]
     auto TA = [&](int f, int j) -> float2 { return tp[f * P * LZ + j]; };
-    // profile entries per level (see FZ_PA / FZ_PB / FZ_PC)
-    const float4* PA = (const float4*)(zs + FZ_PA * NZP);   // stretch, c^2 rho0, dp0/dz, g rho0/rho0
-    const float4* PB = (const float4*)(zs + FZ_PB * NZP);   // g drho0/dz / rho0, 1/rho0, stretch/rho0, a_z
-    const float* PC = zs + FZ_PC * NZP;                     // b_z
+    // z table entry of row r at level j, as a pair
+    auto Z2 = [&](int r, int j) { return zt2(zs, r * NZP + j); };
 
     // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
     // rather than a (stage 1), fixed at compile time
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         float2 d[CH];
         zsolve<BCX, W>(xl, own, zs, FZ_SX, FZ_LX, nz, top, j0, lo, hi, t, lf, lk, pi, A.cc, d);
         #pragma unroll
-        for (int q = 0; q < CH; ++q) d[q] = pmul(bc2(PA[j0 + q].x), d[q]);
+        for (int q = 0; q < CH; ++q) d[q] = pmul(Z2(FZ_ST, j0 + q), d[q]);
         if (pml_t) {   // psi_vz (displacement.f90 PML rows)
             #pragma unroll
             for (int q = 0; q < CH; ++q) {
@@ -420,7 +424,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
                     const int j = j0 + q, ip = pipv + q;
                     float2 psi = ptile[ip * P + pi];
                     if (hs) psi = psi + beta * spt[ip * P + pi];
-                    spt[ip * P + pi] = PB[j].w * d[q] + PC[j] * psi;
+                    spt[ip * P + pi] = Z2(FZ_AZ, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
                     d[q] = d[q] + psi;
                 }
             }
@@ -439,12 +443,11 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
                 if (hs) { xy = pfma(BT, sc[1][q], xy); vy = pfma(BT, sc[4][q], vy); }
                 div = div + imul(ky, xy);
             }
-            const float4 pa = PA[j], pb = PB[j];
-            const float2 p = pmul(make_float2(-1.f, -1.f), pfma(bc2(pa.z), xz, pmul(bc2(pa.y), div)));
-            qt[q] = pfma(bc2(pb.x), xz, pmul(bc2(pa.w), div));   // -g rho'/rho0
+            const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
+            qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
             xl[j] = p;
             own[q] = p;
-            const float ri = pb.y;
+            const float ri = Z2(FZ_RI, j).x;
             sc[3][q] = pfma(NGD, vx, -ri * imul(kx, p));
             sc[0][q] = vx;
             if (D3) {
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             const int j = j0 + q;
             float2 vz = TA(5, j);
             if (hs) vz = pfma(BT, sc[5][q], vz);
-            sc[5][q] = pfma(NGD, vz, psub(qt[q], pmul(bc2(PB[j].z), d[q])));
+            sc[5][q] = pfma(NGD, vz, psub(qt[q], pmul(Z2(FZ_RIST, j), d[q])));
             sc[2][q] = vz;
         }
         if (pml_t) {   // psi_p
@@ -475,12 +478,11 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             for (int q = 0; q < CH; ++q) {
                 if (pmask & (1u << q)) {
                     const int j = j0 + q, ip = pipv + q;
-                    const float4 pb = PB[j];
-                    const float2 dd = PA[j].x * d[q];
+                    const float2 dd = Z2(FZ_ST, j).x * d[q];
                     float2 psi = ptile[(nzpml + ip) * P + pi];
                     if (hs) psi = psi + beta * spt[(nzpml + ip) * P + pi];
-                    spt[(nzpml + ip) * P + pi] = pb.w * dd + PC[j] * psi;
-                    sc[5][q] = sc[5][q] - pb.y * psi;
+                    spt[(nzpml + ip) * P + pi] = Z2(FZ_AZ, j).x * dd + Z2(FZ_BZ, j).x * psi;
+                    sc[5][q] = sc[5][q] - Z2(FZ_RI, j).x * psi;
                 }
             }
         }

@@ -337,24 +337,21 @@ template <typename T> struct UpdateArgs {
     T dt;
     SlotClock clk;      // the horizontal filter follows each slot's clock
     int block;          // threads per CTA (32, 64 or 128), as the stage kernels
+    int q, chunk;       // lanes per pencil and levels per lane, as the stage kernels
+    CT* ybuf;           // per-source scratch column (the chunked form's staging)
 };
 
 // fused FP32 step (fused.cu)
-// z table of the fused FP32 step: FZ_COUNT blocks of NZP floats (NZP =
-// fused_nzp(nz), padded levels zero), grouped so that the entries a thread
-// uses together at one level come in one vector load:
-//   FZ_PA  [NZP][4]  stretch, c^2 rho0, dp0/dz, g (rho0 / rho0)      (4 blocks)
-//   FZ_PB  [NZP][4]  g (drho0/dz) / rho0, 1/rho0, stretch / rho0, a_z (4 blocks)
-//   FZ_PC  [NZP]     b_z of the PML                                   (1 block)
-//   per boundary code (xi_z at FZ_SX, p' at FZ_SP):
-//     +0  [NZP][2]  1/betad, elimination multiplier m                (2 blocks)
-//     +2  [NZP][2]  chunk products H of m, back-substitution multiplier g (2 blocks)
-//     +4  [NZP]     chunk products G of g                             (1 block)
-//   then the look-back products of each code: a forward block and a backward
-//   block, [chunk t][4] floats each (the products of the multipliers of the
-//   1..4 chunks between chunk t and the chunk 2..5 below / above it)
+// z table of the fused FP32 step, [FZ_COUNT][NZP] (NZP = fused_nzp(nz), padded
+// rows zero): profile rows, then the five elimination rows (1/betad,
+// elimination multiplier m, chunk products H of m, back-substitution
+// multiplier g, chunk products G of g) of the xi_z boundary code and of the p'
+// boundary code, then the look-back products of each code: a forward row and
+// a backward row, [chunk t][4] floats each (the products of the multipliers
+// of the 1..4 chunks between chunk t and the chunk 2..5 below / above it)
 enum {
-    FZ_PA = 0, FZ_PB = 4, FZ_PC = 8, FZ_SX = 9, FZ_SP = 14, FZ_LX = 19, FZ_LP = 21, FZ_COUNT = 23
+    FZ_ST = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_RIST, FZ_AZ, FZ_BZ, FZ_SX = 9, FZ_SP = 14,
+    FZ_LX = 19, FZ_LP = 21, FZ_COUNT = 23
 };
 constexpr int FUSED_KB = 5;    // chunks summed by a look-back carry of the fused step
 // largest product of chunk multipliers over FUSED_KB chunks (the first term a

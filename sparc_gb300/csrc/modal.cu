@@ -581,6 +581,70 @@ __global__ void __launch_bounds__(128) update_kernel(const UpdateArgs<T> A) {
     }
 }
 
+// z filter of FILTER_VARS_3D / _2D (physics.f90:758-786, physics2d.f90:531-561)
+// at one level j of a pencil whose values ld(j') are all available; the same
+// formulas, in the same order, as zfilter_stream.
+template <typename V, typename T, typename Load>
+__device__ __forceinline__ V zfilter_at(int j, int nz, int mode, Load ld) {
+    const T h1 = (T)(0.5 * 0.41015625), h2 = (T)(0.5 * -0.234375), h3 = (T)(0.5 * 0.087890625);
+    const T h4 = (T)(0.5 * -0.01953125), h5 = (T)(0.5 * 0.001953125), c0 = (T)0.75390625, hf = (T)0.5;
+    if (j == 0 || j == nz - 1) return ld(j);
+    if (j >= nz - 5 && j <= nz - 2) return hf * (ld(j + 1) + ld(j - 1));
+    if (j >= 1 && j <= 4) return (mode == 0) ? hf * (ld(j + 1) + ld(j - 1)) : ld(j);
+    return c0 * ld(j) + h1 * (ld(j - 1) + ld(j + 1)) + h2 * (ld(j - 2) + ld(j + 2)) +
+           h3 * (ld(j - 3) + ld(j + 3)) + h4 * (ld(j - 4) + ld(j + 4)) + h5 * (ld(j - 5) + ld(j + 5));
+}
+
+// update_kernel with each pencil on Q lanes of a warp (chunks of A.chunk
+// levels): per field, a + dt*scr of the lane's chunk goes to the pencil's
+// scratch column y, and after a warp barrier the z filter reads its
+// neighbours there and writes a.  Arithmetic identical to update_kernel.
+template <typename T, int Q>
+__global__ void __launch_bounds__(128) update_chunk_kernel(const UpdateArgs<T> A) {
+    typedef typename CplxOf<T>::type CT;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = gt % Q;
+    const int m0 = gt / Q;
+    const bool valid = m0 < A.M;
+    const int m = valid ? m0 : A.M - 1;
+    const int s = blockIdx.y;
+    const int nz = A.nz, C = A.chunk;
+    const int j0 = c * C, j1 = min(j0 + C, nz);
+    const long long M = A.M, fs = A.fs;
+    CT* __restrict__ a = A.a + (long long)s * 6 * fs + m;
+    const CT* __restrict__ scr = A.scr + (long long)s * 6 * fs + m;
+    CT* __restrict__ y = A.ybuf + (long long)s * fs + m;
+    const T dt = A.dt;
+    const T hf = __ldg(&A.pt[PT_HF * M + m]);
+    const bool opt3d = (A.option != 17);
+    const bool hstep = slot_hfilter(A.clk, *A.clk.time - A.clk.t0[s]);
+    for (int f = 0; f < 6; ++f) {
+        CT* af = a + f * fs;
+        const CT* sf = scr + f * fs;
+        const bool hfil = hstep && (opt3d ? (f < 5) : true);
+        if (valid)
+            for (int j = j0; j < j1; ++j) {
+                const long long o = (long long)j * M;
+                y[o] = af[o] + dt * sf[o];
+            }
+        __syncwarp();
+        if (valid)
+            for (int j = j0; j < j1; ++j) {
+                const CT v = zfilter_at<CT, T>(j, nz, opt3d ? 0 : 1, [&](int jj) { return y[(long long)jj * M]; });
+                af[(long long)j * M] = hfil ? hf * v : v;
+            }
+        __syncwarp();      // the next field overwrites y
+    }
+    if (valid) {
+        CT* pml = A.pml + (long long)s * 2 * A.ps + m;
+        const CT* spml = A.scrpml + (long long)s * 2 * A.ps + m;
+        for (int q = c; q < 2 * A.nzpml; q += Q) {
+            const long long o = (long long)q * M;
+            pml[o] = pml[o] + dt * spml[o];
+        }
+    }
+}
+
 // d/dz (compact FD, bc) x stretch, optionally followed by FILTER_VAR_Z, on
 // complex pencils (n1 of them, stride n1 between z-levels).  Used for the
 // sensitivity-kernel derivatives (ddzkern, kernels.f90:609-621).
@@ -681,6 +745,13 @@ template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStr
 }
 template <typename T> void launch_update(const UpdateArgs<T>& A, int nsrc, cudaStream_t s) {
     const int b = A.block == 32 ? 32 : A.block == 64 ? 64 : 128;
+    if (A.q > 1) {
+        dim3 grid((unsigned)(((long long)A.M * A.q + b - 1) / b), nsrc);
+        if (A.q == 2) update_chunk_kernel<T, 2><<<grid, b, 0, s>>>(A);
+        else if (A.q == 4) update_chunk_kernel<T, 4><<<grid, b, 0, s>>>(A);
+        else update_chunk_kernel<T, 8><<<grid, b, 0, s>>>(A);
+        return;
+    }
     dim3 grid((A.M + b - 1) / b, nsrc);
     update_kernel<T><<<grid, b, 0, s>>>(A);
 }
