@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--serve-compress", type=float, default=120.0, help="request-length compression")
     ap.add_argument("--full-length", default="", choices=["", "config4", "config3", "serving"],
                     help="one full-length workload instead of the bench line (see full_length_*)")
+    ap.add_argument("--fl-hours", type=float, default=0.0,
+                    help="solar hours of the full-length run (0: the configuration's own; a short check otherwise)")
     return ap.parse_args()
 
 
@@ -482,7 +484,7 @@ def _tt_shifts(a, b, dt):
     return [abs(compute_tt(a[:, r], b[:, r], dt)) for r in range(a.shape[1]) if rms[r] >= 1e-2 * rms.max()]
 
 
-def full_length_config4(batch=8, segment=24, compare=2):
+def full_length_config4(batch=8, segment=24, compare=2, hours=0.0):
     """The 32-source forward x adjoint kernel workflow at full length: 256^2 x
     300 quiet Sun, 4 h of solar time (the pipeline's forward run, adjoint run
     and forward recomputation from device checkpoints), FP32 fields with FP64
@@ -493,6 +495,8 @@ def full_length_config4(batch=8, segment=24, compare=2):
     from sparc_gb300 import sources
     from sparc_gb300.pipeline import KernelPipeline
     p0, tab = workload(False)
+    if hours > 0:
+        p0 = p0.replace(solartime=hours)
     S = 32
     series = sources.ricker_series(p0, p0.maxtime + 10)
     pix = sources.receiver_pixels(p0)
@@ -539,7 +543,7 @@ def full_length_config4(batch=8, segment=24, compare=2):
     return out
 
 
-def full_length_config3(hours_fp64=1.0):
+def full_length_config3(hours_fp64=1.0, hours=4.0):
     """The flux-tube configuration at full length: option 10 on the
     magnetohydrostatic tube, 256^2 x 300, one source 20 Mm from the axis,
     4 h of solar time forward in FP32, and the first `hours_fp64` hours in FP64
@@ -552,7 +556,8 @@ def full_length_config3(hours_fp64=1.0):
     from sparc_gb300.params import config_flux_tube_256
     from sparc_gb300.solver import Solver
     pm, tab = config_flux_tube_256()
-    pm = pm.replace(nsrc=1, solartime=4.0)
+    pm = pm.replace(nsrc=1, solartime=hours)
+    hours_fp64 = min(hours_fp64, hours)
     pix = sources.receiver_pixels(pm, n=8, radius_mm=10.0, x0_mm=20.0)
     plane = sources.gaussian_plane(pm, 1.0, 20.0, 0.0)
     series = sources.ricker_series(pm, pm.maxtime + 10)
@@ -738,8 +743,11 @@ def main():
     from sparc_gb300 import dist as sd
     p0, tab = workload(args.small)
     if args.full_length:
-        fn = {"config4": full_length_config4, "config3": full_length_config3,
-              "serving": lambda: serving_section("f32", args.serve_requests, min(args.serve_compress, 4.0),
+        h = args.fl_hours
+        fn = {"config4": lambda: full_length_config4(hours=h),
+              "config3": lambda: full_length_config3(hours=h) if h > 0 else full_length_config3(),
+              "serving": lambda: serving_section("f32", args.serve_requests,
+                                                 min(args.serve_compress, 4.0) if h <= 0 else args.serve_compress,
                                                  max_wall=1800.0)}[args.full_length]
         print(json.dumps({"full_length": args.full_length, "result": fn()}), flush=True)
         return 0

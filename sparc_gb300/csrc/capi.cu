@@ -95,6 +95,29 @@ FusedRows fused_rows(int nz, int nzp, const Tri& t) {
     return r;
 }
 
+// The elimination rows of the same solve for y(j) = sig(j) x(j): forward
+// variable sig(j) u(j), so 1/betad -> sig(j)/betad(j) and m(j) -> m(j)
+// sig(j)/sig(j-1); back substitution y(j) = sig(j) u(j) + g(j) sig(j)/sig(j+1)
+// y(j+1); the chunk products H, G are those of the new multipliers.  Same
+// recurrences, the scale applied inside them (sig = 1 on padding levels).
+FusedRows fused_rows_scaled(const FusedRows& r, const std::vector<double>& sig) {
+    FusedRows o = r;
+    const int nzp = (int)r.ibd.size();
+    for (int j = 0; j < nzp; ++j) {
+        o.ibd[j] = r.ibd[j] * sig[j];
+        o.mm[j] = (j == 0) ? r.mm[j] : r.mm[j] * sig[j] / sig[j - 1];
+        o.gg[j] = (j == nzp - 1) ? r.gg[j] : r.gg[j] * sig[j] / sig[j + 1];
+    }
+    for (int j0 = 0; j0 < nzp; j0 += FUSED_CH) {
+        const int j1 = j0 + FUSED_CH;
+        double pr = 1.0;
+        for (int j = j0; j < j1; ++j) { pr *= o.mm[j]; o.HH[j] = pr; }
+        pr = 1.0;
+        for (int j = j1 - 1; j >= j0; --j) { pr *= o.gg[j]; o.GG[j] = pr; }
+    }
+    return o;
+}
+
 // Look-back products of the fused step's carries: fwd[4t + i-2] is the
 // product of the chunk multipliers Mc(t-1)..Mc(t-i+1) (i = 2..5), the factor
 // of chunk t-i's value in the carry into chunk t; bwd[4t + i-2] likewise with
@@ -573,14 +596,13 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
             std::vector<float> ft((size_t)FZ_COUNT * NZP, 0.f);
             auto put = [&](int row, int j, double v) { ft[(size_t)row * NZP + j] = (float)v; };
             for (int j = 0; j < nz; ++j) {
-                const double st = ZR(ZT_STRETCH)[j], ri = ZR(ZT_RHOINV)[j], g = ZR(ZT_G)[j];
-                put(FZ_ST, j, st);
+                const double ri = ZR(ZT_RHOINV)[j], g = ZR(ZT_G)[j];
+                put(FZ_AZR, j, ZR(ZT_AZ)[j] / ri);   // a_z of psi_p times rho0, the scale of the p' solve undone
                 put(FZ_C2R, j, ZR(ZT_C2RHO0)[j]);
                 put(FZ_GP, j, ZR(ZT_GRADP0)[j]);
                 put(FZ_RI, j, ri);
                 put(FZ_E1, j, g * ri * ZR(ZT_RHO0)[j]);
                 put(FZ_E2, j, g * ri * ZR(ZT_GRADRHO0)[j]);
-                put(FZ_RIST, j, ri * st);
                 put(FZ_AZ, j, ZR(ZT_AZ)[j]);
                 put(FZ_BZ, j, ZR(ZT_BZ)[j]);
             }
@@ -589,7 +611,9 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
             const int lbase[2] = {FZ_LX, FZ_LP};
             const int tp = NZP / FUSED_CH;
             for (int k = 0; k < 2; ++k) {
-                const FusedRows fr = fused_rows(nz, NZP, tri[bcs[k]]);
+                std::vector<double> sig(NZP, 1.0);
+                for (int j = 0; j < nz; ++j) sig[j] = ZR(ZT_STRETCH)[j] * (k == 1 ? ZR(ZT_RHOINV)[j] : 1.0);
+                const FusedRows fr = fused_rows_scaled(fused_rows(nz, NZP, tri[bcs[k]]), sig);
                 const std::vector<double>* rows[5] = {&fr.ibd, &fr.mm, &fr.HH, &fr.gg, &fr.GG};
                 for (int r = 0; r < 5; ++r)
                     for (int j = 0; j < NZP; ++j) put(base[k] + r, j, (*rows[r])[j]);
@@ -955,6 +979,7 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
         Fz.pencils = c->fused_pencils;
         Fz.err = c->d_flag + 1;
         Fz.no_copy = c->fused_test_nocopy;
+        Fz.pf_stride = 1;
         Fz.wait_limit = c->fused_test_nocopy ? 64 : (1 << 22);
     }
     for (int it = 0; it < nsteps; ++it) {

@@ -35,7 +35,12 @@
 //     Each thread then adds H(j)*carry-in to its levels, H(j) the product of
 //     the multipliers from its chunk start to j.  This is the LU elimination
 //     and back substitution of the sequential form, re-associated.  Padding
-//     rows carry zero multipliers, so they never reach a real row.
+//     rows carry zero multipliers, so they never reach a real row.  The
+//     tables solve for the scaled unknown s(j) x(j) (s = stretch for xi_z,
+//     stretch / rho0 for p'), so each solve returns the derivative in the
+//     form the step uses, without a multiply and a table read per level;
+//   * the state tile of the CTA that starts one resident-CTA count later is
+//     prefetched into L2 while this CTA computes, so its load phase reads L2.
 // HBM traffic per step: read a, write a (+ the PML planes and source planes),
 // and scr only on steps whose right-hand side is requested (outputs).
 #include <type_traits>
@@ -286,21 +291,20 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         constexpr int RPI = TP;                       // rows advanced per pass: blockDim.x / P
         const int q = threadIdx.x % P;
         const bool qv = m0 + q < M;
-        int z = threadIdx.x / P, f = 0;
-        while (z >= nz) { z -= nz; ++f; }
-        for (; f < 6;) {
-            float2* dst = tile + f * P * LZ + q * LZ + GZ + z;
-            if (qv) {
-                const float2* src = gA + f * fs + (long long)z * M + m0 + q;
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
-                                 (unsigned)__cvta_generic_to_shared(dst)),
-                             "l"(__cvta_generic_to_global(src))
-                             : "memory");
-            } else {
-                *dst = make_float2(0.f, 0.f);
+        const int z0 = threadIdx.x / P;
+        if (qv) {
+            const unsigned d0 = (unsigned)__cvta_generic_to_shared(tile + q * LZ + GZ + z0);
+            const float2* s0 = gA + (long long)z0 * M + m0 + q;
+            #pragma unroll 1
+            for (int f = 0; f < 6; ++f) {
+                unsigned dst = d0 + f * (P * LZ * 8);
+                size_t src = __cvta_generic_to_global(s0 + f * fs);
+                for (int z = z0; z < nz; z += RPI, dst += RPI * 8, src += (size_t)RPI * M * 8)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
             }
-            z += RPI;
-            while (z >= nz) { z -= nz; ++f; }
+        } else {
+            for (int f = 0; f < 6; ++f)
+                for (int z = z0; z < nz; z += RPI) tile[f * P * LZ + q * LZ + GZ + z] = make_float2(0.f, 0.f);
         }
         for (int r = threadIdx.x / P; r < 2 * nzpml; r += RPI) {
             float2* dst = ptile + r * P + q;
@@ -337,6 +341,23 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             if (!A.no_copy) mbar_wait(mbar, 1 << 22);
         }
         return;
+    }
+
+    // ---- L2 prefetch of the rows of the CTA that starts pf_stride CTAs
+    // later (about when this one ends): its tile load then comes from L2 ----
+    if (A.pf_stride > 0) {
+        const long long nid = (long long)blockIdx.y * gridDim.x + blockIdx.x + A.pf_stride;
+        if (nid < (long long)gridDim.x * gridDim.y) {
+            const int ns = (int)(nid / gridDim.x), nm0 = (int)(nid - (long long)ns * gridDim.x) * P;
+            const float2* nA = A.a + (long long)ns * 6 * fs + nm0;
+            for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
+                const int f = r / nz, z = r - f * nz;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(nA + f * fs + (long long)z * M)));
+            }
+            const float2* nP = A.pml + (long long)ns * 2 * A.ps + nm0;
+            for (int r = threadIdx.x; r < 2 * nzpml; r += nthr)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(nP + (long long)r * M)));
+        }
     }
 
     const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
@@ -414,9 +435,8 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         float2 d[CH];
+        // d: the stretched derivative (the solve's tables carry the stretch)
         zsolve<BCX, W>(xl, own, zs, FZ_SX, FZ_LX, nz, top, j0, lo, hi, t, lf, lk, pi, A.cc, d);
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) d[q] = pmul(Z2(FZ_ST, j0 + q), d[q]);
         if (pml_t) {   // psi_vz (displacement.f90 PML rows)
             #pragma unroll
             for (int q = 0; q < CH; ++q) {
@@ -464,13 +484,14 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
         pencil_sync(pi, TP);
         // ---- dp'/dz, RHS v_z and xi_z ----
+        // d: (stretch / rho0) dp'/dz, scaled by the solve's tables
         zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
             float2 vz = TA(5, j);
             if (hs) vz = pfma(BT, sc[5][q], vz);
-            sc[5][q] = pfma(NGD, vz, psub(qt[q], pmul(Z2(FZ_RIST, j), d[q])));
+            sc[5][q] = pfma(NGD, vz, psub(qt[q], d[q]));
             sc[2][q] = vz;
         }
         if (pml_t) {   // psi_p
@@ -478,10 +499,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             for (int q = 0; q < CH; ++q) {
                 if (pmask & (1u << q)) {
                     const int j = j0 + q, ip = pipv + q;
-                    const float2 dd = Z2(FZ_ST, j).x * d[q];
                     float2 psi = ptile[(nzpml + ip) * P + pi];
                     if (hs) psi = psi + beta * spt[(nzpml + ip) * P + pi];
-                    spt[(nzpml + ip) * P + pi] = Z2(FZ_AZ, j).x * dd + Z2(FZ_BZ, j).x * psi;
+                    spt[(nzpml + ip) * P + pi] = Z2(FZ_AZR, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
                     sc[5][q] = sc[5][q] - Z2(FZ_RI, j).x * psi;
                 }
             }
@@ -660,7 +680,15 @@ template <bool D3, int W, int P>
 static void launch_fused_t(const FusedArgs& A, int nsrc, cudaStream_t s) {
     const size_t sm = (size_t)fused_layout(P, W, A.nzpml).total;
     dim3 grid((A.M + P - 1) / P, nsrc);
-    fused_step_kernel<D3, W, P><<<grid, P * 32 * W, sm, s>>>(A);
+    FusedArgs B = A;
+    if (B.pf_stride > 0) {
+        int dev = 0, nsm = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fused_step_kernel<D3, W, P>, P * 32 * W, sm);
+        B.pf_stride = (nsm > 0 && occ > 0) ? nsm * occ : 0;
+    }
+    fused_step_kernel<D3, W, P><<<grid, P * 32 * W, sm, s>>>(B);
 }
 
 template <bool D3, int W>

@@ -348,10 +348,14 @@ template <typename T> struct UpdateArgs {
 // multiplier g, chunk products G of g) of the xi_z boundary code and of the p'
 // boundary code, then the look-back products of each code: a forward row and
 // a backward row, [chunk t][4] floats each (the products of the multipliers
-// of the 1..4 chunks between chunk t and the chunk 2..5 below / above it)
+// of the 1..4 chunks between chunk t and the chunk 2..5 below / above it).
+// The elimination rows solve for s(j) x(j) instead of x(j), s = stretch for
+// xi_z and stretch / rho0 for p' (the factors the step applies to the two
+// derivatives): 1/betad and the multipliers carry the ratios of s, so the
+// solves return the scaled derivatives directly.
 enum {
-    FZ_ST = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_RIST, FZ_AZ, FZ_BZ, FZ_SX = 9, FZ_SP = 14,
-    FZ_LX = 19, FZ_LP = 21, FZ_COUNT = 23
+    FZ_AZR = 0, FZ_C2R, FZ_GP, FZ_RI, FZ_E1, FZ_E2, FZ_AZ, FZ_BZ, FZ_SX = 8, FZ_SP = 13,
+    FZ_LX = 18, FZ_LP = 20, FZ_COUNT = 22
 };
 constexpr int FUSED_KB = 5;    // chunks summed by a look-back carry of the fused step
 // largest product of chunk multipliers over FUSED_KB chunks (the first term a
@@ -376,6 +380,8 @@ struct FusedArgs {
     int* err;           // set to 1 if the bounded wait for the z-table bulk copy gave up
     int wait_limit;     // polls of that wait before it gives up
     int no_copy;        // test switch: issue no bulk copy, so the wait runs out with nothing in flight
+    int pf_stride;      // > 0: each CTA prefetches into L2 the rows of the CTA pf_stride later in launch
+                        // order (set by the launcher to the CTAs resident at once); 0: no prefetch
 };
 constexpr int FUSED_CH = 5;
 void fused_prepare(int nz, int nzpml);
