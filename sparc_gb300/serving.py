@@ -282,9 +282,20 @@ def poisson_stream(n: int, rate: float = 4.0, seed: int = 0, mix=None, hours=(1.
 
 
 def latency_stats(done: list[Request]) -> dict:
+    """p50/p95/p99 of finish - arrival over all requests, and per background
+    (quiet Sun, flux tube) with the admission wait (admitted - arrival)."""
     lat = np.array([r.latency for r in done])
-    return {"n": len(done), "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
-            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}
+    out = {"n": len(done), "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
+           "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}
+    by = {}
+    for bg in sorted({r.background for r in done}):
+        rs = [r for r in done if r.background == bg]
+        lb = np.array([r.latency for r in rs])
+        wb = np.array([r.admitted - r.arrival for r in rs])
+        by[bg] = {"n": len(rs), "p50_s": float(np.percentile(lb, 50)), "p99_s": float(np.percentile(lb, 99)),
+                  "wait_p50_s": float(np.percentile(wb, 50))}
+    out["by_background"] = by
+    return out
 
 
 def main(argv=None):
