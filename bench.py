@@ -170,6 +170,7 @@ def make_pair(p, tab, nplanes, src_ids, seed=0):
     from sparc_gb300.solver import Solver
     pa = p.replace(compute_forward=False, compute_adjoint=True)
     fwd, adj = Solver(p, tab), Solver(pa, tab)
+    adj.set_rhs_output(False)          # the adjoint side of the kernel snapshot reads no scr
     series = sources.ricker_series(p, 20000)
     for s, gi in enumerate(src_ids):
         plane, adjp = source_inputs(p, nplanes, gi, seed)

@@ -209,6 +209,16 @@ int sparc_gpu_slot_time(const sparc_ctx* ctx, int src_idx, int* slot_time);
 /* Only slots 0..nactive-1 are stepped (default: all). */
 int sparc_gpu_set_active(sparc_ctx* ctx, int nactive);
 
+/* Whether the last step of each sparc_gpu_step call leaves that step's
+ * right-hand side in scr (default 1).  scr is what get_field returns for
+ * fields nf..2nf-1, and the forward kernel snapshot reads it (f_acc,
+ * kernels.f90:197-263), so sparc_gpu_snapshot fails with SPARC_ESTATE while it
+ * is 0.  An adjoint context of the kernel workflow reads no scr; turning the
+ * output off there saves the fused FP32 step one full-state write per call.
+ * The state itself does not depend on it.  No counterpart in the reference,
+ * which keeps scr in memory at all times (step.f90:24-128). */
+int sparc_gpu_set_rhs_output(sparc_ctx* ctx, int on);
+
 /* Checkpoint / restore of every slot (state, PML, time) to one file with a
  * checksum; restore rejects a corrupt or mismatching file with SPARC_EIO.
  * A restore restarts every slot clock at the restored time index. */

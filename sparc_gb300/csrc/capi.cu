@@ -364,7 +364,10 @@ int sparc_gpu_create(const sparc_params* p, sparc_ctx** out) {
     c->t0.assign(c->S, 0);
     c->active_n = c->S;
     c->use_graphs = getenv("SPARC_NO_GRAPHS") == nullptr && !mhd_form;
-    if (c->use_fused) fused_prepare(c->nz, c->nzpml);
+    if (c->use_fused) {
+        fused_prepare(c->nz, c->nzpml);
+        if ((rc = dalloc(c, &c->src_plane, (size_t)c->S * c->M * 8))) return bail(rc);
+    }
     if (mhd_form && (rc = mhd_create(c))) return bail(rc);
     // twiddles cos/sin(2 pi q / n), q < n/2, exact pi; the FP32 copy (rounded
     // from FP64) follows the FP64 table in the same allocation
@@ -980,11 +983,16 @@ static int enqueue_steps(sparc_ctx* c, int nsteps) {
         Fz.err = c->d_flag + 1;
         Fz.no_copy = c->fused_test_nocopy;
         Fz.pf_stride = 1;
+        Fz.src_plane = (float2*)c->src_plane;
         Fz.wait_limit = c->fused_test_nocopy ? 64 : (1 << 22);
     }
     for (int it = 0; it < nsteps; ++it) {
         if (fused) {
-            Fz.write_scr = (it == nsteps - 1) ? 1 : 0;
+            Fz.write_scr = (it == nsteps - 1 && c->rhs_out) ? 1 : 0;
+            if (Fz.src_mode == 2) {
+                launch_source_plane(Fz, c->active_n, c->stream);
+                c->launches += 1;
+            }
             launch_fused(Fz, c->active_n, c->stream);
             c->launches += 1;
             CKL();
@@ -1280,6 +1288,14 @@ int sparc_gpu_slot_time(const sparc_ctx* c, int src, int* local_time) {
     return SPARC_OK;
 }
 
+int sparc_gpu_set_rhs_output(sparc_ctx* c, int on) {
+    if (!c) return SPARC_EINVAL;
+    const int v = on ? 1 : 0;
+    if (c->rhs_out != v) c->epoch++;    // the flag is an argument of the captured step kernels
+    c->rhs_out = v;
+    return SPARC_OK;
+}
+
 int sparc_gpu_set_active(sparc_ctx* c, int nactive) {
     if (!c) return SPARC_EINVAL;
     if (nactive < 1 || nactive > c->S) return fail(c, SPARC_EINVAL, "nactive out of range");
@@ -1436,6 +1452,9 @@ int sparc_gpu_snapshot(sparc_ctx* c, int snap, int nsnap) {
     if (c->P.option == 2 || (c->mhd && c->P.option != 18))
         return fail(c, SPARC_EINVAL, "sensitivity kernels are built for the displacement forms 4, 17 and 18 "
                                      "(the reference computes kernels in 2-D)");
+    if (!c->rhs_out)
+        return fail(c, SPARC_ESTATE, "the forward snapshot reads the stage right-hand side (f_acc): "
+                                     "sparc_gpu_set_rhs_output(ctx, 1) first");
     if (!c->store) {
         if (nsnap < 1) return fail(c, SPARC_EINVAL, "nsnap < 1");
         int rc = dalloc(c, &c->store, (size_t)nsnap * c->S * 7 * c->N * esz(c));

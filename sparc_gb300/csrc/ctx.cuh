@@ -54,6 +54,8 @@ struct sparc_ctx {
     double2* spec64b = nullptr;
     double2* tmp64 = nullptr;
     int* d_flag = nullptr;
+    void* src_plane = nullptr;    // [S][M] float2: the fused step's interpolated source plane
+    int rhs_out = 1;              // the last step of each step call leaves its right-hand side in scr
 
     // sources
     int src_mode = 0;

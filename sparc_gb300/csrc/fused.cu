@@ -2,14 +2,15 @@
 // the horizontal filter of one time step in a single kernel, with the state
 // of each z-pencil held on chip for the whole step.
 //
-// Work decomposition.  A CTA owns P = 4 consecutive horizontal modes m of one
-// source.  Each mode's z-pencil is split into chunks of CH = 5 levels, one
+// Work decomposition.  A CTA owns P = 2, 4 or 8 consecutive horizontal modes
+// m of one source.  Each mode's z-pencil is split into chunks of CH = 5 levels, one
 // chunk per thread: TP = 32*W threads per pencil, W = ceil(nz / 160) warps,
 // and the pencil is padded to NZP = TP*CH levels.
 //   * a (6 fields) lives in shared memory as a tile [field][mode][z] with
-//     zero ghost rows on both ends; global rows [field][z][m0..m0+3] are 32 B,
-//     so the tile is loaded and stored with sector-efficient cooperative
-//     copies once per step;
+//     zero ghost rows on both ends; global rows [field][z][m0..m0+P-1] are
+//     8P bytes, so the tile is loaded (cp.async, each value into its
+//     transposed place) and stored (float4) with sector-efficient
+//     cooperative copies once per step;
 //   * scr (the stage right-hand side, 6 fields) lives in registers of the
 //     owning thread -- every use of scr is point-wise;
 //   * stencil neighbours of the compact-FD right-hand sides are exchanged
@@ -40,7 +41,10 @@
 //     stretch / rho0 for p'), so each solve returns the derivative in the
 //     form the step uses, without a multiply and a table read per level;
 //   * the state tile of the CTA that starts one resident-CTA count later is
-//     prefetched into L2 while this CTA computes, so its load phase reads L2.
+//     prefetched into L2 while this CTA computes, so its load phase reads L2;
+//   * a LAGRANGE_INTERP source (the adjoint's) is interpolated to the step by
+//     a small kernel launched before it (source_plane_kernel), so no CTA
+//     spends its critical path on the seven FP64 weights.
 // HBM traffic per step: read a, write a (+ the PML planes and source planes),
 // and scr only on steps whose right-hand side is requested (outputs).
 #include <type_traits>
@@ -185,7 +189,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, int limit) {
 
 // shared-memory layout (byte offsets), identical on host and device
 struct FusedLayout {
-    int tile, xl, ptile, spt, lines, zs, lagw, lagi, mbar, total;
+    int tile, xl, ptile, spt, lines, zs, mbar, total;
 };
 __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
     const int NZP = 160 * W, LZ = NZP + 2 * GZ, LX = NZP + 2 * GX, LL = 32 * W + 2 * KB;
@@ -199,8 +203,6 @@ __host__ __device__ inline FusedLayout fused_layout(int P, int W, int nzpml) {
     o = (o + 15) & ~15;
     L.zs = o;    o += FZ_COUNT * NZP * 4;
     o = (o + 15) & ~15;
-    L.lagw = o;  o += 8 * 8;
-    L.lagi = o;  o += 8 * 4;
     o = (o + 7) & ~7;
     L.mbar = o;  o += 8;                  // mbarrier of the z-table bulk copy
     L.total = (o + 15) & ~15;
@@ -227,9 +229,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     float2* spt = (float2*)(smraw + Ly.spt);              // [2][nzpml][P] PML right-hand sides
     float2* lines = (float2*)(smraw + Ly.lines);          // [P][2][LL], chunk t at KB + t
     float* zs = (float*)(smraw + Ly.zs);                  // [FZ_COUNT][NZP]
-    double* lagw = (double*)(smraw + Ly.lagw);            // [8] Lagrange weights of this slot
     const unsigned mbar = (unsigned)__cvta_generic_to_shared(smraw + Ly.mbar);
-    int* lagi = (int*)(smraw + Ly.lagi);                  // [8]: sample index of each weight
     const int nthr = blockDim.x;
     const int pi = threadIdx.x / TP;                      // pencil within the CTA
     const int t = threadIdx.x - pi * TP;                  // chunk index
@@ -321,14 +321,6 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     }
     const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
     const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
-    if (threadIdx.x < 7 && src_on && A.src_mode == 2) {
-        // weight l on thread l (LAGRANGE_INTERP, physics.f90:683-734);
-        // samples that take no part get weight 0 and index 0
-        int id;
-        const double w = lagrange_weight(A.clk, tl, A.L, threadIdx.x, &id);
-        lagw[threadIdx.x] = w;
-        lagi[threadIdx.x] = id < 0 ? 0 : id;
-    }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();                                      // the tiles are in, the mbarrier is initialised
     // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
@@ -386,14 +378,12 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     // forcing of this step for this mode (only the thread owning the source plane uses it)
     float2 F = make_float2(0.f, 0.f);
     if (src_t) {
-        const float2* pl = A.planes + (long long)s * A.plane_ss + m;
         if (A.src_mode == 1) {
+            const float2* pl = A.planes + (long long)s * A.plane_ss + m;
             float w = (tl < A.nseries) ? (float)A.series[(long long)s * A.nseries + tl] : 0.f;
             F = w * pl[0];
-        } else {
-            #pragma unroll
-            for (int l = 0; l < 7; ++l)
-                if (lagw[l] != 0.0) F = F + (float)lagw[l] * pl[(long long)lagi[l] * M];
+        } else {   // this step's interpolated plane, from source_plane_kernel
+            F = A.src_plane[(long long)s * M + m];
         }
         F = A.src_scale * F;
     }
@@ -638,6 +628,38 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             }
         }
     }
+}
+
+// LAGRANGE_INTERP source of the fused step (physics.f90:683-734): the plane
+// of every slot interpolated to the step about to run, sum over l of
+// w(l) * vr(l) with the FP64 weights of the slot's clock (samples that take
+// no part have weight 0 and are skipped), in FP32 in the order of l.  One
+// launch before each fused step, so that the step's CTAs read one value
+// instead of each computing the seven FP64 weights on its critical path.
+__global__ void __launch_bounds__(256) source_plane_kernel(const FusedArgs A) {
+    __shared__ double w[8];
+    __shared__ int id[8];
+    const int s = blockIdx.y;
+    if (threadIdx.x < 7) {
+        const int tl = *A.clk.time - A.clk.t0[s];
+        int i;
+        const double v = lagrange_weight(A.clk, tl, A.L, threadIdx.x, &i);
+        w[threadIdx.x] = v;
+        id[threadIdx.x] = i < 0 ? 0 : i;
+    }
+    __syncthreads();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= A.M) return;
+    const float2* pl = A.planes + (long long)s * A.plane_ss + m;
+    float2 F = make_float2(0.f, 0.f);
+    #pragma unroll
+    for (int l = 0; l < 7; ++l)
+        if (w[l] != 0.0) F = F + (float)w[l] * pl[(long long)id[l] * A.M];
+    A.src_plane[(long long)s * A.M + m] = F;
+}
+
+void launch_source_plane(const FusedArgs& A, int nsrc, cudaStream_t s) {
+    source_plane_kernel<<<dim3((A.M + 255) / 256, nsrc), 256, 0, s>>>(A);
 }
 
 int fused_w(int nz) { return (nz + 32 * CH - 1) / (32 * CH); }

@@ -380,6 +380,7 @@ struct FusedArgs {
     int* err;           // set to 1 if the bounded wait for the z-table bulk copy gave up
     int wait_limit;     // polls of that wait before it gives up
     int no_copy;        // test switch: issue no bulk copy, so the wait runs out with nothing in flight
+    float2* src_plane;  // [S][M] this step's interpolated source plane (src_mode 2, source_plane_kernel)
     int pf_stride;      // > 0: each CTA prefetches into L2 the rows of the CTA pf_stride later in launch
                         // order (set by the launcher to the CTAs resident at once); 0: no prefetch
 };
@@ -391,6 +392,7 @@ int fused_supported(int nz);
 int fused_w(int nz);
 int fused_nzp(int nz);
 void launch_fused(const FusedArgs& A, int nsrc, cudaStream_t s);
+void launch_source_plane(const FusedArgs& A, int nsrc, cudaStream_t s);
 
 // launchers (modal.cu)
 template <typename T> void launch_stage(const StageArgs<T>& A, int nsrc, cudaStream_t s);

@@ -101,6 +101,7 @@ class KernelPipeline:
     # ---- 3. adjoint run with kernel accumulation ----
     def kernels(self, fwd: Solver, adj_planes: np.ndarray, sum_slots: bool = False):
         adj = Solver(self.pa, self.table)
+        adj.set_rhs_output(False)              # the adjoint snapshot reads no scr
         for s in range(self.p.nsrc):
             adj.set_source_lagrange(adj_planes[s], slot=s)
         self._accumulate(fwd, adj)
@@ -116,6 +117,7 @@ class KernelPipeline:
         """As kernels(..., sum_slots=True), the sum written into the device
         buffer at out_ptr (3 * N doubles) instead of host arrays."""
         adj = Solver(self.pa, self.table)
+        adj.set_rhs_output(False)
         try:
             for s in range(self.p.nsrc):
                 adj.set_source_lagrange(adj_planes[s], slot=s)

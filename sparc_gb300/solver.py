@@ -233,6 +233,12 @@ class Solver:
     def set_active(self, n: int):
         self._ck(self.L.sparc_gpu_set_active(self.h, int(n)))
 
+    def set_rhs_output(self, on: bool):
+        """Whether each step call's last step leaves its right-hand side in
+        scr (default True; the forward snapshot needs it, an adjoint context
+        of the kernel workflow does not)."""
+        self._ck(self.L.sparc_gpu_set_rhs_output(self.h, int(bool(on))))
+
     def save_device(self, idx: int, capacity: int):
         self._ck(self.L.sparc_gpu_save_device(self.h, int(idx), int(capacity)))
 

@@ -86,3 +86,41 @@ def test_fused_cta_shapes_agree(gpu_lib, nz, monkeypatch):
         for k in range(2):
             assert np.array_equal(out[P][k][0], out["4"][k][0]) and np.array_equal(out[P][k][1], out["4"][k][1])
     assert np.abs(out["4"][0][0]).max() > 0
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_rhs_output_off_keeps_the_state_and_guards_the_snapshot(gpu_lib, prec):
+    """sparc_gpu_set_rhs_output(ctx, 0): the state after several step calls
+    is bit for bit that of the default context; the forward snapshot, which
+    reads scr, is refused with SPARC_ESTATE until the output is back on."""
+    from sparc_gb300 import sources
+    from sparc_gb300.native import SPARC_ESTATE, SparcError
+    from sparc_gb300.solver import Solver
+    p = small_params(precision=prec, nsrc=2)
+    tab = table_for(p)
+    a0, pml0 = random_state(p)
+    plane = gaussian_plane(p)
+    series = sources.ricker_series(p, 400) * 1e3
+    out = []
+    for on in (True, False):
+        g = Solver(p, tab)
+        g.set_rhs_output(on)
+        for s in range(p.nsrc):
+            g.set_state(a0 * (s + 1), pml0, slot=s)
+            g.set_source_series(plane, series, slot=s)
+        for n in (3, 1, 5):
+            g.step(n)
+        g.sync(check_finite=True)
+        out.append([g.state(slot=s) for s in range(p.nsrc)])
+        if not on:
+            with pytest.raises(SparcError) as e:
+                g.snapshot(0, 2)
+            assert e.value.status == SPARC_ESTATE
+            g.set_rhs_output(True)
+            g.step(1)
+            g.snapshot(0, 2)
+            g.sync()
+        g.close()
+    for s in range(p.nsrc):
+        assert np.array_equal(out[0][s][0], out[1][s][0])
+        assert np.array_equal(out[0][s][1], out[1][s][1])
