@@ -219,6 +219,19 @@ int sparc_gpu_set_active(sparc_ctx* ctx, int nactive);
  * which keeps scr in memory at all times (step.f90:24-128). */
 int sparc_gpu_set_rhs_output(sparc_ctx* ctx, int on);
 
+/* Scheduling priority of the context's stream(s): level 0 is the default
+ * (least urgent), each level above it one step more urgent, clamped to the
+ * device's range.  The context waits for its queued work and moves to new
+ * streams, so call it between steps.  When contexts share a GPU, the
+ * scheduler starts the CTAs of more urgent streams first: a serving loop
+ * gives its cheap requests' contexts the higher levels.  No counterpart in
+ * the reference (one MPI process per source). */
+int sparc_gpu_set_stream_priority(sparc_ctx* ctx, int level);
+
+/* Non-blocking: *busy = 1 while work queued on the context's stream has not
+ * finished, 0 once it has (cudaStreamQuery). */
+int sparc_gpu_query(sparc_ctx* ctx, int* busy);
+
 /* Checkpoint / restore of every slot (state, PML, time) to one file with a
  * checksum; restore rejects a corrupt or mismatching file with SPARC_EIO.
  * A restore restarts every slot clock at the restored time index. */

@@ -1288,6 +1288,34 @@ int sparc_gpu_slot_time(const sparc_ctx* c, int src, int* local_time) {
     return SPARC_OK;
 }
 
+int sparc_gpu_set_stream_priority(sparc_ctx* c, int level) {
+    if (!c) return SPARC_EINVAL;
+    if (level < 0) return fail(c, SPARC_EINVAL, "priority level < 0");
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int pr = std::max(greatest, least - level);     // CUDA: numerically lower is more urgent
+    CK(cudaStreamSynchronize(c->stream));
+    cudaStream_t ns = nullptr;
+    CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, pr));
+    cudaStreamDestroy(c->stream);
+    c->stream = ns;
+    c->epoch++;                         // step graphs are captured again on first use
+    if (c->mhd) return mhd_set_stream_priority(c, pr);
+    return SPARC_OK;
+}
+
+int sparc_gpu_query(sparc_ctx* c, int* busy) {
+    if (!c || !busy) return SPARC_EINVAL;
+    const cudaError_t e = cudaStreamQuery(c->stream);
+    if (e == cudaSuccess) { *busy = 0; return SPARC_OK; }
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError();            // not an error: the stream still has work
+        *busy = 1;
+        return SPARC_OK;
+    }
+    return fail(c, SPARC_ECUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(e));
+}
+
 int sparc_gpu_set_rhs_output(sparc_ctx* c, int on) {
     if (!c) return SPARC_EINVAL;
     const int v = on ? 1 : 0;

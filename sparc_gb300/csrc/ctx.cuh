@@ -146,6 +146,7 @@ template <typename T> typename CplxOf<T>::type* CP(void* p) { return (typename C
 // option 10 (mhd.cu)
 int mhd_create(sparc_ctx* c);
 void mhd_destroy(sparc_ctx* c);
+int mhd_set_stream_priority(sparc_ctx* c, int cuda_priority);   // the second stream's priority
 int mhd_set_background(sparc_ctx* c, const double* rho, const double* cs, const double* p, const double* bx,
                        const double* by, const double* bz);
 int mhd2d_set_background(sparc_ctx* c, const double* p, const double* rho, const double* cs, const double* psi);

@@ -1060,6 +1060,16 @@ int mhd_create(sparc_ctx* c) {
     return SPARC_OK;
 }
 
+int mhd_set_stream_priority(sparc_ctx* c, int cuda_priority) {
+    MhdState& m = *c->mhd;
+    CK(cudaStreamSynchronize(m.s2));
+    cudaStream_t ns = nullptr;
+    CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, cuda_priority));
+    cudaStreamDestroy(m.s2);
+    m.s2 = ns;
+    return SPARC_OK;
+}
+
 void mhd_destroy(sparc_ctx* c) {
     delete c->mhd;
     c->mhd = nullptr;

@@ -35,7 +35,7 @@ EXPORTS = [
     "sparc_gpu_set_state", "sparc_gpu_get_state", "sparc_gpu_record_surface",
     "sparc_gpu_get_records", "sparc_gpu_checkpoint", "sparc_gpu_restore",
     "sparc_gpu_save_device", "sparc_gpu_load_device", "sparc_gpu_slot_reset", "sparc_gpu_slot_time",
-    "sparc_gpu_set_active", "sparc_gpu_set_rhs_output",
+    "sparc_gpu_set_active", "sparc_gpu_set_rhs_output", "sparc_gpu_set_stream_priority", "sparc_gpu_query",
     "sparc_gpu_snapshot", "sparc_gpu_kernel_accumulate", "sparc_gpu_kernel_reset",
     "sparc_gpu_kernels", "sparc_gpu_ddx", "sparc_gpu_ddy", "sparc_gpu_ddz", "sparc_gpu_damp",
     "sparc_gpu_stream", "sparc_gpu_launch_count", "sparc_gpu_device_bytes", "sparc_gpu_info",
@@ -117,6 +117,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "sparc_gpu_slot_time": ([P, I, ctypes.POINTER(I)], I),
         "sparc_gpu_set_active": ([P, I], I),
         "sparc_gpu_set_rhs_output": ([P, I], I),
+        "sparc_gpu_set_stream_priority": ([P, I], I),
+        "sparc_gpu_query": ([P, ctypes.POINTER(I)], I),
         "sparc_gpu_snapshot": ([P, I, I], I),
         "sparc_gpu_kernel_accumulate": ([P, I, P], I),
         "sparc_gpu_kernel_reset": ([P], I),

@@ -81,11 +81,17 @@ class Pool:
     """One batched context (one grid size, one role) with `slots` slots."""
 
     def __init__(self, p: SparcParams, table, role: str, slots: int, max_records: int, background: str = QUIET,
-                 tube_cache: dict | None = None):
+                 tube_cache: dict | None = None, priority: int = 0):
+        import torch
         self.role = role
         self.background = background
         self.p = p.replace(nsrc=slots, compute_forward=(role == "fwd"), compute_adjoint=(role == "adj"))
         self.solver = Solver(self.p, table)
+        if priority > 0:
+            self.solver.set_stream_priority(priority)
+        self.stream = torch.cuda.ExternalStream(self.solver.stream_ptr)
+        self.inflight: list = []        # events of the queued output intervals, oldest first
+        self.done_at: dict = {}         # slot -> event after which its request has all its steps
         if background == TUBE:
             # the magnetohydrostatic tube of this grid, built once (FP64, with
             # this context's FP64 z derivative) and shared by its pools
@@ -123,17 +129,38 @@ class Pool:
         s.set_active(max(i for i, r in enumerate(self.requests) if r is not None) + 1)
         return slot
 
-    def advance(self, nsteps: int):
-        if self.busy:
-            self.solver.step(nsteps)
+    def advance(self, nsteps: int) -> bool:
+        """Queue nsteps more steps, unless two intervals are still queued: the
+        GPU queues stay short, so the streams' priorities decide the order of
+        the pools' work.  Returns whether steps were queued."""
+        import torch
+        if not self.busy:
+            return False
+        while self.inflight and self.inflight[0].query():
+            self.inflight.pop(0)
+        if len(self.inflight) >= 2:
+            return False
+        self.solver.step(nsteps)
+        ev = torch.cuda.Event()
+        ev.record(self.stream)
+        self.inflight.append(ev)
+        for slot, req in enumerate(self.requests):
+            if req is not None and slot not in self.done_at and self.solver.slot_time(slot) >= req.nsteps:
+                self.done_at[slot] = ev
+        return True
 
     def collect(self) -> list:
+        """Requests whose last step has finished on the GPU (non-blocking),
+        with their records up to their own length."""
         done = []
-        for slot, req in enumerate(self.requests):
-            if req is not None and self.solver.slot_time(slot) >= req.nsteps:
-                done.append((req, self.solver.records(slot=slot)))
+        for slot in sorted(self.done_at):
+            if self.done_at[slot].query():
+                req = self.requests[slot]
+                nrec = req.nsteps // self.p.steps     # the records of its own steps (the slot may have run on)
+                done.append((req, self.solver.records(slot=slot)[:nrec]))
                 self.requests[slot] = None
-        if self.busy:
+                del self.done_at[slot]
+        if done and self.busy:
             self.solver.set_active(max(i for i, r in enumerate(self.requests) if r is not None) + 1)
         return done
 
@@ -188,9 +215,20 @@ class Engine:
             idle[0].close()
             self.pools.remove(idle[0])
         pl = Pool(p, self._table(p.nz, background), role, slots, self.max_steps // self.cad + 1, background,
-                  self.tubes)
+                  self.tubes, priority=self._priority(grid, background))
         self.pools.append(pl)
         return pl
+
+    def _priority(self, grid, background) -> int:
+        """Stream priority level of a pool: the cheaper a step of its
+        configuration (grid points, times about 12 for the flux tube's
+        physical-space path), the more urgent, so short requests finish
+        first while long ones keep the GPU busy.  0 for the most expensive."""
+        def cost(g, bg):
+            return g[0] * g[1] * g[2] * (12 if bg == TUBE else 1)
+        keys = {(tuple(g), bg) for g in list(self.slots) + [tuple(grid)] for bg in (QUIET, TUBE)}
+        ranked = sorted({cost(g, bg) for g, bg in keys}, reverse=True)
+        return ranked.index(cost(tuple(grid), background))
 
     def _adjoint_planes(self, pl: Pool, req: Request):
         pix = sources.receiver_pixels(pl.p, n=8, radius_mm=10.0, x0_mm=req.x0_mm, y0_mm=req.y0_mm)
@@ -231,10 +269,13 @@ class Engine:
                     # nothing runs, nothing arrives, and the queue cannot be admitted
                     raise RuntimeError("serving: queued requests cannot be admitted within the HBM budget")
                 continue
-            for pl in self.pools:            # every pool advances one output interval; streams overlap
-                pl.advance(self.cad)
+            moved = False
+            for pl in self.pools:            # every pool queues one more output interval; streams overlap
+                moved |= bool(pl.advance(self.cad))
+            finished = 0
             for pl in self.pools:
                 for req, recs in pl.collect():
+                    finished += 1
                     t = (time.perf_counter() - t_start) / time_scale
                     if pl.role == "fwd":
                         req.records = recs
@@ -246,6 +287,8 @@ class Engine:
                         req.adj_records = recs
                     req.finished = t
                     done.append(req)
+            if not moved and not finished:
+                time.sleep(0.0002)           # every pool has two intervals queued
         return done
 
     def close(self):

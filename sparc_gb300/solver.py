@@ -233,6 +233,18 @@ class Solver:
     def set_active(self, n: int):
         self._ck(self.L.sparc_gpu_set_active(self.h, int(n)))
 
+    def set_stream_priority(self, level: int):
+        """Scheduling priority of this context's stream(s): 0 is the default,
+        higher levels are more urgent (clamped to the device's range)."""
+        self._ck(self.L.sparc_gpu_set_stream_priority(self.h, int(level)))
+
+    def busy(self) -> bool:
+        """True while work queued on this context's stream has not finished
+        (non-blocking)."""
+        b = ctypes.c_int(0)
+        self._ck(self.L.sparc_gpu_query(self.h, ctypes.byref(b)))
+        return bool(b.value)
+
     def set_rhs_output(self, on: bool):
         """Whether each step call's last step leaves its right-hand side in
         scr (default True; the forward snapshot needs it, an adjoint context

@@ -9,7 +9,7 @@ from sparc_gb300 import serving
 class FakePool:
     created = 0
 
-    def __init__(self, p, table, role, slots, max_records, background="quiet", tube_cache=None):
+    def __init__(self, p, table, role, slots, max_records, background="quiet", tube_cache=None, priority=0):
         FakePool.created += 1
         self.role = role
         self.background = background
@@ -32,6 +32,7 @@ class FakePool:
         for i, r in enumerate(self.requests):
             if r is not None:
                 self.clock[i] += n
+        return self.busy
 
     def collect(self):
         out = []
@@ -100,3 +101,15 @@ def test_stream_mixes_backgrounds():
     reqs = serving.poisson_stream(200, seed=3, p_tube=0.25)
     n_tube = sum(r.background == serving.TUBE for r in reqs)
     assert 30 < n_tube < 70
+
+
+def test_pool_priorities_follow_the_cost_of_a_step():
+    """Cheaper configurations get more urgent streams: 128^2 quiet first,
+    the 512^2 flux tube last (level 0)."""
+    eng = serving.Engine("f32", hbm_budget=1e12,
+                         slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2}, max_steps=30)
+    Q, T = serving.QUIET, serving.TUBE
+    order = [((128, 128, 150), Q), ((256, 256, 300), Q), ((128, 128, 150), T), ((512, 512, 300), Q),
+             ((256, 256, 300), T), ((512, 512, 300), T)]
+    levels = [eng._priority(g, bg) for g, bg in order]
+    assert levels == sorted(levels, reverse=True) and levels[-1] == 0 and len(set(levels)) == len(levels)
