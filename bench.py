@@ -270,6 +270,9 @@ def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, 
     eng = Engine(precision=precision, hbm_budget=budget,
                  slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
                  max_steps=max(r.nsteps for r in reqs))
+    tw = time.perf_counter()
+    npools = eng.warm()                  # contexts set up before the stream, as at server start
+    warm_s = time.perf_counter() - tw
     t0 = time.perf_counter()
     try:
         done = eng.run(reqs, max_wall=max_wall)
@@ -280,6 +283,7 @@ def serving_section(precision: str, n: int, compress: float, rate: float = 4.0, 
     st = latency_stats(done)
     st.update({"precision": precision, "Mpoint_steps_per_s": pts / wall / 1e6, "wall_s": wall,
                "compress": compress, "rate_per_s": rate, "hbm_budget_gb": budget / 1e9,
+               "warm_pools": npools, "warm_s": warm_s,
                "flux_tube_requests": sum(r.background == "tube" for r in done)})
     return st
 

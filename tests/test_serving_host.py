@@ -113,3 +113,18 @@ def test_pool_priorities_follow_the_cost_of_a_step():
              ((256, 256, 300), T), ((512, 512, 300), T)]
     levels = [eng._priority(g, bg) for g, bg in order]
     assert levels == sorted(levels, reverse=True) and levels[-1] == 0 and len(set(levels)) == len(levels)
+
+
+def test_warm_creates_pools_within_the_budget_without_eviction(fake):
+    """Engine.warm: one pool per (grid, background, role), cheapest first,
+    stopping at the HBM budget; the stream then runs on them."""
+    slots = {(128, 128, 150): 8, (256, 256, 300): 4, (512, 512, 300): 2}
+    eng = serving.Engine("f32", hbm_budget=1e12, slots=slots, max_steps=30)
+    assert eng.warm() == 12 and fake.created == 12
+    reqs = [serving.Request(i, (128, 128, 150), "fwd+adj", 30, 0.0, 0.0, 0.0) for i in range(4)]
+    done = eng.run(reqs, max_wall=30.0)
+    assert len(done) == 4 and fake.created == 12            # served by the warmed pools
+    small = serving.Engine("f32", hbm_budget=14e9, slots=slots, max_steps=30)
+    n = small.warm()
+    assert 0 < n < 12 and sum(pl.bytes for pl in small.pools) <= 14e9
+    assert all(not pl.closed for pl in small.pools)          # nothing released on the way
