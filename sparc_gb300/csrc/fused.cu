@@ -74,14 +74,14 @@ __device__ __forceinline__ void pencil_sync(int pi, int nthreads) {
 }
 
 // Carry of a chunk from the KB = 5 nearest chunk values of a look-back line:
-// sum over i = 1..5 of prod(i) * v(i), prod(1) = 1, prod(2..5) = pr.x..pr.w;
-// the far terms first.
+// sum over i = 1..5 of prod(i) * v(i), prod(1) = 1, prod(2..5) = pr.x..pr.w,
+// as two independent partial sums (a shorter dependency chain).
 __device__ __forceinline__ float2 lookback(float4 pr, float2 v1, float2 v2, float2 v3, float2 v4, float2 v5) {
-    float2 c = pmul(bc2(pr.w), v5);
-    c = pfma(bc2(pr.z), v4, c);
-    c = pfma(bc2(pr.y), v3, c);
-    c = pfma(bc2(pr.x), v2, c);
-    return padd(v1, c);
+    float2 c1 = pmul(bc2(pr.w), v5);
+    c1 = pfma(bc2(pr.z), v4, c1);
+    float2 c2 = pmul(bc2(pr.y), v3);
+    c2 = pfma(bc2(pr.x), v2, c2);
+    return padd(v1, padd(c1, c2));
 }
 
 // d/dz (without stretch) of the values of one exchange line (xp[j], j in
@@ -444,24 +444,36 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
-            float2 xx = TA(0, j), xz = TA(2, j), vx = TA(3, j);
-            if (hs) { xx = pfma(BT, sc[0][q], xx); xz = pfma(BT, sc[2][q], xz); vx = pfma(BT, sc[3][q], vx); }
+            float2 xx = TA(0, j), xz = TA(2, j);
+            if (hs) { xx = pfma(BT, sc[0][q], xx); xz = pfma(BT, sc[2][q], xz); }
             float2 div = imul(kx, xx) + d[q];
-            float2 xy, vy;
             if (D3) {
-                xy = TA(1, j); vy = TA(4, j);
-                if (hs) { xy = pfma(BT, sc[1][q], xy); vy = pfma(BT, sc[4][q], vy); }
+                float2 xy = TA(1, j);
+                if (hs) xy = pfma(BT, sc[1][q], xy);
                 div = div + imul(ky, xy);
             }
             const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
             qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
             xl[j] = p;
             own[q] = p;
+        }
+        pencil_sync(pi, TP);
+        // ---- dp'/dz, RHS v_z and xi_z ----
+        // d: (stretch / rho0) dp'/dz, scaled by the solve's tables
+        zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
+        // ---- horizontal right-hand sides (they do not feed the p' solve) ----
+        #pragma unroll
+        for (int q = 0; q < CH; ++q) {
+            const int j = j0 + q;
+            float2 vx = TA(3, j);
+            if (hs) vx = pfma(BT, sc[3][q], vx);
             const float ri = Z2(FZ_RI, j).x;
-            sc[3][q] = pfma(NGD, vx, -ri * imul(kx, p));
+            sc[3][q] = pfma(NGD, vx, -ri * imul(kx, own[q]));
             sc[0][q] = vx;
             if (D3) {
-                sc[4][q] = pfma(NGD, vy, -ri * imul(ky, p));
+                float2 vy = TA(4, j);
+                if (hs) vy = pfma(BT, sc[4][q], vy);
+                sc[4][q] = pfma(NGD, vy, -ri * imul(ky, own[q]));
                 sc[1][q] = vy;
             }
         }
@@ -472,10 +484,6 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             for (int q = 0; q < CH; ++q)
                 if (j0 + q == nz - 1) sc[0][q] = sc[1][q] = sc[3][q] = sc[4][q] = make_float2(0.f, 0.f);
         }
-        pencil_sync(pi, TP);
-        // ---- dp'/dz, RHS v_z and xi_z ----
-        // d: (stretch / rho0) dp'/dz, scaled by the solve's tables
-        zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;

@@ -130,9 +130,13 @@ class Pool:
         return slot
 
     def advance(self, nsteps: int) -> bool:
-        """Queue nsteps more steps, unless two intervals are still queued: the
-        GPU queues stay short, so the streams' priorities decide the order of
-        the pools' work.  Returns whether steps were queued."""
+        """Queue nsteps more steps (one step on the flux tube), unless two
+        such chunks are still queued: the GPU queues stay short, so the
+        streams' priorities decide the order of the pools' work.  A flux-tube
+        step is hundreds of separate launches (its per-slot filter schedule
+        keeps it out of graphs); queuing one at a time keeps the host from
+        blocking on a full launch queue while cheap pools wait.  Returns
+        whether steps were queued."""
         import torch
         if not self.busy:
             return False
@@ -140,7 +144,7 @@ class Pool:
             self.inflight.pop(0)
         if len(self.inflight) >= 2:
             return False
-        self.solver.step(nsteps)
+        self.solver.step(nsteps if self.background == QUIET else 1)
         ev = torch.cuda.Event()
         ev.record(self.stream)
         self.inflight.append(ev)
