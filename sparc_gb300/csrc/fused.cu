@@ -155,9 +155,9 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     // carry into the chunk: ud(j0-1) from the chunk values below
     constexpr int TP = 32 * W;
     lf[t] = run;
+    const float4 prf = *(const float4*)(zs + lb * NZP + 4 * t);      // read before the barrier
     pencil_sync(pi, TP);
-    const float2 uin = lookback(*(const float4*)(zs + lb * NZP + 4 * t), lf[t - 1], lf[t - 2], lf[t - 3],
-                                lf[t - 4], lf[t - 5]);
+    const float2 uin = lookback(prf, lf[t - 1], lf[t - 2], lf[t - 3], lf[t - 4], lf[t - 5]);
     #pragma unroll
     for (int q = 0; q < CH; ++q) u[q] = pfma(Z(HH, j0 + q), uin, u[q]);
     // back substitution x(j) = u(j) + g(j) x(j+1)
@@ -169,9 +169,9 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     }
     // carry from above: x(j0+CH) from the chunk values above
     lk[t] = xr;
+    const float4 prb = *(const float4*)(zs + (lb + 1) * NZP + 4 * t);
     pencil_sync(pi, TP);
-    const float2 xin = lookback(*(const float4*)(zs + (lb + 1) * NZP + 4 * t), lk[t + 1], lk[t + 2],
-                                lk[t + 3], lk[t + 4], lk[t + 5]);
+    const float2 xin = lookback(prb, lk[t + 1], lk[t + 2], lk[t + 3], lk[t + 4], lk[t + 5]);
     #pragma unroll
     for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
 }
@@ -444,8 +444,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         #pragma unroll
         for (int q = 0; q < CH; ++q) {
             const int j = j0 + q;
-            float2 xx = TA(0, j), xz = TA(2, j);
-            if (hs) { xx = pfma(BT, sc[0][q], xx); xz = pfma(BT, sc[2][q], xz); }
+            float2 xx = TA(0, j);
+            const float2 xz = own[q];      // the xi_z stage argument, still in registers
+            if (hs) xx = pfma(BT, sc[0][q], xx);
             float2 div = imul(kx, xx) + d[q];
             if (D3) {
                 float2 xy = TA(1, j);
