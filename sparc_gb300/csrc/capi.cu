@@ -118,6 +118,21 @@ FusedRows fused_rows_scaled(const FusedRows& r, const std::vector<double>& sig) 
     return o;
 }
 
+// The fused step's carry table K: the response of the chunk's back
+// substitution (zero carry from above) to the carry uin from below,
+// K(j) = H(j) + g(j) K(j+1) within the chunk, K(last) = H(last).  The rows
+// keep H's place; the look-back products use H itself.
+std::vector<double> fused_k_row(const FusedRows& r) {
+    const int nzp = (int)r.HH.size();
+    std::vector<double> K(nzp, 0.0);
+    for (int j0 = 0; j0 < nzp; j0 += FUSED_CH) {
+        const int j1 = j0 + FUSED_CH;
+        K[j1 - 1] = r.HH[j1 - 1];
+        for (int j = j1 - 2; j >= j0; --j) K[j] = r.HH[j] + r.gg[j] * K[j + 1];
+    }
+    return K;
+}
+
 // Look-back products of the fused step's carries: fwd[4t + i-2] is the
 // product of the chunk multipliers Mc(t-1)..Mc(t-i+1) (i = 2..5), the factor
 // of chunk t-i's value in the carry into chunk t; bwd[4t + i-2] likewise with
@@ -617,7 +632,8 @@ int sparc_gpu_set_background(sparc_ctx* c, const double* zin, const double* cin,
                 std::vector<double> sig(NZP, 1.0);
                 for (int j = 0; j < nz; ++j) sig[j] = ZR(ZT_STRETCH)[j] * (k == 1 ? ZR(ZT_RHOINV)[j] : 1.0);
                 const FusedRows fr = fused_rows_scaled(fused_rows(nz, NZP, tri[bcs[k]]), sig);
-                const std::vector<double>* rows[5] = {&fr.ibd, &fr.mm, &fr.HH, &fr.gg, &fr.GG};
+                const std::vector<double> kk = fused_k_row(fr);
+                const std::vector<double>* rows[5] = {&fr.ibd, &fr.mm, &kk, &fr.gg, &fr.GG};
                 for (int r = 0; r < 5; ++r)
                     for (int j = 0; j < NZP; ++j) put(base[k] + r, j, (*rows[r])[j]);
                 std::vector<double> lf, lb;

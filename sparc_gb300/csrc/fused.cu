@@ -33,9 +33,12 @@
 //     from a per-pencil line in shared memory after one barrier.  The terms
 //     left out are below 2^-32 of a chunk value (checked on the host for
 //     every boundary code, else the context runs the per-stage kernels).
-//     Each thread then adds H(j)*carry-in to its levels, H(j) the product of
-//     the multipliers from its chunk start to j.  This is the LU elimination
-//     and back substitution of the sequential form, re-associated.  Padding
+//     Each thread back-substitutes its chunk with zero carries before the
+//     first barrier, and the carries enter afterwards as
+//     x(j) = x0(j) + K(j)*carry-in + G(j)*carry-from-above, K and G host
+//     tables (K(j) = H(j) + g(j) K(j+1), H(j) the product of the multipliers
+//     from the chunk start to j).  This is the LU elimination and back
+//     substitution of the sequential form, re-associated.  Padding
 //     rows carry zero multipliers, so they never reach a real row.  The
 //     tables solve for the scaled unknown s(j) x(j) (s = stretch for xi_z,
 //     stretch / rho0 for p'), so each solve returns the derivative in the
@@ -89,7 +92,7 @@ __device__ __forceinline__ float2 lookback(float4 pr, float2 v1, float2 v2, floa
 // levels j0..j0+CH-1,
 // boundary code BC (dbyd2.f90:94-173 for the right-hand side; top is the
 // caller-set value of bc 3).  zs, r0: the z tables and the first of the five
-// elimination rows (1/betad, m, H, g, G) of BC; lb, lb+1: its forward and
+// elimination rows (1/betad, m, K, g, G) of BC; lb, lb+1: its forward and
 // backward look-back product tables ([t][4] floats each); lf, lk:
 // this pencil's forward and backward look-back lines (chunk t at index t,
 // zero entries at -KB..-1 and TP..TP+KB-1).
@@ -155,25 +158,25 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
     // carry into the chunk: ud(j0-1) from the chunk values below
     constexpr int TP = 32 * W;
     lf[t] = run;
-    const float4 prf = *(const float4*)(zs + lb * NZP + 4 * t);      // read before the barrier
-    pencil_sync(pi, TP);
-    const float2 uin = lookback(prf, lf[t - 1], lf[t - 2], lf[t - 3], lf[t - 4], lf[t - 5]);
-    #pragma unroll
-    for (int q = 0; q < CH; ++q) u[q] = pfma(Z(HH, j0 + q), uin, u[q]);
-    // back substitution x(j) = u(j) + g(j) x(j+1)
+    // back substitution x0(j) = u(j) + g(j) x0(j+1) with zero carries, while
+    // the other chunks reach the barrier; the carries enter afterwards as
+    // x(j) = x0(j) + K(j) uin + G(j) xin, K(j) = H(j) + g(j) K(j+1) (host table)
     float2 xr = make_float2(0.f, 0.f);
     #pragma unroll
     for (int q = CH - 1; q >= 0; --q) {
         xr = pfma(Z(gg, j0 + q), xr, u[q]);
         out[q] = xr;
     }
+    const float4 prf = *(const float4*)(zs + lb * NZP + 4 * t);      // read before the barrier
+    pencil_sync(pi, TP);
+    const float2 uin = lookback(prf, lf[t - 1], lf[t - 2], lf[t - 3], lf[t - 4], lf[t - 5]);
     // carry from above: x(j0+CH) from the chunk values above
-    lk[t] = xr;
+    lk[t] = pfma(Z(HH, j0), uin, xr);
     const float4 prb = *(const float4*)(zs + (lb + 1) * NZP + 4 * t);
     pencil_sync(pi, TP);
     const float2 xin = lookback(prb, lk[t + 1], lk[t + 2], lk[t + 3], lk[t + 4], lk[t + 5]);
     #pragma unroll
-    for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, out[q]);
+    for (int q = 0; q < CH; ++q) out[q] = pfma(Z(GG, j0 + q), xin, pfma(Z(HH, j0 + q), uin, out[q]));
 }
 
 // Poll phase 0 of an mbarrier at most `limit` times; true once it completed.

@@ -344,7 +344,8 @@ template <typename T> struct UpdateArgs {
 // fused FP32 step (fused.cu)
 // z table of the fused FP32 step, [FZ_COUNT][NZP] (NZP = fused_nzp(nz), padded
 // rows zero): profile rows, then the five elimination rows (1/betad,
-// elimination multiplier m, chunk products H of m, back-substitution
+// elimination multiplier m, the carry response K = H + g K(next) of the
+// chunk's back substitution, H the chunk products of m, back-substitution
 // multiplier g, chunk products G of g) of the xi_z boundary code and of the p'
 // boundary code, then the look-back products of each code: a forward row and
 // a backward row, [chunk t][4] floats each (the products of the multipliers
