@@ -119,7 +119,7 @@ __device__ __forceinline__ void zsolve(const float2* __restrict__ xp, const floa
         u[q] = pfma(C2p, psub(bp2, bm2), pmul(C1p, psub(bp1, bm1)));
     }
     if (lo) {   // rows 0 and 1 (dbyd2.f90:104-173)
-        const float2 b0 = xp[0], b1 = xp[1], b2 = xp[2], b3 = xp[3], b4 = xp[4];
+        const float2 b0 = own[0], b1 = own[1], b2 = own[2], b3 = own[3], b4 = own[4];   // j0 = 0
         const float2 r1 = c.Cb[0] * b0 + c.Cb[1] * b1 + c.Cb[2] * b2 + c.Cb[3] * b3 + c.Cb[4] * b4;
         u[1] = r1;
         if (BC == 0 || BC == 2) {
@@ -414,7 +414,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             float2 v = TA(2, j0 + q);
             if (hs) v = pfma(BT, sc[2][q], v);
             own[q] = v;
-            xl[j0 + q] = v;
+            // level j0+2 is no neighbour's stencil value; only the top rows'
+            // closure (levels nz-5..nz-1) may read it from the line
+            if (q != 2 || j0 + 2 >= nz - 5) xl[j0 + q] = v;
         }
         float2 top = make_float2(0.f, 0.f);
         if (!D3 && hi) {   // caller-set top value of bc 3 (physics2d.f90:960)
@@ -458,7 +460,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             }
             const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
             qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
-            xl[j] = p;
+            if (q != 2 || j0 + 2 >= nz - 5) xl[j] = p;
             own[q] = p;
         }
         pencil_sync(pi, TP);
