@@ -597,26 +597,38 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         for (int q = 0; q < CH; ++q) prev[q] = out[q];
     }
     __syncthreads();   // the store below copies every pencil's rows
-    // ---- store a and the PML planes ----
-    for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
-        const int f = r / nz, z = r - f * nz;
-        float2* dst = gA + f * fs + (long long)z * M + m0;
-        const float2* srcp = tile + f * P * LZ + GZ + z;
-        if (vec) {
-            #pragma unroll
-            for (int v = 0; v < P / 2; ++v) {
-                const float2 w0 = srcp[(2 * v) * LZ], w1 = srcp[(2 * v + 1) * LZ];
-                *(float4*)(dst + 2 * v) = make_float4(w0.x, w0.y, w1.x, w1.y);
+    // ---- store a and the PML planes.  A row [f][z] of the CTA's P modes is
+    // 8P contiguous bytes in HBM; P/2 consecutive lanes write it as P/2
+    // float4, so every warp store covers whole rows (full sectors) instead
+    // of 16 bytes in each of 32 rows ----
+    constexpr int LPR = P / 2;                            // lanes per row
+    const int lq = threadIdx.x % LPR;                     // this lane's modes: 2 lq, 2 lq + 1
+    auto store_rows = [&](float2* gbase) {
+        #pragma unroll 1
+        for (int f = 0; f < 6; ++f) {
+            for (int z = threadIdx.x / LPR; z < nz; z += nthr / LPR) {
+                float2* dst = gbase + f * fs + (long long)z * M + m0 + 2 * lq;
+                const float2* srcp = tile + f * P * LZ + (2 * lq) * LZ + GZ + z;
+                if (vec) {
+                    const float2 w0 = srcp[0], w1 = srcp[LZ];
+                    *(float4*)dst = make_float4(w0.x, w0.y, w1.x, w1.y);
+                } else {
+                    if (m0 + 2 * lq < M) dst[0] = srcp[0];
+                    if (m0 + 2 * lq + 1 < M) dst[1] = srcp[LZ];
+                }
             }
-        } else {
-            for (int q = 0; q < P; ++q)
-                if (m0 + q < M) dst[q] = srcp[q * LZ];
         }
-    }
-    for (int r = threadIdx.x; r < 2 * nzpml; r += nthr) {
-        float2* dst = gP + (long long)r * M + m0;
-        for (int q = 0; q < P; ++q)
-            if (m0 + q < M) dst[q] = ptile[r * P + q];
+    };
+    store_rows(gA);
+    for (int r = threadIdx.x / LPR; r < 2 * nzpml; r += nthr / LPR) {
+        float2* dst = gP + (long long)r * M + m0 + 2 * lq;
+        const float2* srcp = ptile + r * P + 2 * lq;
+        if (vec) {
+            *(float4*)dst = *(const float4*)srcp;
+        } else {
+            if (m0 + 2 * lq < M) dst[0] = srcp[0];
+            if (m0 + 2 * lq + 1 < M) dst[1] = srcp[1];
+        }
     }
     // ---- the last stage's right-hand side, when an output needs it ----
     if (A.write_scr) {
@@ -626,21 +638,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
             #pragma unroll
             for (int q = 0; q < CH; ++q) tp[f * P * LZ + j0 + q] = sc[f][q];
         __syncthreads();
-        for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
-            const int f = r / nz, z = r - f * nz;
-            float2* dst = gS + f * fs + (long long)z * M + m0;
-            const float2* srcp = tile + f * P * LZ + GZ + z;
-            if (vec) {
-                #pragma unroll
-                for (int v = 0; v < P / 2; ++v) {
-                    const float2 w0 = srcp[(2 * v) * LZ], w1 = srcp[(2 * v + 1) * LZ];
-                    *(float4*)(dst + 2 * v) = make_float4(w0.x, w0.y, w1.x, w1.y);
-                }
-            } else {
-                for (int q = 0; q < P; ++q)
-                    if (m0 + q < M) dst[q] = srcp[q * LZ];
-            }
-        }
+        store_rows(gS);
     }
 }
 
