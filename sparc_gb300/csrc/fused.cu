@@ -324,6 +324,10 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     }
     const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
     const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
+    // this mode's multipliers, loaded while the tile copies are in flight
+    const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
+    const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;
+    const float gd = (mvalid && A.damp) ? A.pt[PT_DAMP * M + m] : 0.f;
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();                                      // the tiles are in, the mbarrier is initialised
     // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
@@ -355,9 +359,6 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
     }
 
-    const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
-    const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;
-    const float gd = (mvalid && A.damp) ? A.pt[PT_DAMP * M + m] : 0.f;
     const float2 NGD = bc2(-gd);
     // threads that own rows with special rules
     const bool lo = (j0 == 0);                                       // rows 0, 1
