@@ -9,8 +9,9 @@
 //   * a (6 fields) lives in shared memory as a tile [field][mode][z] with
 //     zero ghost rows on both ends; global rows [field][z][m0..m0+P-1] are
 //     8P bytes, so the tile is loaded (cp.async, each value into its
-//     transposed place) and stored (float4) with sector-efficient
-//     cooperative copies once per step;
+//     transposed place) and stored (P/2 lanes per row, one float4 each, so
+//     a warp store covers whole rows) with sector-efficient cooperative
+//     copies once per step;
 //   * scr (the stage right-hand side, 6 fields) lives in registers of the
 //     owning thread -- every use of scr is point-wise;
 //   * stencil neighbours of the compact-FD right-hand sides are exchanged
