@@ -2,8 +2,11 @@
 // the horizontal filter of one time step in a single kernel, with the state
 // of each z-pencil held on chip for the whole step.
 //
-// Work decomposition.  A CTA owns P = 2, 4 or 8 consecutive horizontal modes
-// m of one source.  Each mode's z-pencil is split into chunks of CH = 5 levels, one
+// Work decomposition.  A work item is P = 2, 4 or 8 consecutive horizontal
+// modes m of one source; the launch has one CTA per resident slot (one per SM
+// at P = 8), and CTA b takes items b, b + G, b + 2G, ... (G CTAs), loading the
+// z tables once and issuing each item's tile copies right after the previous
+// item's stores have read the tile out of shared memory.  Each mode's z-pencil is split into chunks of CH = 5 levels, one
 // chunk per thread: TP = 32*W threads per pencil, W = ceil(nz / 160) warps,
 // and the pencil is padded to NZP = TP*CH levels.
 //   * a (6 fields) lives in shared memory as a tile [field][mode][z] with
@@ -51,6 +54,7 @@
 //     spends its critical path on the seven FP64 weights.
 // HBM traffic per step: read a, write a (+ the PML planes and source planes),
 // and scr only on steps whose right-hand side is requested (outputs).
+#include <algorithm>
 #include <type_traits>
 
 #include "internal.cuh"
@@ -237,19 +241,14 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     const int nthr = blockDim.x;
     const int pi = threadIdx.x / TP;                      // pencil within the CTA
     const int t = threadIdx.x - pi * TP;                  // chunk index
-    const int m0 = blockIdx.x * P;
-    const int m = m0 + pi;
-    const bool mvalid = m < M;
-    const int s = blockIdx.y;
     const int j0 = t * CH;
     float2* xl = xlb + pi * LX + GX;
     float2* lf = lines + (2 * pi) * LL + KB;
     float2* lk = lines + (2 * pi + 1) * LL + KB;
-    float2* gA = A.a + (long long)s * 6 * fs;
-    float2* gS = A.scr + (long long)s * 6 * fs;
-    float2* gP = A.pml + (long long)s * 2 * A.ps;
-    // 16 B vector copies need every row start z*M + m0 to be even (M even)
-    const bool vec = ((M & 1) == 0) && (m0 + P <= M);
+    // work items: (source, group of P modes); CTA b takes items b, b + G, ...
+    const int ntile = (M + P - 1) / P;
+    const int nitem = ntile * A.nsrc;
+    if ((int)blockIdx.x >= nitem) return;           // (the launch never has more CTAs than items)
 
     // ---- the z tables: one bulk copy (TMA engine) into shared memory, issued
     // by thread 0 and awaited, with a bounded wait, after the cooperative
@@ -286,6 +285,26 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         for (int r = threadIdx.x; r < 2 * P * 2 * KB; r += nthr) {
             const int line = r / (2 * KB), k = r - line * (2 * KB);
             lines[line * LL + (k < KB ? k : TP + k)] = make_float2(0.f, 0.f);
+        }
+    }
+    for (int item = blockIdx.x; item < nitem; item += gridDim.x) {
+    const bool first = item == (int)blockIdx.x;
+    const int s = item / ntile;
+    const int m0 = (item - s * ntile) * P;
+    const int m = m0 + pi;
+    const bool mvalid = m < M;
+    float2* gA = A.a + (long long)s * 6 * fs;
+    float2* gS = A.scr + (long long)s * 6 * fs;
+    float2* gP = A.pml + (long long)s * 2 * A.ps;
+    // 16 B vector copies need every row start z*M + m0 to be even (M even)
+    const bool vec = ((M & 1) == 0) && (m0 + P <= M);
+    if (!first) {
+        // the previous item's update and filter wrote the padding levels
+        // nz..NZP-1 of every row: zero them again
+        const int np = NZP - nz;
+        for (int r = threadIdx.x; r < 6 * P * np; r += nthr) {
+            const int row = r / np, k = r - row * np;
+            tile[row * LZ + GZ + nz + k] = make_float2(0.f, 0.f);
         }
     }
     // ---- load the a tile and the PML tile: every complex value by its own
@@ -335,7 +354,7 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     // reports it and leaves without computing or storing (its modes keep the
     // state of the previous step), thread 0 first waiting out a copy still in
     // flight so that nothing lands in shared memory after the CTA has gone
-    if (__syncthreads_or(!mbar_wait(mbar, A.wait_limit))) {
+    if (first && __syncthreads_or(!mbar_wait(mbar, A.wait_limit))) {
         if (threadIdx.x == 0) {
             atomicExch(A.err, 1);
             if (!A.no_copy) mbar_wait(mbar, 1 << 22);
@@ -346,9 +365,9 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
     // ---- L2 prefetch of the rows of the CTA that starts pf_stride CTAs
     // later (about when this one ends): its tile load then comes from L2 ----
     if (A.pf_stride > 0) {
-        const long long nid = (long long)blockIdx.y * gridDim.x + blockIdx.x + A.pf_stride;
-        if (nid < (long long)gridDim.x * gridDim.y) {
-            const int ns = (int)(nid / gridDim.x), nm0 = (int)(nid - (long long)ns * gridDim.x) * P;
+        const int nid = item + gridDim.x;             // this CTA's next item
+        if (nid < nitem) {
+            const int ns = nid / ntile, nm0 = (nid - ns * ntile) * P;
             const float2* nA = A.a + (long long)ns * 6 * fs + nm0;
             for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
                 const int f = r / nz, z = r - f * nz;
@@ -642,6 +661,10 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         __syncthreads();
         store_rows(gS);
     }
+    // every thread has read the tile and the PML tile out for the stores
+    // (in flight now) before the next item's copies overwrite them
+    __syncthreads();
+    }
 }
 
 // LAGRANGE_INTERP source of the fused step (physics.f90:683-734): the plane
@@ -715,16 +738,16 @@ void fused_prepare(int nz, int nzpml) {
 template <bool D3, int W, int P>
 static void launch_fused_t(const FusedArgs& A, int nsrc, cudaStream_t s) {
     const size_t sm = (size_t)fused_layout(P, W, A.nzpml).total;
-    dim3 grid((A.M + P - 1) / P, nsrc);
     FusedArgs B = A;
-    if (B.pf_stride > 0) {
-        int dev = 0, nsm = 0, occ = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fused_step_kernel<D3, W, P>, P * 32 * W, sm);
-        B.pf_stride = (nsm > 0 && occ > 0) ? nsm * occ : 0;
-    }
-    fused_step_kernel<D3, W, P><<<grid, P * 32 * W, sm, s>>>(B);
+    B.nsrc = nsrc;
+    int dev = 0, nsm = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fused_step_kernel<D3, W, P>, P * 32 * W, sm);
+    const long long items = (long long)((A.M + P - 1) / P) * nsrc;
+    const long long resident = (long long)std::max(nsm, 1) * std::max(occ, 1);
+    const int ncta = (int)std::min(items, resident);
+    fused_step_kernel<D3, W, P><<<ncta, P * 32 * W, sm, s>>>(B);
 }
 
 template <bool D3, int W>

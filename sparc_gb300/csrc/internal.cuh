@@ -382,6 +382,7 @@ struct FusedArgs {
     int wait_limit;     // polls of that wait before it gives up
     int no_copy;        // test switch: issue no bulk copy, so the wait runs out with nothing in flight
     float2* src_plane;  // [S][M] this step's interpolated source plane (src_mode 2, source_plane_kernel)
+    int nsrc;           // sources of the launch (set by the launcher)
     int pf_stride;      // > 0: each CTA prefetches into L2 the rows of the CTA pf_stride later in launch
                         // order (set by the launcher to the CTAs resident at once); 0: no prefetch
 };
