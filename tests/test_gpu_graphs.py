@@ -124,3 +124,31 @@ def test_rhs_output_off_keeps_the_state_and_guards_the_snapshot(gpu_lib, prec):
     for s in range(p.nsrc):
         assert np.array_equal(out[0][s][0], out[1][s][0])
         assert np.array_equal(out[0][s][1], out[1][s][1])
+
+
+def test_stream_priority_and_query(gpu_lib):
+    """sparc_gpu_set_stream_priority moves the context to new streams between
+    steps without changing results; sparc_gpu_query reports the queued work
+    finished once the context is synchronised."""
+    from sparc_gb300 import sources
+    from sparc_gb300.solver import Solver
+    p = small_params(precision="f32", nsrc=2)
+    tab = table_for(p)
+    a0, pml0 = random_state(p)
+    plane = gaussian_plane(p)
+    series = sources.ricker_series(p, 400) * 1e3
+    out = []
+    for level in (0, 3):
+        g = Solver(p, tab)
+        for s in range(p.nsrc):
+            g.set_state(a0, pml0, slot=s)
+            g.set_source_series(plane, series, slot=s)
+        g.step(4)
+        if level:
+            g.set_stream_priority(level)      # between steps: waits for the queued work
+        g.step(5)
+        g.sync()
+        assert g.busy() is False
+        out.append(g.state(slot=1))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
