@@ -6,9 +6,10 @@
 // modes m of one source; the launch has one CTA per resident slot (one per SM
 // at P = 8), and CTA b takes items b, b + G, b + 2G, ... (G CTAs), loading the
 // z tables once and issuing each item's tile copies right after the previous
-// item's stores have read the tile out of shared memory.  Each mode's z-pencil is split into chunks of CH = 5 levels, one
-// chunk per thread: TP = 32*W threads per pencil, W = ceil(nz / 160) warps,
-// and the pencil is padded to NZP = TP*CH levels.
+// item's stores have read the tile out of shared memory.  Each mode's
+// z-pencil is split into chunks of CH = 5 levels, one chunk per thread:
+// TP = 32*W threads per pencil, W = ceil(nz / 160) warps, and the pencil is
+// padded to NZP = TP*CH levels.
 //   * a (6 fields) lives in shared memory as a tile [field][mode][z] with
 //     zero ghost rows on both ends; global rows [field][z][m0..m0+P-1] are
 //     8P bytes, so the tile is loaded (cp.async, each value into its
@@ -288,382 +289,383 @@ __global__ void __launch_bounds__(P * 64, 8 / P) fused_step_kernel(const FusedAr
         }
     }
     for (int item = blockIdx.x; item < nitem; item += gridDim.x) {
-    const bool first = item == (int)blockIdx.x;
-    const int s = item / ntile;
-    const int m0 = (item - s * ntile) * P;
-    const int m = m0 + pi;
-    const bool mvalid = m < M;
-    float2* gA = A.a + (long long)s * 6 * fs;
-    float2* gS = A.scr + (long long)s * 6 * fs;
-    float2* gP = A.pml + (long long)s * 2 * A.ps;
-    // 16 B vector copies need every row start z*M + m0 to be even (M even)
-    const bool vec = ((M & 1) == 0) && (m0 + P <= M);
-    if (!first) {
-        // the previous item's update and filter wrote the padding levels
-        // nz..NZP-1 of every row: zero them again
-        const int np = NZP - nz;
-        for (int r = threadIdx.x; r < 6 * P * np; r += nthr) {
-            const int row = r / np, k = r - row * np;
-            tile[row * LZ + GZ + nz + k] = make_float2(0.f, 0.f);
-        }
-    }
-    // ---- load the a tile and the PML tile: every complex value by its own
-    // asynchronous 8-byte copy into its transposed place, all in flight at
-    // once ([z][m] in HBM, [mode][z] on chip), awaited with the z tables ----
-    {
-        constexpr int RPI = TP;                       // rows advanced per pass: blockDim.x / P
-        const int q = threadIdx.x % P;
-        const bool qv = m0 + q < M;
-        const int z0 = threadIdx.x / P;
-        if (qv) {
-            const unsigned d0 = (unsigned)__cvta_generic_to_shared(tile + q * LZ + GZ + z0);
-            const float2* s0 = gA + (long long)z0 * M + m0 + q;
-            #pragma unroll 1
-            for (int f = 0; f < 6; ++f) {
-                unsigned dst = d0 + f * (P * LZ * 8);
-                size_t src = __cvta_generic_to_global(s0 + f * fs);
-                for (int z = z0; z < nz; z += RPI, dst += RPI * 8, src += (size_t)RPI * M * 8)
-                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+        const bool first = item == (int)blockIdx.x;
+        const int s = item / ntile;
+        const int m0 = (item - s * ntile) * P;
+        const int m = m0 + pi;
+        const bool mvalid = m < M;
+        float2* gA = A.a + (long long)s * 6 * fs;
+        float2* gS = A.scr + (long long)s * 6 * fs;
+        float2* gP = A.pml + (long long)s * 2 * A.ps;
+        // 16 B vector copies need every row start z*M + m0 to be even (M even)
+        const bool vec = ((M & 1) == 0) && (m0 + P <= M);
+        if (!first) {
+            // the previous item's update and filter wrote the padding levels
+            // nz..NZP-1 of every row: zero them again
+            const int np = NZP - nz;
+            for (int r = threadIdx.x; r < 6 * P * np; r += nthr) {
+                const int row = r / np, k = r - row * np;
+                tile[row * LZ + GZ + nz + k] = make_float2(0.f, 0.f);
             }
-        } else {
-            for (int f = 0; f < 6; ++f)
-                for (int z = z0; z < nz; z += RPI) tile[f * P * LZ + q * LZ + GZ + z] = make_float2(0.f, 0.f);
         }
-        for (int r = threadIdx.x / P; r < 2 * nzpml; r += RPI) {
-            float2* dst = ptile + r * P + q;
+        // ---- load the a tile and the PML tile: every complex value by its own
+        // asynchronous 8-byte copy into its transposed place, all in flight at
+        // once ([z][m] in HBM, [mode][z] on chip), awaited with the z tables ----
+        {
+            constexpr int RPI = TP;                       // rows advanced per pass: blockDim.x / P
+            const int q = threadIdx.x % P;
+            const bool qv = m0 + q < M;
+            const int z0 = threadIdx.x / P;
             if (qv) {
-                const float2* src = gP + (long long)r * M + m0 + q;
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
-                                 (unsigned)__cvta_generic_to_shared(dst)),
-                             "l"(__cvta_generic_to_global(src))
-                             : "memory");
+                const unsigned d0 = (unsigned)__cvta_generic_to_shared(tile + q * LZ + GZ + z0);
+                const float2* s0 = gA + (long long)z0 * M + m0 + q;
+                #pragma unroll 1
+                for (int f = 0; f < 6; ++f) {
+                    unsigned dst = d0 + f * (P * LZ * 8);
+                    size_t src = __cvta_generic_to_global(s0 + f * fs);
+                    for (int z = z0; z < nz; z += RPI, dst += RPI * 8, src += (size_t)RPI * M * 8)
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
+                }
             } else {
-                *dst = make_float2(0.f, 0.f);
+                for (int f = 0; f < 6; ++f)
+                    for (int z = z0; z < nz; z += RPI) tile[f * P * LZ + q * LZ + GZ + z] = make_float2(0.f, 0.f);
             }
-        }
-    }
-    const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
-    const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
-    // this mode's multipliers, loaded while the tile copies are in flight
-    const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
-    const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;
-    const float gd = (mvalid && A.damp) ? A.pt[PT_DAMP * M + m] : 0.f;
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();                                      // the tiles are in, the mbarrier is initialised
-    // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
-    // reports it and leaves without computing or storing (its modes keep the
-    // state of the previous step), thread 0 first waiting out a copy still in
-    // flight so that nothing lands in shared memory after the CTA has gone
-    if (first && __syncthreads_or(!mbar_wait(mbar, A.wait_limit))) {
-        if (threadIdx.x == 0) {
-            atomicExch(A.err, 1);
-            if (!A.no_copy) mbar_wait(mbar, 1 << 22);
-        }
-        return;
-    }
-
-    // ---- L2 prefetch of the rows of the CTA that starts pf_stride CTAs
-    // later (about when this one ends): its tile load then comes from L2 ----
-    if (A.pf_stride > 0) {
-        const int nid = item + gridDim.x;             // this CTA's next item
-        if (nid < nitem) {
-            const int ns = nid / ntile, nm0 = (nid - ns * ntile) * P;
-            const float2* nA = A.a + (long long)ns * 6 * fs + nm0;
-            for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
-                const int f = r / nz, z = r - f * nz;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(nA + f * fs + (long long)z * M)));
-            }
-            const float2* nP = A.pml + (long long)ns * 2 * A.ps + nm0;
-            for (int r = threadIdx.x; r < 2 * nzpml; r += nthr)
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(nP + (long long)r * M)));
-        }
-    }
-
-    const float2 NGD = bc2(-gd);
-    // threads that own rows with special rules
-    const bool lo = (j0 == 0);                                       // rows 0, 1
-    const bool hi = (j0 <= nz - 1) && (j0 + CH > nz - 2);            // rows nz-2, nz-1
-    // PML levels of this chunk: bit q of pmask, plane index pipv + q (a chunk
-    // holds contiguous levels of one layer at most)
-    unsigned pmask = 0;
-    int pipv = 0;
-    if (j0 < nb) {
-        pmask = (1u << min(CH, nb - j0)) - 1u;
-        pipv = j0;
-    } else {
-        const int l0 = max(j0, nz - nt), l1 = min(j0 + CH, nz);
-        if (l1 > l0) {
-            pmask = ((1u << (l1 - l0)) - 1u) << (l0 - j0);
-            pipv = nb + (j0 - (nz - nt));
-        }
-    }
-    const bool pml_t = pmask != 0;
-    const bool src_t = src_on && mvalid && A.ksrc >= j0 && A.ksrc < j0 + CH;
-    // forcing of this step for this mode (only the thread owning the source plane uses it)
-    float2 F = make_float2(0.f, 0.f);
-    if (src_t) {
-        if (A.src_mode == 1) {
-            const float2* pl = A.planes + (long long)s * A.plane_ss + m;
-            float w = (tl < A.nseries) ? (float)A.series[(long long)s * A.nseries + tl] : 0.f;
-            F = w * pl[0];
-        } else {   // this step's interpolated plane, from source_plane_kernel
-            F = A.src_plane[(long long)s * M + m];
-        }
-        F = A.src_scale * F;
-    }
-
-    float2 sc[6][CH];
-    #pragma unroll
-    for (int f = 0; f < 6; ++f)
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) sc[f][q] = make_float2(0.f, 0.f);
-
-    float2* tp = tile + pi * LZ + GZ;                    // field f, level j: tp[f*P*LZ + j]
-    auto TA = [&](int f, int j) -> float2 { return tp[f * P * LZ + j]; };
-    // z table entry of row r at level j, as a pair
-    auto Z2 = [&](int r, int j) { return zt2(zs, r * NZP + j); };
-
-    // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
-    // rather than a (stage 1), fixed at compile time
-    auto stage = [&](auto hs_c, const float beta) {
-        constexpr bool hs = decltype(hs_c)::value;
-        const float2 BT = bc2(beta);
-        // ---- temp xi_z into the first exchange line ----
-        float2 own[CH];
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            float2 v = TA(2, j0 + q);
-            if (hs) v = pfma(BT, sc[2][q], v);
-            own[q] = v;
-            // level j0+2 is no neighbour's stencil value; only the top rows'
-            // closure (levels nz-5..nz-1) may read it from the line
-            if (q != 2 || j0 + 2 >= nz - 5) xl[j0 + q] = v;
-        }
-        float2 top = make_float2(0.f, 0.f);
-        if (!D3 && hi) {   // caller-set top value of bc 3 (physics2d.f90:960)
-            float2 last = make_float2(0.f, 0.f);
-            #pragma unroll
-            for (int q = 0; q < CH; ++q)
-                if (j0 + q == nz - 1) last = sc[0][q];
-            float2 xx = TA(0, nz - 1);
-            if (hs) xx = xx + beta * last;
-            top = -(imul(kx, xx) * A.unstr_top);
-        }
-        pencil_sync(pi, TP);
-        float2 d[CH];
-        // d: the stretched derivative (the solve's tables carry the stretch)
-        zsolve<BCX, W>(xl, own, zs, FZ_SX, FZ_LX, nz, top, j0, lo, hi, t, lf, lk, pi, A.cc, d);
-        if (pml_t) {   // psi_vz (displacement.f90 PML rows)
-            #pragma unroll
-            for (int q = 0; q < CH; ++q) {
-                if (pmask & (1u << q)) {
-                    const int j = j0 + q, ip = pipv + q;
-                    float2 psi = ptile[ip * P + pi];
-                    if (hs) psi = psi + beta * spt[ip * P + pi];
-                    spt[ip * P + pi] = Z2(FZ_AZ, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
-                    d[q] = d[q] + psi;
-                }
-            }
-        }
-        // ---- div, p', the buoyancy term, horizontal right-hand sides ----
-        float2 qt[CH];
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            const int j = j0 + q;
-            float2 xx = TA(0, j);
-            const float2 xz = own[q];      // the xi_z stage argument, still in registers
-            if (hs) xx = pfma(BT, sc[0][q], xx);
-            float2 div = imul(kx, xx) + d[q];
-            if (D3) {
-                float2 xy = TA(1, j);
-                if (hs) xy = pfma(BT, sc[1][q], xy);
-                div = div + imul(ky, xy);
-            }
-            const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
-            qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
-            if (q != 2 || j0 + 2 >= nz - 5) xl[j] = p;
-            own[q] = p;
-        }
-        pencil_sync(pi, TP);
-        // ---- dp'/dz, RHS v_z and xi_z ----
-        // d: (stretch / rho0) dp'/dz, scaled by the solve's tables
-        zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
-        // ---- horizontal right-hand sides (they do not feed the p' solve) ----
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            const int j = j0 + q;
-            float2 vx = TA(3, j);
-            if (hs) vx = pfma(BT, sc[3][q], vx);
-            const float ri = Z2(FZ_RI, j).x;
-            sc[3][q] = pfma(NGD, vx, -ri * imul(kx, own[q]));
-            sc[0][q] = vx;
-            if (D3) {
-                float2 vy = TA(4, j);
-                if (hs) vy = pfma(BT, sc[4][q], vy);
-                sc[4][q] = pfma(NGD, vy, -ri * imul(ky, own[q]));
-                sc[1][q] = vy;
-            }
-        }
-        // zero right-hand side rows: j = 0 (and j = nz-1 in 3-D)
-        if (lo) { sc[3][0] = sc[0][0] = make_float2(0.f, 0.f); if (D3) sc[4][0] = sc[1][0] = sc[3][0]; }
-        if (D3 && hi) {
-            #pragma unroll
-            for (int q = 0; q < CH; ++q)
-                if (j0 + q == nz - 1) sc[0][q] = sc[1][q] = sc[3][q] = sc[4][q] = make_float2(0.f, 0.f);
-        }
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            const int j = j0 + q;
-            float2 vz = TA(5, j);
-            if (hs) vz = pfma(BT, sc[5][q], vz);
-            sc[5][q] = pfma(NGD, vz, psub(qt[q], d[q]));
-            sc[2][q] = vz;
-        }
-        if (pml_t) {   // psi_p
-            #pragma unroll
-            for (int q = 0; q < CH; ++q) {
-                if (pmask & (1u << q)) {
-                    const int j = j0 + q, ip = pipv + q;
-                    float2 psi = ptile[(nzpml + ip) * P + pi];
-                    if (hs) psi = psi + beta * spt[(nzpml + ip) * P + pi];
-                    spt[(nzpml + ip) * P + pi] = Z2(FZ_AZR, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
-                    sc[5][q] = sc[5][q] - Z2(FZ_RI, j).x * psi;
-                }
-            }
-        }
-        if (src_t) {
-            #pragma unroll
-            for (int q = 0; q < CH; ++q)
-                if (j0 + q == A.ksrc) sc[5][q] = sc[5][q] + F;
-        }
-        if (lo) sc[5][0] = sc[2][0] = make_float2(0.f, 0.f);
-        if (D3 && hi) {
-            #pragma unroll
-            for (int q = 0; q < CH; ++q)
-                if (j0 + q == nz - 1) sc[5][q] = sc[2][q] = make_float2(0.f, 0.f);
-        }
-    };
-    stage(std::integral_constant<bool, false>(), 0.f);
-    for (int rk = 1; rk < 5; ++rk) {
-        // static parameter indices keep the argument block out of local memory
-        const float beta = rk == 1 ? A.betas[1] : rk == 2 ? A.betas[2] : rk == 3 ? A.betas[3] : A.betas[4];
-        stage(std::integral_constant<bool, true>(), beta);
-    }
-
-    // ---- update a += dt*scr, pml += dt*scrpml (step.f90:114-116) ----
-    const float dt = A.dt;
-    const float2 DT = bc2(dt);
-    #pragma unroll
-    for (int f = 0; f < 6; ++f)
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            float2* a = tp + f * P * LZ + j0 + q;
-            *a = pfma(DT, sc[f][q], *a);
-        }
-    if (pml_t) {
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) {
-            if (pmask & (1u << q)) {
-                const int ip = pipv + q;
-                ptile[ip * P + pi] = ptile[ip * P + pi] + dt * spt[ip * P + pi];
-                ptile[(nzpml + ip) * P + pi] = ptile[(nzpml + ip) * P + pi] + dt * spt[(nzpml + ip) * P + pi];
-            }
-        }
-    }
-    pencil_sync(pi, TP);
-    // ---- z filter (+ horizontal filter): field f is filtered into registers,
-    // and written back after the next barrier, while field f+1 is filtered ----
-    const float hf = mvalid ? A.pt[PT_HF * M + m] : 1.f;
-    const float h1 = 0.5f * 0.41015625f, h2 = 0.5f * -0.234375f, h3 = 0.5f * 0.087890625f;
-    const float h4 = 0.5f * -0.01953125f, h5 = 0.5f * 0.001953125f, c0 = 0.75390625f;
-    const bool hfil_on = slot_hfilter(A.clk, tl);
-    const bool flo = j0 < 5, fhi = (j0 < nz) && (j0 + CH > nz - 5);
-    float2 prev[CH];
-    #pragma unroll
-    for (int f = 0; f < 7; ++f) {
-        float2 out[CH];
-        if (f < 6) {
-            const float2* V = tp + f * P * LZ;
-            #pragma unroll
-            for (int q = 0; q < CH; ++q) {
-                const int j = j0 + q;
-                float2 acc = pmul(bc2(c0), V[j]);
-                acc = pfma(bc2(h1), padd(V[j - 1], V[j + 1]), acc);
-                acc = pfma(bc2(h2), padd(V[j - 2], V[j + 2]), acc);
-                acc = pfma(bc2(h3), padd(V[j - 3], V[j + 3]), acc);
-                acc = pfma(bc2(h4), padd(V[j - 4], V[j + 4]), acc);
-                out[q] = pfma(bc2(h5), padd(V[j - 5], V[j + 5]), acc);
-            }
-            if (flo || fhi) {   // FILTER_VARS_3D / _2D boundary rows
-                #pragma unroll
-                for (int q = 0; q < CH; ++q) {
-                    const int j = j0 + q;
-                    const bool near_bot = (j >= 1 && j <= 4), near_top = (j >= nz - 5 && j <= nz - 2);
-                    if (j == 0 || j == nz - 1) out[q] = V[j];
-                    else if (near_top) out[q] = 0.5f * (V[j + 1] + V[j - 1]);
-                    else if (near_bot) out[q] = D3 ? 0.5f * (V[j + 1] + V[j - 1]) : V[j];
-                }
-            }
-            if (hfil_on && (D3 ? (f < 5) : true)) {
-                #pragma unroll
-                for (int q = 0; q < CH; ++q) out[q] = hf * out[q];
-            }
-        }
-        if (f > 0) {
-            pencil_sync(pi, TP);   // every thread has read field f-1's neighbours
-            #pragma unroll
-            for (int q = 0; q < CH; ++q) tp[(f - 1) * P * LZ + j0 + q] = prev[q];
-        }
-        #pragma unroll
-        for (int q = 0; q < CH; ++q) prev[q] = out[q];
-    }
-    __syncthreads();   // the store below copies every pencil's rows
-    // ---- store a and the PML planes.  A row [f][z] of the CTA's P modes is
-    // 8P contiguous bytes in HBM; P/2 consecutive lanes write it as P/2
-    // float4, so every warp store covers whole rows (full sectors) instead
-    // of 16 bytes in each of 32 rows ----
-    constexpr int LPR = P / 2;                            // lanes per row
-    const int lq = threadIdx.x % LPR;                     // this lane's modes: 2 lq, 2 lq + 1
-    auto store_rows = [&](float2* gbase) {
-        #pragma unroll 1
-        for (int f = 0; f < 6; ++f) {
-            for (int z = threadIdx.x / LPR; z < nz; z += nthr / LPR) {
-                float2* dst = gbase + f * fs + (long long)z * M + m0 + 2 * lq;
-                const float2* srcp = tile + f * P * LZ + (2 * lq) * LZ + GZ + z;
-                if (vec) {
-                    const float2 w0 = srcp[0], w1 = srcp[LZ];
-                    *(float4*)dst = make_float4(w0.x, w0.y, w1.x, w1.y);
+            for (int r = threadIdx.x / P; r < 2 * nzpml; r += RPI) {
+                float2* dst = ptile + r * P + q;
+                if (qv) {
+                    const float2* src = gP + (long long)r * M + m0 + q;
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                                     (unsigned)__cvta_generic_to_shared(dst)),
+                                 "l"(__cvta_generic_to_global(src))
+                                 : "memory");
                 } else {
-                    if (m0 + 2 * lq < M) dst[0] = srcp[0];
-                    if (m0 + 2 * lq + 1 < M) dst[1] = srcp[LZ];
+                    *dst = make_float2(0.f, 0.f);
                 }
             }
         }
-    };
-    store_rows(gA);
-    for (int r = threadIdx.x / LPR; r < 2 * nzpml; r += nthr / LPR) {
-        float2* dst = gP + (long long)r * M + m0 + 2 * lq;
-        const float2* srcp = ptile + r * P + 2 * lq;
-        if (vec) {
-            *(float4*)dst = *(const float4*)srcp;
-        } else {
-            if (m0 + 2 * lq < M) dst[0] = srcp[0];
-            if (m0 + 2 * lq + 1 < M) dst[1] = srcp[1];
+        const int tl = *A.clk.time - A.clk.t0[s];           // this slot's clock
+        const bool src_on = A.src_mode != 0 && slot_src_on(A.clk, tl);
+        // this mode's multipliers, loaded while the tile copies are in flight
+        const float kx = mvalid ? A.pt[PT_KX * M + m] : 0.f;
+        const float ky = mvalid ? A.pt[PT_KY * M + m] : 0.f;
+        const float gd = (mvalid && A.damp) ? A.pt[PT_DAMP * M + m] : 0.f;
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncthreads();                                      // the tiles are in, the mbarrier is initialised
+        // bounded wait for the tables; if it gives up anywhere in the CTA, the CTA
+        // reports it and leaves without computing or storing (its modes keep the
+        // state of the previous step), thread 0 first waiting out a copy still in
+        // flight so that nothing lands in shared memory after the CTA has gone
+        if (first && __syncthreads_or(!mbar_wait(mbar, A.wait_limit))) {
+            if (threadIdx.x == 0) {
+                atomicExch(A.err, 1);
+                if (!A.no_copy) mbar_wait(mbar, 1 << 22);
+            }
+            return;
         }
-    }
-    // ---- the last stage's right-hand side, when an output needs it ----
-    if (A.write_scr) {
-        __syncthreads();
+
+        // ---- L2 prefetch of the rows of the CTA that starts pf_stride CTAs
+        // later (about when this one ends): its tile load then comes from L2 ----
+        if (A.pf_stride > 0) {
+            const int nid = item + gridDim.x;             // this CTA's next item
+            if (nid < nitem) {
+                const int ns = nid / ntile, nm0 = (nid - ns * ntile) * P;
+                const float2* nA = A.a + (long long)ns * 6 * fs + nm0;
+                for (int r = threadIdx.x; r < 6 * nz; r += nthr) {
+                    const int f = r / nz, z = r - f * nz;
+                    const float2* row = nA + f * fs + (long long)z * M;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(row)));
+                }
+                const float2* nP = A.pml + (long long)ns * 2 * A.ps + nm0;
+                for (int r = threadIdx.x; r < 2 * nzpml; r += nthr)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(nP + (long long)r * M)));
+            }
+        }
+
+        const float2 NGD = bc2(-gd);
+        // threads that own rows with special rules
+        const bool lo = (j0 == 0);                                       // rows 0, 1
+        const bool hi = (j0 <= nz - 1) && (j0 + CH > nz - 2);            // rows nz-2, nz-1
+        // PML levels of this chunk: bit q of pmask, plane index pipv + q (a chunk
+        // holds contiguous levels of one layer at most)
+        unsigned pmask = 0;
+        int pipv = 0;
+        if (j0 < nb) {
+            pmask = (1u << min(CH, nb - j0)) - 1u;
+            pipv = j0;
+        } else {
+            const int l0 = max(j0, nz - nt), l1 = min(j0 + CH, nz);
+            if (l1 > l0) {
+                pmask = ((1u << (l1 - l0)) - 1u) << (l0 - j0);
+                pipv = nb + (j0 - (nz - nt));
+            }
+        }
+        const bool pml_t = pmask != 0;
+        const bool src_t = src_on && mvalid && A.ksrc >= j0 && A.ksrc < j0 + CH;
+        // forcing of this step for this mode (only the thread owning the source plane uses it)
+        float2 F = make_float2(0.f, 0.f);
+        if (src_t) {
+            if (A.src_mode == 1) {
+                const float2* pl = A.planes + (long long)s * A.plane_ss + m;
+                float w = (tl < A.nseries) ? (float)A.series[(long long)s * A.nseries + tl] : 0.f;
+                F = w * pl[0];
+            } else {   // this step's interpolated plane, from source_plane_kernel
+                F = A.src_plane[(long long)s * M + m];
+            }
+            F = A.src_scale * F;
+        }
+
+        float2 sc[6][CH];
         #pragma unroll
         for (int f = 0; f < 6; ++f)
             #pragma unroll
-            for (int q = 0; q < CH; ++q) tp[f * P * LZ + j0 + q] = sc[f][q];
+            for (int q = 0; q < CH; ++q) sc[f][q] = make_float2(0.f, 0.f);
+
+        float2* tp = tile + pi * LZ + GZ;                    // field f, level j: tp[f*P*LZ + j]
+        auto TA = [&](int f, int j) -> float2 { return tp[f * P * LZ + j]; };
+        // z table entry of row r at level j, as a pair
+        auto Z2 = [&](int r, int j) { return zt2(zs, r * NZP + j); };
+
+        // one LDDRK stage; HS: the stage argument is a + beta*scr (stages 2-5)
+        // rather than a (stage 1), fixed at compile time
+        auto stage = [&](auto hs_c, const float beta) {
+            constexpr bool hs = decltype(hs_c)::value;
+            const float2 BT = bc2(beta);
+            // ---- temp xi_z into the first exchange line ----
+            float2 own[CH];
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                float2 v = TA(2, j0 + q);
+                if (hs) v = pfma(BT, sc[2][q], v);
+                own[q] = v;
+                // level j0+2 is no neighbour's stencil value; only the top rows'
+                // closure (levels nz-5..nz-1) may read it from the line
+                if (q != 2 || j0 + 2 >= nz - 5) xl[j0 + q] = v;
+            }
+            float2 top = make_float2(0.f, 0.f);
+            if (!D3 && hi) {   // caller-set top value of bc 3 (physics2d.f90:960)
+                float2 last = make_float2(0.f, 0.f);
+                #pragma unroll
+                for (int q = 0; q < CH; ++q)
+                    if (j0 + q == nz - 1) last = sc[0][q];
+                float2 xx = TA(0, nz - 1);
+                if (hs) xx = xx + beta * last;
+                top = -(imul(kx, xx) * A.unstr_top);
+            }
+            pencil_sync(pi, TP);
+            float2 d[CH];
+            // d: the stretched derivative (the solve's tables carry the stretch)
+            zsolve<BCX, W>(xl, own, zs, FZ_SX, FZ_LX, nz, top, j0, lo, hi, t, lf, lk, pi, A.cc, d);
+            if (pml_t) {   // psi_vz (displacement.f90 PML rows)
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    if (pmask & (1u << q)) {
+                        const int j = j0 + q, ip = pipv + q;
+                        float2 psi = ptile[ip * P + pi];
+                        if (hs) psi = psi + beta * spt[ip * P + pi];
+                        spt[ip * P + pi] = Z2(FZ_AZ, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
+                        d[q] = d[q] + psi;
+                    }
+                }
+            }
+            // ---- div, p', the buoyancy term, horizontal right-hand sides ----
+            float2 qt[CH];
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                const int j = j0 + q;
+                float2 xx = TA(0, j);
+                const float2 xz = own[q];      // the xi_z stage argument, still in registers
+                if (hs) xx = pfma(BT, sc[0][q], xx);
+                float2 div = imul(kx, xx) + d[q];
+                if (D3) {
+                    float2 xy = TA(1, j);
+                    if (hs) xy = pfma(BT, sc[1][q], xy);
+                    div = div + imul(ky, xy);
+                }
+                const float2 p = pmul(make_float2(-1.f, -1.f), pfma(Z2(FZ_GP, j), xz, pmul(Z2(FZ_C2R, j), div)));
+                qt[q] = pfma(Z2(FZ_E2, j), xz, pmul(Z2(FZ_E1, j), div));   // -g rho'/rho0
+                if (q != 2 || j0 + 2 >= nz - 5) xl[j] = p;
+                own[q] = p;
+            }
+            pencil_sync(pi, TP);
+            // ---- dp'/dz, RHS v_z and xi_z ----
+            // d: (stretch / rho0) dp'/dz, scaled by the solve's tables
+            zsolve<BCP, W>(xl, own, zs, FZ_SP, FZ_LP, nz, make_float2(0.f, 0.f), j0, lo, hi, t, lf, lk, pi, A.cc, d);
+            // ---- horizontal right-hand sides (they do not feed the p' solve) ----
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                const int j = j0 + q;
+                float2 vx = TA(3, j);
+                if (hs) vx = pfma(BT, sc[3][q], vx);
+                const float ri = Z2(FZ_RI, j).x;
+                sc[3][q] = pfma(NGD, vx, -ri * imul(kx, own[q]));
+                sc[0][q] = vx;
+                if (D3) {
+                    float2 vy = TA(4, j);
+                    if (hs) vy = pfma(BT, sc[4][q], vy);
+                    sc[4][q] = pfma(NGD, vy, -ri * imul(ky, own[q]));
+                    sc[1][q] = vy;
+                }
+            }
+            // zero right-hand side rows: j = 0 (and j = nz-1 in 3-D)
+            if (lo) { sc[3][0] = sc[0][0] = make_float2(0.f, 0.f); if (D3) sc[4][0] = sc[1][0] = sc[3][0]; }
+            if (D3 && hi) {
+                #pragma unroll
+                for (int q = 0; q < CH; ++q)
+                    if (j0 + q == nz - 1) sc[0][q] = sc[1][q] = sc[3][q] = sc[4][q] = make_float2(0.f, 0.f);
+            }
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                const int j = j0 + q;
+                float2 vz = TA(5, j);
+                if (hs) vz = pfma(BT, sc[5][q], vz);
+                sc[5][q] = pfma(NGD, vz, psub(qt[q], d[q]));
+                sc[2][q] = vz;
+            }
+            if (pml_t) {   // psi_p
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    if (pmask & (1u << q)) {
+                        const int j = j0 + q, ip = pipv + q;
+                        float2 psi = ptile[(nzpml + ip) * P + pi];
+                        if (hs) psi = psi + beta * spt[(nzpml + ip) * P + pi];
+                        spt[(nzpml + ip) * P + pi] = Z2(FZ_AZR, j).x * d[q] + Z2(FZ_BZ, j).x * psi;
+                        sc[5][q] = sc[5][q] - Z2(FZ_RI, j).x * psi;
+                    }
+                }
+            }
+            if (src_t) {
+                #pragma unroll
+                for (int q = 0; q < CH; ++q)
+                    if (j0 + q == A.ksrc) sc[5][q] = sc[5][q] + F;
+            }
+            if (lo) sc[5][0] = sc[2][0] = make_float2(0.f, 0.f);
+            if (D3 && hi) {
+                #pragma unroll
+                for (int q = 0; q < CH; ++q)
+                    if (j0 + q == nz - 1) sc[5][q] = sc[2][q] = make_float2(0.f, 0.f);
+            }
+        };
+        stage(std::integral_constant<bool, false>(), 0.f);
+        for (int rk = 1; rk < 5; ++rk) {
+            // static parameter indices keep the argument block out of local memory
+            const float beta = rk == 1 ? A.betas[1] : rk == 2 ? A.betas[2] : rk == 3 ? A.betas[3] : A.betas[4];
+            stage(std::integral_constant<bool, true>(), beta);
+        }
+
+        // ---- update a += dt*scr, pml += dt*scrpml (step.f90:114-116) ----
+        const float dt = A.dt;
+        const float2 DT = bc2(dt);
+        #pragma unroll
+        for (int f = 0; f < 6; ++f)
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                float2* a = tp + f * P * LZ + j0 + q;
+                *a = pfma(DT, sc[f][q], *a);
+            }
+        if (pml_t) {
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) {
+                if (pmask & (1u << q)) {
+                    const int ip = pipv + q;
+                    ptile[ip * P + pi] = ptile[ip * P + pi] + dt * spt[ip * P + pi];
+                    ptile[(nzpml + ip) * P + pi] = ptile[(nzpml + ip) * P + pi] + dt * spt[(nzpml + ip) * P + pi];
+                }
+            }
+        }
+        pencil_sync(pi, TP);
+        // ---- z filter (+ horizontal filter): field f is filtered into registers,
+        // and written back after the next barrier, while field f+1 is filtered ----
+        const float hf = mvalid ? A.pt[PT_HF * M + m] : 1.f;
+        const float h1 = 0.5f * 0.41015625f, h2 = 0.5f * -0.234375f, h3 = 0.5f * 0.087890625f;
+        const float h4 = 0.5f * -0.01953125f, h5 = 0.5f * 0.001953125f, c0 = 0.75390625f;
+        const bool hfil_on = slot_hfilter(A.clk, tl);
+        const bool flo = j0 < 5, fhi = (j0 < nz) && (j0 + CH > nz - 5);
+        float2 prev[CH];
+        #pragma unroll
+        for (int f = 0; f < 7; ++f) {
+            float2 out[CH];
+            if (f < 6) {
+                const float2* V = tp + f * P * LZ;
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    const int j = j0 + q;
+                    float2 acc = pmul(bc2(c0), V[j]);
+                    acc = pfma(bc2(h1), padd(V[j - 1], V[j + 1]), acc);
+                    acc = pfma(bc2(h2), padd(V[j - 2], V[j + 2]), acc);
+                    acc = pfma(bc2(h3), padd(V[j - 3], V[j + 3]), acc);
+                    acc = pfma(bc2(h4), padd(V[j - 4], V[j + 4]), acc);
+                    out[q] = pfma(bc2(h5), padd(V[j - 5], V[j + 5]), acc);
+                }
+                if (flo || fhi) {   // FILTER_VARS_3D / _2D boundary rows
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q) {
+                        const int j = j0 + q;
+                        const bool near_bot = (j >= 1 && j <= 4), near_top = (j >= nz - 5 && j <= nz - 2);
+                        if (j == 0 || j == nz - 1) out[q] = V[j];
+                        else if (near_top) out[q] = 0.5f * (V[j + 1] + V[j - 1]);
+                        else if (near_bot) out[q] = D3 ? 0.5f * (V[j + 1] + V[j - 1]) : V[j];
+                    }
+                }
+                if (hfil_on && (D3 ? (f < 5) : true)) {
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q) out[q] = hf * out[q];
+                }
+            }
+            if (f > 0) {
+                pencil_sync(pi, TP);   // every thread has read field f-1's neighbours
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) tp[(f - 1) * P * LZ + j0 + q] = prev[q];
+            }
+            #pragma unroll
+            for (int q = 0; q < CH; ++q) prev[q] = out[q];
+        }
+        __syncthreads();   // the store below copies every pencil's rows
+        // ---- store a and the PML planes.  A row [f][z] of the CTA's P modes is
+        // 8P contiguous bytes in HBM; P/2 consecutive lanes write it as P/2
+        // float4, so every warp store covers whole rows (full sectors) instead
+        // of 16 bytes in each of 32 rows ----
+        constexpr int LPR = P / 2;                            // lanes per row
+        const int lq = threadIdx.x % LPR;                     // this lane's modes: 2 lq, 2 lq + 1
+        auto store_rows = [&](float2* gbase) {
+            #pragma unroll 1
+            for (int f = 0; f < 6; ++f) {
+                for (int z = threadIdx.x / LPR; z < nz; z += nthr / LPR) {
+                    float2* dst = gbase + f * fs + (long long)z * M + m0 + 2 * lq;
+                    const float2* srcp = tile + f * P * LZ + (2 * lq) * LZ + GZ + z;
+                    if (vec) {
+                        const float2 w0 = srcp[0], w1 = srcp[LZ];
+                        *(float4*)dst = make_float4(w0.x, w0.y, w1.x, w1.y);
+                    } else {
+                        if (m0 + 2 * lq < M) dst[0] = srcp[0];
+                        if (m0 + 2 * lq + 1 < M) dst[1] = srcp[LZ];
+                    }
+                }
+            }
+        };
+        store_rows(gA);
+        for (int r = threadIdx.x / LPR; r < 2 * nzpml; r += nthr / LPR) {
+            float2* dst = gP + (long long)r * M + m0 + 2 * lq;
+            const float2* srcp = ptile + r * P + 2 * lq;
+            if (vec) {
+                *(float4*)dst = *(const float4*)srcp;
+            } else {
+                if (m0 + 2 * lq < M) dst[0] = srcp[0];
+                if (m0 + 2 * lq + 1 < M) dst[1] = srcp[1];
+            }
+        }
+        // ---- the last stage's right-hand side, when an output needs it ----
+        if (A.write_scr) {
+            __syncthreads();
+            #pragma unroll
+            for (int f = 0; f < 6; ++f)
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) tp[f * P * LZ + j0 + q] = sc[f][q];
+            __syncthreads();
+            store_rows(gS);
+        }
+        // every thread has read the tile and the PML tile out for the stores
+        // (in flight now) before the next item's copies overwrite them
         __syncthreads();
-        store_rows(gS);
-    }
-    // every thread has read the tile and the PML tile out for the stores
-    // (in flight now) before the next item's copies overwrite them
-    __syncthreads();
     }
 }
 
